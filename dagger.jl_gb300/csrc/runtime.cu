@@ -1,0 +1,800 @@
+// Host runtime of libdaggergb300: library state, the tile-operation C ABI,
+// and the datadeps engine that turns a recorded region of tile tasks into a
+// multi-stream CUDA graph.
+//
+// Datadeps semantics follow Dagger.spawn_datadeps (src/datadeps/queue.jl:35-63
+// of Dagger.jl): tasks are recorded in submission order; each matrix argument
+// is an In / Out / InOut access over its strided byte footprint (the
+// reference's StridedAliasing, src/memory-spaces.jl:480); a task that writes
+// waits for the last writer and every reader since of every overlapping
+// footprint, a task that reads waits for the last writer
+// (src/datadeps/aliasing.jl:740-776).  Independent tasks may run in parallel;
+// the result equals running the tasks one by one in submission order.
+//
+// Lowering: every task is given a stream from a per-thread pool.  A task
+// reuses the stream of its latest predecessor when that predecessor is still
+// the stream's tail (the edge is then free), otherwise it takes the least
+// recently used stream; each remaining cross-stream edge becomes an event
+// wait.  The issue is captured into a CUDA graph, cached by a hash of the
+// task list (same tasks, same pointers -> same graph), and replayed.
+#include <atomic>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "dg_common.cuh"
+#include "runtime.h"
+
+// ---------------------------------------------------------------------------
+// errors, device properties
+// ---------------------------------------------------------------------------
+static thread_local std::string t_last_error;
+
+void dg_set_last_error(const char *file, int line, const char *msg) {
+  const char *base = strrchr(file, '/');
+  t_last_error = std::string(base ? base + 1 : file) + ":" + std::to_string(line) + ": " + msg;
+}
+
+int dg_num_sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cache[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 1;
+  }
+  return cache[dev];
+}
+
+namespace dg {
+
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches += n; }
+long long launches() { return g_launches.load(); }
+
+DeviceState &device_state() {
+  static std::mutex mu;
+  static std::map<int, std::unique_ptr<DeviceState>> states;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> g(mu);
+  auto &p = states[dev];
+  if (!p) p.reset(new DeviceState());
+  return *p;
+}
+
+// Per-thread pool of non-blocking streams (one pool per device).
+std::vector<cudaStream_t> &stream_pool(int want) {
+  static thread_local std::map<int, std::vector<cudaStream_t>> pools;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto &v = pools[dev];
+  while ((int)v.size() < want) {
+    cudaStream_t s;
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi) != cudaSuccess) break;
+    v.push_back(s);
+  }
+  return v;
+}
+
+int DeviceState::scratch_int(int **p) {
+  std::lock_guard<std::mutex> g(mu);
+  if (!info_words) {
+    if (cudaMalloc((void **)&info_words, sizeof(int) * kInfoWords) != cudaSuccess) {
+      dg_set_last_error(__FILE__, __LINE__, "cudaMalloc of info words failed");
+      return DG_ERR_NOMEM;
+    }
+    cudaMemset(info_words, 0, sizeof(int) * kInfoWords);
+  }
+  *p = info_words + (next_info++ % kInfoWords);
+  return 0;
+}
+
+DeviceState::~DeviceState() {}
+
+// ---------------------------------------------------------------------------
+// strided footprints
+// ---------------------------------------------------------------------------
+Footprint footprint(const void *p, int rows, int cols, int ld, int elem) {
+  Footprint f;
+  f.base = (uintptr_t)p;
+  f.rows = (int64_t)(rows > 0 ? rows : 0) * elem;
+  f.cols = cols > 0 ? cols : 0;
+  f.ld = (int64_t)(ld > 0 ? ld : 1) * elem;
+  f.lo = f.base;
+  f.hi = (f.rows == 0 || f.cols == 0) ? f.base : f.base + (f.cols - 1) * f.ld + f.rows;
+  return f;
+}
+
+static bool ranges_meet(int64_t a0, int64_t a1, int64_t b0, int64_t b1) {
+  return a0 < b1 && b0 < a1;
+}
+
+bool overlaps(const Footprint &a, const Footprint &b) {
+  if (a.hi <= b.lo || b.hi <= a.lo) return false;
+  if (a.ld != b.ld || a.rows > a.ld || b.rows > b.ld) return true;  // conservative
+  const Footprint &x = a.base <= b.base ? a : b;
+  const Footprint &y = a.base <= b.base ? b : a;
+  int64_t d = (int64_t)(y.base - x.base);
+  int64_t cb = d / x.ld, rb = d % x.ld;
+  // y's rows [rb, rb + y.rows) in x's columns [cb, cb + y.cols); rows past
+  // ld wrap into the next column.
+  int64_t r_end = rb + y.rows;
+  if (ranges_meet(0, x.rows, rb, r_end < x.ld ? r_end : x.ld) &&
+      ranges_meet(0, x.cols, cb, cb + y.cols))
+    return true;
+  if (r_end > x.ld && ranges_meet(0, x.rows, 0, r_end - x.ld) &&
+      ranges_meet(0, x.cols, cb + 1, cb + 1 + y.cols))
+    return true;
+  return false;
+}
+
+}  // namespace dg
+
+// ---------------------------------------------------------------------------
+// the region (datadeps engine)
+// ---------------------------------------------------------------------------
+using dg::Footprint;
+
+struct dg_region {
+  struct Access {
+    Footprint f;
+    int mode;
+  };
+  struct Ainfo {
+    Footprint f;
+    int last_writer = -1;
+    std::vector<int> readers;
+  };
+  std::vector<dg_task> tasks;
+  std::vector<std::vector<int>> preds;
+  std::vector<Ainfo> ainfos;
+  std::multimap<uintptr_t, int> by_lo;
+  uint64_t max_len = 0;
+  uint64_t hash = 1469598103934665603ull;
+  int nedges = 0;
+};
+
+static void hash_bytes(uint64_t &h, const void *p, size_t n) {
+  const unsigned char *c = (const unsigned char *)p;
+  for (size_t i = 0; i < n; i++) {
+    h ^= c[i];
+    h *= 1099511628211ull;
+  }
+}
+
+static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out) {
+  out.clear();
+  auto mode = [](int m, int def) { return m ? m : def; };
+  const int E = 8;
+  switch (t.op) {
+    case DG_OP_POTRF:
+      out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), mode(t.mode_c, DG_INOUT)});
+      break;
+    case DG_OP_TRSM: {
+      int ka = (t.side == 'L' || t.side == 'l') ? t.m : t.n;
+      out.push_back({dg::footprint(t.a, ka, ka, t.lda, E), mode(t.mode_a, DG_IN)});
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), mode(t.mode_c, DG_INOUT)});
+      break;
+    }
+    case DG_OP_SYRK: {
+      bool nt = (t.trans == 'N' || t.trans == 'n');
+      out.push_back({dg::footprint(t.a, nt ? t.n : t.k, nt ? t.k : t.n, t.lda, E), mode(t.mode_a, DG_IN)});
+      out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), mode(t.mode_c, DG_INOUT)});
+      break;
+    }
+    case DG_OP_GEMM: {
+      bool na = (t.transa == 'N' || t.transa == 'n'), nb = (t.transb == 'N' || t.transb == 'n');
+      out.push_back({dg::footprint(t.a, na ? t.m : t.k, na ? t.k : t.m, t.lda, E), mode(t.mode_a, DG_IN)});
+      out.push_back({dg::footprint(t.b, nb ? t.k : t.n, nb ? t.n : t.k, t.ldb, E), mode(t.mode_b, DG_IN)});
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), mode(t.mode_c, t.beta == 0.0 ? DG_OUT : DG_INOUT)});
+      break;
+    }
+    case DG_OP_COPY:
+      out.push_back({dg::footprint(t.a, t.m, t.n, t.lda, E), mode(t.mode_a, DG_IN)});
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), mode(t.mode_c, DG_OUT)});
+      break;
+  }
+}
+
+extern "C" dg_region *dg_region_create(void) { return new dg_region(); }
+extern "C" void dg_region_destroy(dg_region *r) { delete r; }
+
+extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
+  DG_CHECK_ARG(r != nullptr, 1);
+  DG_CHECK_ARG(tp != nullptr, 2);
+  const dg_task &t = *tp;
+  DG_CHECK_ARG(t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY, 2);
+  const int id = (int)r->tasks.size();
+  r->tasks.push_back(t);
+  hash_bytes(r->hash, &t, sizeof(dg_task));
+  std::vector<dg_region::Access> acc;
+  task_accesses(t, acc);
+  std::vector<int> p;
+  auto add = [&](int q) {
+    if (q < 0 || q == id) return;
+    for (int x : p)
+      if (x == q) return;
+    p.push_back(q);
+  };
+  std::vector<int> exact(acc.size(), -1);
+  for (size_t ai = 0; ai < acc.size(); ai++) {
+    const Footprint &f = acc[ai].f;
+    if (f.hi == f.lo) continue;
+    uintptr_t from = f.lo > r->max_len ? f.lo - r->max_len : 0;
+    for (auto it = r->by_lo.lower_bound(from); it != r->by_lo.end() && it->first < f.hi; ++it) {
+      dg_region::Ainfo &o = r->ainfos[it->second];
+      if (!dg::overlaps(o.f, f)) continue;
+      if (o.f.base == f.base && o.f.rows == f.rows && o.f.cols == f.cols && o.f.ld == f.ld)
+        exact[ai] = it->second;
+      add(o.last_writer);                       // both reads and writes
+      if (acc[ai].mode & DG_OUT)
+        for (int q : o.readers) add(q);         // writes also wait for readers
+    }
+  }
+  for (size_t ai = 0; ai < acc.size(); ai++) {
+    const Footprint &f = acc[ai].f;
+    if (f.hi == f.lo) continue;
+    int idx = exact[ai];
+    if (idx < 0) {
+      idx = (int)r->ainfos.size();
+      r->ainfos.push_back({f, -1, {}});
+      r->by_lo.emplace(f.lo, idx);
+      if (f.hi - f.lo > r->max_len) r->max_len = f.hi - f.lo;
+      exact[ai] = idx;
+    }
+    dg_region::Ainfo &o = r->ainfos[idx];
+    if (acc[ai].mode & DG_OUT) {
+      o.last_writer = id;
+      o.readers.clear();
+    } else {
+      o.readers.push_back(id);
+    }
+  }
+  // an access both read and written by this task (InOut) ends as a write
+  for (size_t ai = 0; ai < acc.size(); ai++) {
+    if (exact[ai] < 0) continue;
+    dg_region::Ainfo &o = r->ainfos[exact[ai]];
+    if (o.last_writer == id) {
+      std::vector<int> keep;
+      for (int q : o.readers)
+        if (q != id) keep.push_back(q);
+      o.readers.swap(keep);
+    }
+  }
+  r->nedges += (int)p.size();
+  r->preds.push_back(std::move(p));
+  return 0;
+}
+
+extern "C" int dg_region_stats(const dg_region *r, int *ntasks, int *nedges) {
+  DG_CHECK_ARG(r != nullptr, 1);
+  if (ntasks) *ntasks = (int)r->tasks.size();
+  if (nedges) *nedges = r->nedges;
+  return 0;
+}
+
+extern "C" int dg_region_edges(const dg_region *r, int *pairs, int cap) {
+  DG_CHECK_ARG(r != nullptr, 1);
+  int n = 0;
+  for (size_t t = 0; t < r->preds.size(); t++)
+    for (int q : r->preds[t]) {
+      if (n >= cap) return n;
+      pairs[2 * n] = (int)t;
+      pairs[2 * n + 1] = q;
+      n++;
+    }
+  return n;
+}
+
+namespace dg {
+
+int run_task(const dg_task &t, int *info, cudaStream_t s) {
+  switch (t.op) {
+    case DG_OP_POTRF:
+      return potrf_f64(t.uplo, t.n, t.c, t.ldc, info, t.info_offset, s);
+    case DG_OP_TRSM:
+      return trsm_f64(t.side, t.uplo, t.transa, t.diag, t.m, t.n, t.alpha, t.a, t.lda, t.c, t.ldc,
+                      info, s);
+    case DG_OP_SYRK: {
+      bool nt = (t.trans == 'N' || t.trans == 'n');
+      Tri tri = (t.uplo == 'U' || t.uplo == 'u') ? TRI_UPPER : TRI_LOWER;
+      return gemm_f64(nt ? 'N' : 'T', nt ? 'T' : 'N', t.n, t.n, t.k, t.alpha, t.a, t.lda, t.a,
+                      t.lda, t.beta, t.c, t.ldc, tri, info, s);
+    }
+    case DG_OP_GEMM:
+      return gemm_f64(t.transa, t.transb, t.m, t.n, t.k, t.alpha, t.a, t.lda, t.b, t.ldb, t.beta,
+                      t.c, t.ldc, TRI_NONE, info, s);
+    case DG_OP_COPY:
+      if (t.m <= 0 || t.n <= 0) return 0;
+      DG_CUDA_TRY(cudaMemcpy2DAsync(t.c, (size_t)t.ldc * 8, t.a, (size_t)t.lda * 8, (size_t)t.m * 8,
+                                    t.n, cudaMemcpyDeviceToDevice, s));
+      return 0;
+  }
+  return DG_ERR_UNSUPPORTED;
+}
+
+struct Plan {
+  std::vector<int> stream_of;
+  std::vector<char> needs_event;
+  int nstreams = 0;
+};
+
+static Plan plan_streams(const dg_region &r, int pool) {
+  Plan pl;
+  const int n = (int)r.tasks.size();
+  pl.stream_of.assign(n, 0);
+  pl.needs_event.assign(n, 0);
+  std::vector<int> tail(pool, -1);
+  std::vector<long> last_use(pool, -1);
+  int used = 0;
+  for (int t = 0; t < n; t++) {
+    int best = -1, bestp = -1;
+    for (int q : r.preds[t]) {
+      int s = pl.stream_of[q];
+      if (tail[s] == q && q > bestp) { best = s; bestp = q; }
+    }
+    if (best < 0) {
+      // least recently used stream
+      best = 0;
+      for (int s = 1; s < pool; s++)
+        if (last_use[s] < last_use[best]) best = s;
+    }
+    pl.stream_of[t] = best;
+    tail[best] = t;
+    last_use[best] = t;
+    if (best + 1 > used) used = best + 1;
+    for (int q : r.preds[t])
+      if (pl.stream_of[q] != best) pl.needs_event[q] = 1;
+  }
+  pl.nstreams = used;
+  return pl;
+}
+
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  int *info = nullptr;
+  long long nodes = 0;  // kernel launches captured in the graph
+  uint64_t last_used = 0;
+};
+
+static std::mutex g_graph_mu;
+static std::map<std::pair<int, uint64_t>, GraphEntry> g_graphs;
+static uint64_t g_graph_clock = 0;
+static const size_t kMaxGraphs = 32;
+
+static int issue(const dg_region &r, const Plan &pl, int *info, cudaStream_t origin, bool serial,
+                 std::vector<cudaEvent_t> &events) {
+  DG_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), origin));
+  const int n = (int)r.tasks.size();
+  if (serial) {
+    for (int t = 0; t < n; t++) {
+      int rc = run_task(r.tasks[t], info, origin);
+      if (rc) return rc;
+    }
+    return 0;
+  }
+  auto &pool = stream_pool(pl.nstreams);
+  if ((int)pool.size() < pl.nstreams) return DG_ERR_CUDA;
+  cudaEvent_t fork;
+  DG_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  events.push_back(fork);
+  DG_CUDA_TRY(cudaEventRecord(fork, origin));
+  for (int s = 0; s < pl.nstreams; s++) DG_CUDA_TRY(cudaStreamWaitEvent(pool[s], fork, 0));
+  std::vector<cudaEvent_t> ev(n, nullptr);
+  for (int t = 0; t < n; t++) {
+    cudaStream_t s = pool[pl.stream_of[t]];
+    for (int q : r.preds[t])
+      if (pl.stream_of[q] != pl.stream_of[t]) DG_CUDA_TRY(cudaStreamWaitEvent(s, ev[q], 0));
+    int rc = run_task(r.tasks[t], info, s);
+    if (rc) return rc;
+    if (pl.needs_event[t]) {
+      DG_CUDA_TRY(cudaEventCreateWithFlags(&ev[t], cudaEventDisableTiming));
+      events.push_back(ev[t]);
+      DG_CUDA_TRY(cudaEventRecord(ev[t], s));
+    }
+  }
+  for (int s = 0; s < pl.nstreams; s++) {
+    cudaEvent_t j;
+    DG_CUDA_TRY(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+    events.push_back(j);
+    DG_CUDA_TRY(cudaEventRecord(j, pool[s]));
+    DG_CUDA_TRY(cudaStreamWaitEvent(origin, j, 0));
+  }
+  return 0;
+}
+
+static int read_info(int *info, cudaStream_t s) {
+  int h = 0;
+  DG_CUDA_TRY(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DG_CUDA_TRY(cudaStreamSynchronize(s));
+  return h;
+}
+
+// A private non-blocking stream per (thread, device): graphs cannot be
+// captured on the legacy default stream, so a region handed the default
+// stream is captured and launched here, bridged to the caller's stream by
+// events on both sides.
+static cudaStream_t private_stream() {
+  static thread_local std::map<int, cudaStream_t> ps;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto it = ps.find(dev);
+  if (it != ps.end()) return it->second;
+  cudaStream_t s = nullptr;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  ps[dev] = s;
+  return s;
+}
+
+static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t origin,
+                         int stream_pool_size, bool sync);
+
+int region_run(dg_region *r, int use_graph, int serial, cudaStream_t origin, int stream_pool_size,
+               bool sync) {
+  const bool legacy = origin == nullptr || origin == cudaStreamLegacy || origin == cudaStreamPerThread;
+  if (!use_graph || !legacy) return region_run_on(r, use_graph, serial, origin, stream_pool_size, sync);
+  cudaStream_t ps = private_stream();
+  if (!ps) {
+    dg_set_last_error(__FILE__, __LINE__, "cannot create a capture stream");
+    return DG_ERR_CUDA;
+  }
+  cudaEvent_t in, out;
+  DG_CUDA_TRY(cudaEventCreateWithFlags(&in, cudaEventDisableTiming));
+  DG_CUDA_TRY(cudaEventCreateWithFlags(&out, cudaEventDisableTiming));
+  DG_CUDA_TRY(cudaEventRecord(in, origin));
+  DG_CUDA_TRY(cudaStreamWaitEvent(ps, in, 0));
+  int rc = region_run_on(r, use_graph, serial, ps, stream_pool_size, sync);
+  cudaEventRecord(out, ps);
+  cudaStreamWaitEvent(origin, out, 0);
+  cudaEventDestroy(in);
+  cudaEventDestroy(out);
+  return rc;
+}
+
+static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t origin,
+                         int stream_pool_size, bool sync) {
+  const int n = (int)r->tasks.size();
+  if (n == 0) return 0;
+  Plan pl;
+  if (!serial) pl = plan_streams(*r, stream_pool_size);
+  std::vector<cudaEvent_t> events;
+  auto cleanup = [&]() {
+    for (auto e : events) cudaEventDestroy(e);
+  };
+  if (!use_graph) {
+    int *info = nullptr;
+    int rc = device_state().scratch_int(&info);
+    if (rc) return rc;
+    rc = issue(*r, pl, info, origin, serial, events);
+    cleanup();
+    if (rc) return rc;
+    return sync ? read_info(info, origin) : 0;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  uint64_t key = r->hash ^ ((uint64_t)serial << 63) ^ ((uint64_t)stream_pool_size << 40);
+  GraphEntry entry;
+  bool found = false;
+  {
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    auto it = g_graphs.find({dev, key});
+    if (it != g_graphs.end()) {
+      it->second.last_used = ++g_graph_clock;
+      entry = it->second;
+      found = true;
+    }
+  }
+  if (!found) {
+    DG_CUDA_TRY(cudaMalloc((void **)&entry.info, 256));
+    DG_CUDA_TRY(cudaMemset(entry.info, 0, 256));
+    cudaGraph_t graph;
+    DG_CUDA_TRY(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal));
+    const long long before = launches();
+    int rc = issue(*r, pl, entry.info, origin, serial, events);
+    entry.nodes = launches() - before;
+    count_launches(-entry.nodes);  // captured, not executed
+    cudaError_t e = cudaStreamEndCapture(origin, &graph);
+    cleanup();
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(graph);
+      cudaFree(entry.info);
+      return rc;
+    }
+    DG_CUDA_TRY(e);
+    e = cudaGraphInstantiate(&entry.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    DG_CUDA_TRY(e);
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    if (g_graphs.size() >= kMaxGraphs) {
+      auto victim = g_graphs.begin();
+      for (auto it = g_graphs.begin(); it != g_graphs.end(); ++it)
+        if (it->second.last_used < victim->second.last_used) victim = it;
+      cudaGraphExecDestroy(victim->second.exec);
+      cudaFree(victim->second.info);
+      g_graphs.erase(victim);
+    }
+    entry.last_used = ++g_graph_clock;
+    g_graphs[{dev, key}] = entry;
+  }
+  DG_CUDA_TRY(cudaGraphLaunch(entry.exec, origin));
+  count_launches(entry.nodes);
+  return sync ? read_info(entry.info, origin) : 0;
+}
+
+void clear_graphs() {
+  std::lock_guard<std::mutex> g(g_graph_mu);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  for (auto it = g_graphs.begin(); it != g_graphs.end();) {
+    if (it->first.first == dev) {
+      cudaGraphExecDestroy(it->second.exec);
+      cudaFree(it->second.info);
+      it = g_graphs.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
+}  // namespace dg
+
+extern "C" int dg_region_run(dg_region *r, int use_graph, int serial, void *stream) {
+  DG_CHECK_ARG(r != nullptr, 1);
+  return dg::region_run(r, use_graph, serial, (cudaStream_t)stream, dg::kDefaultStreams, true);
+}
+
+// ---------------------------------------------------------------------------
+// tile-operation ABI
+// ---------------------------------------------------------------------------
+static bool is_one_of(char c, const char *set) { return c && strchr(set, c) != nullptr; }
+
+extern "C" const char *dg_version(void) { return "libdaggergb300 0.1 (sm_103a)"; }
+extern "C" const char *dg_last_error(void) { return t_last_error.c_str(); }
+
+extern "C" int dg_finalize(void) {
+  dg::clear_graphs();
+  return 0;
+}
+
+extern "C" long long dg_kernel_launches(void) { return dg::launches(); }
+
+extern "C" int dg_set_f64_engine(int engine) {
+  int old = dg::get_f64_engine();
+  dg::set_f64_engine(engine);
+  return old;
+}
+
+extern "C" int dg_potrf_async(char uplo, int n, double *A, int lda, int *info_dev, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(lda >= (n > 1 ? n : 1), 4);
+  DG_CHECK_ARG(info_dev != nullptr, 5);
+  return dg::potrf_f64(uplo, n, A, lda, info_dev, 0, (cudaStream_t)stream);
+}
+
+extern "C" int dg_potrf(char uplo, int n, double *A, int lda, int *info_host, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(lda >= (n > 1 ? n : 1), 4);
+  cudaStream_t s = (cudaStream_t)stream;
+  int *info = nullptr;
+  int rc = dg::device_state().scratch_int(&info);
+  if (rc) return rc;
+  DG_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), s));
+  rc = dg::potrf_f64(uplo, n, A, lda, info, 0, s);
+  if (rc) return rc;
+  if (!info_host) return 0;
+  int h = dg::read_info(info, s);
+  *info_host = h;
+  return h;
+}
+
+extern "C" int dg_trsm(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+                       const double *A, int lda, double *B, int ldb, void *stream) {
+  DG_CHECK_ARG(is_one_of(side, "LRlr"), 1);
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 2);
+  DG_CHECK_ARG(is_one_of(transa, "NTCntc"), 3);
+  DG_CHECK_ARG(is_one_of(diag, "NUnu"), 4);
+  DG_CHECK_ARG(m >= 0, 5);
+  DG_CHECK_ARG(n >= 0, 6);
+  int ka = (side == 'L' || side == 'l') ? m : n;
+  DG_CHECK_ARG(lda >= (ka > 1 ? ka : 1), 9);
+  DG_CHECK_ARG(ldb >= (m > 1 ? m : 1), 11);
+  return dg::trsm_f64(side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, nullptr,
+                      (cudaStream_t)stream);
+}
+
+extern "C" int dg_syrk(char uplo, char trans, int n, int k, double alpha, const double *A, int lda,
+                       double beta, double *C, int ldc, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(is_one_of(trans, "NTCntc"), 2);
+  DG_CHECK_ARG(n >= 0, 3);
+  DG_CHECK_ARG(k >= 0, 4);
+  bool nt = (trans == 'N' || trans == 'n');
+  int ra = nt ? n : k;
+  DG_CHECK_ARG(lda >= (ra > 1 ? ra : 1), 7);
+  DG_CHECK_ARG(ldc >= (n > 1 ? n : 1), 10);
+  dg::Tri tri = (uplo == 'U' || uplo == 'u') ? dg::TRI_UPPER : dg::TRI_LOWER;
+  return dg::gemm_f64(nt ? 'N' : 'T', nt ? 'T' : 'N', n, n, k, alpha, A, lda, A, lda, beta, C, ldc,
+                      tri, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int dg_gemm(char transa, char transb, int m, int n, int k, double alpha,
+                       const double *A, int lda, const double *B, int ldb, double beta, double *C,
+                       int ldc, void *stream) {
+  DG_CHECK_ARG(is_one_of(transa, "NTCntc"), 1);
+  DG_CHECK_ARG(is_one_of(transb, "NTCntc"), 2);
+  DG_CHECK_ARG(m >= 0, 3);
+  DG_CHECK_ARG(n >= 0, 4);
+  DG_CHECK_ARG(k >= 0, 5);
+  bool na = (transa == 'N' || transa == 'n'), nb = (transb == 'N' || transb == 'n');
+  int ra = na ? m : k, rb = nb ? k : n;
+  DG_CHECK_ARG(lda >= (ra > 1 ? ra : 1), 8);
+  DG_CHECK_ARG(ldb >= (rb > 1 ? rb : 1), 10);
+  DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 13);
+  return dg::gemm_f64(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, dg::TRI_NONE,
+                      nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int dg_trsv(char uplo, char trans, char diag, int n, const double *A, int lda, double *x,
+                       void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(is_one_of(trans, "NTCntc"), 2);
+  DG_CHECK_ARG(is_one_of(diag, "NUnu"), 3);
+  DG_CHECK_ARG(n >= 0, 4);
+  DG_CHECK_ARG(lda >= (n > 1 ? n : 1), 6);
+  return dg::trsm_f64('L', uplo, trans, diag, n, 1, 1.0, A, lda, x, n > 1 ? n : 1, nullptr,
+                      (cudaStream_t)stream);
+}
+
+extern "C" int dg_gemv(char trans, int m, int n, double alpha, const double *A, int lda,
+                       const double *x, double beta, double *y, void *stream) {
+  DG_CHECK_ARG(is_one_of(trans, "NTCntc"), 1);
+  DG_CHECK_ARG(m >= 0, 2);
+  DG_CHECK_ARG(n >= 0, 3);
+  DG_CHECK_ARG(lda >= (m > 1 ? m : 1), 6);
+  bool nt = (trans == 'N' || trans == 'n');
+  int rows = nt ? m : n, inner = nt ? n : m;
+  return dg::gemm_f64(nt ? 'N' : 'T', 'N', rows, 1, inner, alpha, A, lda, x, inner > 1 ? inner : 1,
+                      beta, y, rows > 1 ? rows : 1, dg::TRI_NONE, nullptr, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// whole-call entry points
+// ---------------------------------------------------------------------------
+namespace dg {
+
+void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles) {
+  const int mt = (n + nb - 1) / nb;
+  auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
+  auto T = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
+  const bool up = (uplo == 'U' || uplo == 'u');
+  for (int k = 0; k < mt; k++) {
+    dg_task t;
+    memset(&t, 0, sizeof t);
+    t.op = DG_OP_POTRF; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.c = T(k, k); t.ldc = rows(k);
+    t.info_offset = k * nb;
+    dg_region_add(r, &t);
+    if (up) {
+      for (int j = k + 1; j < mt; j++) {  // cholesky.jl:40-42
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = 'U'; t.transa = 'T'; t.diag = 'N';
+        t.m = rows(k); t.n = rows(j); t.alpha = 1.0;
+        t.a = T(k, k); t.lda = rows(k); t.c = T(k, j); t.ldc = rows(k);
+        dg_region_add(r, &t);
+      }
+      for (int m = k + 1; m < mt; m++) {  // cholesky.jl:43-52
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_SYRK; t.uplo = 'U'; t.trans = 'T'; t.n = rows(m); t.k = rows(k);
+        t.alpha = -1.0; t.beta = 1.0; t.a = T(k, m); t.lda = rows(k); t.c = T(m, m); t.ldc = rows(m);
+        dg_region_add(r, &t);
+        for (int j = m + 1; j < mt; j++) {
+          memset(&t, 0, sizeof t);
+          t.op = DG_OP_GEMM; t.transa = 'T'; t.transb = 'N'; t.m = rows(m); t.n = rows(j);
+          t.k = rows(k); t.alpha = -1.0; t.beta = 1.0; t.a = T(k, m); t.lda = rows(k);
+          t.b = T(k, j); t.ldb = rows(k); t.c = T(m, j); t.ldc = rows(m);
+          dg_region_add(r, &t);
+        }
+      }
+    } else {
+      for (int m = k + 1; m < mt; m++) {  // cholesky.jl:85-87
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_TRSM; t.side = 'R'; t.uplo = 'L'; t.transa = 'T'; t.diag = 'N';
+        t.m = rows(m); t.n = rows(k); t.alpha = 1.0;
+        t.a = T(k, k); t.lda = rows(k); t.c = T(m, k); t.ldc = rows(m);
+        dg_region_add(r, &t);
+      }
+      for (int j = k + 1; j < mt; j++) {  // cholesky.jl:88-97
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_SYRK; t.uplo = 'L'; t.trans = 'N'; t.n = rows(j); t.k = rows(k);
+        t.alpha = -1.0; t.beta = 1.0; t.a = T(j, k); t.lda = rows(j); t.c = T(j, j); t.ldc = rows(j);
+        dg_region_add(r, &t);
+        for (int m = j + 1; m < mt; m++) {
+          memset(&t, 0, sizeof t);
+          t.op = DG_OP_GEMM; t.transa = 'N'; t.transb = 'T'; t.m = rows(m); t.n = rows(j);
+          t.k = rows(k); t.alpha = -1.0; t.beta = 1.0; t.a = T(m, k); t.lda = rows(m);
+          t.b = T(j, k); t.ldb = rows(j); t.c = T(m, j); t.ldc = rows(m);
+          dg_region_add(r, &t);
+        }
+      }
+    }
+  }
+}
+
+// One left-side block solve of trsm.jl:89-140 (alpha = 1) over the factor's
+// tiles and the right-hand side's tiles.
+void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
+                      int nrhs, double *const *btiles) {
+  const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
+  auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
+  auto cols = [&](int j) { return (j + 1) * nb <= nrhs ? nb : nrhs - j * nb; };
+  auto A = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
+  auto B = [&](int i, int j) { return btiles[i + (size_t)j * mt]; };
+  const bool forward = (uplo == 'U') ? (trans != 'N') : (trans == 'N');
+  for (int s = 0; s < mt; s++) {
+    int k = forward ? s : mt - 1 - s;
+    for (int c = 0; c < bnt; c++) {
+      dg_task t;
+      memset(&t, 0, sizeof t);
+      t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = uplo; t.transa = trans; t.diag = 'N';
+      t.m = rows(k); t.n = cols(c); t.alpha = 1.0; t.a = A(k, k); t.lda = rows(k);
+      t.c = B(k, c); t.ldc = rows(k);
+      dg_region_add(r, &t);
+    }
+    for (int s2 = s + 1; s2 < mt; s2++) {
+      int m = forward ? s2 : mt - 1 - s2;
+      int ai = (trans == 'N') ? m : k, aj = (trans == 'N') ? k : m;
+      for (int c = 0; c < bnt; c++) {
+        dg_task t;
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_GEMM; t.transa = trans; t.transb = 'N'; t.m = rows(m); t.n = cols(c);
+        t.k = rows(k); t.alpha = -1.0; t.beta = 1.0; t.a = A(ai, aj); t.lda = rows(ai);
+        t.b = B(k, c); t.ldb = rows(k); t.c = B(m, c); t.ldc = rows(m);
+        dg_region_add(r, &t);
+      }
+    }
+  }
+}
+
+}  // namespace dg
+
+extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(nb > 0, 3);
+  DG_CHECK_ARG(tiles != nullptr || n == 0, 4);
+  if (n == 0) return 0;
+  dg_region r;
+  dg::build_cholesky_region(&r, uplo, n, nb, tiles);
+  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+}
+
+extern "C" int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *tiles, int nrhs,
+                                       double *const *btiles, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(nb > 0, 3);
+  DG_CHECK_ARG(nrhs >= 0, 5);
+  if (n == 0 || nrhs == 0) return 0;
+  DG_CHECK_ARG(tiles != nullptr, 4);
+  DG_CHECK_ARG(btiles != nullptr, 6);
+  dg_region r;
+  const bool up = (uplo == 'U' || uplo == 'u');
+  if (up) {
+    dg::build_solve_pass(&r, 'U', 'T', n, nb, tiles, nrhs, btiles);
+    dg::build_solve_pass(&r, 'U', 'N', n, nb, tiles, nrhs, btiles);
+  } else {
+    dg::build_solve_pass(&r, 'L', 'N', n, nb, tiles, nrhs, btiles);
+    dg::build_solve_pass(&r, 'L', 'T', n, nb, tiles, nrhs, btiles);
+  }
+  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+}

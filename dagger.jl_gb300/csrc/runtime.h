@@ -1,0 +1,46 @@
+// Internal host-runtime declarations shared by the translation units of
+// libdaggergb300 (not part of the public ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/dagger_gb300.h"
+
+namespace dg {
+
+constexpr int kDefaultStreams = 16;
+
+// Library-owned per-device state.
+struct DeviceState {
+  static constexpr int kInfoWords = 4096;
+  std::mutex mu;
+  int *info_words = nullptr;  // ring of device ints for synchronous calls
+  unsigned next_info = 0;
+  int scratch_int(int **p);
+  ~DeviceState();
+};
+
+DeviceState &device_state();
+std::vector<cudaStream_t> &stream_pool(int want);
+
+// Strided byte footprint of a column-major matrix argument.
+struct Footprint {
+  uintptr_t base = 0, lo = 0, hi = 0;
+  int64_t rows = 0, cols = 0, ld = 1;  // rows and ld in bytes
+};
+Footprint footprint(const void *p, int rows, int cols, int ld, int elem);
+bool overlaps(const Footprint &a, const Footprint &b);
+
+int run_task(const dg_task &t, int *info, cudaStream_t s);
+int region_run(dg_region *r, int use_graph, int serial, cudaStream_t origin, int stream_pool_size,
+               bool sync);
+void clear_graphs();
+
+void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles);
+void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
+                      int nrhs, double *const *btiles);
+
+}  // namespace dg

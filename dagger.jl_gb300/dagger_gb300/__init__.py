@@ -1,0 +1,21 @@
+"""dagger_gb300: GB300-native tiled Cholesky factor-and-solve behind
+Dagger.jl's API for that path.
+
+The compute runs in libdaggergb300.so (hand-written sm_103a CUDA kernels
+behind the C ABI of include/dagger_gb300.h); this package is the host-side
+mirror of the reference's interface (DArray/Blocks, cholesky, cholesky!,
+ldiv!, ishermitian, spawn_datadeps with In/Out/InOut and the BLAS/LAPACK
+tile calls).
+"""
+from ._lib import DaggerGB300Error, PosDefException, lib
+from .darray import Blocks, DArray, distribute
+from .datadeps import In, InOut, Out, copyto_, spawn, spawn_datadeps
+from .linalg import (Cholesky, cholesky, cholesky_, gemm_, gemv_, ishermitian, issymmetric,
+                     ldiv_, potrf_, syrk_, trsm_, trsv_)
+
+__all__ = [
+    "Blocks", "DArray", "distribute", "Cholesky", "cholesky", "cholesky_", "ldiv_",
+    "ishermitian", "issymmetric", "potrf_", "trsm_", "syrk_", "gemm_", "trsv_", "gemv_",
+    "spawn_datadeps", "spawn", "In", "Out", "InOut", "copyto_", "PosDefException",
+    "DaggerGB300Error", "lib",
+]

@@ -1,0 +1,137 @@
+"""ctypes binding of libdaggergb300.so (include/dagger_gb300.h).
+
+This is the Python counterpart of the `ccall` binding a Julia backend
+would write: plain pointers, sizes and a stream.  The library must exist:
+there is no CPU fallback, and a missing library raises at import of the
+first compute call.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdaggergb300.so")
+
+DG_OK = 0
+DG_ERR_CUDA = -1000
+DG_ERR_TIMEOUT = -1001
+DG_ERR_NOMEM = -1002
+DG_ERR_UNSUPPORTED = -1003
+DG_ERR_NOCONVERGE = -1004
+DG_ERR_STATE = -1005
+
+DG_IN, DG_OUT, DG_INOUT = 1, 2, 3
+DG_OP_POTRF, DG_OP_TRSM, DG_OP_SYRK, DG_OP_GEMM, DG_OP_COPY = 1, 2, 3, 4, 5
+
+c_char, c_int, c_double, c_void_p = ctypes.c_char, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+c_dp = ctypes.c_void_p  # device pointers are passed as integers
+
+
+class DgTask(ctypes.Structure):
+    _fields_ = [
+        ("op", c_int),
+        ("side", c_char), ("uplo", c_char), ("transa", c_char), ("transb", c_char),
+        ("diag", c_char), ("trans", c_char),
+        ("m", c_int), ("n", c_int), ("k", c_int),
+        ("alpha", c_double), ("beta", c_double),
+        ("a", c_void_p), ("lda", c_int),
+        ("b", c_void_p), ("ldb", c_int),
+        ("c", c_void_p), ("ldc", c_int),
+        ("mode_a", c_int), ("mode_b", c_int), ("mode_c", c_int),
+        ("info_offset", c_int),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/dagger_gb300.h declares.
+SIGNATURES = {
+    "dg_version": (ctypes.c_char_p, []),
+    "dg_last_error": (ctypes.c_char_p, []),
+    "dg_finalize": (c_int, []),
+    "dg_kernel_launches": (ctypes.c_longlong, []),
+    "dg_potrf": (c_int, [c_char, c_int, c_dp, c_int, ctypes.POINTER(c_int), c_void_p]),
+    "dg_potrf_async": (c_int, [c_char, c_int, c_dp, c_int, c_dp, c_void_p]),
+    "dg_trsm": (c_int, [c_char, c_char, c_char, c_char, c_int, c_int, c_double, c_dp, c_int,
+                        c_dp, c_int, c_void_p]),
+    "dg_syrk": (c_int, [c_char, c_char, c_int, c_int, c_double, c_dp, c_int, c_double, c_dp,
+                        c_int, c_void_p]),
+    "dg_gemm": (c_int, [c_char, c_char, c_int, c_int, c_int, c_double, c_dp, c_int, c_dp, c_int,
+                        c_double, c_dp, c_int, c_void_p]),
+    "dg_trsv": (c_int, [c_char, c_char, c_char, c_int, c_dp, c_int, c_dp, c_void_p]),
+    "dg_gemv": (c_int, [c_char, c_int, c_int, c_double, c_dp, c_int, c_dp, c_double, c_dp,
+                        c_void_p]),
+    "dg_region_create": (c_void_p, []),
+    "dg_region_add": (c_int, [c_void_p, ctypes.POINTER(DgTask)]),
+    "dg_region_stats": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "dg_region_edges": (c_int, [c_void_p, ctypes.POINTER(c_int), c_int]),
+    "dg_region_run": (c_int, [c_void_p, c_int, c_int, c_void_p]),
+    "dg_region_destroy": (None, [c_void_p]),
+    "dg_cholesky_tiled": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p]),
+    "dg_cholesky_solve_tiled": (c_int, [c_char, c_int, c_int, c_void_p, c_int, c_void_p,
+                                        c_void_p]),
+    "dg_set_f64_engine": (c_int, [c_int]),
+    "dg_ishermitian_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
+    "dg_chkfinite_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """Loads the library (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not os.path.exists(LIB_PATH):
+                    raise RuntimeError(
+                        f"{LIB_PATH} is missing: build it with dagger.jl_gb300/build.py "
+                        "(there is no CPU fallback)")
+                L = ctypes.CDLL(LIB_PATH)
+                for name, (res, args) in SIGNATURES.items():
+                    fn = getattr(L, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().dg_last_error().decode()
+
+
+class PosDefException(Exception):
+    """LinearAlgebra.PosDefException(info): the leading minor of order info
+    is not positive definite."""
+
+    def __init__(self, info: int):
+        super().__init__(f"matrix is not positive definite; Cholesky factorization failed (info={info})")
+        self.info = info
+
+
+class DaggerGB300Error(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libdaggergb300 error {code}: {msg}")
+        self.code = code
+
+
+def check(rc: int, *, posdef: bool = False) -> int:
+    """Maps a status to Python: >0 info (PosDefException when posdef),
+    -i invalid argument i (ValueError), <= -1000 library error."""
+    if rc == 0:
+        return 0
+    if rc > 0:
+        if posdef:
+            raise PosDefException(rc)
+        return rc
+    if rc > -1000:
+        raise ValueError(f"invalid argument {-rc}: {last_error()}")
+    if rc == DG_ERR_NOMEM:
+        raise MemoryError(last_error())
+    raise DaggerGB300Error(rc, last_error())
+
+
+def ch(c: str) -> bytes:
+    return c.encode() if isinstance(c, str) else c

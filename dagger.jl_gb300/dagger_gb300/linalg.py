@@ -1,0 +1,205 @@
+"""The reference-facing API of the Cholesky factor-and-solve path.
+
+Python mirror of what Dagger.jl exposes for this path, with the same names,
+argument meanings and error behaviour:
+
+  cholesky(DA, uplo)   LinearAlgebra.cholesky on a DArray: cholcopy then the
+                       tiled factor (src/array/cholesky.jl:1,19-108)
+  cholesky_(DA, uplo)  cholesky! (in place)
+  ldiv_(C, B)          ldiv!(C::Cholesky{T,<:DMatrix}, B) (src/array/linalg.jl:352-405)
+  ishermitian / issymmetric on a DArray (linalg.jl:43-124)
+  potrf_, trsm_, syrk_, gemm_, trsv_, gemv_
+                       the BLAS/LAPACK tile calls the reference substitutes
+                       with CUBLAS/CUSOLVER (ext/CUDAExt.jl:329-348), on
+                       column-major torch CUDA tensors
+
+Every compute call goes through libdaggergb300 (C ABI); none has a CPU path.
+A matrix that is not positive definite raises PosDefException(info) from
+cholesky / cholesky_ (potrf_checked!, cholesky.jl:2-18), or returns info
+with check=False (cholesky(A; check=false) in LinearAlgebra).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import PosDefException, ch, check, lib
+from .darray import Blocks, DArray
+
+
+def _stream(stream=None) -> int:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def _colmajor(t: torch.Tensor, name: str):
+    """(pointer, rows, cols, ld) of a column-major FP64 CUDA tensor (a tile)."""
+    if not t.is_cuda or t.dtype != torch.float64:
+        raise TypeError(f"{name} must be a float64 CUDA tensor")
+    if t.dim() == 1:
+        return t.data_ptr(), t.shape[0], 1, max(t.shape[0], 1)
+    r, c = t.shape
+    if t.stride(0) != 1 and not (c == 1):
+        raise ValueError(f"{name} must be column-major (stride(0) == 1)")
+    ld = t.stride(1) if c > 1 else max(r, 1)
+    return t.data_ptr(), r, c, max(ld, 1)
+
+
+# ---------------------------------------------------------------------------
+# tile calls (BLAS / LAPACK conventions)
+# ---------------------------------------------------------------------------
+
+def potrf_(uplo: str, A: torch.Tensor, stream=None):
+    """LAPACK.potrf!(uplo, A) -> (A, info); synchronises like the reference's."""
+    p, r, c, ld = _colmajor(A, "A")
+    if r != c:
+        raise ValueError("potrf_: A must be square")
+    info = ctypes.c_int(0)
+    rc = lib().dg_potrf(ch(uplo), r, p, ld, ctypes.byref(info), _stream(stream))
+    if rc < 0:
+        check(rc)
+    return A, info.value
+
+
+def trsm_(side, uplo, transa, diag, alpha, A, B, stream=None):
+    """BLAS.trsm!(side, uplo, transa, diag, alpha, A, B) -> B."""
+    pa, ra, ca, lda = _colmajor(A, "A")
+    pb, m, n, ldb = _colmajor(B, "B")
+    check(lib().dg_trsm(ch(side), ch(uplo), ch(transa), ch(diag), m, n, float(alpha), pa, lda,
+                        pb, ldb, _stream(stream)))
+    return B
+
+
+def syrk_(uplo, trans, alpha, A, beta, C, stream=None):
+    """BLAS.syrk!(uplo, trans, alpha, A, beta, C) -> C."""
+    pa, ra, ca, lda = _colmajor(A, "A")
+    pc, n, n2, ldc = _colmajor(C, "C")
+    k = ca if trans in ('N', 'n') else ra
+    check(lib().dg_syrk(ch(uplo), ch(trans), n, k, float(alpha), pa, lda, float(beta), pc, ldc,
+                        _stream(stream)))
+    return C
+
+
+def gemm_(transa, transb, alpha, A, B, beta, C, stream=None):
+    """BLAS.gemm!(tA, tB, alpha, A, B, beta, C) -> C."""
+    pa, ra, ca, lda = _colmajor(A, "A")
+    pb, rb, cb, ldb = _colmajor(B, "B")
+    pc, m, n, ldc = _colmajor(C, "C")
+    k = ca if transa in ('N', 'n') else ra
+    check(lib().dg_gemm(ch(transa), ch(transb), m, n, k, float(alpha), pa, lda, pb, ldb,
+                        float(beta), pc, ldc, _stream(stream)))
+    return C
+
+
+def trsv_(uplo, trans, diag, A, x, stream=None):
+    """BLAS.trsv!(uplo, trans, diag, A, x) -> x."""
+    pa, n, _, lda = _colmajor(A, "A")
+    px, _, _, _ = _colmajor(x, "x")
+    check(lib().dg_trsv(ch(uplo), ch(trans), ch(diag), n, pa, lda, px, _stream(stream)))
+    return x
+
+
+def gemv_(trans, alpha, A, x, beta, y, stream=None):
+    """BLAS.gemv!(trans, alpha, A, x, beta, y) -> y."""
+    pa, m, n, lda = _colmajor(A, "A")
+    px, _, _, _ = _colmajor(x, "x")
+    py, _, _, _ = _colmajor(y, "y")
+    check(lib().dg_gemv(ch(trans), m, n, float(alpha), pa, lda, px, float(beta), py,
+                        _stream(stream)))
+    return y
+
+
+# ---------------------------------------------------------------------------
+# whole-array calls
+# ---------------------------------------------------------------------------
+
+class Cholesky:
+    """LinearAlgebra.Cholesky{T,<:DMatrix}: the factor tiles and uplo."""
+
+    def __init__(self, factors: DArray, uplo: str, info: int):
+        self.factors = factors
+        self.uplo = uplo
+        self.info = info
+
+    @property
+    def U(self) -> torch.Tensor:
+        F = self.factors.collect()
+        return torch.triu(F) if self.uplo == 'U' else torch.triu(F.T)
+
+    @property
+    def L(self) -> torch.Tensor:
+        F = self.factors.collect()
+        return torch.tril(F) if self.uplo == 'L' else torch.tril(F.T)
+
+    def issuccess(self) -> bool:
+        return self.info == 0
+
+
+def _square_blocks(A: DArray):
+    if A.ndim != 2 or A.shape[0] != A.shape[1]:
+        raise ValueError(f"matrix is not square: dimensions are {A.shape}")  # checksquare
+    mb, nb = A.partitioning.blocksize
+    if mb != nb:
+        # maybe_copy_buffered(A => Blocks(min_bs, min_bs)) (copy.jl:3-10)
+        raise ValueError("non-square Blocks are re-blocked by the caller: use Blocks(nb, nb)")
+    return nb
+
+
+def cholesky_(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Cholesky:
+    """cholesky!(DA): in-place tiled factorization (_chol!, cholesky.jl:19-108)."""
+    if uplo not in ('U', 'L'):
+        raise ValueError("uplo must be 'U' or 'L'")
+    nb = _square_blocks(A)
+    rc = lib().dg_cholesky_tiled(ch(uplo), A.shape[0], nb, A.tile_ptrs(), _stream(stream))
+    if rc < 0:
+        check(rc)
+    if rc > 0 and check_:
+        raise PosDefException(rc)
+    return Cholesky(A, uplo, rc)
+
+
+def cholesky(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Cholesky:
+    """cholesky(DA): cholcopy (cholesky.jl:1) then cholesky!."""
+    return cholesky_(A.copy(), uplo, check_, stream)
+
+
+def ldiv_(C: Cholesky, B: DArray, stream=None) -> DArray:
+    """ldiv!(C, B): B <- A^-1 B with A = U'U or LL' (linalg.jl:352-405).
+
+    B is an N-vector or an N x r matrix; its row blocking must equal the
+    factor's block size (ldiv! re-blocks B to Blocks(min_bsa, min_bsa),
+    linalg.jl:362-364)."""
+    F = C.factors
+    nb = F.partitioning.blocksize[0]
+    if B.shape[0] != F.shape[0]:
+        raise ValueError("dimension mismatch")
+    if B.partitioning.blocksize[0] != nb or (B.ndim == 2 and B.partitioning.blocksize[1] != nb):
+        raise ValueError("B must be blocked Blocks(nb, nb) (or Blocks(nb)) like the factor")
+    nrhs = 1 if B.ndim == 1 else B.shape[1]
+    rc = lib().dg_cholesky_solve_tiled(ch(C.uplo), F.shape[0], nb, F.tile_ptrs(), nrhs,
+                                       B.tile_ptrs(), _stream(stream))
+    check(rc)
+    return B
+
+
+def _herm_pairs(A: DArray):
+    nb = _square_blocks(A)
+    return nb
+
+
+def ishermitian(A: DArray, stream=None) -> bool:
+    """ishermitian(::DArray) (linalg.jl:90-124): diagonal tiles exactly
+    symmetric; off-diagonal pairs within sqrt(eps) in Frobenius norm."""
+    if A.ndim != 2 or A.shape[0] != A.shape[1]:
+        return False
+    nb = _square_blocks(A)
+    rc = lib().dg_ishermitian_tiled(A.shape[0], nb, A.tile_ptrs(), _stream(stream))
+    if rc < 0:
+        check(rc)
+    return rc == 1
+
+
+issymmetric = ishermitian  # real FP64: the two checks coincide (linalg.jl:55-89)

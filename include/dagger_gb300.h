@@ -1,0 +1,188 @@
+/*
+ * libdaggergb300 — C ABI of the GB300-native tiled Cholesky factor-and-solve.
+ *
+ * This is the boundary a Dagger.jl backend binds with `ccall`.  Every entry
+ * point replaces one call the reference makes on its CUDA path, or hands the
+ * whole datadeps region of one such call to the library.  Conventions:
+ *   - matrices are column-major FP64 (or the stated type) with an explicit
+ *     leading dimension, exactly the LAPACK/BLAS argument conventions;
+ *   - pointers are device pointers unless the name says host;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default
+ *     stream), so the header needs no CUDA include;
+ *   - the return value is a status: 0 = success, > 0 = LAPACK info (the
+ *     1-based order of the first leading minor that is not positive definite),
+ *     -i = argument i is invalid, <= -1000 = one of the DG_ERR_* codes below.
+ *     dg_last_error() returns a message for the last failure on this thread.
+ * Entry points are safe to call from several host threads at once when each
+ * thread uses its own stream (the reference runs each task on its own Julia
+ * task, ext/CUDAExt.jl:309-327).
+ *
+ * Reference paths are within JuliaParallel/Dagger.jl v0.22.0.
+ */
+#ifndef DAGGER_GB300_H
+#define DAGGER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DG_OK 0
+#define DG_ERR_CUDA (-1000)        /* a CUDA runtime call failed              */
+#define DG_ERR_TIMEOUT (-1001)     /* a bounded device wait gave up           */
+#define DG_ERR_NOMEM (-1002)       /* allocation refused / budget exceeded    */
+#define DG_ERR_UNSUPPORTED (-1003) /* option not supported by this build      */
+#define DG_ERR_NOCONVERGE (-1004)  /* iterative refinement did not converge   */
+#define DG_ERR_STATE (-1005)       /* handle used in the wrong state          */
+
+/* ---------------------------------------------------------------------------
+ * Library state
+ * ------------------------------------------------------------------------- */
+
+/* Version string of this build. */
+const char *dg_version(void);
+
+/* Message describing the last failure on the calling thread ("" if none). */
+const char *dg_last_error(void);
+
+/* Number of kernels this process has launched through the library so far
+ * (a graph launch counts every kernel node it contains). */
+long long dg_kernel_launches(void);
+
+/* Frees library-owned workspaces and cached graphs of the current device.
+ * Caller memory is never freed by the library. */
+int dg_finalize(void);
+
+/* ---------------------------------------------------------------------------
+ * Tile operations: the BLAS/LAPACK calls the reference substitutes with
+ * CUBLAS/CUSOLVER through Dagger.move(::CPUProc, ::CuArrayDeviceProc,
+ * ::typeof(fn)) (ext/CUDAExt.jl:329-348).  Same arguments, same meaning.
+ * ------------------------------------------------------------------------- */
+
+/* LAPACK.potrf!(uplo, A) -> (A, info): Cholesky of one tile, in place.
+ * Replaces the call in potrf_checked! (src/array/cholesky.jl:3).  When
+ * info_host is non-NULL the call synchronises `stream` and stores info there
+ * (the reference's potrf! returns info to the host); the return value is then
+ * that info.  When NULL the call is asynchronous and info is not reported;
+ * use dg_potrf_async with a device word of the caller's to read it later. */
+int dg_potrf(char uplo, int n, double *A, int lda, int *info_host, void *stream);
+
+/* Asynchronous form: info (0 or the failing pivot) is written to the device
+ * int info_dev, which must be zero on entry. */
+int dg_potrf_async(char uplo, int n, double *A, int lda, int *info_dev, void *stream);
+
+/* BLAS.trsm!(side, uplo, transa, diag, alpha, A, B): B <- alpha op(A)^-1 B
+ * ('L') or alpha B op(A)^-1 ('R').  Replaces src/array/cholesky.jl:41,86 and
+ * src/array/trsm.jl:95-183. */
+int dg_trsm(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+            const double *A, int lda, double *B, int ldb, void *stream);
+
+/* BLAS.syrk!(uplo, trans, alpha, A, beta, C): C <- alpha A'A + beta C
+ * (trans 'T') or alpha AA' + beta C ('N'), one triangle of C.  Replaces
+ * src/array/cholesky.jl:47,92. */
+int dg_syrk(char uplo, char trans, int n, int k, double alpha, const double *A, int lda,
+            double beta, double *C, int ldc, void *stream);
+
+/* BLAS.gemm!(tA, tB, alpha, A, B, beta, C): C <- alpha op(A) op(B) + beta C.
+ * Replaces src/array/cholesky.jl:50,95 and src/array/trsm.jl:99-183. */
+int dg_gemm(char transa, char transb, int m, int n, int k, double alpha, const double *A,
+            int lda, const double *B, int ldb, double beta, double *C, int ldc, void *stream);
+
+/* BLAS.trsv!(uplo, trans, diag, A, x) and BLAS.gemv!(trans, alpha, A, x,
+ * beta, y): the vector-RHS tile calls of src/array/trsm.jl:21-49. */
+int dg_trsv(char uplo, char trans, char diag, int n, const double *A, int lda, double *x,
+            void *stream);
+int dg_gemv(char trans, int m, int n, double alpha, const double *A, int lda,
+            const double *x, double beta, double *y, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Datadeps regions: the library-side form of Dagger.spawn_datadeps
+ * (src/datadeps/queue.jl:64-106).  Tasks are recorded in submission order with
+ * the BLAS arguments above; each matrix argument carries its access mode
+ * (In / Out / InOut, src/datadeps/aliasing.jl:165-181) and the library derives
+ * the dependencies with the datadeps rules (a writer waits for the last
+ * writer and the readers since; a reader waits for the last writer; overlap
+ * is decided on the strided byte footprint of each argument).  dg_region_run
+ * issues the DAG onto a pool of CUDA streams joined by events, captured into
+ * a CUDA graph that is cached and replayed when the same region (same tasks,
+ * same pointers) runs again.
+ * ------------------------------------------------------------------------- */
+
+typedef struct dg_region dg_region;
+
+#define DG_IN 1
+#define DG_OUT 2
+#define DG_INOUT 3
+
+enum dg_op {
+  DG_OP_POTRF = 1, /* a = tile (InOut)                                     */
+  DG_OP_TRSM = 2,  /* a = triangle (In), c = B (InOut)                      */
+  DG_OP_SYRK = 3,  /* a (In), c (InOut)                                     */
+  DG_OP_GEMM = 4,  /* a, b (In), c (InOut)                                  */
+  DG_OP_COPY = 5   /* a (In) copied to c (Out), same shape                  */
+};
+
+typedef struct dg_task {
+  int op;                     /* enum dg_op                                */
+  char side, uplo, transa, transb, diag, trans;
+  int m, n, k;                /* BLAS sizes of the op                      */
+  double alpha, beta;
+  const double *a; int lda;
+  const double *b; int ldb;
+  double *c; int ldc;
+  int mode_a, mode_b, mode_c; /* DG_IN / DG_OUT / DG_INOUT (0 = default)   */
+  int info_offset;            /* POTRF: global row offset of the tile      */
+} dg_task;
+
+dg_region *dg_region_create(void);
+int dg_region_add(dg_region *r, const dg_task *t);
+/* Number of tasks recorded and of dependency edges derived. */
+int dg_region_stats(const dg_region *r, int *ntasks, int *nedges);
+/* Fills preds (size >= nedges) with (task, predecessor) pairs, in order. */
+int dg_region_edges(const dg_region *r, int *pairs, int cap);
+/* Runs the region on `stream` (the graph is launched there, or the streams
+ * are forked from and joined back to it).  use_graph = 0 issues the same
+ * streams and events without capture; serial = 1 issues every task on
+ * `stream` in submission order (for differential tests).  Returns the LAPACK
+ * info of the first failed POTRF (synchronising), or 0. */
+int dg_region_run(dg_region *r, int use_graph, int serial, void *stream);
+void dg_region_destroy(dg_region *r);
+
+/* ---------------------------------------------------------------------------
+ * Whole-call entry points: the datadeps region of one reference call, built
+ * natively with the reference's task loop and run as one cached graph.
+ * `tiles` is the mt x mt column-major grid of tile pointers of a DArray with
+ * Blocks(nb, nb) (DArray.chunks), tile (i, j) = tiles[i + j*mt], each tile
+ * column-major with leading dimension = its row count (min(nb, n - i*nb)).
+ * ------------------------------------------------------------------------- */
+
+/* LinearAlgebra._chol!(A::DArray, UpperTriangular|LowerTriangular)
+ * (src/array/cholesky.jl:19-108).  Returns info (0 on success). */
+int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles, void *stream);
+
+/* ldiv!(C::Cholesky{T,<:DMatrix}, B) (src/array/linalg.jl:352-405) with the
+ * factor's tiles and B (n x nrhs) blocked Blocks(nb, nb): btiles is the
+ * bmt x bnt column-major grid, bmt = mt, bnt = ceil(nrhs / nb). */
+int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *tiles, int nrhs,
+                            double *const *btiles, void *stream);
+
+/* ishermitian(::DArray) (src/array/linalg.jl:90-124; pair test
+ * is_cross_hermitian, linalg.jl:43-48) over the same tile grid.  Returns 1
+ * (Hermitian), 0 (not), or a negative status.  Synchronises `stream`. */
+int dg_ishermitian_tiled(int n, int nb, double *const *tiles, void *stream);
+
+/* LAPACK.chkfinite(::DArray) (src/array/linalg.jl:138-148): 1 when every
+ * element is finite, 0 otherwise.  Synchronises `stream`. */
+int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream);
+
+/* Selects the FP64 tile engine: 0 = DFMA register tiles, 1 = DMMA
+ * (mma.sync.m8n8k4.f64).  Returns the previous setting. */
+int dg_set_f64_engine(int engine);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DAGGER_GB300_H */
