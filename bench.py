@@ -1,0 +1,552 @@
+"""Benchmark of the tiled Cholesky factor-and-solve (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the plain FP64 drop-in configuration): N = 32768, Blocks(1024,
+1024), A = Q diag(l) Q' with Q the orthogonal factor of the QR of a seeded
+Gaussian N x N matrix and l log-spaced on [1, 1e4], 64 right-hand sides
+N(0, 1).  One step = cholesky(DA) (cholcopy + tiled factor) + ldiv!(C, DB)
+on a fresh copy of B: N^3/3 + 2 N^2 r flops.  Inputs are 8.6 GB, far larger
+than the 129 MB L2, so no flush is needed between steps.
+
+Reported:
+  value        FP64 factor+solve TFLOP/s over the timed steps, inputs resident
+               in HBM (CUDA events on the launching stream, max over ranks)
+  e2e          the same through the public API from pinned host buffers:
+               host->device copy of A and B and device->host copy of X inside
+               every timed step
+  solves_per_s right-hand sides solved per second (factor included)
+  roofline     the dominant kernel (the FP64 tile GEMM of the trailing
+               update, 2 nb^3 flops per launch) timed alone with CUDA events,
+               against the FP64 FMA throughput measured in the same run
+  cpu_baseline the oracle's threaded C restatement of the reference's
+               datadeps Cholesky (OpenBLAS tiles) on the host cores, on a
+               bounded sample (N = 16384, same tiling and RHS count)
+  accuracy     normwise backward error of every RHS (inf-norms) and a
+               probed ||A - U'U|| / ||A|| for the factor
+
+`--impl reference` times only the CPU baseline (the reference's algorithm
+restated in C, run with all host threads) on the same metric.
+Multi-GPU: the path does not shard (one factorization per GPU), so N GPUs
+run N independent replicas; value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "dagger.jl_gb300"))
+
+METRIC = "Cholesky+solve TFLOP/s & solves/s, FP64 vs BF16+IR at 1e-12; serving p50/p99 ms"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=32768)
+    ap.add_argument("--nb", type=int, default=1024)
+    ap.add_argument("--nrhs", type=int, default=64)
+    ap.add_argument("--cond", type=float, default=1e4)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-n", type=int, default=16384)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--mixed-precision", default="auto")
+    ap.add_argument("--batch-count", type=int, default=10000)
+    ap.add_argument("--spd", default="spectrum", choices=["spectrum", "uniform"],
+                    help="input construction; 'uniform' (B B'/N + N I, matmul only) is for "
+                         "profilers that cannot load the QR's solver library")
+    return ap.parse_args()
+
+
+def flops(n, r):
+    return n ** 3 / 3.0 + 2.0 * n * n * r
+
+
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
+
+def make_spd_spectrum_gpu(n, cond, seed, device):
+    """A = Q diag(l) Q' (FP64), Q from the QR of a seeded N x N Gaussian.
+
+    The QR and the product run in FP32 (TF32 off) and the result is widened
+    to FP64 and symmetrised: A is exactly symmetric and its eigenvalues are l
+    up to FP32 rounding (|dl| ~ 1e-7 ||A|| sqrt(N)), so kappa(A) = cond to
+    about a percent at cond = 1e4."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    G = torch.randn(n, n, generator=g, device=device, dtype=torch.float32)
+    Q, _ = torch.linalg.qr(G)
+    del G
+    lam = torch.logspace(0.0, math.log10(cond), n, device=device, dtype=torch.float32)
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    A32 = (Q * lam) @ Q.T
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del Q
+    A = A32.double()
+    del A32
+    A += A.T.clone()
+    A *= 0.5
+    return A
+
+
+def make_spd_uniform_gpu(n, seed, device):
+    """A = B B'/n + n I with B i.i.d. uniform[-1, 1] (FP64)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    Bm = torch.rand(n, n, generator=g, device=device, dtype=torch.float64) * 2 - 1
+    A = Bm @ Bm.T / n
+    del Bm
+    A.diagonal().add_(n)
+    return A
+
+
+def make_rhs_gpu(n, r, seed, device):
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed + 1)
+    return torch.randn(n, r, generator=g, device=device, dtype=torch.float64)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="dg_clocks_", suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's threaded C restatement (OpenBLAS tiles)
+# ---------------------------------------------------------------------------
+
+def cpu_baseline(n, nb, r, A_host=None, B_host=None, reps=1):
+    import numpy as np
+    from oracle import native
+    native.set_blas_threads(1)
+    cores = os.cpu_count() or 1
+    if A_host is None:
+        from oracle import tiled as o
+        A_host = o.spd_uniform(n, 1)
+        B_host = o.rhs_normal(n, r, 1)
+    best = None
+    for _ in range(reps):
+        F = np.array(A_host, order='F', copy=True)
+        X = np.array(B_host, order='F', copy=True)
+        t0 = time.perf_counter()
+        F, info = native.chol_tiled(F, nb, 'U', nthreads=cores, inplace=True)
+        native.ldiv_tiled(F, 'U', X, nb, nthreads=cores)
+        dt = time.perf_counter() - t0
+        assert info == 0
+        best = dt if best is None else min(best, dt)
+    return {"value": flops(n, r) / best / 1e12, "unit": "TFLOP/s", "cores": cores,
+            "kind": "port",
+            "sample": f"CPU restatement of the Dagger datadeps Cholesky + ldiv! (OpenBLAS "
+                      f"single-thread tiles, {cores} worker threads): N={n}, Blocks({nb},{nb}), "
+                      f"{r} RHS, A = Q diag(logspace(0,4)) Q'; {best:.2f} s per factor+solve"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path, all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    n, nb, r = args.cpu_n, args.nb, args.nrhs
+    A, B = _cpu_sample_inputs(n, r, args.cond, args.seed)
+    from oracle import native
+    native.set_blas_threads(1)
+    cores = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        F = np.array(A, order='F', copy=True)
+        X = np.array(B, order='F', copy=True)
+        t0 = time.perf_counter()
+        F, info = native.chol_tiled(F, nb, 'U', nthreads=cores, inplace=True)
+        native.ldiv_tiled(F, 'U', X, nb, nthreads=cores)
+        dt = time.perf_counter() - t0
+        assert info == 0
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = flops(n, r) * len(times) / total / 1e12
+    sample = (f"CPU restatement of the Dagger datadeps Cholesky + ldiv! (OpenBLAS single-thread "
+              f"tiles, {cores} worker threads), N={n}, Blocks({nb},{nb}), {r} RHS per step")
+    out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "impl": "reference",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"tiled Cholesky + solve FP64, N={n} (CPU-bounded sample of "
+                                  f"N={args.n}), Blocks({nb},{nb}), {r} RHS, kappa={args.cond:g}",
+                      "n": n, "nb": nb, "nrhs": r},
+           "solves_per_s": r * len(times) / total,
+           "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def _cpu_sample_inputs(n, r, cond, seed):
+    """Same construction as the GPU workload, at the CPU sample size: built on
+    the GPU when one is present (fast), else with numpy."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            A = make_spd_spectrum_gpu(n, cond, seed, torch.device("cuda"))
+            B = make_rhs_gpu(n, r, seed, torch.device("cuda"))
+            import numpy as np
+            An = np.asfortranarray(A.cpu().numpy())
+            Bn = np.asfortranarray(B.cpu().numpy())
+            del A, B
+            torch.cuda.empty_cache()
+            return An, Bn
+    except Exception:
+        pass
+    from oracle import tiled as o
+    return o.spd_spectrum(n, cond, seed), o.rhs_normal(n, r, seed)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import dagger_gb300 as d
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    L = d.lib()
+    n, nb, r = args.n, args.nb, args.nrhs
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+
+    if args.spd == "spectrum":
+        A = make_spd_spectrum_gpu(n, args.cond, args.seed + rank, dev)
+    else:
+        A = make_spd_uniform_gpu(n, args.seed + rank, dev)
+    B = make_rhs_gpu(n, r, args.seed + rank, dev)
+    part = d.Blocks(nb, nb)
+    DA = d.DArray.from_array(A, part)
+    DB0 = d.DArray.from_array(B, part)
+    W = d.DArray(DA.shape, part, device=dev)
+    DBw = d.DArray(DB0.shape, part, device=dev)
+
+    def step():
+        W.storage.copy_(DA.storage)                # cholcopy
+        C = d.cholesky_(W, 'U', stream=stream)
+        DBw.storage.copy_(DB0.storage)
+        d.ldiv_(C, DBw, stream=stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = L.dg_kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    launches = L.dg_kernel_launches() - l0
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = flops(n, r) * args.steps * world / t / 1e12
+
+    # accuracy of the last step (not timed)
+    X = DBw.collect()
+    R = B - A @ X
+    nA = A.abs().sum(dim=1).max()
+    berr = (R.abs().amax(dim=0) / (nA * X.abs().amax(dim=0) + B.abs().amax(dim=0)))
+    U = torch.triu(W.collect())
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    V = torch.randn(n, 4, device=dev, dtype=torch.float64, generator=gen)
+    fres = float(((A @ V - U.T @ (U @ V)).norm() / (A @ V).norm()).item())
+    del U, R, X
+
+    # e2e through the public API from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        A_h = A.cpu().pin_memory()
+        B_h = B.cpu().pin_memory()
+        X_h = torch.empty(n, r, dtype=torch.float64).pin_memory()
+
+        DAh = d.DArray(DA.shape, part, device=dev)
+        DBh = d.DArray(DB0.shape, part, device=dev)
+
+        def e2e_step():
+            DAh.copy_from(A_h)                         # host -> device + tiling
+            C = d.cholesky_(DAh, 'U', stream=stream)
+            DBh.copy_from(B_h)
+            d.ldiv_(C, DBh, stream=stream)
+            X_h.copy_(DBh.collect(), non_blocking=True)
+
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        f1.record(stream)
+        barrier()
+        te = f0.elapsed_time(f1) / 1e3
+        del DAh, DBh
+        if world > 1:
+            tt = torch.tensor([te], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": flops(n, r) * args.steps * world / te / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": 8 * n * n + 8 * n * r, "d2h_bytes_per_step": 8 * n * r,
+               "ms_per_step": 1e3 * te / args.steps}
+        del A_h, B_h, X_h
+
+    # roofline of the dominant kernel: the FP64 tile GEMM (2 nb^3 flops per launch)
+    Ta = torch.randn(nb, nb, dtype=torch.float64, device=dev)
+    Tb = torch.randn(nb, nb, dtype=torch.float64, device=dev)
+    Tc = torch.randn(nb, nb, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        L.dg_gemm(b'T', b'N', nb, nb, nb, -1.0, Ta.data_ptr(), nb, Tb.data_ptr(), nb, 1.0,
+                  Tc.data_ptr(), nb, s)
+    reps = 20
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(reps):
+        L.dg_gemm(b'T', b'N', nb, nb, nb, -1.0, Ta.data_ptr(), nb, Tb.data_ptr(), nb, 1.0,
+                  Tc.data_ptr(), nb, s)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    tg = g0.elapsed_time(g1) / 1e3 / reps
+    import ctypes
+    pk = ctypes.c_double(0)
+    L.dg_probe_fp64_fma_tflops(20000, ctypes.byref(pk), s)
+    achieved = 2.0 * nb ** 3 / tg / 1e12
+    roof = {"bound": "tensor", "kernel": "gemm_f64_dfma (trailing-update tile GEMM)",
+            "achieved": achieved, "peak": pk.value, "unit": "TFLOP/s",
+            "frac": achieved / pk.value,
+            "peak_source": "FP64 FMA throughput measured in this run (no FP64 figure in the "
+                           "measured-peaks record)",
+            "per_launch": f"2*{nb}^3 flops, {1e6 * tg:.0f} us", "traffic": None}
+
+    del Ta, Tb, Tc
+    mixed = None
+    if not args.no_mixed:
+        del W, DBw
+        torch.cuda.empty_cache()
+        mixed = bench_mixed(args, d, DA, A, B, stream, world)
+    batched = None
+    if not args.no_batched:
+        batched = bench_batched(args, d, dev, rank)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        An, Bn = _cpu_sample_inputs(args.cpu_n, r, args.cond, args.seed)
+        cpu = cpu_baseline(args.cpu_n, nb, r, An, Bn)
+
+    out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded Gaussian QR; no dataset)",
+           "config": {"workload": f"plain FP64 tiled Cholesky + solve, N={n}, Blocks({nb},{nb}), "
+                                  f"{r} RHS, A = Q diag(logspace(0,{math.log10(args.cond):g})) Q'",
+                      "n": n, "nb": nb, "nrhs": r, "cond": args.cond,
+                      "l2": "inputs 8 N^2 bytes >> 129 MB L2 (no flush needed)",
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "solves_per_s": r * args.steps * world / t,
+           "accuracy": {"backward_error_max": float(berr.max().item()),
+                        "factor_residual_probe": fres},
+           "roofline": roof, "gpu_launches": int(launches),
+           "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
+           "mixed": mixed, "batched": batched}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def choose_precision(cond):
+    """Operand precision of the mixed form by conditioning: BF16 hi/lo split up
+    to 1e6, FP32 updates beyond (the factor must stay usable as a
+    preconditioner for GMRES-IR)."""
+    return "bf16x3" if cond <= 1e6 else "fp32"
+
+
+def bench_mixed(args, d, DA, A, B, stream, world):
+    """Mixed-precision factor + refined solve of the same system and RHS:
+    TFLOP/s counted with the same algorithmic flops as the FP64 form."""
+    import torch
+    import torch.distributed as dist
+    n, r = args.n, args.nrhs
+    prec = args.mixed_precision if args.mixed_precision != "auto" else choose_precision(args.cond)
+    X = torch.empty((r, n), dtype=torch.float64, device=A.device).t()
+    Bc = B.t().contiguous().t()
+    reports = []
+
+    def step():
+        F = d.cholesky_mixed(DA, prec, stream=stream)
+        _, rep = F.solve(Bc, tol=1e-12, out=X)
+        st = F.stats()
+        F.close()
+        reports.append((rep, st))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=A.device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    R = B - A @ X
+    nA = A.abs().sum(dim=1).max()
+    berr = (R.abs().amax(dim=0) / (nA * X.abs().amax(dim=0) + B.abs().amax(dim=0)))
+    rep, st = reports[-1]
+    return {"precision": prec, "value": flops(n, r) * args.steps * world / t / 1e12,
+            "unit": "TFLOP/s", "ms_per_step": 1e3 * t / args.steps,
+            "solves_per_s": r * args.steps * world / t,
+            "factor_ms": st["factor_ms"], "refine_ms": rep["solve_ms"],
+            "ir_iterations": rep["iterations"], "gmres_iterations": rep["gmres_iterations"],
+            "fp64_retries": st["retries"],
+            "backward_error_max": float(berr.max().item()),
+            "backward_error_target": 1e-12}
+
+
+def bench_batched(args, d, dev, rank):
+    """10,000 SPD systems, n log-uniform on [32, 1024], 1-8 RHS each, A = B B'/n
+    + n I: FP64 and FP32+IR, each in one persistent launch."""
+    import torch
+    from dagger_gb300.autotune import sample_batch
+    from dagger_gb300.batched import PackedBatch, batched_solve_packed
+    from dagger_gb300.batched import flops as bflops
+    As, Bs = sample_batch(args.batch_count, 32, 1024, seed=args.seed + rank, device=dev)
+    ns = [a.shape[0] for a in As]
+    rs = [b.shape[1] for b in Bs]
+    P = PackedBatch(As, Bs)
+    del As, Bs
+    out = {"systems": len(ns), "n_range": [min(ns), max(ns)]}
+    for mode in ("fp64", "fp32_ir"):
+        reps = []
+        for _ in range(2):
+            if mode == "fp64":
+                P.load_again()
+            reps.append(batched_solve_packed(P, mode))
+        rep = min(reps, key=lambda x: x["elapsed_ms"])
+        t = rep["elapsed_ms"] / 1e3
+        entry = {"ms": rep["elapsed_ms"], "TFLOP_s": bflops(ns, rs) / t / 1e12,
+                 "systems_per_s": len(ns) / t, "failed": rep["failed"],
+                 "widths": rep["widths"], "ctas_per_sm": rep["ctas_per_sm"]}
+        if mode == "fp32_ir":
+            entry["backward_error_max"] = max(rep["backward_error"])
+            entry["ir_iterations_max"] = max(rep["iterations"])
+        out[mode] = entry
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -6,7 +6,7 @@ Each CUDA translation unit under csrc/ is compiled in parallel to
 _build/*.o (only when its sources changed), then linked into
 dagger_gb300/libdaggergb300.so next to the Python host package that loads it.
 No cmake, no torch extension machinery: the library has a plain C ABI
-(include/dagger_gb300.h) and links only the CUDA runtime and driver.
+(include/dagger_gb300.h) and links only the CUDA runtime.
 """
 from __future__ import annotations
 
@@ -67,7 +67,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
     newest = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(OUT) or os.path.getmtime(OUT) < newest:
         tmp = OUT + f".tmp{os.getpid()}"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda", "-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <string.h>
 
 #include "../../include/dagger_gb300.h"
 
@@ -26,39 +27,69 @@
     }                                                                           \
   } while (0)
 
+#define DG_TRY(expr)          \
+  do {                        \
+    int _rc = (expr);         \
+    if (_rc) return _rc;      \
+  } while (0)
+
 void dg_set_last_error(const char *file, int line, const char *msg);
 
 // Number of SMs of the current device (cached per device).
 int dg_num_sms();
 
+// Kernels of one factorization skip their work when either of two device
+// "abort" words is non-zero on entry (a failed pivot or a failed step).
+__device__ __forceinline__ bool aborted(const int *a, const int *b) {
+  return (a && *(volatile const int *)a) || (b && *(volatile const int *)b);
+}
+
 // ---------------------------------------------------------------------------
-// Internal host entry points shared between translation units.  They take a
-// device "abort" word: when non-null and non-zero when a kernel starts, the
-// kernel returns immediately.  The factorization sets it to the LAPACK info
-// of the first failing pivot, so later tile tasks of the same factorization
-// stop instead of computing on a matrix that is not positive definite.
+// Internal host entry points shared between translation units.
 // ---------------------------------------------------------------------------
 namespace dg {
 
 enum Tri { TRI_NONE = 0, TRI_UPPER = 1, TRI_LOWER = 2 };
 
-// C = alpha * op(A) * op(B) + beta * C, FP64, column-major.  tri restricts the
+// C = alpha * op(A) * op(B) + beta * C, column-major.  tri restricts the
 // update (and the stores) to the upper or lower triangle of C (SYRK).
 int gemm_f64(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
              const double *B, int ldb, double beta, double *C, int ldc, Tri tri,
-             const int *abort_flag, cudaStream_t s);
+             const int *abort_flag, cudaStream_t s, const int *abort2 = nullptr);
+int gemm_f32(char ta, char tb, int m, int n, int k, float alpha, const float *A, long long lda,
+             const float *B, long long ldb, float beta, float *C, long long ldc, Tri tri,
+             const int *abort_flag, cudaStream_t s, const int *abort2 = nullptr);
+
+// C = alpha * A * X + beta * C with A the n x n tile grid of a DArray
+// (Blocks(nb, nb)) given as a DEVICE array of tile pointers, tile (i, j) =
+// tiles_dev[i + j*mt], column-major with ld = its row count.
+int gemm_tiles_f64(int n, int nb, int nrhs, double alpha, const double *const *tiles_dev,
+                   const double *X, long long ldx, double beta, double *C, long long ldc,
+                   const int *abort_flag, cudaStream_t s);
+int gemm_tiles_f32(int n, int nb, int nrhs, float alpha, const float *const *tiles_dev,
+                   const float *X, long long ldx, float beta, float *C, long long ldc,
+                   const int *abort_flag, cudaStream_t s);
 
 int trsm_f64(char side, char uplo, char transa, char diag, int m, int n, double alpha,
              const double *A, int lda, double *B, int ldb, const int *abort_flag,
-             cudaStream_t s);
+             cudaStream_t s, const int *abort2 = nullptr);
+int trsm_f32(char side, char uplo, char transa, char diag, int m, int n, float alpha,
+             const float *A, long long lda, float *B, long long ldb, const int *abort_flag,
+             cudaStream_t s, const int *abort2 = nullptr);
 
-// info_dev: device int receiving the LAPACK info (offset + local pivot index,
-// written once, by the first failure).  It doubles as the abort word.
-int potrf_f64(char uplo, int n, double *A, int lda, int *info_dev, int info_offset,
-              cudaStream_t s);
+// Cholesky of one tile.  info_out receives offset + local pivot index of
+// the first failure (written once); kernels skip when info_out, abort_flag
+// or abort2 is already non-zero.  The plain FP64 path passes its info word
+// as both info_out and abort word.
+int potrf_f64(char uplo, int n, double *A, int lda, int *info_out, int info_offset,
+              cudaStream_t s, const int *abort_flag = nullptr, const int *abort2 = nullptr);
+int potrf_f32(char uplo, int n, float *A, long long lda, int *info_out, int info_offset,
+              cudaStream_t s, const int *abort_flag = nullptr, const int *abort2 = nullptr);
 
 int scale_f64(int m, int n, double alpha, double *B, int ldb, const int *abort_flag,
-              cudaStream_t s);
+              cudaStream_t s, const int *abort2 = nullptr);
+int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abort_flag,
+              cudaStream_t s, const int *abort2 = nullptr);
 
 // Kernel launch accounting: every kernel launch site adds to a process-wide
 // counter (graph captures move their launches into the graph's count, which

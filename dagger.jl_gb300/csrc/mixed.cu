@@ -1,0 +1,780 @@
+// Mixed-precision Cholesky factor-and-solve with iterative refinement.
+//
+// The plain FP64 path (runtime.cu) is the drop-in for Dagger.jl's DArray
+// Cholesky; this file is the faster form beside it.  Given the caller's FP64
+// tiles of A it computes, on the GPU:
+//
+//   1. Scaling: s_i = 1/sqrt(a_ii), A~ = S A S (unit diagonal, so every entry
+//      of its Cholesky factor has magnitude <= 1), rounded to FP32 and packed
+//      into upper row panels: panel r holds rows r*nb .. r*nb+nb-1, columns
+//      r*nb .. n-1, column-major with leading dimension nb (about n^2/2 floats).
+//   2. A right-looking blocked factorization over the panels.  Step k:
+//        POTRF of the nb x nb diagonal block in FP32; if a pivot fails, the
+//        block (kept from before the attempt) is widened to FP64 and factored
+//        again by a one-CTA FP64 kernel, which only runs on failure;
+//        TRSM of the rest of panel k in FP32;
+//        conversion of that panel to 16-bit operands: BF16 or FP16, one term
+//        or hi/lo split (x = hi + lo), FP16 with a per-panel power-of-two
+//        scale chosen from the panel's largest entry (FP16's range is narrow);
+//        the trailing update A~[k+1:, k+1:] -= P' P of the upper triangle in
+//        one tcgen05 launch (tc_gemm.cu), FP32 accumulation in TMEM, or on
+//        the FP32 CUDA-core GEMM for the FP32 precision setting.
+//   3. Refinement in FP64: r = b - A x with the caller's FP64 tiles, the
+//      correction from the low-precision factor (FP32 triangular solves on the
+//      packed panels), x += S z.  The normwise backward error of each column,
+//      ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf), decides convergence.
+//      When plain refinement stalls, GMRES-IR takes over: restarted GMRES on
+//      the correction equation, left-preconditioned by the low-precision
+//      factor, with FP64 Krylov vectors and FP64 matrix-vector products.
+// Only the residual, the solution update, the POTRF retry and GMRES's
+// vectors run in FP64.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "dg_common.cuh"
+#include "runtime.h"
+#include "tc_gemm.h"
+
+struct dg_mixed {
+  int n = 0, nb = 0, mt = 0, precision = 0;
+  int dev = 0;
+  float *W = nullptr;            // packed upper panels of the scaled factor
+  double *s = nullptr;           // diagonal scaling
+  double **tiles_dev = nullptr;  // caller's FP64 tiles (device array of pointers)
+  void *P_hi = nullptr, *P_lo = nullptr;  // 16-bit panel operands (T x nb, K-major)
+  float *diag_backup = nullptr;  // diagonal block before its FP32 POTRF
+  double *d64 = nullptr;         // FP64 scratch of the retry
+  float *panel_max = nullptr;    // per-step |panel| maximum (FP16 scaling)
+  float *alpha_dev = nullptr;    // per-step -1/scale^2 of the trailing update
+  int *words = nullptr;          // [0] status, [1] retries, [2] first bad diagonal, [3..] info_k
+  double normA = 0.0;            // ||A||_inf
+  size_t bytes = 0;
+  int info = 0, retries = 0;
+  float factor_ms = 0.f;
+};
+
+namespace dg {
+namespace {
+
+__device__ __forceinline__ const double *tile_ptr(const double *const *tiles, int mt, int i, int j) {
+  return tiles[i + (size_t)j * mt];
+}
+
+// s_i = 1 / sqrt(a_ii); the first non-positive diagonal is recorded (atomicMin).
+__global__ void diag_scale_kernel(const double *const *tiles, int n, int nb, int mt, double *s,
+                                  int *bad) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int t = i / nb, p = i - t * nb;
+    const int rows = min(nb, n - t * nb);
+    const double a = tile_ptr(tiles, mt, t, t)[p + (size_t)p * rows];
+    if (!(a > 0.0)) {
+      atomicMin(bad, i + 1);
+      s[i] = 1.0;
+    } else {
+      s[i] = 1.0 / sqrt(a);
+    }
+  }
+}
+
+// Row sums of |A| over the tile grid (for ||A||_inf).
+__global__ void row_abs_sum_kernel(const double *const *tiles, int n, int nb, int mt, double *out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int t = i / nb, p = i - t * nb;
+    const int rows = min(nb, n - t * nb);
+    double acc = 0.0;
+    for (int tj = 0; tj < mt; tj++) {
+      const double *a = tile_ptr(tiles, mt, t, tj) + p;
+      const int cols = min(nb, n - tj * nb);
+      for (int c = 0; c < cols; c++) acc += fabs(a[(size_t)c * rows]);
+    }
+    out[i] = acc;
+  }
+}
+
+__host__ __device__ inline long long panel_base(long long r, long long n, long long nb) {
+  return nb * (r * n - nb * r * (r - 1) / 2);
+}
+
+// W = float(S A S) on the upper row panels; the strict lower part of each
+// diagonal block and the padding rows of a ragged last panel are zero.
+__global__ void pack_kernel(const double *const *tiles, int n, int nb, int mt, const double *s,
+                            float *W) {
+  const int r = blockIdx.y;
+  const long long w = n - (long long)r * nb;
+  const long long total = (long long)nb * w;
+  float *P = W + panel_base(r, n, nb);
+  const int rows_r = min(nb, n - r * nb);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int p = (int)(e % nb);
+    const long long c = e / nb;
+    const long long i = (long long)r * nb + p, j = (long long)r * nb + c;
+    float v = 0.f;
+    if (p < rows_r && i <= j) {
+      const int tj = (int)(j / nb), cj = (int)(j - (long long)tj * nb);
+      const double a = tile_ptr(tiles, mt, r, tj)[p + (size_t)cj * rows_r];
+      v = (float)(s[i] * a * s[j]);
+    }
+    P[e] = v;
+  }
+}
+
+// FP64 retry of a failed FP32 diagonal-block factorization: one CTA, only
+// when info_k is set.  The block from before the FP32 attempt is widened,
+// factored right-looking in FP64 (lower form, L = U'), narrowed back.
+__global__ void __launch_bounds__(1024) retry_potrf_kernel(int nbk, int ld, const float *backup,
+                                                           double *L, float *diag, int *info_k,
+                                                           int *status, int *retries, int offset) {
+  if (*(volatile int *)info_k == 0 || *(volatile int *)status != 0) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < nbk * nbk; e += nt) {
+    const int j = e % nbk, i = e / nbk;  // read backup(j, i) coalesced along j
+    if (j <= i) L[i + (size_t)j * ld] = (double)backup[j + (size_t)i * ld];
+  }
+  __shared__ int fail;
+  if (tid == 0) fail = -1;
+  __syncthreads();
+  for (int j = 0; j < nbk; j++) {
+    double d = L[j + (size_t)j * ld];
+    if (!(d > 0.0)) {
+      if (tid == 0) fail = j;
+      break;
+    }
+    d = sqrt(d);
+    const double rcp = 1.0 / d;
+    __syncthreads();
+    for (int i = j + 1 + tid; i < nbk; i += nt) L[i + (size_t)j * ld] *= rcp;
+    if (tid == 0) L[j + (size_t)j * ld] = d;
+    __syncthreads();
+    const int w = nbk - j - 1;
+    for (long long e = tid; e < (long long)w * w; e += nt) {
+      const int i = j + 1 + (int)(e % w), k = j + 1 + (int)(e / w);
+      if (k <= i)
+        L[i + (size_t)k * ld] = fma(-L[i + (size_t)j * ld], L[k + (size_t)j * ld], L[i + (size_t)k * ld]);
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (fail >= 0) {
+    if (tid == 0) atomicCAS(status, 0, offset + fail + 1);
+    return;
+  }
+  for (int e = tid; e < nbk * nbk; e += nt) {
+    const int j = e % nbk, i = e / nbk;
+    if (j <= i) diag[j + (size_t)i * ld] = (float)L[i + (size_t)j * ld];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    *info_k = 0;
+    atomicAdd(retries, 1);
+  }
+}
+
+__global__ void absmax_kernel(const float *x, long long n, float *out, const int *a1, const int *a2) {
+  if (aborted(a1, a2)) return;
+  float m = 0.f;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[e]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax((int *)out, __float_as_int(m));  // m >= 0: int order
+}
+
+// Panel -> 16-bit operands.  FP16 panels are scaled by a power of two so the
+// largest entry lands near 2^12; the trailing update's alpha is -1/scale^2.
+template <bool FP16>
+__global__ void convert_kernel(const float *src, long long n, int terms, void *hi_, void *lo_,
+                               const float *pmax, float *alpha_out, const int *a1, const int *a2) {
+  if (aborted(a1, a2)) return;
+  float scale = 1.f;
+  if (FP16) {
+    const float m = *pmax;
+    int e = 0;
+    if (m > 0.f) frexpf(m, &e);  // m in [2^(e-1), 2^e)
+    scale = ldexpf(1.f, 12 - e);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = -1.f / (scale * scale);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float x = src[i] * scale;
+    if (FP16) {
+      const __half h = __float2half_rn(x);
+      ((__half *)hi_)[i] = h;
+      if (terms == 3) ((__half *)lo_)[i] = __float2half_rn(x - __half2float(h));
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      ((__nv_bfloat16 *)hi_)[i] = h;
+      if (terms == 3) ((__nv_bfloat16 *)lo_)[i] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+  }
+}
+
+// Z = float(s .* R) and X += s .* double(Z), column by column.
+__global__ void scale_to_f32_kernel(const double *R, long long ldr, const double *s, float *Z,
+                                    long long ldz, int n, int r) {
+  const long long total = (long long)n * r;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    Z[i + j * ldz] = (float)(s[i] * R[i + j * ldr]);
+  }
+}
+
+__global__ void update_x_kernel(double *X, long long ldx, const double *s, const float *Z,
+                                long long ldz, int n, int r) {
+  const long long total = (long long)n * r;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    X[i + j * ldx] += s[i] * (double)Z[i + j * ldz];
+  }
+}
+
+// out[j] = max_i |M(i, j)| (one CTA per column).
+__global__ void colmax_kernel(const double *M, long long ld, int n, double *out) {
+  const int j = blockIdx.x;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(M[i + j * ld]));
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) out[j] = m;
+  }
+}
+
+int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  long long cap = 8LL * dg_num_sms();
+  return (int)std::max(1LL, std::min(b, cap));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// factorization
+// ---------------------------------------------------------------------------
+int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
+  const int n = f->n, nb = f->nb, mt = f->mt;
+  int *status = f->words, *retries = f->words + 1, *bad = f->words + 2, *info = f->words + 3;
+  DG_CUDA_TRY(cudaMemsetAsync(f->words, 0, sizeof(int) * (3 + mt), s));
+  DG_CUDA_TRY(cudaMemsetAsync(bad, 0x7f, sizeof(int), s));
+  diag_scale_kernel<<<grid_for(n), 256, 0, s>>>(f->tiles_dev, n, nb, mt, f->s, bad);
+  pack_kernel<<<dim3(std::max(1, std::min(1024, (int)((long long)nb * n / 256 + 1))), mt), 256, 0,
+                s>>>(f->tiles_dev, n, nb, mt, f->s, f->W);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(2);
+  const int prec = f->precision;
+  const bool fp16 = (prec == DG_PREC_FP16 || prec == DG_PREC_FP16X3);
+  const int terms = (prec == DG_PREC_BF16X3 || prec == DG_PREC_FP16X3) ? 3 : 1;
+  for (int k = 0; k < mt; k++) {
+    float *Pk = f->W + panel_base(k, n, nb);
+    const int nbk = std::min(nb, n - k * nb);
+    const long long T = (long long)n - (long long)(k + 1) * nb;
+    int *ik = info + k;
+    DG_CUDA_TRY(cudaMemcpyAsync(f->diag_backup, Pk, sizeof(float) * (size_t)nb * nbk,
+                                cudaMemcpyDeviceToDevice, s));
+    DG_TRY(potrf_f32('U', nbk, Pk, nb, ik, k * nb, s, status));
+    retry_potrf_kernel<<<1, 1024, 0, s>>>(nbk, nb, f->diag_backup, f->d64, Pk, ik, status, retries,
+                                          k * nb);
+    DG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    if (T <= 0) break;
+    float *Rk = Pk + (size_t)nb * nb;  // the rest of panel k: nb x T
+    DG_TRY(trsm_f32('L', 'U', 'T', 'N', nbk, (int)T, 1.f, Pk, nb, Rk, nb, ik, s, status));
+    if (prec == DG_PREC_FP32) {
+      // trailing update on the FP32 CUDA-core GEMM, one call per row panel
+      for (int r = k + 1; r < mt; r++) {
+        float *Pr = f->W + panel_base(r, n, nb);
+        const int nbr = std::min(nb, n - r * nb);
+        const long long wr = (long long)n - (long long)r * nb;
+        const float *Ar = Rk + (size_t)(r - k - 1) * nb * nb;  // columns r*nb.. of panel k
+        DG_TRY(gemm_f32('T', 'N', nbr, (int)wr, nbk, -1.f, Ar, nb, Ar, nb, 1.f, Pr, nb,
+                        TRI_UPPER, ik, s, status));
+      }
+      continue;
+    }
+    float *pmax = f->panel_max + k;
+    float *alpha = f->alpha_dev + k;
+    const long long elems = (long long)nb * T;
+    if (fp16) {
+      DG_CUDA_TRY(cudaMemsetAsync(pmax, 0, sizeof(float), s));
+      absmax_kernel<<<grid_for(elems), 256, 0, s>>>(Rk, elems, pmax, ik, status);
+      convert_kernel<true><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, f->P_hi, f->P_lo, pmax,
+                                                           alpha, ik, status);
+      count_launches(2);
+    } else {
+      convert_kernel<false><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, f->P_hi, f->P_lo,
+                                                            nullptr, alpha, ik, status);
+      count_launches(1);
+    }
+    DG_CUDA_TRY(cudaGetLastError());
+    TcGemmArgs g;
+    memset(&g, 0, sizeof g);
+    g.m = (int)T; g.n = (int)T; g.k = nb; g.terms = terms; g.fp16 = fp16;
+    g.a_hi = f->P_hi; g.a_lo = f->P_lo; g.lda = nb; g.a_rows = (int)T;
+    g.b_hi = f->P_hi; g.b_lo = f->P_lo; g.ldb = nb; g.b_rows = (int)T;
+    g.alpha = -1.f; g.alpha_dev = alpha; g.beta = 1.f;
+    g.c = f->W; g.layout = 1; g.upper = 1;
+    g.off = (long long)(k + 1) * nb; g.nb = nb; g.ntot = n;
+    g.bn = 128; g.status = status;
+    DG_TRY(tc_gemm_bf16(g, s));
+  }
+  return 0;
+}
+
+// Solves U~' U~ Z = Z in place (FP32, n x r, column-major ldz) on the packed panels.
+int mixed_tri_solve(const dg_mixed *f, float *Z, long long ldz, int r, cudaStream_t s) {
+  const int n = f->n, nb = f->nb, mt = f->mt;
+  for (int k = 0; k < mt; k++) {  // forward: U' y = z
+    const float *Pk = f->W + panel_base(k, n, nb);
+    const int nbk = std::min(nb, n - k * nb);
+    const long long T = (long long)n - (long long)(k + 1) * nb;
+    DG_TRY(trsm_f32('L', 'U', 'T', 'N', nbk, r, 1.f, Pk, nb, Z + (size_t)k * nb, ldz, nullptr, s));
+    if (T > 0)
+      DG_TRY(gemm_f32('T', 'N', (int)T, r, nbk, -1.f, Pk + (size_t)nb * nb, nb, Z + (size_t)k * nb,
+                      ldz, 1.f, Z + (size_t)(k + 1) * nb, ldz, TRI_NONE, nullptr, s));
+  }
+  for (int k = mt - 1; k >= 0; k--) {  // backward: U x = y
+    const float *Pk = f->W + panel_base(k, n, nb);
+    const int nbk = std::min(nb, n - k * nb);
+    const long long T = (long long)n - (long long)(k + 1) * nb;
+    if (T > 0)
+      DG_TRY(gemm_f32('N', 'N', nbk, r, (int)T, -1.f, Pk + (size_t)nb * nb, nb,
+                      Z + (size_t)(k + 1) * nb, ldz, 1.f, Z + (size_t)k * nb, ldz, TRI_NONE,
+                      nullptr, s));
+    DG_TRY(trsm_f32('L', 'U', 'N', 'N', nbk, r, 1.f, Pk, nb, Z + (size_t)k * nb, ldz, nullptr, s));
+  }
+  return 0;
+}
+
+}  // namespace dg
+
+using dg::grid_for;
+
+extern "C" int dg_mixed_factor(dg_mixed **out, int n, int nb, double *const *tiles, int precision,
+                               void *stream) {
+  DG_CHECK_ARG(out != nullptr, 1);
+  DG_CHECK_ARG(n > 0, 2);
+  DG_CHECK_ARG(nb >= 64 && nb % 64 == 0, 3);
+  DG_CHECK_ARG(tiles != nullptr, 4);
+  DG_CHECK_ARG(precision == DG_PREC_BF16 || precision == DG_PREC_BF16X3 ||
+                   precision == DG_PREC_FP16 || precision == DG_PREC_FP16X3 ||
+                   precision == DG_PREC_FP32,
+               5);
+  cudaStream_t s = (cudaStream_t)stream;
+  dg_mixed *f = new dg_mixed();
+  f->n = n; f->nb = nb; f->mt = (n + nb - 1) / nb; f->precision = precision;
+  cudaGetDevice(&f->dev);
+  const int mt = f->mt;
+  const long long wsize = dg::panel_base(mt, n, nb) + (long long)nb * nb;
+  const long long tmax = std::max(0LL, (long long)n - nb);
+  auto fail = [&](int rc) {
+    dg_mixed_destroy(f);
+    return rc;
+  };
+  struct Alloc { void **p; size_t bytes; };
+  Alloc allocs[] = {
+      {(void **)&f->W, sizeof(float) * (size_t)wsize},
+      {(void **)&f->s, sizeof(double) * (size_t)n},
+      {(void **)&f->tiles_dev, sizeof(double *) * (size_t)mt * mt},
+      {(void **)&f->P_hi, 2 * (size_t)std::max(1LL, tmax) * nb},
+      {(void **)&f->P_lo, 2 * (size_t)std::max(1LL, tmax) * nb},
+      {(void **)&f->diag_backup, sizeof(float) * (size_t)nb * nb},
+      {(void **)&f->d64, sizeof(double) * (size_t)nb * nb},
+      {(void **)&f->panel_max, sizeof(float) * (size_t)mt},
+      {(void **)&f->alpha_dev, sizeof(float) * (size_t)mt},
+      {(void **)&f->words, sizeof(int) * (size_t)(3 + mt)},
+  };
+  for (auto &a : allocs) {
+    if (cudaMalloc(a.p, a.bytes) != cudaSuccess) {
+      cudaGetLastError();
+      dg_set_last_error(__FILE__, __LINE__, "device allocation for the mixed factor failed");
+      return fail(DG_ERR_NOMEM);
+    }
+    f->bytes += a.bytes;
+  }
+  if (cudaMemcpyAsync(f->tiles_dev, tiles, sizeof(double *) * (size_t)mt * mt,
+                      cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return fail(DG_ERR_CUDA);
+  // ||A||_inf
+  double *rows = nullptr, *dmax = nullptr;
+  if (cudaMallocAsync((void **)&rows, sizeof(double) * (n + 1), s) != cudaSuccess)
+    return fail(DG_ERR_NOMEM);
+  dmax = rows + n;
+  dg::row_abs_sum_kernel<<<grid_for(n), 256, 0, s>>>(f->tiles_dev, n, nb, mt, rows);
+  dg::colmax_kernel<<<1, 1024, 0, s>>>(rows, n, n, dmax);
+  dg::count_launches(2);
+  cudaMemcpyAsync(&f->normA, dmax, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(rows, s);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  int rc = dg::mixed_factor_run(f, s);
+  cudaEventRecord(e1, s);
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return fail(rc);
+  }
+  int words[3];
+  if (cudaMemcpyAsync(words, f->words, sizeof(words), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return fail(DG_ERR_CUDA);
+  }
+  cudaEventElapsedTime(&f->factor_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  f->retries = words[1];
+  int info = words[0];
+  if (words[2] != 0x7f7f7f7f && words[2] > 0) info = words[2];  // non-positive diagonal
+  f->info = info;
+  *out = f;
+  if (info < 0) {
+    dg_set_last_error(__FILE__, __LINE__, "a bounded device wait timed out in the trailing update");
+    return info;
+  }
+  return info;
+}
+
+extern "C" void dg_mixed_destroy(dg_mixed *f) {
+  if (!f) return;
+  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
+                f->panel_max, f->alpha_dev, f->words};
+  for (void *p : ps)
+    if (p) cudaFree(p);
+  delete f;
+}
+
+extern "C" int dg_mixed_info(const dg_mixed *f, dg_mixed_stats *st) {
+  DG_CHECK_ARG(f != nullptr, 1);
+  DG_CHECK_ARG(st != nullptr, 2);
+  st->n = f->n;
+  st->nb = f->nb;
+  st->precision = f->precision;
+  st->info = f->info;
+  st->retries = f->retries;
+  st->factor_ms = f->factor_ms;
+  st->norm_inf = f->normA;
+  st->device_bytes = (long long)f->bytes;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// refinement
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Work {
+  double *R = nullptr, *V = nullptr;  // residual; GMRES basis
+  float *Z = nullptr;
+  double *cm = nullptr;               // column maxima scratch (3 r)
+};
+
+int correction(const dg_mixed *f, const double *R, long long ldr, double *X, long long ldx,
+               float *Z, int r, cudaStream_t s) {
+  const int n = f->n;
+  dg::scale_to_f32_kernel<<<grid_for((long long)n * r), 256, 0, s>>>(R, ldr, f->s, Z, n, n, r);
+  dg::count_launches(1);
+  DG_TRY(dg::mixed_tri_solve(f, Z, n, r, s));
+  dg::update_x_kernel<<<grid_for((long long)n * r), 256, 0, s>>>(X, ldx, f->s, Z, n, n, r);
+  dg::count_launches(1);
+  DG_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// R = B - A X (FP64, A from the caller's tiles)
+int residual(const dg_mixed *f, const double *B, long long ldb, const double *X, long long ldx,
+             double *R, int r, cudaStream_t s) {
+  const int n = f->n;
+  DG_CUDA_TRY(cudaMemcpy2DAsync(R, sizeof(double) * n, B, sizeof(double) * ldb,
+                                sizeof(double) * n, r, cudaMemcpyDeviceToDevice, s));
+  return dg::gemm_tiles_f64(n, f->nb, r, -1.0, (const double *const *)f->tiles_dev, X, ldx, 1.0, R,
+                            n, nullptr, s);
+}
+
+int backward_errors(const dg_mixed *f, const double *B, long long ldb, const double *X,
+                    long long ldx, const double *R, int r, double *cm, std::vector<double> &berr,
+                    cudaStream_t s) {
+  const int n = f->n;
+  dg::colmax_kernel<<<r, 256, 0, s>>>(R, n, n, cm);
+  dg::colmax_kernel<<<r, 256, 0, s>>>(X, ldx, n, cm + r);
+  dg::colmax_kernel<<<r, 256, 0, s>>>(B, ldb, n, cm + 2 * r);
+  dg::count_launches(3);
+  std::vector<double> h(3 * (size_t)r);
+  DG_CUDA_TRY(cudaMemcpyAsync(h.data(), cm, sizeof(double) * 3 * r, cudaMemcpyDeviceToHost, s));
+  DG_CUDA_TRY(cudaStreamSynchronize(s));
+  berr.resize(r);
+  for (int j = 0; j < r; j++) {
+    const double den = f->normA * h[r + j] + h[2 * r + j];
+    berr[j] = den > 0 ? h[j] / den : (h[j] == 0 ? 0.0 : INFINITY);
+  }
+  return 0;
+}
+
+// ---- small batched vector kernels for GMRES (one column per CTA) ----
+__global__ void dots_kernel(const double *U, long long ldu, const double *V, long long ldv, int n,
+                            double *out) {
+  const int j = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += U[i + j * ldu] * V[i + j * ldv];
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) out[j] = acc;
+  }
+}
+
+// V(:, j) = a[j] * U(:, j) + b[j] * V(:, j)   (coefficients from device memory)
+__global__ void axpby_kernel(const double *U, long long ldu, double *V, long long ldv, int n, int r,
+                             const double *a, const double *b, int neg_a) {
+  const long long total = (long long)n * r;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const double aj = neg_a ? -a[j] : a[j];
+    const double bj = b ? b[j] : 1.0;
+    V[i + j * ldv] = aj * U[i + j * ldu] + bj * V[i + j * ldv];
+  }
+}
+
+__global__ void inv_kernel(const double *x, double *y, int r) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < r) y[j] = x[j] > 0 ? 1.0 / sqrt(x[j]) : 0.0;
+}
+
+// z = M^-1 y for FP64 y (M = the low-precision factor of A, with the scaling)
+int precond(const dg_mixed *f, const double *Y, double *Zo, float *Z32, int r, cudaStream_t s) {
+  const int n = f->n;
+  DG_CUDA_TRY(cudaMemsetAsync(Zo, 0, sizeof(double) * (size_t)n * r, s));
+  return correction(f, Y, n, Zo, n, Z32, r, s);
+}
+
+// Restarted GMRES(m) on A d = r0 (FP64), left preconditioned by the factor,
+// each column an independent Krylov space.  x += d.  Returns iterations.
+int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int r, int m,
+             int max_iters, double inner_tol, cudaStream_t s, int *iters_out) {
+  const int n = f->n;
+  const size_t col = (size_t)n;
+  double *V = nullptr, *W = nullptr, *D = nullptr, *sc = nullptr;
+  float *Z32 = nullptr;
+  if (cudaMallocAsync((void **)&V, sizeof(double) * col * r * (m + 1), s) != cudaSuccess ||
+      cudaMallocAsync((void **)&W, sizeof(double) * col * r * 2, s) != cudaSuccess ||
+      cudaMallocAsync((void **)&D, sizeof(double) * col * r, s) != cudaSuccess ||
+      cudaMallocAsync((void **)&sc, sizeof(double) * r * (m + 4), s) != cudaSuccess ||
+      cudaMallocAsync((void **)&Z32, sizeof(float) * col * r, s) != cudaSuccess) {
+    cudaGetLastError();
+    return DG_ERR_NOMEM;
+  }
+  double *T = W + col * r;  // second scratch block
+  auto Vk = [&](int k) { return V + col * r * k; };
+  std::vector<double> H((size_t)(m + 1) * m * r), g((size_t)(m + 1) * r), hcol(r), cs(m * r), sn(m * r);
+  int total_it = 0;
+  int rc = 0;
+  DG_CUDA_TRY(cudaMemsetAsync(D, 0, sizeof(double) * col * r, s));
+  // z0 = M^-1 r0
+  rc = precond(f, R0, Vk(0), Z32, r, s);
+  std::vector<double> beta0(r);
+  while (!rc && total_it < max_iters) {
+    // beta = ||v0||, v0 /= beta
+    dots_kernel<<<r, 256, 0, s>>>(Vk(0), n, Vk(0), n, n, sc);
+    cudaMemcpyAsync(hcol.data(), sc, sizeof(double) * r, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int j = 0; j < r; j++) {
+      beta0[j] = std::sqrt(hcol[j]);
+      g[j] = beta0[j];
+      for (int i = 1; i <= m; i++) g[i * r + j] = 0.0;
+    }
+    inv_kernel<<<(r + 127) / 128, 128, 0, s>>>(sc, sc + r, r);
+    cudaMemsetAsync(sc + 2 * r, 0, sizeof(double) * r, s);
+    axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(Vk(0), n, Vk(0), n, n, r, sc + r, sc + 2 * r, 0);
+    dg::count_launches(3);
+    int kdone = 0;
+    for (int k = 0; k < m && total_it < max_iters; k++, total_it++) {
+      // w = M^-1 A v_k
+      rc = dg::gemm_tiles_f64(n, f->nb, r, 1.0, (const double *const *)f->tiles_dev, Vk(k), n, 0.0,
+                              T, n, nullptr, s);
+      if (rc) break;
+      rc = precond(f, T, W, Z32, r, s);
+      if (rc) break;
+      // modified Gram-Schmidt
+      for (int i = 0; i <= k; i++) {
+        dots_kernel<<<r, 256, 0, s>>>(W, n, Vk(i), n, n, sc + 3 * r);
+        cudaMemcpyAsync(hcol.data(), sc + 3 * r, sizeof(double) * r, cudaMemcpyDeviceToHost, s);
+        axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(Vk(i), n, W, n, n, r, sc + 3 * r, nullptr, 1);
+        dg::count_launches(2);
+        cudaStreamSynchronize(s);
+        for (int j = 0; j < r; j++) H[((size_t)i * m + k) * r + j] = hcol[j];
+      }
+      dots_kernel<<<r, 256, 0, s>>>(W, n, W, n, n, sc);
+      cudaMemcpyAsync(hcol.data(), sc, sizeof(double) * r, cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      for (int j = 0; j < r; j++) H[((size_t)(k + 1) * m + k) * r + j] = std::sqrt(hcol[j]);
+      inv_kernel<<<(r + 127) / 128, 128, 0, s>>>(sc, sc + r, r);
+      cudaMemsetAsync(Vk(k + 1), 0, sizeof(double) * col * r, s);
+      axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(W, n, Vk(k + 1), n, n, r, sc + r, nullptr, 0);
+      dg::count_launches(3);
+      // Givens rotations on the host, per column
+      double worst = 0.0;
+      for (int j = 0; j < r; j++) {
+        for (int i = 0; i < k; i++) {
+          double &a = H[((size_t)i * m + k) * r + j], &b = H[((size_t)(i + 1) * m + k) * r + j];
+          const double t = cs[i * r + j] * a + sn[i * r + j] * b;
+          b = -sn[i * r + j] * a + cs[i * r + j] * b;
+          a = t;
+        }
+        double &a = H[((size_t)k * m + k) * r + j], &b = H[((size_t)(k + 1) * m + k) * r + j];
+        const double den = std::hypot(a, b);
+        const double c = den > 0 ? a / den : 1.0, sv = den > 0 ? b / den : 0.0;
+        cs[k * r + j] = c;
+        sn[k * r + j] = sv;
+        a = den;
+        b = 0.0;
+        g[(k + 1) * r + j] = -sv * g[k * r + j];
+        g[k * r + j] = c * g[k * r + j];
+        const double rel = beta0[j] > 0 ? std::fabs(g[(k + 1) * r + j]) / beta0[j] : 0.0;
+        worst = std::max(worst, rel);
+      }
+      kdone = k + 1;
+      if (worst <= inner_tol) break;
+    }
+    if (rc) break;
+    // y = H^-1 g per column, D += V y
+    std::vector<double> y((size_t)kdone * r);
+    for (int j = 0; j < r; j++)
+      for (int i = kdone - 1; i >= 0; i--) {
+        double acc = g[i * r + j];
+        for (int l = i + 1; l < kdone; l++) acc -= H[((size_t)i * m + l) * r + j] * y[l * r + j];
+        const double h = H[((size_t)i * m + i) * r + j];
+        y[i * r + j] = h != 0 ? acc / h : 0.0;
+      }
+    for (int i = 0; i < kdone; i++) {
+      cudaMemcpyAsync(sc + 3 * r, &y[(size_t)i * r], sizeof(double) * r, cudaMemcpyHostToDevice, s);
+      axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(Vk(i), n, D, n, n, r, sc + 3 * r, nullptr, 0);
+      dg::count_launches(1);
+      cudaStreamSynchronize(s);
+    }
+    break;  // one cycle per outer refinement step; the outer loop restarts
+  }
+  if (!rc) {
+    // x += d
+    std::vector<double> ones(r, 1.0);
+    cudaMemcpyAsync(sc, ones.data(), sizeof(double) * r, cudaMemcpyHostToDevice, s);
+    axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(D, n, X, ldx, n, r, sc, nullptr, 0);
+    dg::count_launches(1);
+    cudaStreamSynchronize(s);
+  }
+  cudaFreeAsync(V, s);
+  cudaFreeAsync(W, s);
+  cudaFreeAsync(D, s);
+  cudaFreeAsync(sc, s);
+  cudaFreeAsync(Z32, s);
+  *iters_out = total_it;
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int ldb, double *X,
+                              int ldx, const dg_ir_opts *opts, dg_ir_report *rep, void *stream) {
+  DG_CHECK_ARG(f != nullptr, 1);
+  DG_CHECK_ARG(nrhs > 0, 2);
+  DG_CHECK_ARG(B != nullptr, 3);
+  DG_CHECK_ARG(ldb >= f->n, 4);
+  DG_CHECK_ARG(X != nullptr, 5);
+  DG_CHECK_ARG(ldx >= f->n, 6);
+  if (f->info != 0) {
+    dg_set_last_error(__FILE__, __LINE__, "the factorization failed; no solve");
+    return DG_ERR_STATE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = f->n, r = nrhs;
+  dg_ir_opts o;
+  o.tol = 1e-12; o.max_iter = 30; o.gmres = 0; o.restart = 30; o.gmres_inner_tol = 1e-4;
+  if (opts) o = *opts;
+  double *R = nullptr, *cm = nullptr;
+  float *Z = nullptr;
+  if (cudaMallocAsync((void **)&R, sizeof(double) * (size_t)n * r, s) != cudaSuccess ||
+      cudaMallocAsync((void **)&cm, sizeof(double) * 3 * r, s) != cudaSuccess ||
+      cudaMallocAsync((void **)&Z, sizeof(float) * (size_t)n * r, s) != cudaSuccess) {
+    cudaGetLastError();
+    return DG_ERR_NOMEM;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  DG_CUDA_TRY(cudaMemset2DAsync(X, sizeof(double) * ldx, 0, sizeof(double) * n, r, s));
+  DG_CUDA_TRY(cudaMemcpy2DAsync(R, sizeof(double) * n, B, sizeof(double) * ldb, sizeof(double) * n,
+                                r, cudaMemcpyDeviceToDevice, s));
+  std::vector<double> berr, prev;
+  int it = 0, rc = 0, gm_iters = 0, outer = 0;
+  bool converged = false, use_gmres = (o.gmres == 1);
+  for (it = 0; it < o.max_iter; it++) {
+    if (!use_gmres) {
+      rc = correction(f, R, n, X, ldx, Z, r, s);
+    } else {
+      int gi = 0;
+      rc = gmres_ir(f, R, X, ldx, r, o.restart, o.restart, o.gmres_inner_tol, s, &gi);
+      gm_iters += gi;
+    }
+    if (rc) break;
+    outer++;
+    rc = residual(f, B, ldb, X, ldx, R, r, s);
+    if (rc) break;
+    rc = backward_errors(f, B, ldb, X, ldx, R, r, cm, berr, s);
+    if (rc) break;
+    double worst = 0.0;
+    for (double b : berr) worst = std::max(worst, std::isfinite(b) ? b : INFINITY);
+    if (worst <= o.tol) {
+      converged = true;
+      break;
+    }
+    // plain refinement stalls: the error no longer halves -> GMRES-IR
+    if (!use_gmres && o.gmres == 0 && !prev.empty()) {
+      double pw = 0.0;
+      for (double b : prev) pw = std::max(pw, b);
+      if (!(worst < 0.5 * pw)) use_gmres = true;
+    }
+    prev = berr;
+  }
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(R, s);
+  cudaFreeAsync(cm, s);
+  cudaFreeAsync(Z, s);
+  if (rep) {
+    rep->iterations = outer;
+    rep->gmres_iterations = gm_iters;
+    rep->used_gmres = use_gmres ? 1 : 0;
+    rep->converged = converged ? 1 : 0;
+    double worst = 0.0;
+    for (double b : berr) worst = std::max(worst, b);
+    rep->backward_error = worst;
+    rep->solve_ms = ms;
+  }
+  if (rc) return rc;
+  if (!converged) {
+    dg_set_last_error(__FILE__, __LINE__, "iterative refinement did not reach the tolerance");
+    return DG_ERR_NOCONVERGE;
+  }
+  return 0;
+}

@@ -1,0 +1,416 @@
+// BF16 tensor-core GEMM on tcgen05 with TMEM accumulators and TMA-staged
+// operands: the trailing SYRK/GEMM update of the mixed-precision Cholesky.
+//
+//   C(i, j) <- alpha * sum_t sum_p A_t(p, i) * B_t(p, j) + beta * C(i, j)
+//
+// A and B are "K-major" BF16 panels: row i of the panel holds the K values
+// A(0..K-1, i) contiguously (a column-major nb x n tile of the factor's row
+// panel is already in this order).  With `terms` = 3 the operands are given
+// as hi/lo BF16 pairs (x = hi + lo, lo = bf16(x - hi)) and the three products
+// hi*hi + hi*lo + lo*hi accumulate into the same FP32 TMEM accumulator,
+// carrying about 16 significant bits per operand instead of 8.
+//
+// One CTA computes a 128 x BN tile of C with 4 warps:
+//   warp 0, one thread   TMA producer: per K-block of 64, loads the A and B
+//                        slabs (128B-swizzled, 1024-byte aligned stages) and
+//                        arms the stage's "full" mbarrier with the byte count
+//   warp 1, one thread   MMA issuer: waits "full", issues 4 (x terms)
+//                        tcgen05.mma kind::f16 (M=128, N=BN, K=16) into TMEM,
+//                        and tcgen05.commit's the stage's "empty" mbarrier so
+//                        the producer can refill it; a final commit arms
+//                        the accumulator barrier
+//   warps 0-3            epilogue: tcgen05.ld 32x32b.x32 of their 32 TMEM
+//                        lanes (rows), then a coalesced read-modify-write of C
+// Output addressing: plain column-major C, or the packed upper row-panel
+// layout of the mixed factor (row panel r holds columns r*nb..n-1 of rows
+// r*nb..r*nb+nb-1, column-major with leading dimension nb), where only the
+// upper triangle (i <= j) is updated.
+//
+// Every mbarrier wait is bounded by the global timer (about 2 s).  A wait that
+// gives up records DG_ERR_TIMEOUT in the status word, stops issuing, drains
+// the copies and MMAs already issued (again bounded), frees its TMEM and
+// returns; nothing traps.
+#include <cuda.h>
+
+#include "dg_common.cuh"
+#include "runtime.h"
+#include "tc_gemm.h"
+
+namespace dg {
+namespace {
+
+constexpr int BM = 128, BK = 64;
+constexpr uint64_t kWaitNs = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer() - t0 > kWaitNs) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// rows of 64 BF16 (128 B), 8-row atoms of 1024 B stacked along M/N.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                           // leading byte offset (unused here)
+  d |= (uint64_t)(1024 >> 4) << 32;                 // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                           // descriptor version
+  d |= (uint64_t)2 << 61;                           // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B
+// both BF16 (bits 7-9, 10-12 = 1) or both FP16 (= 0), both K-major (bits
+// 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_f16kind(int bn, bool fp16) {
+  return (1u << 4) | ((fp16 ? 0u : 1u) << 7) | ((fp16 ? 0u : 1u) << 10) |
+         ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN, int TERMS>
+struct Smem {
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = TERMS == 1 ? (A_BYTES + B_BYTES) : 2 * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = TERMS == 1 ? (BN == 128 ? 4 : 4) : (BN == 128 ? 3 : 2);
+  static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <int BN, int TERMS>
+__global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__ TcParams p) {
+  using S = Smem<BN, TERMS>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(smem + S::STAGES * S::STAGE_BYTES);
+  uint64_t *empty = full + S::STAGES;
+  uint64_t *accum = empty + S::STAGES;
+  uint32_t *tmem_slot = (uint32_t *)(accum + 1);
+  int *abort_flag = (int *)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bi = blockIdx.x, bj = blockIdx.y;
+  const int i0 = bi * BM, j0 = bj * BN;
+  // tiles wholly below the diagonal of an upper-triangular update do nothing
+  if (p.upper && i0 > j0 + BN - 1) return;
+  if (p.status && *(volatile int *)p.status) return;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S::STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const int nk = (p.k + BK - 1) / BK;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer ----------------
+    int issued = 0;
+    for (int kb = 0; kb < nk; kb++) {
+      const int s = kb % S::STAGES;
+      const uint32_t round = kb / S::STAGES;
+      if (kb >= S::STAGES && !mbar_wait(&empty[s], (round - 1) & 1)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      if (*(volatile int *)abort_flag) break;
+      uint8_t *st = smem + s * S::STAGE_BYTES;
+      mbar_expect_tx(&full[s], S::STAGE_BYTES);
+      const int kx = kb * BK;
+      tma_load_2d(st, &p.a_hi, &full[s], kx, p.a_row0 + i0);
+      tma_load_2d(st + S::A_BYTES, &p.b_hi, &full[s], kx, p.b_row0 + j0);
+      if (TERMS == 3) {
+        tma_load_2d(st + S::A_BYTES + S::B_BYTES, &p.a_lo, &full[s], kx, p.a_row0 + i0);
+        tma_load_2d(st + 2 * S::A_BYTES + S::B_BYTES, &p.b_lo, &full[s], kx, p.b_row0 + j0);
+      }
+      issued++;
+    }
+    // drain: every load issued must land before the CTA may exit
+    for (int kb = (issued > S::STAGES ? issued - S::STAGES : 0); kb < issued; kb++)
+      if (!mbar_wait(&full[kb % S::STAGES], (kb / S::STAGES) & 1)) atomicExch(abort_flag, 1);
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t idesc = p.idesc;
+    const uint32_t sbase = smem_u32(smem);
+    int done = 0;
+    for (int kb = 0; kb < nk; kb++) {
+      const int s = kb % S::STAGES;
+      if (!mbar_wait(&full[s], (kb / S::STAGES) & 1)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t st = sbase + s * S::STAGE_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; kk++) {
+        const uint32_t koff = kk * 32;  // 16 BF16 along K inside the swizzled row
+        const uint64_t a = sw128_desc(st + koff);
+        const uint64_t b = sw128_desc(st + S::A_BYTES + koff);
+        mma_bf16(tmem, a, b, idesc, (kb | kk) ? 1u : 0u);
+        if (TERMS == 3) {
+          const uint64_t alo = sw128_desc(st + S::A_BYTES + S::B_BYTES + koff);
+          const uint64_t blo = sw128_desc(st + 2 * S::A_BYTES + S::B_BYTES + koff);
+          mma_bf16(tmem, a, blo, idesc, 1u);
+          mma_bf16(tmem, alo, b, idesc, 1u);
+        }
+      }
+      mma_commit(&empty[s]);
+      done++;
+    }
+    mma_commit(accum);
+    (void)done;
+  }
+  __syncwarp();
+
+  // ---------------- epilogue (all 4 warps) ----------------
+  const bool ok = mbar_wait(accum, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (!ok) atomicExch(abort_flag, 1);
+  __syncthreads();
+  const bool aborted = *(volatile int *)abort_flag != 0;
+  const float alpha = p.alpha_dev ? *p.alpha_dev : p.alpha;
+  if (!aborted && nk > 0) {
+    const int row = i0 + warp * 32 + lane;  // TMEM lane == row of the tile
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+      if (row >= p.m) continue;
+      if (p.layout == 0) {
+#pragma unroll
+        for (int c = 0; c < 32; c++) {
+          const int col = j0 + c0 + c;
+          if (col >= p.n) break;
+          if (p.upper && row > col) continue;
+          float *cp = p.c + (size_t)row + (size_t)col * p.ldc;
+          *cp = p.beta == 0.f ? alpha * v[c] : fmaf(alpha, v[c], p.beta * *cp);
+        }
+      } else {
+        // packed upper row panels; global indices shifted by the trailing offset
+        const long long gi = p.off + row;
+        const long long r = gi / p.nb;
+        const long long base = (long long)p.nb * (r * p.ntot - p.nb * r * (r - 1) / 2);
+        float *rowp = p.c + base + (gi - r * p.nb);
+#pragma unroll
+        for (int c = 0; c < 32; c++) {
+          const int col = j0 + c0 + c;
+          if (col >= p.n) break;
+          if (row > col) continue;
+          const long long gj = p.off + col;
+          float *cp = rowp + (gj - r * p.nb) * p.nb;
+          *cp = fmaf(alpha, v[c], *cp);
+        }
+      }
+    }
+  }
+  if (aborted && threadIdx.x == 0 && p.status) atomicCAS(p.status, 0, DG_ERR_TIMEOUT);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN)
+                 : "memory");
+}
+
+// cuTensorMapEncodeTiled is a driver API call; it is resolved through the
+// runtime's entry-point query so the library does not link libcuda (it then
+// loads on machines without a driver, e.g. for ABI checks).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+bool encode_map(CUtensorMap *map, const void *base, int kdim, int rows, int ldk, int box_rows,
+                bool fp16) {
+  EncodeTiledFn cuTensorMapEncodeTiled = encode_fn();
+  if (!cuTensorMapEncodeTiled) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ldk * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = cuTensorMapEncodeTiled(map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <int BN, int TERMS>
+int launch(const TcParams &p, cudaStream_t s) {
+  using S = Smem<BN, TERMS>;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr_set[dev & 63]) {
+    DG_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<BN, TERMS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+    attr_set[dev & 63] = true;
+  }
+  dim3 grid((p.m + BM - 1) / BM, (p.n + BN - 1) / BN);
+  tc_gemm_kernel<BN, TERMS><<<grid, 128, S::TOTAL, s>>>(p);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return 0;
+}
+
+}  // namespace
+
+int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
+  if (g.m <= 0 || g.n <= 0) return 0;
+  if (g.terms != 1 && g.terms != 3) return DG_ERR_UNSUPPORTED;
+  if (g.k <= 0 || g.k % 8 != 0 || g.lda % 8 != 0 || g.ldb % 8 != 0) return DG_ERR_UNSUPPORTED;
+  if (((uintptr_t)g.a_hi | (uintptr_t)g.b_hi) & 15) return DG_ERR_UNSUPPORTED;
+  if (g.terms == 3 && (((uintptr_t)g.a_lo | (uintptr_t)g.b_lo) & 15)) return DG_ERR_UNSUPPORTED;
+  const int bn = g.bn == 256 ? 256 : 128;
+  TcParams p;
+  memset(&p, 0, sizeof p);
+  const bool h = g.fp16 != 0;
+  if (!encode_map(&p.a_hi, g.a_hi, g.k, g.a_rows, g.lda, BM, h) ||
+      !encode_map(&p.b_hi, g.b_hi, g.k, g.b_rows, g.ldb, bn, h)) {
+    dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
+    return DG_ERR_CUDA;
+  }
+  if (g.terms == 3 && (!encode_map(&p.a_lo, g.a_lo, g.k, g.a_rows, g.lda, BM, h) ||
+                       !encode_map(&p.b_lo, g.b_lo, g.k, g.b_rows, g.ldb, bn, h))) {
+    dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
+    return DG_ERR_CUDA;
+  }
+  p.m = g.m; p.n = g.n; p.k = g.k;
+  p.a_row0 = g.a_row0; p.b_row0 = g.b_row0;
+  p.alpha = g.alpha; p.beta = g.beta;
+  p.c = g.c; p.ldc = g.ldc;
+  p.layout = g.layout; p.upper = g.upper;
+  p.off = g.off; p.nb = g.nb; p.ntot = g.ntot;
+  p.status = g.status;
+  p.idesc = idesc_f16kind(bn, h);
+  p.alpha_dev = g.alpha_dev;
+  if (g.terms == 1)
+    return bn == 256 ? launch<256, 1>(p, s) : launch<128, 1>(p, s);
+  return bn == 256 ? launch<256, 3>(p, s) : launch<128, 3>(p, s);
+}
+
+}  // namespace dg
+
+// Building-block entry: C = alpha * A' B + beta * C with 16-bit K-major
+// operands (A is k x m column-major, B is k x n column-major) and FP32 C.
+extern "C" int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const void *a_hi,
+                             const void *a_lo, int lda, const void *b_hi, const void *b_lo, int ldb,
+                             float alpha, float beta, float *C, int ldc, int bn, int *status,
+                             void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(k > 0 && k % 8 == 0, 3);
+  DG_CHECK_ARG(terms == 1 || terms == 3, 4);
+  DG_CHECK_ARG(lda >= k && lda % 8 == 0, 8);
+  DG_CHECK_ARG(ldb >= k && ldb % 8 == 0, 11);
+  DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 15);
+  dg::TcGemmArgs g;
+  memset(&g, 0, sizeof g);
+  g.m = m; g.n = n; g.k = k; g.terms = terms;
+  g.a_hi = a_hi; g.a_lo = a_lo; g.lda = lda; g.a_rows = m;
+  g.b_hi = b_hi; g.b_lo = b_lo; g.ldb = ldb; g.b_rows = n;
+  g.alpha = alpha; g.beta = beta; g.c = C; g.ldc = ldc;
+  g.layout = 0; g.upper = 0; g.bn = bn; g.status = status; g.fp16 = fp16;
+  return dg::tc_gemm_bf16(g, (cudaStream_t)stream);
+}

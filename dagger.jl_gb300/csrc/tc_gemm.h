@@ -1,0 +1,49 @@
+// Internal interface of the tcgen05 BF16 GEMM (tc_gemm.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace dg {
+
+// Kernel parameters (passed as one __grid_constant__ struct so the tensor
+// maps stay in parameter space, as TMA requires).
+struct TcParams {
+  CUtensorMap a_hi, b_hi, a_lo, b_lo;
+  int m, n, k;
+  int a_row0, b_row0;  // first panel row of the A / B operand
+  float alpha, beta;
+  float *c;
+  long long ldc;
+  int layout;          // 0 = column-major C (ldc); 1 = packed upper row panels
+  int upper;           // update only i <= j
+  long long off;       // layout 1: global index of row/column 0 of this update
+  int nb;              // layout 1: row-panel height
+  long long ntot;      // layout 1: order of the whole matrix
+  int *status;         // device status word: non-zero on entry = skip; timeout recorded
+  uint32_t idesc;      // tcgen05 instruction descriptor (operand types, M, N)
+  const float *alpha_dev;  // when set, alpha is read from device memory
+};
+
+struct TcGemmArgs {
+  int m, n, k, terms;                 // terms: 1 (bf16) or 3 (bf16 hi/lo split)
+  const void *a_hi, *a_lo;            // K-major BF16 panels
+  int lda, a_rows, a_row0;
+  const void *b_hi, *b_lo;
+  int ldb, b_rows, b_row0;
+  float alpha, beta;
+  float *c;
+  long long ldc;
+  int layout, upper;
+  long long off;
+  int nb;
+  long long ntot;
+  int bn;                             // 128 or 256 columns per CTA tile
+  int *status;
+  int fp16;                           // operands are FP16 instead of BF16
+  const float *alpha_dev;             // optional device-resident alpha
+};
+
+int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s);
+
+}  // namespace dg

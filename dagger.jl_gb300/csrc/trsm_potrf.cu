@@ -1,0 +1,312 @@
+// Triangular solve (TRSM) and Cholesky (POTRF) of one tile, FP64 and FP32.
+//
+// FP64 replaces LAPACK.potrf! in potrf_checked! (src/array/cholesky.jl:3 of
+// Dagger.jl) and BLAS.trsm! in the panel step (cholesky.jl:41,86) and in the
+// block solves (src/array/trsm.jl:95-183).  FP32 is the diagonal-block
+// factorization, panel solve and triangular solves of the mixed-precision
+// form.
+//
+// Both are recursive: the triangle is halved until a 64 x 64 diagonal block
+// remains, and the off-diagonal work of each level is a GEMM / SYRK on the
+// tile GEMM kernels (gemm_tile.cu), so nearly all flops run in the GEMM.  The
+// 64 x 64 base cases are shared-memory kernels:
+//   trsm_base: the 64 x 64 triangle and a 64 x 8 slab of the right-hand side
+//              are staged in shared memory; each warp solves one column by
+//              forward/backward substitution with the column held in two
+//              registers per lane and the solved entry broadcast by shuffle
+//              (the reciprocal of each pivot is formed once, as OpenBLAS's
+//              trsm kernels do).
+//   potrf_base: one CTA factors the 64 x 64 block in shared memory
+//              (right-looking, column by column).  A pivot that is not
+//              positive (or NaN) records the LAPACK info in a device word and
+//              stops; every later kernel of the same factorization checks the
+//              word on entry and returns at once.
+// Every access is bounds-checked against the block length, so ragged last
+// tiles (n not a multiple of the block size) need no padding.
+#include "dg_common.cuh"
+
+namespace dg {
+
+namespace {
+
+constexpr int TB = 64;     // base block size
+constexpr int TRSM_W = 8;  // right-hand-side columns per CTA (one per warp)
+
+template <typename T>
+struct TriView {
+  const T *T_;
+  long long ld;
+  bool trans;  // M(i, j) = T(j, i)
+  bool lower;  // M is lower triangular
+  bool unit;   // unit diagonal
+};
+
+// Solve M[r0:r0+len, r0:r0+len] X = X in place for the columns handled by
+// this CTA.  X(i, c) lives at X[i * rs + c * cs].
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_base_kernel(TriView<T> tv, int r0, int len, T *X,
+                                                        long long rs, long long cs, int nn,
+                                                        const int *a1, const int *a2) {
+  if (aborted(a1, a2)) return;
+  __shared__ T Ms[TB][TB + 1];
+  __shared__ T dinv[TB];
+  __shared__ T Xs[TB][TRSM_W + 1];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int c0 = blockIdx.x * TRSM_W;
+  const int wcols = min(TRSM_W, nn - c0);
+  for (int e = tid; e < len * len; e += nt) {
+    int i, j;
+    if (!tv.trans) { i = e % len; j = e / len; } else { j = e % len; i = e / len; }
+    if (tv.lower ? (j <= i) : (j >= i)) {
+      size_t off = tv.trans ? (size_t)(r0 + j) + (size_t)(r0 + i) * tv.ld
+                            : (size_t)(r0 + i) + (size_t)(r0 + j) * tv.ld;
+      Ms[i][j] = tv.T_[off];
+    }
+  }
+  for (int e = tid; e < len * wcols; e += nt) {
+    int i, c;
+    if (rs == 1) { i = e % len; c = e / len; } else { c = e % wcols; i = e / wcols; }
+    Xs[i][c] = X[(size_t)(r0 + i) * rs + (size_t)(c0 + c) * cs];
+  }
+  __syncthreads();
+  if (tid < len) dinv[tid] = tv.unit ? T(1) : T(1) / Ms[tid][tid];
+  __syncthreads();
+  const int lane = tid & 31, warp = tid >> 5;
+  if (warp < wcols) {
+    const int c = warp;
+    T x0 = lane < len ? Xs[lane][c] : T(0);
+    T x1 = lane + 32 < len ? Xs[lane + 32][c] : T(0);
+    if (tv.lower) {
+      for (int i = 0; i < len; i++) {
+        T xi = __shfl_sync(0xffffffffu, i < 32 ? x0 : x1, i & 31) * dinv[i];
+        if (i < 32) { if (lane == i) x0 = xi; } else { if (lane == i - 32) x1 = xi; }
+        if (lane > i && lane < len) x0 = fma(-Ms[lane][i], xi, x0);
+        if (lane + 32 > i && lane + 32 < len) x1 = fma(-Ms[lane + 32][i], xi, x1);
+      }
+    } else {
+      for (int i = len - 1; i >= 0; i--) {
+        T xi = __shfl_sync(0xffffffffu, i < 32 ? x0 : x1, i & 31) * dinv[i];
+        if (i < 32) { if (lane == i) x0 = xi; } else { if (lane == i - 32) x1 = xi; }
+        if (lane < i) x0 = fma(-Ms[lane][i], xi, x0);
+        if (lane + 32 < i) x1 = fma(-Ms[lane + 32][i], xi, x1);
+      }
+    }
+    if (lane < len) Xs[lane][c] = x0;
+    if (lane + 32 < len) Xs[lane + 32][c] = x1;
+  }
+  __syncthreads();
+  for (int e = tid; e < len * wcols; e += nt) {
+    int i, c;
+    if (rs == 1) { i = e % len; c = e / len; } else { c = e % wcols; i = e / wcols; }
+    X[(size_t)(r0 + i) * rs + (size_t)(c0 + c) * cs] = Xs[i][c];
+  }
+}
+
+// Cholesky of one block of length len <= 64 at A (leading dimension lda).
+// Works on the lower triangle L; for uplo 'U' the block is staged transposed
+// (U' = L) and written back transposed, so only the uplo triangle is touched.
+template <typename T>
+__global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *A, long long lda,
+                                                         int *info, int info_offset,
+                                                         const int *a1, const int *a2) {
+  if (aborted(info, a1) || aborted(a2, nullptr)) return;
+  __shared__ T Ms[TB][TB + 1];
+  __shared__ int fail_at;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < len * len; e += nt) {
+    int i, j;
+    if (!upper) { i = e % len; j = e / len; } else { j = e % len; i = e / len; }
+    if (j <= i) Ms[i][j] = upper ? A[(size_t)j + (size_t)i * lda] : A[(size_t)i + (size_t)j * lda];
+  }
+  if (tid == 0) fail_at = -1;
+  __syncthreads();
+  for (int j = 0; j < len; j++) {
+    T d = Ms[j][j];
+    if (!(d > T(0))) {  // not positive, or NaN: LAPACK's test in dpotrf2/dpotf2
+      if (tid == 0) fail_at = j;
+      break;            // d is the same for every thread: uniform exit
+    }
+    d = sqrt(d);
+    const T r = T(1) / d;
+    __syncthreads();    // every thread has read Ms[j][j]
+    for (int i = j + 1 + tid; i < len; i += nt) Ms[i][j] *= r;
+    if (tid == 0) Ms[j][j] = d;
+    __syncthreads();
+    const int w = len - j - 1;
+    for (int e = tid; e < w * w; e += nt) {
+      int i = j + 1 + e % w, k = j + 1 + e / w;
+      if (k <= i) Ms[i][k] = fma(-Ms[i][j], Ms[k][j], Ms[i][k]);
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (fail_at >= 0 && tid == 0) atomicCAS(info, 0, info_offset + fail_at + 1);
+  for (int e = tid; e < len * len; e += nt) {
+    int i, j;
+    if (!upper) { i = e % len; j = e / len; } else { j = e % len; i = e / len; }
+    if (j <= i) {
+      if (upper) A[(size_t)j + (size_t)i * lda] = Ms[i][j];
+      else A[(size_t)i + (size_t)j * lda] = Ms[i][j];
+    }
+  }
+}
+
+inline int split_point(int len) {
+  int h = ((len / 2) + TB - 1) / TB * TB;
+  return h >= len ? len - TB : h;
+}
+
+template <typename T>
+int gemm_t(char ta, char tb, int m, int n, int k, T alpha, const T *A, long long lda, const T *B,
+           long long ldb, T beta, T *C, long long ldc, Tri tri, const int *a1, cudaStream_t s,
+           const int *a2);
+
+template <>
+int gemm_t<double>(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                   long long lda, const double *B, long long ldb, double beta, double *C,
+                   long long ldc, Tri tri, const int *a1, cudaStream_t s, const int *a2) {
+  return gemm_f64(ta, tb, m, n, k, alpha, A, (int)lda, B, (int)ldb, beta, C, (int)ldc, tri, a1, s,
+                  a2);
+}
+
+template <>
+int gemm_t<float>(char ta, char tb, int m, int n, int k, float alpha, const float *A,
+                  long long lda, const float *B, long long ldb, float beta, float *C,
+                  long long ldc, Tri tri, const int *a1, cudaStream_t s, const int *a2) {
+  return gemm_f32(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, a1, s, a2);
+}
+
+template <typename T>
+struct TrsmPlan {
+  TriView<T> tv;
+  bool side_right;
+  T *B;
+  long long ldb;
+  int nn;  // right-hand-side columns of the canonical (left) problem
+  const int *a1, *a2;
+  cudaStream_t s;
+};
+
+template <typename T>
+int trsm_rec(const TrsmPlan<T> &p, int r0, int len) {
+  if (len <= 0) return 0;
+  if (len <= TB) {
+    long long rs = p.side_right ? p.ldb : 1, cs = p.side_right ? 1 : p.ldb;
+    int grid = (p.nn + TRSM_W - 1) / TRSM_W;
+    trsm_base_kernel<T><<<grid, 32 * TRSM_W, 0, p.s>>>(p.tv, r0, len, p.B, rs, cs, p.nn, p.a1,
+                                                       p.a2);
+    DG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return 0;
+  }
+  const int h = split_point(len);
+  int a0, alen, b0, blen;
+  if (p.tv.lower) { a0 = r0; alen = h; b0 = r0 + h; blen = len - h; }
+  else { a0 = r0 + h; alen = len - h; b0 = r0; blen = h; }
+  DG_TRY(trsm_rec(p, a0, alen));
+  // X[b] -= M[b, a] X[a]
+  const T *Msub;
+  char opM;
+  if (!p.tv.trans) { Msub = p.tv.T_ + (size_t)b0 + (size_t)a0 * p.tv.ld; opM = 'N'; }
+  else { Msub = p.tv.T_ + (size_t)a0 + (size_t)b0 * p.tv.ld; opM = 'T'; }
+  if (!p.side_right) {
+    DG_TRY(gemm_t<T>(opM, 'N', blen, p.nn, alen, T(-1), Msub, p.tv.ld, p.B + a0, p.ldb, T(1),
+                     p.B + b0, p.ldb, TRI_NONE, p.a1, p.s, p.a2));
+  } else {
+    // rows of X' are columns of B: B[:, b] -= B[:, a] * M[b, a]'
+    DG_TRY(gemm_t<T>('N', opM == 'N' ? 'T' : 'N', p.nn, blen, alen, T(-1),
+                     p.B + (size_t)a0 * p.ldb, p.ldb, Msub, p.tv.ld, T(1),
+                     p.B + (size_t)b0 * p.ldb, p.ldb, TRI_NONE, p.a1, p.s, p.a2));
+  }
+  return trsm_rec(p, b0, blen);
+}
+
+template <typename T>
+int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, const T *A,
+           long long lda, T *B, long long ldb, const int *a1, cudaStream_t s, const int *a2) {
+  if (m <= 0 || n <= 0) return 0;
+  const bool right = (side == 'R' || side == 'r');
+  const bool tr = !(transa == 'N' || transa == 'n');
+  TrsmPlan<T> p;
+  p.side_right = right;
+  p.tv.T_ = A;
+  p.tv.ld = lda;
+  p.tv.trans = tr != right;
+  p.tv.lower = (uplo == 'L' || uplo == 'l') != p.tv.trans;
+  p.tv.unit = (diag == 'U' || diag == 'u');
+  p.B = B;
+  p.ldb = ldb;
+  p.nn = right ? m : n;
+  p.a1 = a1;
+  p.a2 = a2;
+  p.s = s;
+  if (alpha != T(1)) {
+    if (sizeof(T) == 8)
+      DG_TRY(scale_f64(m, n, (double)alpha, (double *)B, (int)ldb, a1, s, a2));
+    else
+      DG_TRY(scale_f32(m, n, (float)alpha, (float *)B, ldb, a1, s, a2));
+    if (alpha == T(0)) return 0;
+  }
+  return trsm_rec(p, 0, right ? n : m);
+}
+
+template <typename T>
+int potrf_rec(bool upper, int n, T *A, long long lda, int *info, int off, cudaStream_t s,
+              const int *a1, const int *a2) {
+  if (n <= 0) return 0;
+  if (n <= TB) {
+    potrf_base_kernel<T><<<1, 256, 0, s>>>(upper ? 1 : 0, n, A, lda, info, off, a1, a2);
+    DG_CUDA_TRY(cudaGetLastError());
+    count_launches(1);
+    return 0;
+  }
+  const int n1 = split_point(n), n2 = n - n1;
+  DG_TRY(potrf_rec<T>(upper, n1, A, lda, info, off, s, a1, a2));
+  // the remaining kernels stop when this factorization's info is set, or on
+  // either caller abort word (two words per kernel: info + the first caller
+  // word; the base kernel checks all three)
+  const int *k1 = info, *k2 = a1 ? a1 : a2;
+  T *A22 = A + (size_t)n1 + (size_t)n1 * lda;
+  if (upper) {
+    T *A12 = A + (size_t)n1 * lda;
+    DG_TRY(trsm_t<T>('L', 'U', 'T', 'N', n1, n2, T(1), A, lda, A12, lda, k1, s, k2));
+    DG_TRY(gemm_t<T>('T', 'N', n2, n2, n1, T(-1), A12, lda, A12, lda, T(1), A22, lda, TRI_UPPER,
+                     k1, s, k2));
+  } else {
+    T *A21 = A + n1;
+    DG_TRY(trsm_t<T>('R', 'L', 'T', 'N', n2, n1, T(1), A, lda, A21, lda, k1, s, k2));
+    DG_TRY(gemm_t<T>('N', 'T', n2, n2, n1, T(-1), A21, lda, A21, lda, T(1), A22, lda, TRI_LOWER,
+                     k1, s, k2));
+  }
+  return potrf_rec<T>(upper, n2, A22, lda, info, off + n1, s, a1, a2);
+}
+
+}  // namespace
+
+int trsm_f64(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+             const double *A, int lda, double *B, int ldb, const int *abort_flag,
+             cudaStream_t s, const int *abort2) {
+  return trsm_t<double>(side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, abort_flag, s,
+                        abort2);
+}
+
+int trsm_f32(char side, char uplo, char transa, char diag, int m, int n, float alpha,
+             const float *A, long long lda, float *B, long long ldb, const int *abort_flag,
+             cudaStream_t s, const int *abort2) {
+  return trsm_t<float>(side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, abort_flag, s,
+                       abort2);
+}
+
+int potrf_f64(char uplo, int n, double *A, int lda, int *info_out, int info_offset, cudaStream_t s,
+              const int *abort_flag, const int *abort2) {
+  return potrf_rec<double>(uplo == 'U' || uplo == 'u', n, A, lda, info_out, info_offset, s,
+                           abort_flag, abort2);
+}
+
+int potrf_f32(char uplo, int n, float *A, long long lda, int *info_out, int info_offset,
+              cudaStream_t s, const int *abort_flag, const int *abort2) {
+  return potrf_rec<float>(uplo == 'U' || uplo == 'u', n, A, lda, info_out, info_offset, s,
+                          abort_flag, abort2);
+}
+
+}  // namespace dg

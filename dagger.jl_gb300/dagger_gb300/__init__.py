@@ -12,6 +12,7 @@ from .darray import Blocks, DArray, distribute
 from .datadeps import In, InOut, Out, copyto_, spawn, spawn_datadeps
 from .linalg import (Cholesky, cholesky, cholesky_, gemm_, gemv_, ishermitian, issymmetric,
                      ldiv_, potrf_, syrk_, trsm_, trsv_)
+from .mixed import MixedCholesky, cholesky_mixed
 
 __all__ = [
     "Blocks", "DArray", "distribute", "Cholesky", "cholesky", "cholesky_", "ldiv_",

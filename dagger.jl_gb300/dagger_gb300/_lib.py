@@ -44,6 +44,24 @@ class DgTask(ctypes.Structure):
     ]
 
 
+class DgMixedStats(ctypes.Structure):
+    _fields_ = [("n", c_int), ("nb", c_int), ("precision", c_int), ("info", c_int),
+                ("retries", c_int), ("factor_ms", ctypes.c_float), ("norm_inf", c_double),
+                ("device_bytes", ctypes.c_longlong)]
+
+
+class DgIrOpts(ctypes.Structure):
+    _fields_ = [("tol", c_double), ("max_iter", c_int), ("gmres", c_int), ("restart", c_int),
+                ("gmres_inner_tol", c_double)]
+
+
+class DgIrReport(ctypes.Structure):
+    _fields_ = [("iterations", c_int), ("gmres_iterations", c_int), ("used_gmres", c_int),
+                ("converged", c_int), ("backward_error", c_double), ("solve_ms", ctypes.c_float)]
+
+
+DG_PREC = {"bf16": 1, "bf16x3": 3, "fp16": 11, "fp16x3": 13, "fp32": 32}
+
 # name -> (restype, argtypes); every symbol include/dagger_gb300.h declares.
 SIGNATURES = {
     "dg_version": (ctypes.c_char_p, []),
@@ -73,6 +91,21 @@ SIGNATURES = {
     "dg_set_f64_engine": (c_int, [c_int]),
     "dg_ishermitian_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
     "dg_chkfinite_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
+    "dg_probe_fp64_fma_tflops": (c_int, [c_int, ctypes.POINTER(c_double), c_void_p]),
+    "dg_mixed_factor": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_void_p, c_int,
+                                c_void_p]),
+    "dg_mixed_solve": (c_int, [c_void_p, c_int, c_dp, c_int, c_dp, c_int,
+                               ctypes.POINTER(DgIrOpts), ctypes.POINTER(DgIrReport), c_void_p]),
+    "dg_mixed_info": (c_int, [c_void_p, ctypes.POINTER(DgMixedStats)]),
+    "dg_mixed_destroy": (None, [c_void_p]),
+    "dg_gemm_tc_tn": (c_int, [c_int, c_int, c_int, c_int, c_int, c_dp, c_dp, c_int, c_dp, c_dp,
+                              c_int, ctypes.c_float, ctypes.c_float, c_dp, c_int, c_int, c_dp,
+                              c_void_p]),
+    "dg_batched_potrs": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_void_p,
+                                 c_void_p, c_void_p, c_int, c_double, c_int,
+                                 ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int),
+                                 ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_float),
+                                 c_void_p]),
 }
 
 _lib = None

@@ -181,6 +181,92 @@ int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream);
  * (mma.sync.m8n8k4.f64).  Returns the previous setting. */
 int dg_set_f64_engine(int engine);
 
+/* ---------------------------------------------------------------------------
+ * Mixed-precision form (no counterpart in the reference: a faster path beside
+ * the FP64 drop-in, reached from the same DArray tiles).  The factor of the
+ * diagonally scaled matrix is computed with 16-bit tensor-core trailing
+ * updates (tcgen05, FP32 accumulation), FP32 diagonal blocks with an FP64
+ * retry on a failed pivot, and FP32 panel solves; solutions are refined in
+ * FP64 (iterative refinement, GMRES-IR when it stalls) to a normwise backward
+ * error tolerance.  The caller's FP64 tiles must stay valid while the handle
+ * is used (they give the FP64 residuals).
+ * ------------------------------------------------------------------------- */
+
+#define DG_PREC_BF16 1    /* BF16 operands                                   */
+#define DG_PREC_BF16X3 3  /* BF16 hi/lo split, three products               */
+#define DG_PREC_FP16 11   /* FP16 operands, per-panel power-of-two scaling   */
+#define DG_PREC_FP16X3 13 /* FP16 hi/lo split with per-panel scaling        */
+#define DG_PREC_FP32 32   /* FP32 CUDA-core trailing updates                */
+
+typedef struct dg_mixed dg_mixed;
+
+typedef struct dg_mixed_stats {
+  int n, nb, precision;
+  int info;              /* 0, or the order of the first non-positive pivot */
+  int retries;           /* diagonal blocks refactored in FP64              */
+  float factor_ms;       /* device time of the factorization                */
+  double norm_inf;       /* ||A||_inf                                       */
+  long long device_bytes;
+} dg_mixed_stats;
+
+typedef struct dg_ir_opts {
+  double tol;            /* normwise backward error target (default 1e-12)  */
+  int max_iter;          /* outer refinement steps (default 30)             */
+  int gmres;             /* 0 = switch when refinement stalls, 1 = always,
+                            2 = never                                       */
+  int restart;           /* GMRES cycle length (default 30)                 */
+  double gmres_inner_tol;/* relative residual of each GMRES cycle (1e-4)    */
+} dg_ir_opts;
+
+typedef struct dg_ir_report {
+  int iterations, gmres_iterations, used_gmres, converged;
+  double backward_error; /* worst column                                    */
+  float solve_ms;
+} dg_ir_report;
+
+/* Factors the n x n FP64 tile grid (same layout as dg_cholesky_tiled; nb a
+ * multiple of 64).  Returns 0, the info of a failed pivot (> 0, the handle is
+ * still returned for inspection), or a negative status. */
+int dg_mixed_factor(dg_mixed **out, int n, int nb, double *const *tiles, int precision,
+                    void *stream);
+
+/* X = A^-1 B (FP64, device, column-major) by refinement with the factor. */
+int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int ldb, double *X, int ldx,
+                   const dg_ir_opts *opts, dg_ir_report *report, void *stream);
+int dg_mixed_info(const dg_mixed *f, dg_mixed_stats *stats);
+void dg_mixed_destroy(dg_mixed *f);
+
+/* The tensor-core building block: C = alpha A'B + beta C with 16-bit K-major
+ * operands (A k x m and B k x n column-major, BF16 or FP16 when fp16 = 1),
+ * terms = 1 or 3 (hi/lo split), FP32 C.  k, lda, ldb multiples of 8. */
+int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const void *a_hi, const void *a_lo,
+                  int lda, const void *b_hi, const void *b_lo, int ldb, float alpha, float beta,
+                  float *C, int ldc, int bn, int *status, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Batched persistent launch (no counterpart in the reference, which would
+ * spawn one datadeps region per system): `count` independent SPD systems of
+ * order n[i] <= 1024 with nrhs[i] <= 8 right-hand sides, all factored and
+ * solved in ONE launch.  A[i] (n x n, column-major, ld n) is overwritten by
+ * its lower Cholesky factor in mode 0 (FP64) and left intact in mode 1 (FP32
+ * factor + FP64 iterative refinement to normwise backward error `tol`, at
+ * most max_iter steps).  B[i], X[i]: n x nrhs, ld n.  bucket_w (5 entries,
+ * for n <= 64, 128, 256, 512, 1024) gives each size bucket's panel width (16
+ * or 32; NULL = 32), ctas_per_sm the persistent grid per SM.  info (2*count
+ * ints, may be NULL) receives each system's pivot info and refinement steps,
+ * berr (count doubles, may be NULL) its backward error (mode 1).  Returns 0,
+ * or 1 + the index of the first system whose factorization failed.
+ * ------------------------------------------------------------------------- */
+int dg_batched_potrs(int count, const int *n, const int *nrhs, double *const *A,
+                     const double *const *B, double *const *X, int mode, double tol, int max_iter,
+                     const int *bucket_w, int ctas_per_sm, int *info, double *berr,
+                     float *elapsed_ms, void *stream);
+
+/* Measures the device's FP64 fused-multiply-add throughput (TFLOP/s) with
+ * independent FMA chains on every SM; the benchmark's FP64 roofline.  No
+ * counterpart in the reference (measurement utility). */
+int dg_probe_fp64_fma_tflops(int iters, double *tflops, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
