@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--mixed-precision", default="auto")
     ap.add_argument("--batch-count", type=int, default=10000)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-count", type=int, default=60)
+    ap.add_argument("--serve-rates", default="10,40")
     ap.add_argument("--spd", default="spectrum", choices=["spectrum", "uniform"],
                     help="input construction; 'uniform' (B B'/N + N I, matmul only) is for "
                          "profilers that cannot load the QR's solver library")
@@ -426,6 +429,9 @@ def run_ours(args):
     batched = None
     if not args.no_batched:
         batched = bench_batched(args, d, dev, rank)
+    serving = None
+    if not args.no_serving and rank == 0:
+        serving = bench_serving(args, dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -446,7 +452,7 @@ def run_ours(args):
                         "factor_residual_probe": fres},
            "roofline": roof, "gpu_launches": int(launches),
            "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
-           "mixed": mixed, "batched": batched}
+           "mixed": mixed, "batched": batched, "serving": serving}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -537,6 +543,45 @@ def bench_batched(args, d, dev, rank):
             entry["backward_error_max"] = max(rep["backward_error"])
             entry["ir_iterations_max"] = max(rep["iterations"])
         out[mode] = entry
+    return out
+
+
+def bench_serving(args, dev):
+    """Serving loop: Poisson arrivals at swept rates, n log-uniform on [64,
+    16384], kappa log-uniform on [1e2, 1e6], 1-64 RHS, 30% of requests
+    reusing a resident factor, 150 GB HBM admission budget."""
+    import torch
+    from dagger_gb300.serving import MatrixFactory, Server, latency_stats, make_workload, run_workload
+    fac = MatrixFactory(dev, args.seed)
+    out = {"budget_gb": 150, "requests_per_rate": args.serve_count, "slots": 8, "rates": []}
+    for rate in [float(x) for x in args.serve_rates.split(",") if x]:
+        work = make_workload(args.serve_count, rate, seed=args.seed + int(rate), factory=fac)
+        torch.cuda.synchronize()
+        srv = Server(budget_bytes=150e9, slots=8)
+        wall = run_workload(srv, work, realtime=True)
+        srv.close()
+        reqs = [r for _, r in work]
+        st = latency_stats(reqs)
+        worst = 0.0
+        fl = 0.0
+        for r in reqs:
+            if r.error is not None:
+                continue
+            R = r.B - r.A @ r.X
+            nA = r.A.abs().sum(dim=1).max()
+            be = (R.abs().amax(dim=0) / (nA * r.X.abs().amax(dim=0) + r.B.abs().amax(dim=0))).max()
+            worst = max(worst, float(be.item()))
+            fl += 2.0 * r.n * r.n * r.nrhs
+        factored = {r.matrix_id: r.n for r in reqs if r.error is None}
+        fl += sum(n ** 3 / 3.0 for n in factored.values())
+        out["rates"].append({"rate_per_s": rate, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                             "mean_ms": st.get("mean_ms"), "completed": st["count"],
+                             "rejected": sum(1 for r in reqs if r.error is not None),
+                             "throughput_req_per_s": st["count"] / wall,
+                             "throughput_TFLOP_s": fl / wall / 1e12,
+                             "backward_error_max": worst, "wall_s": wall})
+        del work, reqs
+        torch.cuda.empty_cache()
     return out
 
 

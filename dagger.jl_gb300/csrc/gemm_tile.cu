@@ -160,10 +160,29 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) gemm_fma(GemmArgs g) {
     if (kt + 1 < nk) ld.store(g, As[cur ^ 1], Bs[cur ^ 1], tid);
     __syncthreads();
   }
+  // epilogue: all reads of C are issued before any write, so the TM x TN
+  // read-modify-writes overlap instead of serialising on possible aliasing
+  T old[TM][TN];
 #pragma unroll
   for (int r = 0; r < TM; r++)
 #pragma unroll
-    for (int c = 0; c < TN; c++) store_c<T>(g, row0 + tx + NX * r, col0 + ty + NY * c, acc[r][c]);
+    for (int c = 0; c < TN; c++) {
+      const int i = row0 + tx + NX * r, j = col0 + ty + NY * c;
+      old[r][c] = (g.beta != 0.0 && i < g.m && j < g.n)
+                      ? ((const T *)g.C)[(size_t)i + (size_t)j * g.ldc] : T(0);
+    }
+#pragma unroll
+  for (int r = 0; r < TM; r++)
+#pragma unroll
+    for (int c = 0; c < TN; c++) {
+      const int i = row0 + tx + NX * r, j = col0 + ty + NY * c;
+      if (i >= g.m || j >= g.n) continue;
+      if (g.tri == TRI_UPPER && i > j) continue;
+      if (g.tri == TRI_LOWER && i < j) continue;
+      T v = T(g.alpha) * acc[r][c];
+      if (g.beta != 0.0) v = fma(T(g.beta), old[r][c], v);
+      ((T *)g.C)[(size_t)i + (size_t)j * g.ldc] = v;
+    }
 }
 
 // DMMA engine (FP64 only): 4 warps in a 2 x 2 grid, warp tile 32 x 32 =

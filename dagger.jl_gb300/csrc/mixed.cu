@@ -55,6 +55,8 @@ struct dg_mixed {
   size_t bytes = 0;
   int info = 0, retries = 0;
   float factor_ms = 0.f;
+  cudaStream_t stream = nullptr;  // allocations are stream-ordered on this stream
+  double shift = 0.0;             // added to the unit diagonal of S A S before factoring
 };
 
 namespace dg {
@@ -102,7 +104,7 @@ __host__ __device__ inline long long panel_base(long long r, long long n, long l
 // W = float(S A S) on the upper row panels; the strict lower part of each
 // diagonal block and the padding rows of a ragged last panel are zero.
 __global__ void pack_kernel(const double *const *tiles, int n, int nb, int mt, const double *s,
-                            float *W) {
+                            float *W, double shift) {
   const int r = blockIdx.y;
   const long long w = n - (long long)r * nb;
   const long long total = (long long)nb * w;
@@ -117,7 +119,7 @@ __global__ void pack_kernel(const double *const *tiles, int n, int nb, int mt, c
     if (p < rows_r && i <= j) {
       const int tj = (int)(j / nb), cj = (int)(j - (long long)tj * nb);
       const double a = tile_ptr(tiles, mt, r, tj)[p + (size_t)cj * rows_r];
-      v = (float)(s[i] * a * s[j]);
+      v = (float)(s[i] * a * s[j] + (i == j ? shift : 0.0));
     }
     P[e] = v;
   }
@@ -268,7 +270,7 @@ int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
   DG_CUDA_TRY(cudaMemsetAsync(bad, 0x7f, sizeof(int), s));
   diag_scale_kernel<<<grid_for(n), 256, 0, s>>>(f->tiles_dev, n, nb, mt, f->s, bad);
   pack_kernel<<<dim3(std::max(1, std::min(1024, (int)((long long)nb * n / 256 + 1))), mt), 256, 0,
-                s>>>(f->tiles_dev, n, nb, mt, f->s, f->W);
+                s>>>(f->tiles_dev, n, nb, mt, f->s, f->W, f->shift);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(2);
   const int prec = f->precision;
@@ -359,8 +361,16 @@ int mixed_tri_solve(const dg_mixed *f, float *Z, long long ldz, int r, cudaStrea
 
 using dg::grid_for;
 
+extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *tiles,
+                                  int precision, double shift, void *stream);
+
 extern "C" int dg_mixed_factor(dg_mixed **out, int n, int nb, double *const *tiles, int precision,
                                void *stream) {
+  return dg_mixed_factor_ex(out, n, nb, tiles, precision, 0.0, stream);
+}
+
+extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *tiles,
+                                  int precision, double shift, void *stream) {
   DG_CHECK_ARG(out != nullptr, 1);
   DG_CHECK_ARG(n > 0, 2);
   DG_CHECK_ARG(nb >= 64 && nb % 64 == 0, 3);
@@ -369,9 +379,11 @@ extern "C" int dg_mixed_factor(dg_mixed **out, int n, int nb, double *const *til
                    precision == DG_PREC_FP16 || precision == DG_PREC_FP16X3 ||
                    precision == DG_PREC_FP32,
                5);
+  DG_CHECK_ARG(shift >= 0.0, 6);
   cudaStream_t s = (cudaStream_t)stream;
   dg_mixed *f = new dg_mixed();
   f->n = n; f->nb = nb; f->mt = (n + nb - 1) / nb; f->precision = precision;
+  f->shift = shift;
   cudaGetDevice(&f->dev);
   const int mt = f->mt;
   const long long wsize = dg::panel_base(mt, n, nb) + (long long)nb * nb;
@@ -393,8 +405,9 @@ extern "C" int dg_mixed_factor(dg_mixed **out, int n, int nb, double *const *til
       {(void **)&f->alpha_dev, sizeof(float) * (size_t)mt},
       {(void **)&f->words, sizeof(int) * (size_t)(3 + mt)},
   };
+  f->stream = s;
   for (auto &a : allocs) {
-    if (cudaMalloc(a.p, a.bytes) != cudaSuccess) {
+    if (cudaMallocAsync(a.p, a.bytes, s) != cudaSuccess) {
       cudaGetLastError();
       dg_set_last_error(__FILE__, __LINE__, "device allocation for the mixed factor failed");
       return fail(DG_ERR_NOMEM);
@@ -452,7 +465,7 @@ extern "C" void dg_mixed_destroy(dg_mixed *f) {
   void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
                 f->panel_max, f->alpha_dev, f->words};
   for (void *p : ps)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, f->stream);  // stream-ordered: no device-wide synchronisation
   delete f;
 }
 
@@ -467,6 +480,7 @@ extern "C" int dg_mixed_info(const dg_mixed *f, dg_mixed_stats *st) {
   st->factor_ms = f->factor_ms;
   st->norm_inf = f->normA;
   st->device_bytes = (long long)f->bytes;
+  st->shift = f->shift;
   return 0;
 }
 

@@ -567,6 +567,55 @@ extern "C" int dg_finalize(void) {
 
 extern "C" long long dg_kernel_launches(void) { return dg::launches(); }
 
+extern "C" int dg_set_device(int device) {
+  DG_CUDA_TRY(cudaSetDevice(device));
+  return 0;
+}
+
+extern "C" int dg_device_alloc(size_t bytes, void **out) {
+  DG_CHECK_ARG(out != nullptr, 2);
+  *out = nullptr;
+  if (bytes == 0) return 0;
+  if (cudaMalloc(out, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    dg_set_last_error(__FILE__, __LINE__, "cudaMalloc failed");
+    return DG_ERR_NOMEM;
+  }
+  return 0;
+}
+
+extern "C" int dg_device_free(void *p) {
+  if (p) DG_CUDA_TRY(cudaFree(p));
+  return 0;
+}
+
+extern "C" int dg_copy(void *dst, const void *src, size_t bytes, int kind, void *stream) {
+  DG_CHECK_ARG(kind >= 0 && kind <= 2, 4);
+  static const cudaMemcpyKind kinds[3] = {cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost,
+                                          cudaMemcpyDeviceToDevice};
+  if (bytes == 0) return 0;
+  DG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, kinds[kind], (cudaStream_t)stream));
+  return 0;
+}
+
+extern "C" int dg_stream_create(void **out) {
+  DG_CHECK_ARG(out != nullptr, 1);
+  cudaStream_t s;
+  DG_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *out = (void *)s;
+  return 0;
+}
+
+extern "C" int dg_stream_destroy(void *stream) {
+  if (stream) DG_CUDA_TRY(cudaStreamDestroy((cudaStream_t)stream));
+  return 0;
+}
+
+extern "C" int dg_stream_synchronize(void *stream) {
+  DG_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return 0;
+}
+
 extern "C" int dg_set_f64_engine(int engine) {
   int old = dg::get_f64_engine();
   dg::set_f64_engine(engine);

@@ -265,30 +265,37 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
       float v[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
       if (row >= p.m) continue;
+      // Each lane owns one row; the 32 columns of the chunk are 32 separate
+      // coalesced warp accesses.  All reads of C are issued before any write
+      // so the read-modify-writes overlap instead of serialising.
+      float *cp0;
+      long long cstride;
       if (p.layout == 0) {
-#pragma unroll
-        for (int c = 0; c < 32; c++) {
-          const int col = j0 + c0 + c;
-          if (col >= p.n) break;
-          if (p.upper && row > col) continue;
-          float *cp = p.c + (size_t)row + (size_t)col * p.ldc;
-          *cp = p.beta == 0.f ? alpha * v[c] : fmaf(alpha, v[c], p.beta * *cp);
-        }
+        cp0 = p.c + (size_t)row + (size_t)(j0 + c0) * p.ldc;
+        cstride = p.ldc;
       } else {
         // packed upper row panels; global indices shifted by the trailing offset
         const long long gi = p.off + row;
         const long long r = gi / p.nb;
         const long long base = (long long)p.nb * (r * p.ntot - p.nb * r * (r - 1) / 2);
-        float *rowp = p.c + base + (gi - r * p.nb);
+        cp0 = p.c + base + (gi - r * p.nb) + (p.off + j0 + c0 - r * p.nb) * p.nb;
+        cstride = p.nb;
+      }
+      const bool upper = p.layout == 1 || p.upper;
+      const bool read_c = p.layout == 1 || p.beta != 0.f;
+      float old[32];
 #pragma unroll
-        for (int c = 0; c < 32; c++) {
-          const int col = j0 + c0 + c;
-          if (col >= p.n) break;
-          if (row > col) continue;
-          const long long gj = p.off + col;
-          float *cp = rowp + (gj - r * p.nb) * p.nb;
-          *cp = fmaf(alpha, v[c], *cp);
-        }
+      for (int c = 0; c < 32; c++) {
+        const int col = j0 + c0 + c;
+        const bool in = col < p.n && !(upper && row > col);
+        old[c] = (in && read_c) ? cp0[(size_t)c * cstride] : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        const int col = j0 + c0 + c;
+        if (col >= p.n || (upper && row > col)) continue;
+        const float b = p.layout == 1 ? 1.f : p.beta;
+        cp0[(size_t)c * cstride] = read_c ? fmaf(alpha, v[c], b * old[c]) : alpha * v[c];
       }
     }
   }

@@ -47,7 +47,7 @@ class DgTask(ctypes.Structure):
 class DgMixedStats(ctypes.Structure):
     _fields_ = [("n", c_int), ("nb", c_int), ("precision", c_int), ("info", c_int),
                 ("retries", c_int), ("factor_ms", ctypes.c_float), ("norm_inf", c_double),
-                ("device_bytes", ctypes.c_longlong)]
+                ("device_bytes", ctypes.c_longlong), ("shift", c_double)]
 
 
 class DgIrOpts(ctypes.Structure):
@@ -68,6 +68,13 @@ SIGNATURES = {
     "dg_last_error": (ctypes.c_char_p, []),
     "dg_finalize": (c_int, []),
     "dg_kernel_launches": (ctypes.c_longlong, []),
+    "dg_set_device": (c_int, [c_int]),
+    "dg_device_alloc": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
+    "dg_device_free": (c_int, [c_void_p]),
+    "dg_copy": (c_int, [c_void_p, c_void_p, ctypes.c_size_t, c_int, c_void_p]),
+    "dg_stream_create": (c_int, [ctypes.POINTER(c_void_p)]),
+    "dg_stream_destroy": (c_int, [c_void_p]),
+    "dg_stream_synchronize": (c_int, [c_void_p]),
     "dg_potrf": (c_int, [c_char, c_int, c_dp, c_int, ctypes.POINTER(c_int), c_void_p]),
     "dg_potrf_async": (c_int, [c_char, c_int, c_dp, c_int, c_dp, c_void_p]),
     "dg_trsm": (c_int, [c_char, c_char, c_char, c_char, c_int, c_int, c_double, c_dp, c_int,
@@ -94,6 +101,8 @@ SIGNATURES = {
     "dg_probe_fp64_fma_tflops": (c_int, [c_int, ctypes.POINTER(c_double), c_void_p]),
     "dg_mixed_factor": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_void_p, c_int,
                                 c_void_p]),
+    "dg_mixed_factor_ex": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_void_p, c_int,
+                                   c_double, c_void_p]),
     "dg_mixed_solve": (c_int, [c_void_p, c_int, c_dp, c_int, c_dp, c_int,
                                ctypes.POINTER(DgIrOpts), ctypes.POINTER(DgIrReport), c_void_p]),
     "dg_mixed_info": (c_int, [c_void_p, ctypes.POINTER(DgMixedStats)]),

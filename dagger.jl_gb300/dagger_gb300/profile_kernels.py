@@ -1,0 +1,93 @@
+"""Launches one hot kernel of the library a few times on a fixed workload, so
+a profiler can capture exactly that kernel (ncu -k regex:<name> -c N).
+
+    python -m dagger_gb300.profile_kernels gemm_f64   [--nb 1024] [--reps 4]
+    python -m dagger_gb300.profile_kernels tc_gemm    [--m 8192] [--k 1024] [--terms 3]
+    python -m dagger_gb300.profile_kernels trsm_f64   [--nb 1024]
+    python -m dagger_gb300.profile_kernels batched    [--count 2000]
+
+gemm_f64   the FP64 trailing-update tile GEMM of the plain path,
+           C(nb x nb) -= A' B with nb x nb tiles (2 nb^3 flops per launch)
+tc_gemm    the tcgen05 trailing SYRK/GEMM of the mixed form on an m x m
+           output with K = k (2 m^2 k flops x terms per launch, BF16)
+trsm_f64   the panel TRSM of one nb x nb tile
+batched    the persistent batched launch on `count` systems, n in [32, 1024]
+Each prints the per-launch time measured with CUDA events.
+"""
+from __future__ import annotations
+
+import argparse
+
+import torch
+
+from . import _lib
+from .linalg import _stream
+
+
+def _time(fn, reps):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched"])
+    ap.add_argument("--nb", type=int, default=1024)
+    ap.add_argument("--m", type=int, default=8192)
+    ap.add_argument("--k", type=int, default=1024)
+    ap.add_argument("--terms", type=int, default=3)
+    ap.add_argument("--count", type=int, default=2000)
+    ap.add_argument("--reps", type=int, default=4)
+    a = ap.parse_args(argv)
+    L = _lib.lib()
+    s = _stream(None)
+    dev = torch.device("cuda")
+    if a.kernel == "gemm_f64":
+        nb = a.nb
+        A, B, C = (torch.randn(nb, nb, dtype=torch.float64, device=dev) for _ in range(3))
+        ms = _time(lambda: L.dg_gemm(b'T', b'N', nb, nb, nb, -1.0, A.data_ptr(), nb, B.data_ptr(),
+                                     nb, 1.0, C.data_ptr(), nb, s), a.reps)
+        print(f"gemm_f64 {nb}^3: {ms * 1e3:.1f} us/launch, {2 * nb ** 3 / ms / 1e9:.3f} TFLOP/s")
+    elif a.kernel == "tc_gemm":
+        m, k = a.m, a.k
+        P = torch.randn(m, k, device=dev)
+        hi = P.bfloat16()
+        lo = (P - hi.float()).bfloat16()
+        C = torch.zeros(m, m, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        ms = _time(lambda: L.dg_gemm_tc_tn(m, m, k, a.terms, 0, hi.data_ptr(), lo.data_ptr(), k,
+                                           hi.data_ptr(), lo.data_ptr(), k, -1.0, 1.0,
+                                           C.data_ptr(), m, 128, st.data_ptr(), s), a.reps)
+        fl = 2.0 * m * m * k * a.terms
+        print(f"tc_gemm m={m} k={k} terms={a.terms}: {ms * 1e3:.1f} us/launch, "
+              f"{fl / ms / 1e9:.1f} TFLOP/s")
+    elif a.kernel == "trsm_f64":
+        nb = a.nb
+        T = torch.randn(nb, nb, dtype=torch.float64, device=dev) * 0.01
+        T.diagonal().add_(1.0)
+        B = torch.randn(nb, nb, dtype=torch.float64, device=dev)
+        ms = _time(lambda: L.dg_trsm(b'L', b'U', b'T', b'N', nb, nb, 1.0, T.data_ptr(), nb,
+                                     B.data_ptr(), nb, s), a.reps)
+        print(f"trsm_f64 {nb}^2 x {nb}: {ms * 1e3:.1f} us/call, {nb ** 3 / ms / 1e9:.3f} TFLOP/s")
+    else:
+        from .autotune import sample_batch
+        from .batched import PackedBatch, batched_solve_packed, flops
+        As, Bs = sample_batch(a.count, 32, 1024, seed=1, device=dev)
+        P = PackedBatch(As, Bs)
+        for mode in ("fp64", "fp32_ir"):
+            P.load_again()
+            rep = batched_solve_packed(P, mode)
+            fl = flops([x.shape[0] for x in As], [x.shape[1] for x in Bs])
+            print(f"batched {mode} count={a.count}: {rep['elapsed_ms']:.1f} ms, "
+                  f"{fl / rep['elapsed_ms'] / 1e9:.3f} TFLOP/s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+# GB300Ext: a Dagger.jl package extension binding libdaggergb300 through its
+# C ABI (include/dagger_gb300.h), with no CUDA.jl, CUBLAS or CUSOLVER on the
+# Cholesky path.  It follows the shape of Dagger's own CUDA extension
+# (ext/CUDAExt.jl:25-65 processor and memory space, :131-154 moves,
+# :309-327 execute!, :329-348 the BLAS/LAPACK substitution table):
+#
+#   * GB300Array{T,N}: a device buffer allocated through dg_device_alloc;
+#   * GB300Proc / GB300MemorySpace: the processor and memory space Dagger's
+#     scheduler and datadeps planner place tasks and chunks on;
+#   * Dagger.move(::CPUProc, ::GB300Proc, ::typeof(f)) for LAPACK.potrf!,
+#     BLAS.trsm!, syrk!, gemm!, trsv!, gemv!: each returns a ccall wrapper, so
+#     Dagger's unchanged _chol! (src/array/cholesky.jl) and trsm!/trsv!
+#     (src/array/trsm.jl) run their tile tasks on the GB300 kernels;
+#   * cholesky_gb300! / ldiv_gb300!: the whole datadeps region of a DArray
+#     handed to the library in one call (dg_cholesky_tiled /
+#     dg_cholesky_solve_tiled), issued as one cached multi-stream CUDA graph.
+#
+# This file is not exercised in this repository's tests (no Julia toolchain
+# here); the Python package dagger_gb300 drives the same ABI and is tested.
+module GB300Ext
+
+using Dagger
+using Distributed
+using LinearAlgebra
+import LinearAlgebra: BLAS, LAPACK
+
+const libdg = get(ENV, "DAGGER_GB300_LIB",
+                  joinpath(@__DIR__, "..", "dagger_gb300", "libdaggergb300.so"))
+
+dgcheck(rc::Integer) = rc < 0 ?
+    error("libdaggergb300 error $rc: " * unsafe_string(ccall((:dg_last_error, libdg), Cstring, ()))) : rc
+
+# ---------------------------------------------------------------------------
+# device arrays
+# ---------------------------------------------------------------------------
+mutable struct GB300Array{T,N} <: DenseArray{T,N}
+    ptr::Ptr{T}
+    dims::NTuple{N,Int}
+    device::Int
+    function GB300Array{T,N}(::UndefInitializer, dims::NTuple{N,Int}; device::Int=0) where {T,N}
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        dgcheck(ccall((:dg_set_device, libdg), Cint, (Cint,), device))
+        dgcheck(ccall((:dg_device_alloc, libdg), Cint, (Csize_t, Ptr{Ptr{Cvoid}}),
+                      sizeof(T) * prod(dims), out))
+        x = new{T,N}(Ptr{T}(out[]), dims, device)
+        finalizer(x) do a
+            ccall((:dg_device_free, libdg), Cint, (Ptr{Cvoid},), a.ptr)
+        end
+        return x
+    end
+end
+Base.size(x::GB300Array) = x.dims
+Base.pointer(x::GB300Array) = x.ptr
+Base.unsafe_convert(::Type{Ptr{T}}, x::GB300Array{T}) where T = x.ptr
+Base.strides(x::GB300Array{T,2}) where T = (1, x.dims[1])
+Base.stride(x::GB300Array{T,2}, i::Int) where T = i == 1 ? 1 : x.dims[1]
+
+const STREAMS = Dict{Int,Ptr{Cvoid}}()
+function stream(device::Int)
+    get!(STREAMS, device) do
+        s = Ref{Ptr{Cvoid}}(C_NULL)
+        dgcheck(ccall((:dg_stream_create, libdg), Cint, (Ptr{Ptr{Cvoid}},), s))
+        s[]
+    end
+end
+synchronize(device::Int) = dgcheck(ccall((:dg_stream_synchronize, libdg), Cint, (Ptr{Cvoid},), stream(device)))
+
+function GB300Array(x::Array{T,N}; device::Int=0) where {T,N}
+    y = GB300Array{T,N}(undef, size(x); device)
+    dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
+                  y.ptr, pointer(x), sizeof(x), 0, stream(device)))
+    synchronize(device)
+    return y
+end
+function Base.Array(x::GB300Array{T,N}) where {T,N}
+    y = Array{T,N}(undef, x.dims)
+    dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
+                  pointer(y), x.ptr, sizeof(y), 1, stream(x.device)))
+    synchronize(x.device)
+    return y
+end
+
+# ---------------------------------------------------------------------------
+# processor and memory space (ext/CUDAExt.jl:25-65)
+# ---------------------------------------------------------------------------
+struct GB300Proc <: Dagger.Processor
+    owner::Int
+    device::Int
+end
+Dagger.get_parent(proc::GB300Proc) = Dagger.OSProc(proc.owner)
+Dagger.root_worker_id(proc::GB300Proc) = proc.owner
+Dagger.short_name(proc::GB300Proc) = "W: $(proc.owner), GB300: $(proc.device)"
+Dagger.@gpuproc(GB300Proc, GB300Array)
+
+struct GB300MemorySpace <: Dagger.MemorySpace
+    owner::Int
+    device::Int
+end
+Dagger.root_worker_id(space::GB300MemorySpace) = space.owner
+Dagger.memory_space(x::GB300Array) = GB300MemorySpace(myid(), x.device)
+Dagger.memory_spaces(proc::GB300Proc) = Set([GB300MemorySpace(proc.owner, proc.device)])
+Dagger.processors(space::GB300MemorySpace) = Set([GB300Proc(space.owner, space.device)])
+function Dagger.aliasing(x::GB300Array{T}) where T
+    space = Dagger.memory_space(x)
+    rptr = Dagger.RemotePtr{Cvoid}(UInt64(x.ptr), space)
+    return Dagger.ContiguousAliasing(Dagger.MemorySpan{GB300MemorySpace}(rptr, sizeof(T) * length(x)))
+end
+Dagger.unsafe_free!(x::GB300Array) = (finalize(x); nothing)
+
+# moves between host and device (ext/CUDAExt.jl:131-154)
+function Dagger.move!(::GB300MemorySpace, ::Dagger.CPURAMMemorySpace, to::GB300Array{T}, from::Array{T}) where T
+    dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
+                  to.ptr, pointer(from), sizeof(from), 0, stream(to.device)))
+    return
+end
+function Dagger.move!(::Dagger.CPURAMMemorySpace, ::GB300MemorySpace, to::Array{T}, from::GB300Array{T}) where T
+    dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
+                  pointer(to), from.ptr, sizeof(to), 1, stream(from.device)))
+    synchronize(from.device)
+    return
+end
+Dagger.move(::Dagger.CPUProc, to_proc::GB300Proc, x::Array) = GB300Array(x; device=to_proc.device)
+Dagger.move(::GB300Proc, ::Dagger.CPUProc, x::GB300Array) = Array(x)
+
+# execute! on the device's stream (ext/CUDAExt.jl:309-327); kernels are
+# stream-ordered, so no synchronisation here
+function Dagger.execute!(proc::GB300Proc, f, args...; kwargs...)
+    dgcheck(ccall((:dg_set_device, libdg), Cint, (Cint,), proc.device))
+    return f(args...; kwargs...)
+end
+
+# ---------------------------------------------------------------------------
+# tile calls: the substitution table (ext/CUDAExt.jl:329-348)
+# ---------------------------------------------------------------------------
+ld(A::GB300Array{T,2}) where T = max(1, size(A, 1))
+
+function gb300_potrf!(uplo::AbstractChar, A::GB300Array{Float64,2})
+    info = Ref{Cint}(0)
+    rc = ccall((:dg_potrf, libdg), Cint, (Cchar, Cint, Ptr{Float64}, Cint, Ptr{Cint}, Ptr{Cvoid}),
+               uplo, size(A, 1), A, ld(A), info, stream(A.device))
+    dgcheck(rc)
+    return A, Int(info[])
+end
+function gb300_trsm!(side, uplo, transa, diag, alpha::Float64, A::GB300Array{Float64,2}, B::GB300Array{Float64,2})
+    dgcheck(ccall((:dg_trsm, libdg), Cint,
+                  (Cchar, Cchar, Cchar, Cchar, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ptr{Cvoid}),
+                  side, uplo, transa, diag, size(B, 1), size(B, 2), alpha, A, ld(A), B, ld(B), stream(B.device)))
+    return B
+end
+function gb300_syrk!(uplo, trans, alpha::Float64, A::GB300Array{Float64,2}, beta::Float64, C::GB300Array{Float64,2})
+    k = trans == 'N' ? size(A, 2) : size(A, 1)
+    dgcheck(ccall((:dg_syrk, libdg), Cint,
+                  (Cchar, Cchar, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Cvoid}),
+                  uplo, trans, size(C, 1), k, alpha, A, ld(A), beta, C, ld(C), stream(C.device)))
+    return C
+end
+function gb300_gemm!(ta, tb, alpha::Float64, A::GB300Array{Float64,2}, B::GB300Array{Float64,2}, beta::Float64, C::GB300Array{Float64,2})
+    k = ta == 'N' ? size(A, 2) : size(A, 1)
+    dgcheck(ccall((:dg_gemm, libdg), Cint,
+                  (Cchar, Cchar, Cint, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Cvoid}),
+                  ta, tb, size(C, 1), size(C, 2), k, alpha, A, ld(A), B, ld(B), beta, C, ld(C), stream(C.device)))
+    return C
+end
+function gb300_trsv!(uplo, trans, diag, A::GB300Array{Float64,2}, x::GB300Array{Float64,1})
+    dgcheck(ccall((:dg_trsv, libdg), Cint, (Cchar, Cchar, Cchar, Cint, Ptr{Float64}, Cint, Ptr{Float64}, Ptr{Cvoid}),
+                  uplo, trans, diag, size(A, 1), A, ld(A), x, stream(x.device)))
+    return x
+end
+function gb300_gemv!(trans, alpha::Float64, A::GB300Array{Float64,2}, x::GB300Array{Float64,1}, beta::Float64, y::GB300Array{Float64,1})
+    dgcheck(ccall((:dg_gemv, libdg), Cint, (Cchar, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Float64}, Cdouble, Ptr{Float64}, Ptr{Cvoid}),
+                  trans, size(A, 1), size(A, 2), alpha, A, ld(A), x, beta, y, stream(y.device)))
+    return y
+end
+
+Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(LAPACK.potrf!)) = gb300_potrf!
+Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.trsm!)) = gb300_trsm!
+Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.syrk!)) = gb300_syrk!
+Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.gemm!)) = gb300_gemm!
+Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.trsv!)) = gb300_trsv!
+Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.gemv!)) = gb300_gemv!
+
+# ---------------------------------------------------------------------------
+# whole-region calls: one ccall per cholesky! / ldiv!
+# ---------------------------------------------------------------------------
+tile_pointers(A::DArray) = [pointer(fetch(c)::GB300Array{Float64,2}) for c in A.chunks]
+
+"""
+    cholesky_gb300!(A::DArray{Float64,2}, uplo='U') -> Cholesky
+
+The datadeps region of `_chol!` (src/array/cholesky.jl:19-108) run by the
+library as one captured multi-stream CUDA graph.  All chunks must be
+GB300Arrays with Blocks(nb, nb) partitioning.  Throws PosDefException(info)
+like `potrf_checked!`.
+"""
+function cholesky_gb300!(A::DArray{Float64,2}, uplo::Char='U')
+    n = size(A, 1)
+    nb = A.partitioning.blocksize[1]
+    ptrs = tile_pointers(A)
+    info = ccall((:dg_cholesky_tiled, libdg), Cint, (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
+                 uplo, n, nb, ptrs, C_NULL)
+    dgcheck(info)
+    info > 0 && throw(PosDefException(Int(info)))
+    return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0))
+end
+
+"""
+    ldiv_gb300!(C::Cholesky{Float64,<:DMatrix}, B::DMatrix) -> B
+
+ldiv! (src/array/linalg.jl:352-405) as one library call.
+"""
+function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, B::DArray{Float64})
+    F = C.factors
+    n = size(F, 1)
+    nb = F.partitioning.blocksize[1]
+    nrhs = ndims(B) == 1 ? 1 : size(B, 2)
+    dgcheck(ccall((:dg_cholesky_solve_tiled, libdg), Cint,
+                  (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
+                  C.uplo, n, nb, tile_pointers(F), nrhs, tile_pointers(B), C_NULL))
+    return B
+end
+
+end # module

@@ -55,6 +55,19 @@ long long dg_kernel_launches(void);
  * Caller memory is never freed by the library. */
 int dg_finalize(void);
 
+/* Device memory and streams for hosts that do not link a CUDA binding (the
+ * reference reaches the GPU through CUDA.jl; a backend on this library
+ * allocates its tiles here instead: CuArray allocation and copies in
+ * ext/CUDAExt.jl:120-154 are what these replace).  kind: 0 host->device,
+ * 1 device->host, 2 device->device. */
+int dg_set_device(int device);
+int dg_device_alloc(size_t bytes, void **out);
+int dg_device_free(void *p);
+int dg_copy(void *dst, const void *src, size_t bytes, int kind, void *stream);
+int dg_stream_create(void **out);
+int dg_stream_destroy(void *stream);
+int dg_stream_synchronize(void *stream);
+
 /* ---------------------------------------------------------------------------
  * Tile operations: the BLAS/LAPACK calls the reference substitutes with
  * CUBLAS/CUSOLVER through Dagger.move(::CPUProc, ::CuArrayDeviceProc,
@@ -207,6 +220,7 @@ typedef struct dg_mixed_stats {
   float factor_ms;       /* device time of the factorization                */
   double norm_inf;       /* ||A||_inf                                       */
   long long device_bytes;
+  double shift;          /* diagonal shift the factor was computed with     */
 } dg_mixed_stats;
 
 typedef struct dg_ir_opts {
@@ -230,10 +244,20 @@ typedef struct dg_ir_report {
 int dg_mixed_factor(dg_mixed **out, int n, int nb, double *const *tiles, int precision,
                     void *stream);
 
+/* As dg_mixed_factor, factoring S A S + shift I instead (S = diag(a_ii)^-1/2,
+ * so the scaled matrix has a unit diagonal).  A small shift keeps the
+ * low-precision factorization of a very ill-conditioned matrix from breaking
+ * down; the factor then serves as a preconditioner and refinement (GMRES-IR)
+ * still converges to the solution of A x = b. */
+int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *tiles, int precision,
+                       double shift, void *stream);
+
 /* X = A^-1 B (FP64, device, column-major) by refinement with the factor. */
 int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int ldb, double *X, int ldx,
                    const dg_ir_opts *opts, dg_ir_report *report, void *stream);
 int dg_mixed_info(const dg_mixed *f, dg_mixed_stats *stats);
+/* Frees the handle's device memory, stream-ordered on the stream the factor
+ * was created on (work on other streams that uses the handle must be complete). */
 void dg_mixed_destroy(dg_mixed *f);
 
 /* The tensor-core building block: C = alpha A'B + beta C with 16-bit K-major

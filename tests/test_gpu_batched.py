@@ -78,5 +78,6 @@ def test_batched_widths_agree():
     for w in (16, 32):
         P = PackedBatch(tA, tB)
         batched_solve_packed(P, "fp64", widths=[w] * 5, ctas_per_sm=2)
-        outs.append(P.X.clone())
-    assert torch.allclose(outs[0], outs[1], rtol=1e-12, atol=1e-14)
+        outs.append([P.solution(i).clone() for i in range(P.count)])
+    for x16, x32 in zip(*outs):
+        assert torch.allclose(x16, x32, rtol=1e-12, atol=1e-14)

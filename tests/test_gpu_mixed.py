@@ -80,8 +80,9 @@ def test_mixed_solve(precision, n, nb, cond, nrhs):
     berr = o.backward_error(A, Xh, B)
     assert rep["converged"] == 1 and berr.max() <= 1e-12, (rep, berr.max())
     Xr = o.lapack_solve(A, B)
-    kappa = np.linalg.cond(A)
-    assert np.abs(Xh - Xr).max() / np.abs(Xr).max() <= kappa * 1e-12
+    kappa = np.linalg.cond(A, np.inf)
+    # forward error allowed by a backward error of 1e-12 (with a factor for n)
+    assert np.abs(Xh - Xr).max() / np.abs(Xr).max() <= 10 * kappa * 1e-12
     st = F.stats()
     assert st["info"] == 0 and st["n"] == n
     F.close()
@@ -99,7 +100,7 @@ def test_gmres_ir_ill_conditioned(precision):
     F = d.cholesky_mixed(d.DArray.from_array(A, d.Blocks(nb, nb)), precision)
     X, rep = F.solve(torch.from_numpy(B).cuda(), tol=1e-12, gmres="auto", max_iter=40)
     berr = o.backward_error(A, X.cpu().numpy(), B)
-    assert rep["converged"] == 1 and berr.max() <= 1e-12, (rep, berr.max())
+    assert rep["converged"] == 1 and berr.max() <= 1e-12, (rep, berr.max(), F.stats())
 
 
 def test_gmres_forced_matches():
@@ -117,14 +118,29 @@ def test_gmres_forced_matches():
 
 def test_fp64_retry_of_a_failed_fp32_pivot():
     """kappa = 1e9 inside one diagonal block: FP32 POTRF breaks down, the FP64
-    retry of the block succeeds and the factorization completes."""
+    retry of the block succeeds and the factorization completes unshifted."""
     import dagger_gb300 as d
     from oracle import tiled as o
     n, nb = 128, 128
     A = o.spd_spectrum(n, 1e9, 4)
-    F = d.cholesky_mixed(d.DArray.from_array(A, d.Blocks(nb, nb)), "fp32")
+    F = d.cholesky_mixed(d.DArray.from_array(A, d.Blocks(nb, nb)), "fp32", auto_shift=False)
     st = F.stats()
-    assert st["info"] == 0 and st["retries"] >= 1, st
+    assert st["info"] == 0 and st["retries"] >= 1 and st["shift"] == 0.0, st
+
+
+def test_shift_when_the_low_precision_factor_breaks_down():
+    """kappa = 1e8 across several panels: the FP32-accumulated Schur
+    complement loses definiteness; the factor of S A S + shift I is used as a
+    preconditioner and GMRES-IR still reaches 1e-12 on A x = b."""
+    import torch
+    import dagger_gb300 as d
+    from oracle import tiled as o
+    n, nb = 1024, 128
+    A = o.spd_spectrum(n, 1e8, 21)
+    B = o.rhs_normal(n, 2, 21)
+    F = d.cholesky_mixed(d.DArray.from_array(A, d.Blocks(nb, nb)), "fp32")
+    X, rep = F.solve(torch.from_numpy(B).cuda(), tol=1e-12, max_iter=60)
+    assert o.backward_error(A, X.cpu().numpy(), B).max() <= 1e-12, (rep, F.stats())
 
 
 def test_mixed_not_posdef():
