@@ -101,7 +101,12 @@ class Server:
         return time.perf_counter() - self.t0
 
     def submit(self, req: Request):
+        """Queues a request.  Its tensors may still be in flight on the
+        submitting thread's current stream: the request's worker stream waits
+        on an event recorded here before it reads them."""
         req.arrival = self.now()
+        req._ready = torch.cuda.Event()
+        req._ready.record(torch.cuda.current_stream(self.device))
         self.q.put(req)
         return req
 
@@ -209,6 +214,7 @@ class Server:
         stream = self.streams[req._stream]
         try:
             req.start = self.now()
+            stream.wait_event(req._ready)
             with torch.cuda.stream(stream):
                 ent = self.resident.get(req.matrix_id)
                 if ent is None:
@@ -237,6 +243,7 @@ class Server:
             t = self.now()
             for r in grp:
                 r.start = t
+                stream.wait_event(r._ready)
             with torch.cuda.stream(stream):
                 P = PackedBatch([r.A for r in grp], [r.B.reshape(r.n, -1) for r in grp])
                 rep = batched_solve_packed(P, "fp32_ir", tol=min(r.tol for r in grp),
