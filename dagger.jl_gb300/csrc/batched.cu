@@ -359,6 +359,19 @@ __global__ void __launch_bounds__(NT) batched_kernel(BatchParams p) {
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// The kernel's dynamic shared memory (solution, residual and correction
+// vectors) exceeds the 48 KiB default; the limit is raised once per device.
+static int set_batched_smem() {
+  static bool done[64] = {false};
+  int dev = 0;
+  DG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && done[dev]) return 0;
+  DG_CUDA_TRY(cudaFuncSetAttribute(dg::batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)((sizeof(double) * 2 + sizeof(float)) * dg::NSMEM_X)));
+  if (dev >= 0 && dev < 64) done[dev] = true;
+  return 0;
+}
+
 extern "C" int dg_batched_potrs(int count, const int *n, const int *nrhs, double *const *A,
                                 const double *const *B, double *const *X, int mode, double tol,
                                 int max_iter, const int *bucket_w, int ctas_per_sm, int *info,
@@ -428,12 +441,7 @@ extern "C" int dg_batched_potrs(int count, const int *n, const int *nrhs, double
   p.max_iter = max_iter > 0 ? max_iter : 30;
   const size_t dyn = mode ? (sizeof(double) * 2 + sizeof(float)) * dg::NSMEM_X
                           : sizeof(double) * dg::NSMEM_X;
-  static bool attr[2] = {false, false};
-  if (!attr[mode]) {
-    DG_CUDA_TRY(cudaFuncSetAttribute(dg::batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)((sizeof(double) * 2 + sizeof(float)) * dg::NSMEM_X)));
-    attr[mode] = true;
-  }
+  DG_TRY(set_batched_smem());
   if (ctas_per_sm < 1) ctas_per_sm = 1;
   const int grid = std::min(count, dg_num_sms() * ctas_per_sm);
   cudaEvent_t e0, e1;
@@ -469,4 +477,146 @@ extern "C" int dg_batched_potrs(int count, const int *n, const int *nrhs, double
     if (hinfo[2 * i] && !first_bad) first_bad = i + 1;
   }
   return first_bad;  // 0, or 1 + index of the first system whose factorization failed
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point
+// ---------------------------------------------------------------------------
+// Some callers cannot allocate device memory while they run: a host that
+// reserved all of its device memory up front (a serving process that admits
+// work against a fixed memory budget), a pool-based allocator that must not
+// be bypassed, or a real-time loop that forbids allocation after start-up.
+// dg_batched_potrs allocates its descriptors and FP32 workspaces per call;
+// this variant takes them from one file-scope device array instead.
+//
+// The array lives in every GPU that loads the library until the process
+// exits.  In host code the symbol is only a host-side stand-in, so its device
+// address is looked up once per device (cudaGetSymbolAddress, with that device
+// current) by the first call on that device; make that first call before any
+// stream capture.  Every call shares the array and it keeps the previous
+// call's contents, so the ticket counters and error words are cleared on each
+// call; calls that overlap on the GPU (concurrent streams) race on it.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB
+constexpr int kNoAllocMaxSystems = 4096;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+void *g_noalloc_addr[64] = {nullptr};
+thread_local dg::BatchSys t_sys[kNoAllocMaxSystems];
+thread_local int t_idx[kNoAllocMaxSystems];
+thread_local int t_info[2 * kNoAllocMaxSystems];
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int noalloc_scratch(void **out) {
+  int dev = 0;
+  DG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return DG_ERR_UNSUPPORTED;
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    DG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs,
+                                        double *const *A, const double *const *B,
+                                        double *const *X, int mode, double tol, int max_iter,
+                                        const int *bucket_w, int ctas_per_sm, int *info,
+                                        double *berr, void *stream) {
+  DG_CHECK_ARG(count >= 0 && count <= kNoAllocMaxSystems, 1);
+  DG_CHECK_ARG(mode == 0 || mode == 1, 7);
+  if (count == 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int i = 0; i < count; i++) {
+    DG_CHECK_ARG(n[i] > 0 && n[i] <= 1024, 2);
+    DG_CHECK_ARG(nrhs[i] > 0 && nrhs[i] <= dg::RMAX, 3);
+  }
+  // layout of the scratch: descriptors | order | tickets | info | berr | FP32 workspaces
+  const size_t o_sys = 0;
+  const size_t o_order = align256(o_sys + sizeof(dg::BatchSys) * count);
+  const size_t o_tick = align256(o_order + sizeof(int) * count);
+  const size_t o_info = align256(o_tick + sizeof(int) * 8);
+  const size_t o_berr = align256(o_info + sizeof(int) * 2 * count);
+  const size_t o_ws = align256(o_berr + sizeof(double) * count);
+  size_t ws = 0;
+  for (int i = 0; i < count; i++) ws += mode ? align256(sizeof(float) * (size_t)n[i] * n[i]) : 0;
+  if (o_ws + ws > kNoAllocScratchBytes) {
+    dg_set_last_error(__FILE__, __LINE__,
+                      "batch exceeds the 64 MiB scratch of dg_batched_potrs_noalloc");
+    return DG_ERR_NOMEM;
+  }
+  void *base = nullptr;
+  DG_TRY(noalloc_scratch(&base));
+  unsigned char *sc = (unsigned char *)base;
+  for (int i = 0; i < count; i++) t_idx[i] = i;
+  std::stable_sort(t_idx, t_idx + count, [&](int a, int b) { return n[a] > n[b]; });
+  dg::BatchParams p;
+  memset(&p, 0, sizeof p);
+  const int edges[] = {64, 128, 256, 512, 1024};
+  int pos = 0;
+  for (int bb = 4; bb >= 0; bb--) {
+    const int lo = bb ? edges[bb - 1] : 0, hi = edges[bb];
+    dg::BucketCfg &c = p.bucket[p.nbuckets];
+    c.start = pos;
+    while (pos < count && n[t_idx[pos]] > lo && n[t_idx[pos]] <= hi) pos++;
+    c.count = pos - c.start;
+    c.w = (bucket_w && bucket_w[bb] == 16) ? 16 : 32;
+    p.nbuckets++;
+  }
+  size_t off = o_ws;
+  for (int i = 0; i < count; i++) {
+    dg::BatchSys &d = t_sys[i];
+    d.n = n[i];
+    d.nrhs = nrhs[i];
+    d.A = A[i];
+    d.B = B[i];
+    d.X = X[i];
+    d.W32 = mode ? (float *)(sc + off) : nullptr;
+    off += mode ? align256(sizeof(float) * (size_t)n[i] * n[i]) : 0;
+    d.info = (int *)(sc + o_info) + 2 * i;
+    d.berr = (double *)(sc + o_berr) + i;
+  }
+  DG_CUDA_TRY(cudaMemcpyAsync(sc + o_sys, t_sys, sizeof(dg::BatchSys) * count,
+                              cudaMemcpyHostToDevice, s));
+  DG_CUDA_TRY(cudaMemcpyAsync(sc + o_order, t_idx, sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  // the array keeps the last call's contents: clear what must start at zero
+  DG_CUDA_TRY(cudaMemsetAsync(sc + o_tick, 0, sizeof(int) * 8, s));
+  DG_CUDA_TRY(cudaMemsetAsync(sc + o_info, 0, sizeof(int) * 2 * count, s));
+  DG_CUDA_TRY(cudaMemsetAsync(sc + o_berr, 0, sizeof(double) * count, s));
+  p.sys = (const dg::BatchSys *)(sc + o_sys);
+  p.order = (const int *)(sc + o_order);
+  p.tickets = (int *)(sc + o_tick);
+  p.mode = mode;
+  p.tol = tol > 0 ? tol : 1e-12;
+  p.max_iter = max_iter > 0 ? max_iter : 30;
+  DG_TRY(set_batched_smem());
+  const size_t dyn = mode ? (sizeof(double) * 2 + sizeof(float)) * dg::NSMEM_X
+                          : sizeof(double) * dg::NSMEM_X;
+  if (ctas_per_sm < 1) ctas_per_sm = 1;
+  const int grid = std::min(count, dg_num_sms() * ctas_per_sm);
+  dg::batched_kernel<<<grid, dg::NT, dyn, s>>>(p);
+  DG_CUDA_TRY(cudaGetLastError());
+  dg::count_launches(1);
+  DG_CUDA_TRY(cudaMemcpyAsync(t_info, sc + o_info, sizeof(int) * 2 * count,
+                              cudaMemcpyDeviceToHost, s));
+  if (berr)
+    DG_CUDA_TRY(cudaMemcpyAsync(berr, sc + o_berr, sizeof(double) * count,
+                                cudaMemcpyDeviceToHost, s));
+  DG_CUDA_TRY(cudaStreamSynchronize(s));
+  int first_bad = 0;
+  for (int i = 0; i < count; i++) {
+    if (info) {
+      info[2 * i] = t_info[2 * i];
+      info[2 * i + 1] = t_info[2 * i + 1];
+    }
+    if (t_info[2 * i] && !first_bad) first_bad = i + 1;
+  }
+  return first_bad;
 }

@@ -115,6 +115,10 @@ SIGNATURES = {
                                  ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int),
                                  ctypes.POINTER(c_double), ctypes.POINTER(ctypes.c_float),
                                  c_void_p]),
+    "dg_batched_potrs_noalloc": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                         c_void_p, c_void_p, c_void_p, c_int, c_double, c_int,
+                                         ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int),
+                                         ctypes.POINTER(c_double), c_void_p]),
 }
 
 _lib = None

@@ -286,6 +286,27 @@ int dg_batched_potrs(int count, const int *n, const int *nrhs, double *const *A,
                      const int *bucket_w, int ctas_per_sm, int *info, double *berr,
                      float *elapsed_ms, void *stream);
 
+/* Allocation-free form of dg_batched_potrs (no counterpart in the reference).
+ * For callers that must not allocate device memory while they run: a server
+ * that reserved its whole device budget at start-up and admits work against
+ * it, a host whose pool allocator must not be bypassed, or a real-time loop
+ * that forbids allocation after initialisation.  dg_batched_potrs allocates
+ * descriptors and FP32 workspaces per call; this entry point takes them from
+ * one library-owned static device array of 64 MiB instead (held by every GPU
+ * that loads the library until exit) and calls no allocator.  Limits: at most
+ * 4096 systems, and in mode 1 the FP32 workspaces (4 n^2 bytes per system,
+ * 256-byte aligned) plus the descriptors must fit the 64 MiB; a larger batch
+ * returns DG_ERR_NOMEM without launching.  The first call on a device looks up
+ * the array's device address (set-up, once per device): make that first call
+ * before any stream capture.  Every call uses the same array, so calls that
+ * overlap on the GPU (on different streams) race; serialise them.  The call
+ * synchronises `stream`.  Arguments and results as dg_batched_potrs, without
+ * the timing output. */
+int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs, double *const *A,
+                             const double *const *B, double *const *X, int mode, double tol,
+                             int max_iter, const int *bucket_w, int ctas_per_sm, int *info,
+                             double *berr, void *stream);
+
 /* Measures the device's FP64 fused-multiply-add throughput (TFLOP/s) with
  * independent FMA chains on every SM; the benchmark's FP64 roofline.  No
  * counterpart in the reference (measurement utility). */
