@@ -91,6 +91,22 @@ int scale_f64(int m, int n, double alpha, double *B, int ldb, const int *abort_f
 int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abort_flag,
               cudaStream_t s, const int *abort2 = nullptr);
 
+// FP64 GEMM emulated on the BF16 tensor cores (oz_gemm.cu).  oz_split cuts
+// ncols FP64 vectors of length K (element k of vector c at
+// src[c*cstride + k*kstride]) into 8 BF16 slices (slice s of vector c at
+// slices + s*sstride + c*ldk) and per-vector exponents e; oz_gemm computes
+// C(m x n) = alpha * sum_p A(p, i) B(p, j) + beta * C from the slices of the m
+// A-vectors and n B-vectors (K <= 1024, ldk a multiple of 8); tri 1 / 2
+// stores only the upper / lower triangle.
+constexpr int kOzSlices = 8;
+int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
+             void *slices, long long ldk, long long sstride, int *e, const int *abort_flag,
+             cudaStream_t s);
+int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
+            long long a_sstride, const int *ea, const void *b_slices, long long ldb_k,
+            long long b_sstride, const int *eb, double beta, double *C, long long ldc, int tri,
+            int *status, cudaStream_t s);
+
 // Kernel launch accounting: every kernel launch site adds to a process-wide
 // counter (graph captures move their launches into the graph's count, which
 // is added back each time the graph is launched).
@@ -98,8 +114,10 @@ void count_launches(long long n);
 long long launches();
 
 // Selects the FP64 inner product engine: 0 = DFMA register tiles, 1 = DMMA
-// (mma.sync m8n8k4 f64).  Default DFMA: on GB300 it measures faster (1.25 vs
-// 1.10 TFLOP/s on a 4096^3 GEMM).
+// (mma.sync m8n8k4 f64), 2 = DFMA tiles plus, for the trailing SYRK/GEMM
+// tasks of the tiled Cholesky region, the emulated FP64 GEMM on the tensor
+// cores.  DFMA measures faster than DMMA on GB300 (1.25 vs 1.10 TFLOP/s on a
+// 4096^3 GEMM).
 void set_f64_engine(int engine);
 int get_f64_engine();
 

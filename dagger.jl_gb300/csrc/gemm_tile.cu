@@ -281,10 +281,16 @@ int launch(const GemmArgs &g, cudaStream_t s) {
   if (sizeof(T) == 8) {
     dim3 grid((g.m + 63) / 64, (g.n + 63) / 64);
     if (grid.y > 65535) return DG_ERR_UNSUPPORTED;
-    if (g_engine && !g.tnb)
+    if (g_engine == 1 && !g.tnb)
       gemm_dmma<<<grid, 128, 0, s>>>(g);
     else
       gemm_fma<double, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(g);
+  } else if (g.n <= 64 || (long long)g.m * g.n < 128LL * 128 * 2 * dg_num_sms()) {
+    // narrow or small outputs (the triangular solves' few right-hand sides):
+    // 32 x 64 tiles give enough CTAs to fill the GPU
+    dim3 grid((g.m + 31) / 32, (g.n + 63) / 64);
+    if (grid.y > 65535) return DG_ERR_UNSUPPORTED;
+    gemm_fma<float, 32, 64, 16, 2, 4><<<grid, 256, 0, s>>>(g);
   } else {
     dim3 grid((g.m + 127) / 128, (g.n + 127) / 128);
     if (grid.y > 65535) return DG_ERR_UNSUPPORTED;
@@ -297,7 +303,7 @@ int launch(const GemmArgs &g, cudaStream_t s) {
 
 }  // namespace
 
-void set_f64_engine(int engine) { g_engine = engine ? 1 : 0; }
+void set_f64_engine(int engine) { g_engine = (engine >= 0 && engine <= 2) ? engine : 0; }
 int get_f64_engine() { return g_engine; }
 
 int gemm_f64(char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

@@ -50,6 +50,7 @@ struct dg_mixed {
   double *d64 = nullptr;         // FP64 scratch of the retry
   float *panel_max = nullptr;    // per-step |panel| maximum (FP16 scaling)
   float *alpha_dev = nullptr;    // per-step -1/scale^2 of the trailing update
+  float *Vinv = nullptr;         // inverses of the diagonal blocks (mt x nb x nb)
   int *words = nullptr;          // [0] status, [1] retries, [2] first bad diagonal, [3..] info_k
   double normA = 0.0;            // ||A||_inf
   size_t bytes = 0;
@@ -57,6 +58,8 @@ struct dg_mixed {
   float factor_ms = 0.f;
   cudaStream_t stream = nullptr;  // allocations are stream-ordered on this stream
   double shift = 0.0;             // added to the unit diagonal of S A S before factoring
+  cudaStream_t aux = nullptr;     // lookahead stream (the next panel's POTRF/TRSM)
+  cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
 };
 
 namespace dg {
@@ -263,9 +266,115 @@ int grid_for(long long n) {
 // ---------------------------------------------------------------------------
 // factorization
 // ---------------------------------------------------------------------------
+namespace {
+__global__ void identity_kernel(float *V, int nbk, int ld) {
+  const long long total = (long long)ld * nbk;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e % ld), j = (int)(e / ld);
+    V[e] = (i == j && i < nbk) ? 1.f : 0.f;
+  }
+}
+}  // namespace
+
+int mixed_invert_diagonal_block(dg_mixed *f, int k, cudaStream_t s);
+
+// Step k's panel: FP32 POTRF of the diagonal block (FP64 retry on a failed
+// pivot), the inverse of the block (kept for the solves), the FP32 TRSM of the
+// rest of the panel, and its conversion to 16-bit operands in P buffer k % 2.
+static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
+  const int n = f->n, nb = f->nb;
+  int *status = f->words, *retries = f->words + 1, *ik = f->words + 3 + k;
+  float *Pk = f->W + panel_base(k, n, nb);
+  const int nbk = std::min(nb, n - k * nb);
+  const long long T = (long long)n - (long long)(k + 1) * nb;
+  DG_CUDA_TRY(cudaMemcpyAsync(f->diag_backup, Pk, sizeof(float) * (size_t)nb * nbk,
+                              cudaMemcpyDeviceToDevice, s));
+  DG_TRY(potrf_f32('U', nbk, Pk, nb, ik, k * nb, s, status));
+  retry_potrf_kernel<<<1, 1024, 0, s>>>(nbk, nb, f->diag_backup, f->d64, Pk, ik, status, retries,
+                                        k * nb);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  DG_TRY(mixed_invert_diagonal_block(f, k, s));
+  if (T <= 0) return 0;
+  float *Rk = Pk + (size_t)nb * nb;  // the rest of panel k: nb x T
+  DG_TRY(trsm_f32('L', 'U', 'T', 'N', nbk, (int)T, 1.f, Pk, nb, Rk, nb, ik, s, status));
+  if (f->precision == DG_PREC_FP32) return 0;
+  const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
+  const int terms = (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
+  const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;  // elements per P buffer
+  void *hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
+  void *lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
+  float *pmax = f->panel_max + k;
+  float *alpha = f->alpha_dev + k;
+  const long long elems = (long long)nb * T;
+  if (fp16) {
+    DG_CUDA_TRY(cudaMemsetAsync(pmax, 0, sizeof(float), s));
+    absmax_kernel<<<grid_for(elems), 256, 0, s>>>(Rk, elems, pmax, ik, status);
+    convert_kernel<true><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, hi, lo, pmax, alpha, ik,
+                                                         status);
+    count_launches(2);
+  } else {
+    convert_kernel<false><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, hi, lo, nullptr, alpha,
+                                                          ik, status);
+    count_launches(1);
+  }
+  DG_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// Step k's trailing update on the tensor cores, in two parts: `next` = the
+// block row of panel k+1 (so the next panel can start), else the rest.
+static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
+  const int n = f->n, nb = f->nb;
+  const long long T = (long long)n - (long long)(k + 1) * nb;
+  if (T <= 0) return 0;
+  const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
+  const int terms = (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
+  const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;
+  TcGemmArgs g;
+  memset(&g, 0, sizeof g);
+  const int nb1 = (int)std::min<long long>(nb, T);
+  if (next) {
+    g.m = nb1; g.n = (int)T; g.a_row0 = 0; g.b_row0 = 0;
+    g.off = (long long)(k + 1) * nb;
+  } else {
+    if (T <= nb) return 0;
+    g.m = (int)(T - nb); g.n = (int)(T - nb); g.a_row0 = nb; g.b_row0 = nb;
+    g.off = (long long)(k + 2) * nb;
+  }
+  g.k = nb; g.terms = terms; g.fp16 = fp16;
+  g.a_hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
+  g.a_lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
+  g.b_hi = g.a_hi; g.b_lo = g.a_lo;
+  g.lda = nb; g.ldb = nb; g.a_rows = (int)T; g.b_rows = (int)T;
+  g.alpha = -1.f; g.alpha_dev = f->alpha_dev + k; g.beta = 1.f;
+  g.c = f->W; g.layout = 1; g.upper = 1;
+  g.nb = nb; g.ntot = n;
+  g.bn = 128; g.status = f->words;
+  return tc_gemm_bf16(g, s);
+}
+
+// Step k's trailing update on the FP32 CUDA-core GEMM, one call per row panel.
+static int trailing_f32(dg_mixed *f, int k, cudaStream_t s) {
+  const int n = f->n, nb = f->nb, mt = f->mt;
+  float *Pk = f->W + panel_base(k, n, nb);
+  const int nbk = std::min(nb, n - k * nb);
+  const float *Rk = Pk + (size_t)nb * nb;
+  for (int r = k + 1; r < mt; r++) {
+    float *Pr = f->W + panel_base(r, n, nb);
+    const int nbr = std::min(nb, n - r * nb);
+    const long long wr = (long long)n - (long long)r * nb;
+    const float *Ar = Rk + (size_t)(r - k - 1) * nb * nb;  // columns r*nb.. of panel k
+    DG_TRY(gemm_f32('T', 'N', nbr, (int)wr, nbk, -1.f, Ar, nb, Ar, nb, 1.f, Pr, nb, TRI_UPPER,
+                    f->words + 3 + k, s, f->words));
+  }
+  return 0;
+}
+
 int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
   const int n = f->n, nb = f->nb, mt = f->mt;
-  int *status = f->words, *retries = f->words + 1, *bad = f->words + 2, *info = f->words + 3;
+  int *bad = f->words + 2;
   DG_CUDA_TRY(cudaMemsetAsync(f->words, 0, sizeof(int) * (3 + mt), s));
   DG_CUDA_TRY(cudaMemsetAsync(bad, 0x7f, sizeof(int), s));
   diag_scale_kernel<<<grid_for(n), 256, 0, s>>>(f->tiles_dev, n, nb, mt, f->s, bad);
@@ -273,86 +382,77 @@ int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
                 s>>>(f->tiles_dev, n, nb, mt, f->s, f->W, f->shift);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(2);
-  const int prec = f->precision;
-  const bool fp16 = (prec == DG_PREC_FP16 || prec == DG_PREC_FP16X3);
-  const int terms = (prec == DG_PREC_BF16X3 || prec == DG_PREC_FP16X3) ? 3 : 1;
-  for (int k = 0; k < mt; k++) {
-    float *Pk = f->W + panel_base(k, n, nb);
-    const int nbk = std::min(nb, n - k * nb);
-    const long long T = (long long)n - (long long)(k + 1) * nb;
-    int *ik = info + k;
-    DG_CUDA_TRY(cudaMemcpyAsync(f->diag_backup, Pk, sizeof(float) * (size_t)nb * nbk,
-                                cudaMemcpyDeviceToDevice, s));
-    DG_TRY(potrf_f32('U', nbk, Pk, nb, ik, k * nb, s, status));
-    retry_potrf_kernel<<<1, 1024, 0, s>>>(nbk, nb, f->diag_backup, f->d64, Pk, ik, status, retries,
-                                          k * nb);
-    DG_CUDA_TRY(cudaGetLastError());
-    count_launches(1);
-    if (T <= 0) break;
-    float *Rk = Pk + (size_t)nb * nb;  // the rest of panel k: nb x T
-    DG_TRY(trsm_f32('L', 'U', 'T', 'N', nbk, (int)T, 1.f, Pk, nb, Rk, nb, ik, s, status));
-    if (prec == DG_PREC_FP32) {
-      // trailing update on the FP32 CUDA-core GEMM, one call per row panel
-      for (int r = k + 1; r < mt; r++) {
-        float *Pr = f->W + panel_base(r, n, nb);
-        const int nbr = std::min(nb, n - r * nb);
-        const long long wr = (long long)n - (long long)r * nb;
-        const float *Ar = Rk + (size_t)(r - k - 1) * nb * nb;  // columns r*nb.. of panel k
-        DG_TRY(gemm_f32('T', 'N', nbr, (int)wr, nbk, -1.f, Ar, nb, Ar, nb, 1.f, Pr, nb,
-                        TRI_UPPER, ik, s, status));
-      }
-      continue;
+  const bool tensor = f->precision != DG_PREC_FP32;
+  DG_TRY(panel_step(f, 0, s));
+  if (!tensor) {
+    for (int k = 0; k + 1 < f->mt; k++) {
+      DG_TRY(trailing_f32(f, k, s));
+      DG_TRY(panel_step(f, k + 1, s));
     }
-    float *pmax = f->panel_max + k;
-    float *alpha = f->alpha_dev + k;
-    const long long elems = (long long)nb * T;
-    if (fp16) {
-      DG_CUDA_TRY(cudaMemsetAsync(pmax, 0, sizeof(float), s));
-      absmax_kernel<<<grid_for(elems), 256, 0, s>>>(Rk, elems, pmax, ik, status);
-      convert_kernel<true><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, f->P_hi, f->P_lo, pmax,
-                                                           alpha, ik, status);
-      count_launches(2);
-    } else {
-      convert_kernel<false><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, f->P_hi, f->P_lo,
-                                                            nullptr, alpha, ik, status);
-      count_launches(1);
-    }
-    DG_CUDA_TRY(cudaGetLastError());
-    TcGemmArgs g;
-    memset(&g, 0, sizeof g);
-    g.m = (int)T; g.n = (int)T; g.k = nb; g.terms = terms; g.fp16 = fp16;
-    g.a_hi = f->P_hi; g.a_lo = f->P_lo; g.lda = nb; g.a_rows = (int)T;
-    g.b_hi = f->P_hi; g.b_lo = f->P_lo; g.ldb = nb; g.b_rows = (int)T;
-    g.alpha = -1.f; g.alpha_dev = alpha; g.beta = 1.f;
-    g.c = f->W; g.layout = 1; g.upper = 1;
-    g.off = (long long)(k + 1) * nb; g.nb = nb; g.ntot = n;
-    g.bn = 128; g.status = status;
-    DG_TRY(tc_gemm_bf16(g, s));
+    return 0;
+  }
+  // one-step lookahead: the next panel is factored on the auxiliary stream
+  // while the rest of the trailing matrix is updated on `s`
+  if (!f->aux) DG_CUDA_TRY(cudaStreamCreateWithFlags(&f->aux, cudaStreamNonBlocking));
+  if (!f->ev_next) DG_CUDA_TRY(cudaEventCreateWithFlags(&f->ev_next, cudaEventDisableTiming));
+  if (!f->ev_panel) DG_CUDA_TRY(cudaEventCreateWithFlags(&f->ev_panel, cudaEventDisableTiming));
+  DG_CUDA_TRY(cudaEventRecord(f->ev_panel, s));
+  DG_CUDA_TRY(cudaStreamWaitEvent(f->aux, f->ev_panel, 0));
+  for (int k = 0; k + 1 < f->mt; k++) {
+    DG_TRY(trailing_tc(f, k, /*next=*/true, s));
+    DG_CUDA_TRY(cudaEventRecord(f->ev_next, s));
+    DG_CUDA_TRY(cudaStreamWaitEvent(f->aux, f->ev_next, 0));
+    DG_TRY(panel_step(f, k + 1, f->aux));
+    DG_CUDA_TRY(cudaEventRecord(f->ev_panel, f->aux));
+    DG_TRY(trailing_tc(f, k, /*next=*/false, s));
+    DG_CUDA_TRY(cudaStreamWaitEvent(s, f->ev_panel, 0));
   }
   return 0;
 }
 
-// Solves U~' U~ Z = Z in place (FP32, n x r, column-major ldz) on the packed panels.
-int mixed_tri_solve(const dg_mixed *f, float *Z, long long ldz, int r, cudaStream_t s) {
+
+// Vinv_k = U~_kk^-1 for diagonal block k (FP32, upper triangular, zero
+// below): the triangular solves of refinement then become GEMMs, whose
+// parallelism does not depend on the number of right-hand sides.
+int mixed_invert_diagonal_block(dg_mixed *f, int k, cudaStream_t s) {
+  const int n = f->n, nb = f->nb;
+  const float *Pk = f->W + panel_base(k, n, nb);
+  const int nbk = std::min(nb, n - k * nb);
+  float *V = f->Vinv + (size_t)k * nb * nb;
+  identity_kernel<<<grid_for((long long)nb * nbk), 256, 0, s>>>(V, nbk, nb);
+  count_launches(1);
+  DG_CUDA_TRY(cudaGetLastError());
+  return trsm_f32('L', 'U', 'N', 'N', nbk, nbk, 1.f, Pk, nb, V, nb, f->words + 3 + k, s, f->words);
+}
+
+// Solves U~' U~ Z = Z (FP32, n x r, column-major ldz) on the packed panels,
+// with Z2 (same shape) as the second buffer: forward Z2_k = Vinv_k' Z_k and
+// Z_(k+1:) -= U~_(k,k+1:)' Z2_k; backward Z2_k -= U~_(k,k+1:) Z_(k+1:) and
+// Z_k = Vinv_k Z2_k.  The result is in Z.
+int mixed_tri_solve(const dg_mixed *f, float *Z, float *Z2, long long ldz, int r, cudaStream_t s) {
   const int n = f->n, nb = f->nb, mt = f->mt;
-  for (int k = 0; k < mt; k++) {  // forward: U' y = z
+  for (int k = 0; k < mt; k++) {
     const float *Pk = f->W + panel_base(k, n, nb);
+    const float *V = f->Vinv + (size_t)k * nb * nb;
     const int nbk = std::min(nb, n - k * nb);
     const long long T = (long long)n - (long long)(k + 1) * nb;
-    DG_TRY(trsm_f32('L', 'U', 'T', 'N', nbk, r, 1.f, Pk, nb, Z + (size_t)k * nb, ldz, nullptr, s));
+    DG_TRY(gemm_f32('T', 'N', nbk, r, nbk, 1.f, V, nb, Z + (size_t)k * nb, ldz, 0.f,
+                    Z2 + (size_t)k * nb, ldz, TRI_NONE, nullptr, s));
     if (T > 0)
-      DG_TRY(gemm_f32('T', 'N', (int)T, r, nbk, -1.f, Pk + (size_t)nb * nb, nb, Z + (size_t)k * nb,
+      DG_TRY(gemm_f32('T', 'N', (int)T, r, nbk, -1.f, Pk + (size_t)nb * nb, nb, Z2 + (size_t)k * nb,
                       ldz, 1.f, Z + (size_t)(k + 1) * nb, ldz, TRI_NONE, nullptr, s));
   }
-  for (int k = mt - 1; k >= 0; k--) {  // backward: U x = y
+  for (int k = mt - 1; k >= 0; k--) {
     const float *Pk = f->W + panel_base(k, n, nb);
+    const float *V = f->Vinv + (size_t)k * nb * nb;
     const int nbk = std::min(nb, n - k * nb);
     const long long T = (long long)n - (long long)(k + 1) * nb;
     if (T > 0)
       DG_TRY(gemm_f32('N', 'N', nbk, r, (int)T, -1.f, Pk + (size_t)nb * nb, nb,
-                      Z + (size_t)(k + 1) * nb, ldz, 1.f, Z + (size_t)k * nb, ldz, TRI_NONE,
+                      Z + (size_t)(k + 1) * nb, ldz, 1.f, Z2 + (size_t)k * nb, ldz, TRI_NONE,
                       nullptr, s));
-    DG_TRY(trsm_f32('L', 'U', 'N', 'N', nbk, r, 1.f, Pk, nb, Z + (size_t)k * nb, ldz, nullptr, s));
+    DG_TRY(gemm_f32('N', 'N', nbk, r, nbk, 1.f, V, nb, Z2 + (size_t)k * nb, ldz, 0.f,
+                    Z + (size_t)k * nb, ldz, TRI_NONE, nullptr, s));
   }
   return 0;
 }
@@ -397,13 +497,14 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
       {(void **)&f->W, sizeof(float) * (size_t)wsize},
       {(void **)&f->s, sizeof(double) * (size_t)n},
       {(void **)&f->tiles_dev, sizeof(double *) * (size_t)mt * mt},
-      {(void **)&f->P_hi, 2 * (size_t)std::max(1LL, tmax) * nb},
-      {(void **)&f->P_lo, 2 * (size_t)std::max(1LL, tmax) * nb},
+      {(void **)&f->P_hi, 2 * 2 * (size_t)std::max(1LL, tmax) * nb},
+      {(void **)&f->P_lo, 2 * 2 * (size_t)std::max(1LL, tmax) * nb},
       {(void **)&f->diag_backup, sizeof(float) * (size_t)nb * nb},
       {(void **)&f->d64, sizeof(double) * (size_t)nb * nb},
       {(void **)&f->panel_max, sizeof(float) * (size_t)mt},
       {(void **)&f->alpha_dev, sizeof(float) * (size_t)mt},
       {(void **)&f->words, sizeof(int) * (size_t)(3 + mt)},
+      {(void **)&f->Vinv, sizeof(float) * (size_t)mt * nb * nb},
   };
   f->stream = s;
   for (auto &a : allocs) {
@@ -463,9 +564,12 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
 extern "C" void dg_mixed_destroy(dg_mixed *f) {
   if (!f) return;
   void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
-                f->panel_max, f->alpha_dev, f->words};
+                f->panel_max, f->alpha_dev, f->words, f->Vinv};
   for (void *p : ps)
     if (p) cudaFreeAsync(p, f->stream);  // stream-ordered: no device-wide synchronisation
+  if (f->ev_next) cudaEventDestroy(f->ev_next);
+  if (f->ev_panel) cudaEventDestroy(f->ev_panel);
+  if (f->aux) cudaStreamDestroy(f->aux);
   delete f;
 }
 
@@ -500,7 +604,7 @@ int correction(const dg_mixed *f, const double *R, long long ldr, double *X, lon
   const int n = f->n;
   dg::scale_to_f32_kernel<<<grid_for((long long)n * r), 256, 0, s>>>(R, ldr, f->s, Z, n, n, r);
   dg::count_launches(1);
-  DG_TRY(dg::mixed_tri_solve(f, Z, n, r, s));
+  DG_TRY(dg::mixed_tri_solve(f, Z, Z + (size_t)n * r, n, r, s));
   dg::update_x_kernel<<<grid_for((long long)n * r), 256, 0, s>>>(X, ldx, f->s, Z, n, n, r);
   dg::count_launches(1);
   DG_CUDA_TRY(cudaGetLastError());
@@ -590,7 +694,7 @@ int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int 
       cudaMallocAsync((void **)&W, sizeof(double) * col * r * 2, s) != cudaSuccess ||
       cudaMallocAsync((void **)&D, sizeof(double) * col * r, s) != cudaSuccess ||
       cudaMallocAsync((void **)&sc, sizeof(double) * r * (m + 4), s) != cudaSuccess ||
-      cudaMallocAsync((void **)&Z32, sizeof(float) * col * r, s) != cudaSuccess) {
+      cudaMallocAsync((void **)&Z32, sizeof(float) * col * r * 2, s) != cudaSuccess) {
     cudaGetLastError();
     return DG_ERR_NOMEM;
   }
@@ -724,7 +828,7 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
   float *Z = nullptr;
   if (cudaMallocAsync((void **)&R, sizeof(double) * (size_t)n * r, s) != cudaSuccess ||
       cudaMallocAsync((void **)&cm, sizeof(double) * 3 * r, s) != cudaSuccess ||
-      cudaMallocAsync((void **)&Z, sizeof(float) * (size_t)n * r, s) != cudaSuccess) {
+      cudaMallocAsync((void **)&Z, sizeof(float) * (size_t)n * r * 2, s) != cudaSuccess) {
     cudaGetLastError();
     return DG_ERR_NOMEM;
   }

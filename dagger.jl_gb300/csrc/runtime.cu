@@ -98,6 +98,34 @@ int DeviceState::scratch_int(int **p) {
   return 0;
 }
 
+// Grow-only workspace for the slice slots; growing it invalidates the cached
+// graphs that captured the old address.
+int DeviceState::oz_workspace(size_t bytes, void **p) {
+  std::lock_guard<std::mutex> g(mu);
+  if (oz_ring_bytes < bytes) {
+    if (oz_ring) {
+      cudaDeviceSynchronize();
+      cudaFree(oz_ring);
+      oz_ring = nullptr;
+      oz_ring_bytes = 0;
+      clear_graphs();
+    }
+    if (cudaMalloc(&oz_ring, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      dg_set_last_error(__FILE__, __LINE__, "cudaMalloc of the emulated-FP64 slice slots failed");
+      return DG_ERR_NOMEM;
+    }
+    oz_ring_bytes = bytes;
+  }
+  *p = oz_ring;
+  return 0;
+}
+
+size_t oz_slot_bytes(long long ldk, long long cap) {
+  size_t b = (size_t)kOzSlices * ldk * cap * 2 + (size_t)cap * 4;
+  return (b + 255) & ~(size_t)255;
+}
+
 DeviceState::~DeviceState() {}
 
 // ---------------------------------------------------------------------------
@@ -202,6 +230,17 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
       out.push_back({dg::footprint(t.a, t.m, t.n, t.lda, E), mode(t.mode_a, DG_IN)});
       out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), mode(t.mode_c, DG_OUT)});
       break;
+    case dg::OP_OZ_SPLIT: {
+      const bool cols = (t.trans == 'N');
+      out.push_back({dg::footprint(t.a, cols ? t.m : t.n, cols ? t.n : t.m, t.lda, E), DG_IN});
+      out.push_back({dg::footprint(t.c, (int)dg::oz_slot_bytes(t.ldc, t.k), 1, 1, 1), DG_OUT});
+      break;
+    }
+    case dg::OP_OZ_GEMM:
+      out.push_back({dg::footprint(t.a, (int)dg::oz_slot_bytes(t.lda, t.ldb), 1, 1, 1), DG_IN});
+      out.push_back({dg::footprint(t.b, (int)dg::oz_slot_bytes(t.lda, t.ldb), 1, 1, 1), DG_IN});
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_INOUT});
+      break;
   }
 }
 
@@ -212,7 +251,9 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(r != nullptr, 1);
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
-  DG_CHECK_ARG(t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY, 2);
+  DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) || t.op == dg::OP_OZ_SPLIT ||
+                   t.op == dg::OP_OZ_GEMM,
+               2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
   hash_bytes(r->hash, &t, sizeof(dg_task));
@@ -313,6 +354,21 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case DG_OP_GEMM:
       return gemm_f64(t.transa, t.transb, t.m, t.n, t.k, t.alpha, t.a, t.lda, t.b, t.ldb, t.beta,
                       t.c, t.ldc, TRI_NONE, info, s);
+    case OP_OZ_SPLIT: {
+      const bool cols = (t.trans == 'N');
+      const long long sstride = (long long)t.ldc * t.k;
+      int *e = (int *)((char *)t.c + (size_t)kOzSlices * sstride * 2);
+      return oz_split(t.a, cols ? t.lda : 1, cols ? 1 : t.lda, t.m, t.n, t.c, t.ldc, sstride, e,
+                      info, s);
+    }
+    case OP_OZ_GEMM: {
+      const long long sstride = (long long)t.lda * t.ldb;
+      const int *ea = (const int *)((const char *)t.a + (size_t)kOzSlices * sstride * 2);
+      const int *eb = (const int *)((const char *)t.b + (size_t)kOzSlices * sstride * 2);
+      const int tri = (t.uplo == 'U' || t.uplo == 'u') ? 1 : (t.uplo == 'L' || t.uplo == 'l') ? 2 : 0;
+      return oz_gemm(t.m, t.n, t.k, t.alpha, t.a, t.lda, sstride, ea, t.b, t.lda, sstride, eb,
+                     t.beta, t.c, t.ldc, tri, info, s);
+    }
     case DG_OP_COPY:
       if (t.m <= 0 || t.n <= 0) return 0;
       DG_CUDA_TRY(cudaMemcpy2DAsync(t.c, (size_t)t.ldc * 8, t.a, (size_t)t.lda * 8, (size_t)t.m * 8,
@@ -722,11 +778,79 @@ extern "C" int dg_gemv(char trans, int m, int n, double alpha, const double *A, 
 // ---------------------------------------------------------------------------
 namespace dg {
 
-void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles) {
+size_t oz_ring_bytes_for(int n, int nb) {
+  const int mt = (n + nb - 1) / nb;
+  return (size_t)kOzRingDepth * mt * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+}
+
+// The emulated-FP64 form of the same task graph: after TRSM(k, j) a split
+// task cuts tile (k, j)'s vectors into BF16 slices once, into ring slot
+// (k mod depth, j), and every SYRK/GEMM of step k reads its operands from the
+// slots.  The datadeps rules order a slot's reuse after its last reader.
+static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, double *const *tiles,
+                                     void *ring) {
+  const int mt = (n + nb - 1) / nb;
+  auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
+  auto T = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
+  const int ldk = (nb + 7) / 8 * 8;
+  const size_t sb = oz_slot_bytes(ldk, nb);
+  auto slot = [&](int k, int j) {
+    return (double *)((char *)ring + ((size_t)(k % kOzRingDepth) * mt + j) * sb);
+  };
+  for (int k = 0; k < mt; k++) {
+    dg_task t;
+    memset(&t, 0, sizeof t);
+    t.op = DG_OP_POTRF; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.c = T(k, k); t.ldc = rows(k);
+    t.info_offset = k * nb;
+    dg_region_add(r, &t);
+    for (int j = k + 1; j < mt; j++) {
+      memset(&t, 0, sizeof t);
+      t.op = DG_OP_TRSM; t.diag = 'N'; t.transa = 'T'; t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
+      if (up) {  // cholesky.jl:40-42
+        t.side = 'L'; t.uplo = 'U'; t.m = rows(k); t.n = rows(j); t.c = T(k, j); t.ldc = rows(k);
+      } else {   // cholesky.jl:85-87
+        t.side = 'R'; t.uplo = 'L'; t.m = rows(j); t.n = rows(k); t.c = T(j, k); t.ldc = rows(j);
+      }
+      dg_region_add(r, &t);
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_SPLIT; t.m = rows(k); t.n = rows(j); t.c = slot(k, j); t.ldc = ldk; t.k = nb;
+      if (up) {  // columns of U(k, j)
+        t.trans = 'N'; t.a = T(k, j); t.lda = rows(k);
+      } else {   // rows of L(j, k)
+        t.trans = 'T'; t.a = T(j, k); t.lda = rows(j);
+      }
+      dg_region_add(r, &t);
+    }
+    // cholesky.jl:43-52 (upper) / 88-97 (lower): C(m, j) -= V_m' V_j over the
+    // vectors V of step k; the diagonal tiles keep one triangle (SYRK).
+    for (int m = k + 1; m < mt; m++) {
+      for (int j = m; j < mt; j++) {
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_GEMM; t.k = rows(k); t.alpha = -1.0; t.beta = 1.0;
+        t.lda = ldk; t.ldb = nb;
+        if (up) {
+          t.m = rows(m); t.n = rows(j); t.a = slot(k, m); t.b = slot(k, j);
+          t.c = T(m, j); t.ldc = rows(m); t.uplo = (j == m) ? 'U' : 'N';
+        } else {
+          t.m = rows(j); t.n = rows(m); t.a = slot(k, j); t.b = slot(k, m);
+          t.c = T(j, m); t.ldc = rows(j); t.uplo = (j == m) ? 'L' : 'N';
+        }
+        dg_region_add(r, &t);
+      }
+    }
+  }
+}
+
+void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
+                           void *oz_ring) {
   const int mt = (n + nb - 1) / nb;
   auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
   auto T = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
   const bool up = (uplo == 'U' || uplo == 'u');
+  if (oz_ring) {
+    build_cholesky_region_oz(r, up, n, nb, tiles, oz_ring);
+    return;
+  }
   for (int k = 0; k < mt; k++) {
     dg_task t;
     memset(&t, 0, sizeof t);
@@ -823,7 +947,10 @@ extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles,
   DG_CHECK_ARG(tiles != nullptr || n == 0, 4);
   if (n == 0) return 0;
   dg_region r;
-  dg::build_cholesky_region(&r, uplo, n, nb, tiles);
+  void *ring = nullptr;
+  if (dg::get_f64_engine() == 2 && nb <= 1024)
+    DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+  dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring);
   return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
 }
 

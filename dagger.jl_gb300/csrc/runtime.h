@@ -13,6 +13,20 @@ namespace dg {
 
 constexpr int kDefaultStreams = 16;
 
+// Internal task kinds of the tiled Cholesky region with the emulated FP64
+// engine (not part of the public dg_op enumeration):
+//   OP_OZ_SPLIT  a = FP64 tile (lda), m = vector length K, n = vectors,
+//                trans 'N' = the tile's columns, 'T' = its rows; c = slice slot,
+//                ldc = ldk, k = slot capacity in vectors
+//   OP_OZ_GEMM   a, b = slice slots (lda = ldk, ldb = slot capacity), c = FP64
+//                tile (ldc), m x n output, k = K, alpha, beta; uplo 'U' / 'L'
+//                stores one triangle
+constexpr int OP_OZ_SPLIT = 100;
+constexpr int OP_OZ_GEMM = 101;
+constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
+size_t oz_slot_bytes(long long ldk, long long cap);
+size_t oz_ring_bytes_for(int n, int nb);
+
 // Library-owned per-device state.
 struct DeviceState {
   static constexpr int kInfoWords = 4096;
@@ -20,6 +34,9 @@ struct DeviceState {
   int *info_words = nullptr;  // ring of device ints for synchronous calls
   unsigned next_info = 0;
   int scratch_int(int **p);
+  void *oz_ring = nullptr;     // slice slots of the emulated FP64 engine
+  size_t oz_ring_bytes = 0;
+  int oz_workspace(size_t bytes, void **p);
   ~DeviceState();
 };
 
@@ -39,7 +56,10 @@ int region_run(dg_region *r, int use_graph, int serial, cudaStream_t origin, int
                bool sync);
 void clear_graphs();
 
-void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles);
+// oz_ring != nullptr selects the emulated-FP64 trailing updates, with
+// oz_ring_bytes_for(n, nb) bytes of slice slots (nb <= 1024).
+void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
+                           void *oz_ring = nullptr);
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
                       int nrhs, double *const *btiles);
 

@@ -110,6 +110,8 @@ SIGNATURES = {
     "dg_gemm_tc_tn": (c_int, [c_int, c_int, c_int, c_int, c_int, c_dp, c_dp, c_int, c_dp, c_dp,
                               c_int, ctypes.c_float, ctypes.c_float, c_dp, c_int, c_int, c_dp,
                               c_void_p]),
+    "dg_gemm_f64_emulated_tn": (c_int, [c_int, c_int, c_int, c_double, c_void_p, c_int, c_void_p,
+                                        c_int, c_double, c_void_p, c_int, c_void_p]),
     "dg_batched_potrs": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_void_p,
                                  c_void_p, c_void_p, c_int, c_double, c_int,
                                  ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int),

@@ -94,6 +94,34 @@ def gemm_(transa, transb, alpha, A, B, beta, C, stream=None):
     return C
 
 
+def gemm_f64_emulated_tn(alpha, A, B, beta, C, stream=None):
+    """C = alpha A'B + beta C in FP64 with the products on the BF16 tensor
+    cores (A k x m, B k x n, k <= 1024): the tile update of engine 2."""
+    pa, k, m, lda = _colmajor(A, "A")
+    pb, kb, n, ldb = _colmajor(B, "B")
+    pc, mc, nc, ldc = _colmajor(C, "C")
+    if kb != k or mc != m or nc != n:
+        raise ValueError("gemm_f64_emulated_tn: shapes A'%dx%d, B %dx%d, C %dx%d do not match"
+                         % (m, k, kb, n, mc, nc))
+    check(lib().dg_gemm_f64_emulated_tn(m, n, k, float(alpha), pa, lda, pb, ldb, float(beta), pc,
+                                        ldc, _stream(stream)))
+    return C
+
+
+F64_ENGINES = {"dfma": 0, "dmma": 1, "emulated": 2}
+
+
+def set_f64_engine(engine) -> str:
+    """Selects the engine of the FP64 tile updates ("dfma", "dmma" or
+    "emulated": trailing SYRK/GEMM on the tensor cores with FP64 accuracy,
+    POTRF/TRSM on DFMA); returns the previous one.  Process-wide."""
+    code = F64_ENGINES[engine] if isinstance(engine, str) else int(engine)
+    if code not in F64_ENGINES.values():
+        raise ValueError("unknown FP64 engine %r" % (engine,))
+    old = lib().dg_set_f64_engine(code)
+    return {v: k for k, v in F64_ENGINES.items()}[old]
+
+
 def trsv_(uplo, trans, diag, A, x, stream=None):
     """BLAS.trsv!(uplo, trans, diag, A, x) -> x."""
     pa, n, _, lda = _colmajor(A, "A")

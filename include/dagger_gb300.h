@@ -191,7 +191,12 @@ int dg_ishermitian_tiled(int n, int nb, double *const *tiles, void *stream);
 int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream);
 
 /* Selects the FP64 tile engine: 0 = DFMA register tiles, 1 = DMMA
- * (mma.sync.m8n8k4.f64).  Returns the previous setting. */
+ * (mma.sync.m8n8k4.f64), 2 = DFMA for POTRF/TRSM plus, inside
+ * dg_cholesky_tiled with nb <= 1024, the trailing SYRK/GEMM tile updates
+ * emulated on the BF16 tensor cores with FP64 accuracy (8 slices of 7 bits
+ * per operand vector, exact products, FP64 sum; see
+ * dg_gemm_f64_emulated_tn).  Returns the previous setting.  The setting is
+ * process-wide. */
 int dg_set_f64_engine(int engine);
 
 /* ---------------------------------------------------------------------------
@@ -266,6 +271,15 @@ void dg_mixed_destroy(dg_mixed *f);
 int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const void *a_hi, const void *a_lo,
                   int lda, const void *b_hi, const void *b_lo, int ldb, float alpha, float beta,
                   float *C, int ldc, int bn, int *status, void *stream);
+
+/* FP64 GEMM emulated on the BF16 tensor cores: C = alpha A'B + beta C with
+ * A k x m, B k x n and C m x n column-major FP64 on the device, k <= 1024.
+ * The building block of engine 2's trailing updates (BLAS.gemm!('T', 'N')
+ * of src/array/cholesky.jl:50); its error is that of an FP64 GEMM relative
+ * to max|A(:, i)| max|B(:, j)| k.  Allocates stream-ordered scratch. */
+int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const double *A, int lda,
+                            const double *B, int ldb, double beta, double *C, int ldc,
+                            void *stream);
 
 /* ---------------------------------------------------------------------------
  * Batched persistent launch (no counterpart in the reference, which would

@@ -1,0 +1,159 @@
+"""FP64 engine 2: the trailing SYRK/GEMM tile updates emulated on the BF16
+tensor cores (8 slices of 7 bits per vector, exact products, FP64 sum).
+
+The building block is checked against numpy's FP64 GEMM with the bound of an
+FP64 GEMM taken over each output's vectors:
+    |C - C_ref|_ij <= 4e-16 * k * max_p |A(p, i)| * max_p |B(p, j)| * |alpha|
+and the tiled Cholesky run with engine 2 is held to the plain path's parity
+bar against the oracle (1e-13 normwise, both uplo, ragged tilings, tile
+sizes that are not multiples of 8), with the oracle's LAPACK info on
+non-positive-definite inputs.
+"""
+import numpy as np
+import pytest
+
+from helpers import FP64_RTOL, dev_f, host_f, rel_err
+
+pytestmark = pytest.mark.gpu
+
+GEMM_BOUND = 4e-16
+
+
+@pytest.fixture
+def emulated():
+    import dagger_gb300 as d
+    old = d.set_f64_engine("emulated")
+    yield d
+    d.set_f64_engine(old)
+
+
+def _emulated_gemm_error(m, n, k, alpha, beta, seed, scale_rows=False):
+    import dagger_gb300 as d
+    r = np.random.default_rng(seed)
+    A = np.asfortranarray(r.uniform(-1, 1, (k, m)))
+    B = np.asfortranarray(r.standard_normal((k, n)))
+    if scale_rows:  # vectors of very different magnitudes
+        A *= np.exp2(r.integers(-30, 30, m))[None, :]
+        B *= np.exp2(r.integers(-30, 30, n))[None, :]
+    C0 = np.asfortranarray(r.standard_normal((m, n)))
+    Cg = dev_f(C0)
+    d.gemm_f64_emulated_tn(alpha, dev_f(A), dev_f(B), beta, Cg)
+    got = host_f(Cg)
+    ref = alpha * (A.T @ B) + beta * C0
+    scale = abs(alpha) * k * np.abs(A).max(0)[:, None] * np.abs(B).max(0)[None, :]
+    scale = scale + np.abs(beta * C0) * 2.0 ** -52
+    return float((np.abs(got - ref) / scale).max())
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 64, 64), (1, 1, 1), (257, 129, 100), (1000, 700, 1024),
+                                   (130, 70, 513), (64, 300, 8), (1024, 1024, 1024)])
+def test_emulated_gemm_vs_fp64(m, n, k):
+    assert _emulated_gemm_error(m, n, k, -1.0, 1.0, m + n + k) <= GEMM_BOUND
+
+
+def test_emulated_gemm_alpha_beta_and_scales():
+    assert _emulated_gemm_error(300, 200, 777, 0.37, -2.5, 5, scale_rows=True) <= GEMM_BOUND
+    assert _emulated_gemm_error(200, 300, 256, 2.0, 0.0, 6) <= GEMM_BOUND
+
+
+def test_emulated_gemm_exact_on_small_integers():
+    """Integers below 2^7 are one slice: the product must be exact."""
+    import dagger_gb300 as d
+    r = np.random.default_rng(3)
+    A = np.asfortranarray(r.integers(-127, 128, (512, 96)).astype(np.float64))
+    B = np.asfortranarray(r.integers(-127, 128, (512, 80)).astype(np.float64))
+    Cg = dev_f(np.zeros((96, 80), order='F'))
+    d.gemm_f64_emulated_tn(1.0, dev_f(A), dev_f(B), 0.0, Cg)
+    assert np.array_equal(host_f(Cg), A.T @ B)
+
+
+def test_emulated_gemm_zero_vectors():
+    import dagger_gb300 as d
+    r = np.random.default_rng(4)
+    A = np.asfortranarray(r.standard_normal((64, 130)))
+    A[:, 7] = 0.0
+    B = np.asfortranarray(r.standard_normal((64, 70)))
+    B[:, 3] = 0.0
+    Cg = dev_f(np.ones((130, 70), order='F'))
+    d.gemm_f64_emulated_tn(1.0, dev_f(A), dev_f(B), 1.0, Cg)
+    got = host_f(Cg)
+    assert np.array_equal(got[7, :], np.ones(70))
+    assert np.array_equal(got[:, 3], np.ones(130))
+    assert rel_err(got, A.T @ B + 1.0) <= 1e-14
+
+
+def test_emulated_gemm_argument_errors():
+    import dagger_gb300 as d
+    r = np.random.default_rng(5)
+    A = dev_f(r.standard_normal((1025, 4)))
+    B = dev_f(r.standard_normal((1025, 4)))
+    C = dev_f(np.zeros((4, 4), order='F'))
+    with pytest.raises(ValueError):
+        d.gemm_f64_emulated_tn(1.0, A, B, 0.0, C)   # k > 1024
+
+
+@pytest.mark.parametrize("uplo", "UL")
+@pytest.mark.parametrize("n,nb", [(64, 16), (128, 32), (130, 32), (1000, 100), (1024, 128),
+                                  (1000, 128), (300, 300), (2048, 1024), (700, 60)])
+def test_factor_engine2_vs_oracle(emulated, uplo, n, nb):
+    d = emulated
+    from oracle import tiled as o
+    A = o.spd_uniform(n, n + nb)
+    F, info = o.chol_tiled(A, nb, uplo)
+    assert info == 0
+    C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), uplo)
+    G = C.factors.numpy()
+    tri = np.triu if uplo == 'U' else np.tril
+    assert rel_err(tri(G), tri(F)) <= FP64_RTOL
+    mask = tri(np.ones((n, n))) == 0
+    assert np.array_equal(G[mask], A[mask])
+    assert o.factor_residual(A, G, uplo) < 1e-14
+
+
+@pytest.mark.parametrize("uplo", "UL")
+def test_solve_engine2_vs_oracle(emulated, uplo):
+    d = emulated
+    from oracle import tiled as o
+    n, nb, nrhs = 1000, 128, 16
+    A = o.spd_uniform(n, 3 * n)
+    B = o.rhs_normal(n, nrhs, n)
+    F, _ = o.chol_tiled(A, nb, uplo)
+    X = B.copy(order='F')
+    o.ldiv_cholesky(F, uplo, X, nb)
+    C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), uplo)
+    DB = d.DArray.from_array(B, d.Blocks(nb, nb))
+    d.ldiv_(C, DB)
+    assert rel_err(DB.numpy(), X) <= FP64_RTOL
+    assert o.backward_error(A, DB.numpy(), B).max() < 1e-14
+
+
+@pytest.mark.parametrize("uplo", "UL")
+@pytest.mark.parametrize("bad", [0, 40, 127])
+def test_not_posdef_engine2(emulated, uplo, bad):
+    d = emulated
+    from oracle import tiled as o
+    A = o.spd_uniform(128, 77)
+    A[bad, bad] = -100.0
+    _, info_ref = o.chol_tiled(A, 32, uplo)
+    with pytest.raises(d.PosDefException) as e:
+        d.cholesky(d.DArray.from_array(A, d.Blocks(32, 32)), uplo)
+    assert e.value.info == info_ref == bad + 1
+
+
+def test_engine2_cpu_config_4096(emulated):
+    """N = 4096, Blocks(512, 512), 16 RHS against the threaded oracle."""
+    d = emulated
+    from oracle import native, tiled as o
+    n, nb = 4096, 512
+    A = o.spd_uniform(n, 2024)
+    B = o.rhs_normal(n, 16, 2024)
+    native.set_blas_threads(1)
+    F, info = native.chol_tiled(A, nb, 'U', nthreads=8)
+    assert info == 0
+    X = B.copy(order='F')
+    native.ldiv_tiled(F, 'U', X, nb, nthreads=8)
+    C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), 'U')
+    assert rel_err(np.triu(C.factors.numpy()), np.triu(F)) <= FP64_RTOL
+    DB = d.DArray.from_array(B, d.Blocks(nb, nb))
+    d.ldiv_(C, DB)
+    assert rel_err(DB.numpy(), X) <= FP64_RTOL
