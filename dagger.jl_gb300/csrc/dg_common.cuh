@@ -77,6 +77,16 @@ int trsm_f32(char side, char uplo, char transa, char diag, int m, int n, float a
              const float *A, long long lda, float *B, long long ldb, const int *abort_flag,
              cudaStream_t s, const int *abort2 = nullptr);
 
+// The same with the off-diagonal updates of the recursion emulated on the
+// tensor cores, slices in `scratch` (FP64 engine 2).  status (TRSM) and
+// info_out (POTRF) are the factorization's info word: kernels skip when it
+// is set, and a timeout records DG_ERR_TIMEOUT there.
+int trsm_f64_oz(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+                const double *A, int lda, double *B, int ldb, void *scratch, size_t bytes,
+                int *status, cudaStream_t s);
+int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_offset,
+                 void *scratch, size_t bytes, cudaStream_t s);
+
 // Cholesky of one tile.  info_out receives offset + local pivot index of
 // the first failure (written once); kernels skip when info_out, abort_flag
 // or abort2 is already non-zero.  The plain FP64 path passes its info word
@@ -97,15 +107,25 @@ int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abo
 // slices + s*sstride + c*ldk) and per-vector exponents e; oz_gemm computes
 // C(m x n) = alpha * sum_p A(p, i) B(p, j) + beta * C from the slices of the m
 // A-vectors and n B-vectors (K <= 1024, ldk a multiple of 8); tri 1 / 2
-// stores only the upper / lower triangle.
+// stores only the upper / lower triangle.  Kernels skip when *status or
+// *abort2 is non-zero; a timed-out wait records DG_ERR_TIMEOUT in *status.
 constexpr int kOzSlices = 8;
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
              void *slices, long long ldk, long long sstride, int *e, const int *abort_flag,
-             cudaStream_t s);
+             cudaStream_t s, const int *abort2 = nullptr);
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
             long long a_sstride, const int *ea, const void *b_slices, long long ldb_k,
             long long b_sstride, const int *eb, double beta, double *C, long long ldc, int tri,
-            int *status, cudaStream_t s);
+            int *status, cudaStream_t s, const int *abort2 = nullptr);
+// C = alpha op(A) op(B) + beta C (BLAS gemm / syrk arguments; tri as above)
+// through split + oz_gemm with the slices in caller scratch of `bytes`
+// (oz_scratch_bytes).  Returns 1 without work when k > 1024 or the scratch
+// is too small, so the caller can use the FP64 kernels instead.
+size_t oz_scratch_bytes(int m, int n, int k, bool same_operand);
+int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                    long long lda, const double *B, long long ldb, double beta, double *C,
+                    long long ldc, int tri, void *scratch, size_t bytes, int *status,
+                    const int *abort2, cudaStream_t s);
 
 // Kernel launch accounting: every kernel launch site adds to a process-wide
 // counter (graph captures move their launches into the graph's count, which

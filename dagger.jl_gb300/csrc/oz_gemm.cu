@@ -6,30 +6,38 @@
 //
 // Splitting (oz_split_kernel): each operand vector v (a row of op(A) or a
 // column of op(B), K values) is scaled by 2^-e with 2^(e-1) <= max|v| < 2^e,
-// and cut into S = 8 slices of 7 bits:
-//     v = 2^e * sum_{s=1..8} d_s 2^(-7 s) + r,   d_s integer, |d_s| <= 127,
-//     |r| < 2^(e-56).
-// Slice s is stored as the BF16 value d_s 2^(-7s): exact, since |d_s| has at
-// most 7 significant bits and the factor is a power of two.
+// and cut into S = 8 slices by rounding to nearest:
+//     v = 2^e * sum_{s=1..8} d_s 2^(-7 s) + r,   d_s integer,
+//     |d_1| <= 128, |d_s| <= 64 (s >= 2), |r| <= 2^(e-57).
+// Slice s is stored as the BF16 value d_s 2^(-7s): exact, since every
+// integer of magnitude <= 256 has at most 8 significant bits.
 //
 // Products (oz_gemm_kernel): C = alpha * 2^(ea_i + eb_j) * sum_{s+t<=9} A_s B_t'
-// + beta * C, K <= 1024.  One product A_s B_t' sums K terms d_s d_t 2^(-7(s+t))
-// with |d_s d_t| < 2^14, so its FP32 accumulation in TMEM is exact (the
-// integer part stays below 2^24).  Products of level s+t <= 6 (15 of them)
-// are accumulated separately, each exactly, and added in FP64; the 21
-// products of levels 7..9 share one FP32 accumulator, whose rounding is below
-// 2^-54 of |C|'s scale.  The dropped levels (>= 10) and the slicing remainder
-// are below 2^-56.  The result has an FP64 GEMM's accuracy relative to
-// 2^(ea_i + eb_j) K.
+// + beta * C, K <= 1024.  A product A_s B_t' sums terms d_s d_t 2^(-7(s+t)).
+// Level L = s + t collects the L - 1 products of that weight.  Over a window
+// of 512 values of K the sum of level L <= 6 stays within 2^24 units of
+// 2^(-7L) (level 6: (2*128*64 + 2*64*64 + 64*64) * 512 < 2^24; levels 2 and
+// 3 within 2^24 over all 1024), so its FP32 accumulation in TMEM is exact.
+// Levels 2..6 are read exactly after each window and summed as 64-bit
+// integers in units of 2^-42 (|sum| < 2^53 over K = 1024, exact again in the
+// final conversion to FP64).  Levels 7..9 accumulate in FP32 over the whole
+// K; their rounding is below 2^-56 of |C|'s scale, and the dropped levels
+// (>= 10) and the slicing remainder are below 2^-55.  The result has an FP64
+// GEMM's accuracy relative to 2^(ea_i + eb_j) K.
 //
-// CTA tile: 128 rows (TMEM lanes) x 64 columns, K in blocks of 64, 6 warps:
-// warps 0-3 accumulate in FP64 (one row per thread, 64 doubles), warp 4
-// issues the TMA loads, warp 5 the MMAs.  Job s (s = 1..8) streams A_s and
-// the B_t it pairs with (t = 1..9-s) through two 80 KiB shared-memory stages
-// (TMA, 128-byte swizzle); its exact products go to TMEM accumulators
-// E_1..E_5 (64 columns each), its grouped products to G.  After a job with
-// exact products warps 0-3 add E into their FP64 registers before the next
-// job reuses E.
+// TMEM holds one 64-column accumulator per level, level L at columns
+// 64 (L - 2) .. 64 (L - 1) - 1 (all 512 columns).  The B slices of a stage
+// are stored one after the other, so B_t .. B_u form one operand of
+// 64 (u - t + 1) rows, and A_s x [B_t .. B_u] is ONE MMA whose output
+// columns fall exactly on levels s + t .. s + u.  Per 16 values of K that is
+// 14 MMAs of N = 64..256: 8 onto levels 7..9 and 6 onto levels 2..6.
+//
+// CTA tile: 128 rows (TMEM lanes) x 64 columns.  K advances in stages of 32:
+// one stage holds the 8 slices of the A tile and of the B tile (96 KiB, two
+// 3-D TMA loads with 64-byte swizzle), and two stages are in flight.  6
+// warps: warp 4 issues the TMA loads, warp 5 the MMAs (levels 7..9 first),
+// warps 0-3 read levels 2..6 at the end of each window (one row per thread,
+// 64 integers) while the next stage's MMAs onto levels 7..9 run.
 // All waits are bounded (1 s): a timeout records DG_ERR_TIMEOUT and the CTA
 // drains and returns.
 #include <cuda_bf16.h>
@@ -43,11 +51,12 @@ namespace {
 
 using namespace ptx;
 
-constexpr int OZ_S = 8;           // slices per operand
-constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 64;
-constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;   // 16 KiB
-constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;   // 8 KiB
-constexpr int OZ_STAGE = OZ_A_BYTES + 8 * OZ_B_BYTES;  // 80 KiB
+constexpr int OZ_S = 8;                                   // slices per operand
+constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;        // K per stage
+constexpr int OZ_WIN = 16;                                // stages per exact window (K 512)
+constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB
+constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB
+constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 96 KiB
 constexpr int OZ_STAGES = 2;
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE + 1024 + 256;
 
@@ -59,20 +68,18 @@ struct OzParams {
   int m, n, k;
   double alpha, beta;
   int tri;                // 1: store only i <= j, 2: only i >= j
-  int *status;
+  int *status;            // skip when non-zero; DG_ERR_TIMEOUT recorded here
+  const int *abort2;      // skip when non-zero (read only)
 };
-
-__device__ __forceinline__ int n_pair(int s) { return 9 - s; }           // t = 1..9-s
-__device__ __forceinline__ int n_exact(int s) { return s <= 5 ? 6 - s : 0; }  // t with s+t <= 6
 
 __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__ OzParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + OZ_STAGES * OZ_STAGE);
   uint64_t *empty = full + OZ_STAGES;
-  uint64_t *ready = empty + OZ_STAGES;   // MMA -> epilogue: exact accumulators complete
-  uint64_t *drained = ready + 1;         // epilogue -> MMA: exact accumulators read
-  uint64_t *done = drained + 1;          // MMA -> epilogue: everything complete
+  uint64_t *ready = empty + OZ_STAGES;   // MMA -> readers: a window's exact sums complete
+  uint64_t *drained = ready + 1;         // readers -> MMA: exact accumulators read
+  uint64_t *done = drained + 1;          // MMA -> readers: everything complete
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   int *abort_flag = (int *)(tmem_slot + 1);
 
@@ -80,7 +87,8 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
   const int i0 = blockIdx.x * OZ_BM, j0 = blockIdx.y * OZ_BN;
   if ((p.tri == 1 && i0 > j0 + OZ_BN - 1) || (p.tri == 2 && j0 > i0 + OZ_BM - 1)) return;
   // one read of the status word decides for the whole CTA
-  if (threadIdx.x == 0) *abort_flag = (p.status && *(volatile int *)p.status) ? 1 : 0;
+  if (threadIdx.x == 0)
+    *abort_flag = aborted(p.status, p.abort2) ? 1 : 0;
   __syncthreads();
   if (*(volatile int *)abort_flag) return;
   __syncthreads();
@@ -108,143 +116,142 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t G = tmem;                    // columns 0..63
-  const int nk = (p.k + OZ_BK - 1) / OZ_BK;
+  const int nst = (p.k + OZ_BK - 1) / OZ_BK;  // stages
+  const int nwin = (nst + OZ_WIN - 1) / OZ_WIN;
 
   if (warp == 4) {
     if (lane == 0) {
-    // ---------------- TMA producer ----------------
-    int it = 0;
-    for (int s = 1; s <= OZ_S && !*(volatile int *)abort_flag; s++) {
-      const int np = n_pair(s);
-      const uint32_t bytes = OZ_A_BYTES + np * OZ_B_BYTES;
-      for (int kb = 0; kb < nk; kb++, it++) {
+      // ---------------- TMA producer ----------------
+      int it = 0;
+      for (; it < nst && !*(volatile int *)abort_flag; it++) {
         const int st = it % OZ_STAGES;
         if (it >= OZ_STAGES && !mbar_wait(&empty[st], ((it / OZ_STAGES) - 1) & 1)) {
           atomicExch(abort_flag, 1);
           break;
         }
         uint8_t *dst = smem + st * OZ_STAGE;
-        mbar_expect_tx(&full[st], bytes);
-        tma_load_3d(dst, &p.a, &full[st], kb * OZ_BK, i0, s - 1);
-        for (int t = 1; t <= np; t++)
-          tma_load_3d(dst + OZ_A_BYTES + (t - 1) * OZ_B_BYTES, &p.b, &full[st], kb * OZ_BK, j0,
-                      t - 1);
+        mbar_expect_tx(&full[st], OZ_STAGE);
+        tma_load_3d(dst, &p.a, &full[st], it * OZ_BK, i0, 0);
+        tma_load_3d(dst + OZ_S * OZ_A_SLICE, &p.b, &full[st], it * OZ_BK, j0, 0);
       }
-    }
-    // drain the loads in flight
-    for (int q = (it > OZ_STAGES ? it - OZ_STAGES : 0); q < it; q++)
-      if (!mbar_wait(&full[q % OZ_STAGES], (q / OZ_STAGES) & 1)) atomicExch(abort_flag, 1);
+      // drain the loads in flight
+      for (int q = (it > OZ_STAGES ? it - OZ_STAGES : 0); q < it; q++)
+        if (!mbar_wait(&full[q % OZ_STAGES], (q / OZ_STAGES) & 1)) atomicExch(abort_flag, 1);
     }
     __syncwarp();
   } else if (warp == 5) {
     if (lane == 0) {
-    // ---------------- MMA issuer ----------------
-    const uint32_t idesc = idesc_f16kind(OZ_BM, OZ_BN, false);
-    const uint32_t sbase = smem_u32(smem);
-    int it = 0, flushes = 0;
-    bool g_started = false;
-    for (int s = 1; s <= OZ_S; s++) {
-      const int np = n_pair(s), ne = n_exact(s);
-      // the exact accumulators must have been read by the previous flush
-      if (ne > 0 && flushes > 0 && !mbar_wait(drained, (flushes - 1) & 1)) {
-        atomicExch(abort_flag, 1);
-        break;
-      }
-      bool ok = true;
-      for (int kb = 0; kb < nk; kb++, it++) {
-        const int st = it % OZ_STAGES;
+      // ---------------- MMA issuer ----------------
+      const uint32_t idesc64 = idesc_f16kind(OZ_BM, OZ_BN, false);  // N = 64 c: + (8 (c-1)) << 17
+      const uint32_t sbase = smem_u32(smem);
+      for (int it = 0; it < nst; it++) {
+        const int st = it % OZ_STAGES, w = it / OZ_WIN, wpos = it % OZ_WIN;
         if (!mbar_wait(&full[st], (it / OZ_STAGES) & 1)) {
           atomicExch(abort_flag, 1);
-          ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t sa = sbase + st * OZ_STAGE;
-#pragma unroll
+        // descriptors: base + (byte offset >> 4)
+        const uint64_t da = sw64_desc(sbase + st * OZ_STAGE);
+        const uint64_t db = sw64_desc(sbase + st * OZ_STAGE + OZ_S * OZ_A_SLICE);
+        // A_s x [B_t .. B_u] onto levels s+t .. s+u (TMEM column 64 (s+t-2))
+        auto mma_run = [&](int kk, int s_, int t, int u, uint32_t acc) {
+          mma_bf16(tmem + 64 * (s_ + t - 2), da + (((s_ - 1) * OZ_A_SLICE + kk * 32) >> 4),
+                   db + (((t - 1) * OZ_B_SLICE + kk * 32) >> 4),
+                   idesc64 + ((uint32_t)(8 * (u - t)) << 17), acc);
+        };
+        // levels 7..9: t from max(1, 7 - s) to 9 - s; the first MMA sets them
+#pragma unroll 1
+        for (int kk = 0; kk < OZ_BK / 16; kk++)
+#pragma unroll 1
+          for (int s_ = 1; s_ <= OZ_S; s_++)
+            mma_run(kk, s_, 7 - s_ > 1 ? 7 - s_ : 1, 9 - s_, (it == 0 && kk == 0 && s_ == 1) ? 0u : 1u);
+        // levels 2..6: the previous window's sums must have been read
+        if (wpos == 0 && w > 0 && !mbar_wait(drained, (w - 1) & 1)) {
+          atomicExch(abort_flag, 1);
+          break;
+        }
+        const uint32_t first = (wpos == 0) ? 0u : 1u;
+#pragma unroll 1
         for (int kk = 0; kk < OZ_BK / 16; kk++) {
-          const uint64_t adesc = sw128_desc(sa + kk * 32);
-          for (int t = 1; t <= np; t++) {
-            const uint64_t bdesc = sw128_desc(sa + OZ_A_BYTES + (t - 1) * OZ_B_BYTES + kk * 32);
-            if (t <= ne) {
-              mma_bf16(tmem + 64 * t, adesc, bdesc, idesc, (kb | kk) ? 1u : 0u);
-            } else {
-              mma_bf16(G, adesc, bdesc, idesc, g_started ? 1u : 0u);
-              g_started = true;
-            }
-          }
+          const uint32_t a0 = (kk == 0) ? first : 1u;
+          mma_run(kk, 1, 1, 4, a0);   // levels 2..5
+          mma_run(kk, 1, 5, 5, a0);   // level 6
+          mma_run(kk, 2, 1, 4, 1u);   // levels 3..6
+          mma_run(kk, 3, 1, 3, 1u);   // levels 4..6
+          mma_run(kk, 4, 1, 2, 1u);   // levels 5..6
+          mma_run(kk, 5, 1, 1, 1u);   // level 6
         }
         mma_commit(&empty[st]);
+        if (wpos == OZ_WIN - 1 || it == nst - 1) mma_commit(ready);
       }
-      if (!ok) break;
-      if (ne > 0) {
-        mma_commit(ready);
-        flushes++;
-      }
-    }
-    mma_commit(done);
+      mma_commit(done);
     }
     __syncwarp();
   }
 
-  // ---------------- FP64 accumulation (warps 0-3) ----------------
-  double acc[OZ_BN];
+  // ---------------- exact sums (warps 0-3) ----------------
+  long long acc[OZ_BN];
 #pragma unroll
-  for (int c = 0; c < OZ_BN; c++) acc[c] = 0.0;
+  for (int c = 0; c < OZ_BN; c++) acc[c] = 0;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-  int flush = 0;
-  for (int s = 1; s <= OZ_S && warp < 4; s++) {
-    const int ne = n_exact(s);
-    if (ne == 0) continue;
-    if (!mbar_wait(ready, flush & 1)) {
+  for (int w = 0; w < nwin && warp < 4; w++) {
+    if (!mbar_wait(ready, w & 1)) {
       atomicExch(abort_flag, 1);
       break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    for (int t = 1; t <= ne; t++) {
+#pragma unroll 1
+    for (int lvl = 2; lvl <= 6; lvl++) {
+      const float up = __int_as_float((127 + 7 * lvl) << 23);  // 2^(7 lvl)
+      const long long unit = 1LL << (7 * (6 - lvl));           // 2^(7 (6 - lvl))
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         float v[32];
-        tmem_ld32(tmem + 64 * t + h * 32 + lane_base, v);
+        tmem_ld32(tmem + 64 * (lvl - 2) + h * 32 + lane_base, v);
 #pragma unroll
-        for (int c = 0; c < 32; c++) acc[h * 32 + c] += (double)v[c];
+        for (int c = 0; c < 32; c++) acc[h * 32 + c] += (long long)__float2int_rn(v[c] * up) * unit;
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     mbar_arrive(drained);
-    flush++;
   }
   const bool ok = mbar_wait(done, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!ok) atomicExch(abort_flag, 1);
   __syncthreads();
   const bool aborted = *(volatile int *)abort_flag != 0;
-  if (!aborted && nk > 0 && warp < 4) {
+  if (!aborted && nst > 0 && warp < 4) {
+    const int row = i0 + warp * 32 + lane;
+    const int ea = row < p.m ? p.ea[row] : 0;
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      float v[32];
-      tmem_ld32(G + h * 32 + lane_base, v);
+      // levels 9, 8, 7 summed in FP32 (all lanes: the loads are warp-wide)
+      float v[32], w[32];
+      tmem_ld32(tmem + 64 * 7 + h * 32 + lane_base, v);
+#pragma unroll 1
+      for (int lvl = 8; lvl >= 7; lvl--) {
+        tmem_ld32(tmem + 64 * (lvl - 2) + h * 32 + lane_base, w);
 #pragma unroll
-      for (int c = 0; c < 32; c++) acc[h * 32 + c] += (double)v[c];
-    }
-    const int row = i0 + warp * 32 + lane;
-    if (row < p.m) {
-      const int ea = p.ea[row];
+        for (int c = 0; c < 32; c++) v[c] = w[c] + v[c];
+      }
+      if (row >= p.m) continue;
       // 8 columns at a time: their reads of C are issued before the writes
 #pragma unroll
-      for (int c0 = 0; c0 < OZ_BN; c0 += 8) {
+      for (int c0 = 0; c0 < 32; c0 += 8) {
         double old[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) {
-          const int col = j0 + c0 + c;
+          const int col = j0 + h * 32 + c0 + c;
           const bool in = col < p.n && !(p.tri == 1 && row > col) && !(p.tri == 2 && row < col);
           old[c] = (in && p.beta != 0.0) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
         }
 #pragma unroll
         for (int c = 0; c < 8; c++) {
-          const int col = j0 + c0 + c;
+          const int col = j0 + h * 32 + c0 + c;
           if (col >= p.n || (p.tri == 1 && row > col) || (p.tri == 2 && row < col)) continue;
-          double vout = p.alpha * ldexp(acc[c0 + c], ea + p.eb[col]);
+          const double x = fma((double)acc[h * 32 + c0 + c], 0x1p-42, (double)v[c0 + c]);
+          double vout = p.alpha * ldexp(x, ea + p.eb[col]);
           if (p.beta != 0.0) vout = fma(p.beta, old[c], vout);
           p.c[(size_t)row + (size_t)col * p.ldc] = vout;
         }
@@ -268,8 +275,9 @@ __global__ void __launch_bounds__(128) oz_split_kernel(const double *src, long l
                                                       long long kstride, int K, int ncols,
                                                       __nv_bfloat16 *dst, long long ldk,
                                                       long long sstride, int *e,
-                                                      const int *abort_flag) {
-  if (abort_flag && *(volatile const int *)abort_flag) return;
+                                                      const int *abort_flag,
+                                                      const int *abort2) {
+  if (aborted(abort_flag, abort2)) return;
   const int c = blockIdx.x;
   if (c >= ncols) return;
   const double *v = src + (size_t)c * cstride;
@@ -290,7 +298,7 @@ __global__ void __launch_bounds__(128) oz_split_kernel(const double *src, long l
 #pragma unroll
     for (int s = 0; s < OZ_S; s++) {
       x *= 128.0;
-      const double d = trunc(x);
+      const double d = rint(x);
       x -= d;
       dst[(size_t)s * sstride + (size_t)c * ldk + k] =
           __float2bfloat16_rn(ldexpf((float)d, -7 * (s + 1)));
@@ -323,10 +331,10 @@ bool oz_map(CUtensorMap *map, const void *base, long long ldk, long long rows, l
   if (!enc) return false;
   cuuint64_t dims[3] = {(cuuint64_t)ldk, (cuuint64_t)rows, (cuuint64_t)OZ_S};
   cuuint64_t strides[2] = {(cuuint64_t)ldk * 2, (cuuint64_t)sstride * 2};
-  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, (cuuint32_t)OZ_S};
   cuuint32_t estr[3] = {1, 1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)base, dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -334,10 +342,10 @@ bool oz_map(CUtensorMap *map, const void *base, long long ldk, long long rows, l
 
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
              void *slices, long long ldk, long long sstride, int *e, const int *abort_flag,
-             cudaStream_t s) {
+             cudaStream_t s, const int *abort2) {
   if (ncols <= 0) return 0;
   oz_split_kernel<<<ncols, 128, 0, s>>>(src, cstride, kstride, K, ncols, (__nv_bfloat16 *)slices,
-                                        ldk, sstride, e, abort_flag);
+                                        ldk, sstride, e, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -346,7 +354,7 @@ int oz_split(const double *src, long long cstride, long long kstride, int K, int
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
             long long a_sstride, const int *ea, const void *b_slices, long long ldb_k,
             long long b_sstride, const int *eb, double beta, double *C, long long ldc, int tri,
-            int *status, cudaStream_t s) {
+            int *status, cudaStream_t s, const int *abort2) {
   if (m <= 0 || n <= 0) return 0;
   if (k <= 0 || k > 1024 || lda_k % 8 || ldb_k % 8) return DG_ERR_UNSUPPORTED;
   OzParams p;
@@ -360,6 +368,7 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   p.ea = ea; p.eb = eb; p.c = C; p.ldc = ldc;
   p.m = m; p.n = n; p.k = k; p.alpha = alpha; p.beta = beta; p.tri = tri;
   p.status = status;
+  p.abort2 = abort2;
   static bool attr[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -373,6 +382,45 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
+}
+
+static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t oz_scratch_bytes(int m, int n, int k, bool same) {
+  const size_t ldk = (size_t)(k + 7) / 8 * 8;
+  size_t b = round256((size_t)OZ_S * ldk * m * 2) + round256((size_t)m * 4);
+  if (!same) b += round256((size_t)OZ_S * ldk * n * 2) + round256((size_t)n * 4);
+  return b;
+}
+
+int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                    long long lda, const double *B, long long ldb, double beta, double *C,
+                    long long ldc, int tri, void *scratch, size_t bytes, int *status,
+                    const int *abort2, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  const bool tA = !(ta == 'N' || ta == 'n'), tB = !(tb == 'N' || tb == 'n');
+  // the rows of op(A) are the columns of op(B): one set of slices (SYRK)
+  const bool same = (A == B && lda == ldb && m == n && tA != tB);
+  if (k <= 0 || k > 1024 || !scratch || oz_scratch_bytes(m, n, k, same) > bytes) return 1;
+  const long long ldk = (k + 7) / 8 * 8;
+  char *q = (char *)scratch;
+  void *sa = q;
+  q += round256((size_t)OZ_S * ldk * m * 2);
+  int *ea = (int *)q;
+  q += round256((size_t)m * 4);
+  void *sb = sa;
+  int *eb = ea;
+  // row i of op(A), element p: A[i + p lda] ('N') or A[p + i lda] ('T')
+  DG_TRY(oz_split(A, tA ? lda : 1, tA ? 1 : lda, k, m, sa, ldk, ldk * m, ea, status, s, abort2));
+  if (!same) {
+    sb = q;
+    q += round256((size_t)OZ_S * ldk * n * 2);
+    eb = (int *)q;
+    // column j of op(B), element p: B[p + j ldb] ('N') or B[j + p ldb] ('T')
+    DG_TRY(oz_split(B, tB ? 1 : ldb, tB ? ldb : 1, k, n, sb, ldk, ldk * n, eb, status, s, abort2));
+  }
+  return oz_gemm(m, n, k, alpha, sa, ldk, ldk * m, ea, sb, ldk, same ? ldk * m : ldk * n, eb, beta,
+                 C, ldc, tri, status, s, abort2);
 }
 
 }  // namespace dg
@@ -391,19 +439,11 @@ extern "C" int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const 
   DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 11);
   if (m == 0 || n == 0) return 0;
   cudaStream_t s = (cudaStream_t)stream;
-  const long long ldk = (k + 7) / 8 * 8;
-  const long long sa = ldk * m, sb = ldk * n;
+  const size_t bytes = dg::oz_scratch_bytes(m, n, k, false);
   void *buf = nullptr;
-  const size_t bytes = 2 * (size_t)dg::OZ_S * (sa + sb) + 4 * (size_t)(m + n) + 256;
   DG_CUDA_TRY(cudaMallocAsync(&buf, bytes, s));
-  __nv_bfloat16 *as = (__nv_bfloat16 *)buf;
-  __nv_bfloat16 *bs = as + dg::OZ_S * sa;
-  int *ea = (int *)(bs + dg::OZ_S * sb);
-  int *eb = ea + m;
-  int rc = dg::oz_split(A, lda, 1, k, m, as, ldk, sa, ea, nullptr, s);
-  if (!rc) rc = dg::oz_split(B, ldb, 1, k, n, bs, ldk, sb, eb, nullptr, s);
-  if (!rc)
-    rc = dg::oz_gemm(m, n, k, alpha, as, ldk, sa, ea, bs, ldk, sb, eb, beta, C, ldc, 0, nullptr, s);
+  int rc = dg::oz_gemm_general('T', 'N', m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, buf,
+                               bytes, nullptr, nullptr, s);
   cudaFreeAsync(buf, s);
   return rc;
 }

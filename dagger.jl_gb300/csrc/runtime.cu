@@ -205,12 +205,18 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
   const int E = 8;
   switch (t.op) {
     case DG_OP_POTRF:
+    case dg::OP_OZ_POTRF:
       out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), mode(t.mode_c, DG_INOUT)});
+      if (t.op == dg::OP_OZ_POTRF)
+        out.push_back({dg::footprint(t.b, t.ldb, 1, 1, 256), DG_OUT});  // slice scratch
       break;
-    case DG_OP_TRSM: {
+    case DG_OP_TRSM:
+    case dg::OP_OZ_TRSM: {
       int ka = (t.side == 'L' || t.side == 'l') ? t.m : t.n;
       out.push_back({dg::footprint(t.a, ka, ka, t.lda, E), mode(t.mode_a, DG_IN)});
       out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), mode(t.mode_c, DG_INOUT)});
+      if (t.op == dg::OP_OZ_TRSM)
+        out.push_back({dg::footprint(t.b, t.ldb, 1, 1, 256), DG_OUT});  // slice scratch
       break;
     }
     case DG_OP_SYRK: {
@@ -251,8 +257,8 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(r != nullptr, 1);
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
-  DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) || t.op == dg::OP_OZ_SPLIT ||
-                   t.op == dg::OP_OZ_GEMM,
+  DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) ||
+                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_OZ_POTRF),
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
@@ -345,6 +351,12 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case DG_OP_TRSM:
       return trsm_f64(t.side, t.uplo, t.transa, t.diag, t.m, t.n, t.alpha, t.a, t.lda, t.c, t.ldc,
                       info, s);
+    case OP_OZ_POTRF:
+      return potrf_f64_oz(t.uplo, t.n, t.c, t.ldc, info, t.info_offset, (void *)t.b,
+                          (size_t)t.ldb * 256, s);
+    case OP_OZ_TRSM:
+      return trsm_f64_oz(t.side, t.uplo, t.transa, t.diag, t.m, t.n, t.alpha, t.a, t.lda, t.c,
+                         t.ldc, (void *)t.b, (size_t)t.ldb * 256, info, s);
     case DG_OP_SYRK: {
       bool nt = (t.trans == 'N' || t.trans == 'n');
       Tri tri = (t.uplo == 'U' || t.uplo == 'u') ? TRI_UPPER : TRI_LOWER;
@@ -797,15 +809,20 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
   auto slot = [&](int k, int j) {
     return (double *)((char *)ring + ((size_t)(k % kOzRingDepth) * mt + j) * sb);
   };
+  // POTRF(k) and TRSM(k, j) cut their own recursion's operands into slices
+  // in slot (k, k) (unused by the splits of step k) and slot (k, j) (before
+  // the split of tile j fills it)
+  const int slot_units = (int)(sb / 256);
   for (int k = 0; k < mt; k++) {
     dg_task t;
     memset(&t, 0, sizeof t);
-    t.op = DG_OP_POTRF; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.c = T(k, k); t.ldc = rows(k);
-    t.info_offset = k * nb;
+    t.op = OP_OZ_POTRF; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.c = T(k, k); t.ldc = rows(k);
+    t.info_offset = k * nb; t.b = slot(k, k); t.ldb = slot_units;
     dg_region_add(r, &t);
     for (int j = k + 1; j < mt; j++) {
       memset(&t, 0, sizeof t);
-      t.op = DG_OP_TRSM; t.diag = 'N'; t.transa = 'T'; t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
+      t.op = OP_OZ_TRSM; t.diag = 'N'; t.transa = 'T'; t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
+      t.b = slot(k, j); t.ldb = slot_units;
       if (up) {  // cholesky.jl:40-42
         t.side = 'L'; t.uplo = 'U'; t.m = rows(k); t.n = rows(j); t.c = T(k, j); t.ldc = rows(k);
       } else {   // cholesky.jl:85-87

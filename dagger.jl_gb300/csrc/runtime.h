@@ -21,8 +21,12 @@ constexpr int kDefaultStreams = 16;
 //   OP_OZ_GEMM   a, b = slice slots (lda = ldk, ldb = slot capacity), c = FP64
 //                tile (ldc), m x n output, k = K, alpha, beta; uplo 'U' / 'L'
 //                stores one triangle
+//   OP_OZ_TRSM   DG_OP_TRSM whose recursion updates are emulated, with
+//   OP_OZ_POTRF  (likewise DG_OP_POTRF) b = slice scratch of ldb * 256 bytes
 constexpr int OP_OZ_SPLIT = 100;
 constexpr int OP_OZ_GEMM = 101;
+constexpr int OP_OZ_TRSM = 102;
+constexpr int OP_OZ_POTRF = 103;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 size_t oz_slot_bytes(long long ldk, long long cap);
 size_t oz_ring_bytes_for(int n, int nb);

@@ -23,6 +23,9 @@
 //              word on entry and returns at once.
 // Every access is bounds-checked against the block length, so ragged last
 // tiles (n not a multiple of the block size) need no padding.
+// With the emulated FP64 engine the caller passes scratch for BF16 slices,
+// and the off-diagonal GEMM / SYRK of every level runs on the tensor cores
+// (oz_gemm_general) with FP64 accuracy; the base cases stay FP64.
 #include "dg_common.cuh"
 
 namespace dg {
@@ -176,6 +179,31 @@ int gemm_t<float>(char ta, char tb, int m, int n, int k, float alpha, const floa
   return gemm_f32(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, a1, s, a2);
 }
 
+// Slice scratch of the emulated FP64 engine (none: p == nullptr); status is
+// the writable word that records a timeout.
+struct OzScratch {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int *status = nullptr;
+};
+
+// The off-diagonal update of one recursion level: emulated when the scratch
+// allows it (FP64 only), else the tile GEMM kernels.
+template <typename T>
+int update_t(char ta, char tb, int m, int n, int k, T alpha, const T *A, long long lda, const T *B,
+             long long ldb, T beta, T *C, long long ldc, Tri tri, const int *a1, cudaStream_t s,
+             const int *a2, const OzScratch &oz) {
+  if (sizeof(T) == 8 && oz.p) {
+    // a1 and a2 are both abort words; the status word is a1 itself when given
+    const int *other = (oz.status == a1) ? a2 : (a2 ? a2 : a1);
+    int rc = oz_gemm_general(ta, tb, m, n, k, (double)alpha, (const double *)A, lda,
+                             (const double *)B, ldb, (double)beta, (double *)C, ldc, (int)tri,
+                             oz.p, oz.bytes, oz.status, other, s);
+    if (rc <= 0) return rc;
+  }
+  return gemm_t<T>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, a1, s, a2);
+}
+
 template <typename T>
 struct TrsmPlan {
   TriView<T> tv;
@@ -185,6 +213,7 @@ struct TrsmPlan {
   int nn;  // right-hand-side columns of the canonical (left) problem
   const int *a1, *a2;
   cudaStream_t s;
+  OzScratch oz;
 };
 
 template <typename T>
@@ -210,20 +239,21 @@ int trsm_rec(const TrsmPlan<T> &p, int r0, int len) {
   if (!p.tv.trans) { Msub = p.tv.T_ + (size_t)b0 + (size_t)a0 * p.tv.ld; opM = 'N'; }
   else { Msub = p.tv.T_ + (size_t)a0 + (size_t)b0 * p.tv.ld; opM = 'T'; }
   if (!p.side_right) {
-    DG_TRY(gemm_t<T>(opM, 'N', blen, p.nn, alen, T(-1), Msub, p.tv.ld, p.B + a0, p.ldb, T(1),
-                     p.B + b0, p.ldb, TRI_NONE, p.a1, p.s, p.a2));
+    DG_TRY(update_t<T>(opM, 'N', blen, p.nn, alen, T(-1), Msub, p.tv.ld, p.B + a0, p.ldb, T(1),
+                       p.B + b0, p.ldb, TRI_NONE, p.a1, p.s, p.a2, p.oz));
   } else {
     // rows of X' are columns of B: B[:, b] -= B[:, a] * M[b, a]'
-    DG_TRY(gemm_t<T>('N', opM == 'N' ? 'T' : 'N', p.nn, blen, alen, T(-1),
-                     p.B + (size_t)a0 * p.ldb, p.ldb, Msub, p.tv.ld, T(1),
-                     p.B + (size_t)b0 * p.ldb, p.ldb, TRI_NONE, p.a1, p.s, p.a2));
+    DG_TRY(update_t<T>('N', opM == 'N' ? 'T' : 'N', p.nn, blen, alen, T(-1),
+                       p.B + (size_t)a0 * p.ldb, p.ldb, Msub, p.tv.ld, T(1),
+                       p.B + (size_t)b0 * p.ldb, p.ldb, TRI_NONE, p.a1, p.s, p.a2, p.oz));
   }
   return trsm_rec(p, b0, blen);
 }
 
 template <typename T>
 int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, const T *A,
-           long long lda, T *B, long long ldb, const int *a1, cudaStream_t s, const int *a2) {
+           long long lda, T *B, long long ldb, const int *a1, cudaStream_t s, const int *a2,
+           const OzScratch &oz = OzScratch()) {
   if (m <= 0 || n <= 0) return 0;
   const bool right = (side == 'R' || side == 'r');
   const bool tr = !(transa == 'N' || transa == 'n');
@@ -240,6 +270,7 @@ int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, 
   p.a1 = a1;
   p.a2 = a2;
   p.s = s;
+  p.oz = oz;
   if (alpha != T(1)) {
     if (sizeof(T) == 8)
       DG_TRY(scale_f64(m, n, (double)alpha, (double *)B, (int)ldb, a1, s, a2));
@@ -252,7 +283,7 @@ int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, 
 
 template <typename T>
 int potrf_rec(bool upper, int n, T *A, long long lda, int *info, int off, cudaStream_t s,
-              const int *a1, const int *a2) {
+              const int *a1, const int *a2, const OzScratch &oz = OzScratch()) {
   if (n <= 0) return 0;
   if (n <= TB) {
     potrf_base_kernel<T><<<1, 256, 0, s>>>(upper ? 1 : 0, n, A, lda, info, off, a1, a2);
@@ -261,24 +292,26 @@ int potrf_rec(bool upper, int n, T *A, long long lda, int *info, int off, cudaSt
     return 0;
   }
   const int n1 = split_point(n), n2 = n - n1;
-  DG_TRY(potrf_rec<T>(upper, n1, A, lda, info, off, s, a1, a2));
+  DG_TRY(potrf_rec<T>(upper, n1, A, lda, info, off, s, a1, a2, oz));
   // the remaining kernels stop when this factorization's info is set, or on
   // either caller abort word (two words per kernel: info + the first caller
   // word; the base kernel checks all three)
   const int *k1 = info, *k2 = a1 ? a1 : a2;
   T *A22 = A + (size_t)n1 + (size_t)n1 * lda;
+  OzScratch oz1 = oz;
+  if (oz1.p) oz1.status = info;  // this factorization's word records a timeout
   if (upper) {
     T *A12 = A + (size_t)n1 * lda;
-    DG_TRY(trsm_t<T>('L', 'U', 'T', 'N', n1, n2, T(1), A, lda, A12, lda, k1, s, k2));
-    DG_TRY(gemm_t<T>('T', 'N', n2, n2, n1, T(-1), A12, lda, A12, lda, T(1), A22, lda, TRI_UPPER,
-                     k1, s, k2));
+    DG_TRY(trsm_t<T>('L', 'U', 'T', 'N', n1, n2, T(1), A, lda, A12, lda, k1, s, k2, oz1));
+    DG_TRY(update_t<T>('T', 'N', n2, n2, n1, T(-1), A12, lda, A12, lda, T(1), A22, lda, TRI_UPPER,
+                       k1, s, k2, oz1));
   } else {
     T *A21 = A + n1;
-    DG_TRY(trsm_t<T>('R', 'L', 'T', 'N', n2, n1, T(1), A, lda, A21, lda, k1, s, k2));
-    DG_TRY(gemm_t<T>('N', 'T', n2, n2, n1, T(-1), A21, lda, A21, lda, T(1), A22, lda, TRI_LOWER,
-                     k1, s, k2));
+    DG_TRY(trsm_t<T>('R', 'L', 'T', 'N', n2, n1, T(1), A, lda, A21, lda, k1, s, k2, oz1));
+    DG_TRY(update_t<T>('N', 'T', n2, n2, n1, T(-1), A21, lda, A21, lda, T(1), A22, lda, TRI_LOWER,
+                       k1, s, k2, oz1));
   }
-  return potrf_rec<T>(upper, n2, A22, lda, info, off + n1, s, a1, a2);
+  return potrf_rec<T>(upper, n2, A22, lda, info, off + n1, s, a1, a2, oz);
 }
 
 }  // namespace
@@ -288,6 +321,27 @@ int trsm_f64(char side, char uplo, char transa, char diag, int m, int n, double 
              cudaStream_t s, const int *abort2) {
   return trsm_t<double>(side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, abort_flag, s,
                         abort2);
+}
+
+int trsm_f64_oz(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+                const double *A, int lda, double *B, int ldb, void *scratch, size_t bytes,
+                int *status, cudaStream_t s) {
+  OzScratch oz;
+  oz.p = scratch;
+  oz.bytes = bytes;
+  oz.status = status;
+  return trsm_t<double>(side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, status, s, nullptr,
+                        oz);
+}
+
+int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_offset,
+                 void *scratch, size_t bytes, cudaStream_t s) {
+  OzScratch oz;
+  oz.p = scratch;
+  oz.bytes = bytes;
+  oz.status = info_out;
+  return potrf_rec<double>(uplo == 'U' || uplo == 'u', n, A, lda, info_out, info_offset, s,
+                           nullptr, nullptr, oz);
 }
 
 int trsm_f32(char side, char uplo, char transa, char diag, int m, int n, float alpha,

@@ -5,6 +5,7 @@ a profiler can capture exactly that kernel (ncu -k regex:<name> -c N).
     python -m dagger_gb300.profile_kernels tc_gemm    [--m 8192] [--k 1024] [--terms 3]
     python -m dagger_gb300.profile_kernels trsm_f64   [--nb 1024]
     python -m dagger_gb300.profile_kernels batched    [--count 2000]
+    python -m dagger_gb300.profile_kernels oz_gemm    [--m 8192] [--k 1024]
 
 gemm_f64   the FP64 trailing-update tile GEMM of the plain path,
            C(nb x nb) -= A' B with nb x nb tiles (2 nb^3 flops per launch)
@@ -12,6 +13,9 @@ tc_gemm    the tcgen05 trailing SYRK/GEMM of the mixed form on an m x m
            output with K = k (2 m^2 k flops x terms per launch, BF16)
 trsm_f64   the panel TRSM of one nb x nb tile
 batched    the persistent batched launch on `count` systems, n in [32, 1024]
+oz_gemm    the emulated FP64 GEMM (engine 2) on an m x m output with K = k:
+           two split launches and one oz_gemm_kernel launch per call
+           (2 m^2 k FP64 flops, 36 BF16 products of 2 m^2 k flops each)
 Each prints the per-launch time measured with CUDA events.
 """
 from __future__ import annotations
@@ -38,7 +42,7 @@ def _time(fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched"])
+    ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched", "oz_gemm"])
     ap.add_argument("--nb", type=int, default=1024)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--k", type=int, default=1024)
@@ -68,6 +72,15 @@ def main(argv=None):
         fl = 2.0 * m * m * k * a.terms
         print(f"tc_gemm m={m} k={k} terms={a.terms}: {ms * 1e3:.1f} us/launch, "
               f"{fl / ms / 1e9:.1f} TFLOP/s")
+    elif a.kernel == "oz_gemm":
+        m, k = a.m, a.k
+        A = torch.randn(m, k, dtype=torch.float64, device=dev)   # k x m column-major
+        C = torch.randn(m, m, dtype=torch.float64, device=dev)
+        ms = _time(lambda: L.dg_gemm_f64_emulated_tn(m, m, k, -1.0, A.data_ptr(), k, A.data_ptr(),
+                                                     k, 1.0, C.data_ptr(), m, s), a.reps)
+        fl = 2.0 * m * m * k
+        print(f"oz_gemm m={m} k={k}: {ms * 1e3:.1f} us/call, {fl / ms / 1e9:.2f} FP64-equivalent "
+              f"TFLOP/s, {36 * fl / ms / 1e9:.1f} BF16 TFLOP/s")
     elif a.kernel == "trsm_f64":
         nb = a.nb
         T = torch.randn(nb, nb, dtype=torch.float64, device=dev) * 0.01
