@@ -69,6 +69,12 @@ def parse():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-count", type=int, default=60)
     ap.add_argument("--serve-rates", default="10,40")
+    ap.add_argument("--f64-engine", default="emulated", choices=["emulated", "dfma", "dmma"],
+                    help="FP64 tile engine of the headline: 'emulated' runs the trailing "
+                         "updates and the TRSM/POTRF recursion updates on the BF16 tensor cores "
+                         "with FP64 accuracy; 'dfma' is the plain FP64 pipe")
+    ap.add_argument("--no-dfma", action="store_true",
+                    help="skip the one-step DFMA-engine comparison line")
     ap.add_argument("--spd", default="spectrum", choices=["spectrum", "uniform"],
                     help="input construction; 'uniform' (B B'/N + N I, matmul only) is for "
                          "profilers that cannot load the QR's solver library")
@@ -308,6 +314,8 @@ def run_ours(args):
     W = d.DArray(DA.shape, part, device=dev)
     DBw = d.DArray(DB0.shape, part, device=dev)
 
+    d.set_f64_engine(args.f64_engine)
+
     def step():
         W.storage.copy_(DA.storage)                # cholcopy
         C = d.cholesky_(W, 'U', stream=stream)
@@ -392,7 +400,30 @@ def run_ours(args):
                "ms_per_step": 1e3 * te / args.steps}
         del A_h, B_h, X_h
 
-    # roofline of the dominant kernel: the FP64 tile GEMM (2 nb^3 flops per launch)
+    # the same step on the plain FP64 pipe (DFMA engine), one timed step
+    dfma = None
+    if args.f64_engine != "dfma" and not args.no_dfma:
+        d.set_f64_engine("dfma")
+        step()
+        barrier()
+        h0 = torch.cuda.Event(enable_timing=True)
+        h1 = torch.cuda.Event(enable_timing=True)
+        h0.record(stream)
+        step()
+        h1.record(stream)
+        barrier()
+        th = h0.elapsed_time(h1) / 1e3
+        Xh = DBw.collect()
+        Rh = B - A @ Xh
+        bh = (Rh.abs().amax(dim=0) / (nA * Xh.abs().amax(dim=0) + B.abs().amax(dim=0)))
+        dfma = {"value": flops(n, r) / th / 1e12, "unit": "TFLOP/s", "ms_per_step": 1e3 * th,
+                "steps": 1, "backward_error_max": float(bh.max().item())}
+        del Xh, Rh
+        d.set_f64_engine(args.f64_engine)
+
+    # roofline of the dominant kernel
+    if args.f64_engine == "emulated":
+        roof = roofline_emulated(L, nb, dev, stream, s)
     Ta = torch.randn(nb, nb, dtype=torch.float64, device=dev)
     Tb = torch.randn(nb, nb, dtype=torch.float64, device=dev)
     Tc = torch.randn(nb, nb, dtype=torch.float64, device=dev)
@@ -413,12 +444,16 @@ def run_ours(args):
     pk = ctypes.c_double(0)
     L.dg_probe_fp64_fma_tflops(20000, ctypes.byref(pk), s)
     achieved = 2.0 * nb ** 3 / tg / 1e12
-    roof = {"bound": "tensor", "kernel": "gemm_f64_dfma (trailing-update tile GEMM)",
-            "achieved": achieved, "peak": pk.value, "unit": "TFLOP/s",
-            "frac": achieved / pk.value,
-            "peak_source": "FP64 FMA throughput measured in this run (no FP64 figure in the "
-                           "measured-peaks record)",
-            "per_launch": f"2*{nb}^3 flops, {1e6 * tg:.0f} us", "traffic": None}
+    roof_dfma = {"bound": "fp64", "kernel": "gemm_f64_dfma (trailing-update tile GEMM)",
+                 "achieved": achieved, "peak": pk.value, "unit": "TFLOP/s",
+                 "frac": achieved / pk.value,
+                 "peak_source": "FP64 FMA throughput measured in this run (no FP64 figure in "
+                                "the measured-peaks record)",
+                 "per_launch": f"2*{nb}^3 flops, {1e6 * tg:.0f} us", "traffic": None}
+    if args.f64_engine == "emulated":
+        roof["fp64_pipe_reference"] = roof_dfma
+    else:
+        roof = roof_dfma
 
     del Ta, Tb, Tc
     mixed = None
@@ -447,6 +482,7 @@ def run_ours(args):
                       "n": n, "nb": nb, "nrhs": r, "cond": args.cond,
                       "l2": "inputs 8 N^2 bytes >> 129 MB L2 (no flush needed)",
                       "parallelism": "replicas" if world > 1 else "single GPU"},
+           "f64_engine": args.f64_engine, "dfma_engine": dfma,
            "solves_per_s": r * args.steps * world / t,
            "accuracy": {"backward_error_max": float(berr.max().item()),
                         "factor_residual_probe": fres},
@@ -457,6 +493,59 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def _measured_bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (bf16_tflops, burst)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback 1.9 PFLOP/s"
+
+
+def roofline_emulated(L, nb, dev, stream, s):
+    """The emulated FP64 tile GEMM (oz_gemm_kernel) of the trailing update,
+    C(nb x nb) -= A'B with both operands already cut into slices, timed alone
+    with CUDA events on the launching stream: 36 BF16 products of 2 nb^3
+    flops per launch against the measured BF16 tensor peak."""
+    import torch
+    ldk = (nb + 7) // 8 * 8
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    Ta = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
+    Tb = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
+    Tc = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
+    sa = torch.empty(8 * ldk * nb, dtype=torch.bfloat16, device=dev)
+    sb = torch.empty(8 * ldk * nb, dtype=torch.bfloat16, device=dev)
+    ea = torch.empty(nb, dtype=torch.int32, device=dev)
+    eb = torch.empty(nb, dtype=torch.int32, device=dev)
+    L.dg_f64_slices(nb, nb, Ta.data_ptr(), nb, 1, sa.data_ptr(), ldk, ea.data_ptr(), s)
+    L.dg_f64_slices(nb, nb, Tb.data_ptr(), nb, 1, sb.data_ptr(), ldk, eb.data_ptr(), s)
+
+    def launch():
+        L.dg_gemm_f64_slices(nb, nb, nb, -1.0, sa.data_ptr(), ldk, ea.data_ptr(), sb.data_ptr(),
+                             ldk, eb.data_ptr(), 1.0, Tc.data_ptr(), nb, None, s)
+    for _ in range(3):
+        launch()
+    reps = 20
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(reps):
+        launch()
+    g1.record(stream)
+    torch.cuda.synchronize()
+    tg = g0.elapsed_time(g1) / 1e3 / reps
+    peak, src = _measured_bf16_peak()
+    achieved = 36 * 2.0 * nb ** 3 / tg / 1e12
+    return {"bound": "tensor", "kernel": "oz_gemm_kernel (emulated FP64 tile GEMM of the "
+                                          "trailing update, BF16 tcgen05)",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": src,
+            "per_launch": f"36 x 2*{nb}^3 BF16 flops (= 2*{nb}^3 FP64-equivalent), "
+                          f"{1e6 * tg:.0f} us, {nb // 128} x {nb // 64} CTAs",
+            "fp64_equivalent_tflops": 2.0 * nb ** 3 / tg / 1e12,
+            "traffic": None}
 
 
 def choose_precision(cond):
@@ -507,7 +596,8 @@ def bench_mixed(args, d, DA, A, B, stream, world):
     rep, st = reports[-1]
     return {"precision": prec, "value": flops(n, r) * args.steps * world / t / 1e12,
             "unit": "TFLOP/s", "ms_per_step": 1e3 * t / args.steps,
-            "solves_per_s": r * args.steps * world / t,
+            "f64_engine": args.f64_engine, "dfma_engine": dfma,
+           "solves_per_s": r * args.steps * world / t,
             "factor_ms": st["factor_ms"], "refine_ms": rep["solve_ms"],
             "ir_iterations": rep["iterations"], "gmres_iterations": rep["gmres_iterations"],
             "fp64_retries": st["retries"],

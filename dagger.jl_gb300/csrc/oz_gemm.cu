@@ -52,6 +52,7 @@ namespace {
 using namespace ptx;
 
 constexpr int OZ_S = 8;                                   // slices per operand
+constexpr int kOzNonFinite = 1 << 30;                     // exponent of a non-finite vector
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;        // K per stage
 constexpr int OZ_WIN = 16;                                // stages per exact window (K 512)
 constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB
@@ -251,7 +252,10 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
           const int col = j0 + h * 32 + c0 + c;
           if (col >= p.n || (p.tri == 1 && row > col) || (p.tri == 2 && row < col)) continue;
           const double x = fma((double)acc[h * 32 + c0 + c], 0x1p-42, (double)v[c0 + c]);
-          double vout = p.alpha * ldexp(x, ea + p.eb[col]);
+          const int eb = p.eb[col];
+          double vout = (ea == kOzNonFinite || eb == kOzNonFinite)
+                            ? __longlong_as_double(0x7FF8000000000000ll)
+                            : p.alpha * ldexp(x, ea + eb);
           if (p.beta != 0.0) vout = fma(p.beta, old[c], vout);
           p.c[(size_t)row + (size_t)col * p.ldc] = vout;
         }
@@ -266,42 +270,126 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
                  : "memory");
 }
 
-// Splits `ncols` vectors of length K (element k of vector c at
-// src[c*cstride + k*kstride]: columns of a column-major matrix have
-// kstride 1, rows have cstride 1) into OZ_S BF16 slices: slice s of vector c
-// at dst + s*sstride + c*ldk, and the exponent of vector c at e[c].  One CTA
-// per vector.
-__global__ void __launch_bounds__(128) oz_split_kernel(const double *src, long long cstride,
+// Splitting runs on integer arithmetic (the FP64 pipe is slow on this
+// part): the exponent comes from the bits of max|v|, and the 56-bit integer
+// X = round(v * 2^(56 - e)) (|X| <= 2^56) is cut into base-128 digits
+// d_8 .. d_2 in [-64, 63] by rounding to nearest, leaving d_1 in [-128, 128].
+// A vector holding an infinity or a NaN gets the exponent kOzNonFinite, and
+// every output that uses it is NaN.
+constexpr int SPLIT_V = 32;    // vectors per CTA
+constexpr int SPLIT_K = 128;   // values of K per slicing CTA
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// frexp exponent of the non-negative double with bits b (0 for 0).
+__device__ __forceinline__ int exponent_of(unsigned long long b) {
+  const int eb = (int)(b >> 52);
+  if (eb == 0x7FF) return kOzNonFinite;
+  if (eb) return eb - 1022;
+  if (b == 0) return 0;
+  return (63 - __clzll((long long)b)) + 1 - 1074;  // subnormal: b * 2^-1074
+}
+
+// round(v * 2^(56 - ex)) for |v| < 2^ex.
+__device__ __forceinline__ long long scaled56(double v, int ex) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int eb = (int)((b >> 52) & 0x7FF);
+  unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  if (eb) mant |= 1ull << 52;
+  // v = mant * 2^(max(eb, 1) - 1075)
+  const int sh = (eb ? eb : 1) - 1019 - ex;  // <= 3
+  long long r;
+  if (sh >= 0) r = (long long)(mant << sh);
+  else if (sh > -63) r = (long long)((mant + (1ull << (-sh - 1))) >> (-sh));
+  else r = 0;
+  return (b >> 63) ? -r : r;
+}
+
+// Exponent of each of `ncols` vectors of length K (element k of vector c at
+// src[c*cstride + k*kstride]).  CTA: 32 x 8 threads over 32 vectors, reading
+// along whichever of k or c is contiguous.
+__global__ void __launch_bounds__(256) oz_exp_kernel(const double *src, long long cstride,
+                                                    long long kstride, int K, int ncols, int *e,
+                                                    const int *abort_flag, const int *abort2) {
+  if (aborted(abort_flag, abort2)) return;
+  __shared__ unsigned long long red[8][SPLIT_V + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y, c0 = blockIdx.x * SPLIT_V;
+  if (kstride == 1) {  // columns: lanes along k, warp ty over vectors ty, ty+8, ...
+    for (int vi = ty; vi < SPLIT_V; vi += 8) {
+      const int c = c0 + vi;
+      unsigned long long m = 0;
+      if (c < ncols)
+        for (int k = tx; k < K; k += 32) {
+          const unsigned long long a = abs_bits(src[(size_t)c * cstride + k]);
+          m = a > m ? a : m;
+        }
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long q = __shfl_xor_sync(0xffffffffu, m, o);
+        m = q > m ? q : m;
+      }
+      if (tx == 0 && c < ncols) e[c] = exponent_of(m);
+    }
+  } else {             // rows (or general strides): lanes along vectors
+    const int c = c0 + tx;
+    unsigned long long m = 0;
+    if (c < ncols)
+      for (int k = ty; k < K; k += 8) {
+        const unsigned long long a = abs_bits(src[(size_t)c * cstride + (size_t)k * kstride]);
+        m = a > m ? a : m;
+      }
+    red[ty][tx] = m;
+    __syncthreads();
+    if (ty == 0 && c < ncols) {
+      for (int y = 1; y < 8; y++) m = red[y][tx] > m ? red[y][tx] : m;
+      e[c] = exponent_of(m);
+    }
+  }
+}
+
+// Slices of the vectors [32 bx, 32 bx + 32) over k in [128 by, 128 by + 128)
+// (k < ldk; zeros for k >= K): slice s (0-based) of vector c at
+// dst + s*sstride + c*ldk.  Tiles of 32 x 32 values pass through shared
+// memory so that both the reads and the writes are coalesced.
+__global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long long cstride,
                                                       long long kstride, int K, int ncols,
                                                       __nv_bfloat16 *dst, long long ldk,
-                                                      long long sstride, int *e,
-                                                      const int *abort_flag,
-                                                      const int *abort2) {
+                                                      long long sstride, const int *e,
+                                                      const int *abort_flag, const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
-  const int c = blockIdx.x;
-  if (c >= ncols) return;
-  const double *v = src + (size_t)c * cstride;
-  double m = 0.0;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) m = fmax(m, fabs(v[(size_t)k * kstride]));
-  __shared__ double red[4];
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  m = fmax(fmax(red[0], red[1]), fmax(red[2], red[3]));
-  int ex = 0;
-  if (m > 0.0) {
-    frexp(m, &ex);  // m in [2^(ex-1), 2^ex)
-  }
-  if (threadIdx.x == 0) e[c] = ex;
-  for (int k = threadIdx.x; k < ldk; k += blockDim.x) {
-    double x = k < K ? ldexp(v[(size_t)k * kstride], -ex) : 0.0;  // |x| < 1
+  __shared__ double tile[SPLIT_V][33];
+  __shared__ int ex[SPLIT_V];
+  const int tx = threadIdx.x, ty = threadIdx.y, c0 = blockIdx.x * SPLIT_V;
+  if (ty == 0) ex[tx] = (c0 + tx < ncols) ? e[c0 + tx] : 0;
+  for (int kc = blockIdx.y * SPLIT_K; kc < (blockIdx.y + 1) * SPLIT_K && kc < ldk; kc += 32) {
+    __syncthreads();
+    if (kstride == 1) {
+      for (int vi = ty; vi < SPLIT_V; vi += 8) {
+        const int c = c0 + vi, k = kc + tx;
+        tile[vi][tx] = (c < ncols && k < K) ? src[(size_t)c * cstride + k] : 0.0;
+      }
+    } else {
+      for (int kk = ty; kk < 32; kk += 8) {
+        const int c = c0 + tx, k = kc + kk;
+        tile[tx][kk] = (c < ncols && k < K) ? src[(size_t)c * cstride + (size_t)k * kstride] : 0.0;
+      }
+    }
+    __syncthreads();
+    const int k = kc + tx;
+    if (k >= ldk) continue;
+    for (int vi = ty; vi < SPLIT_V; vi += 8) {
+      const int c = c0 + vi;
+      if (c >= ncols) continue;
+      long long X = (ex[vi] == kOzNonFinite) ? 0 : scaled56(tile[vi][tx], ex[vi]);
+      __nv_bfloat16 *out = dst + (size_t)c * ldk + k;
 #pragma unroll
-    for (int s = 0; s < OZ_S; s++) {
-      x *= 128.0;
-      const double d = rint(x);
-      x -= d;
-      dst[(size_t)s * sstride + (size_t)c * ldk + k] =
-          __float2bfloat16_rn(ldexpf((float)d, -7 * (s + 1)));
+      for (int s = OZ_S; s >= 1; s--) {
+        const long long d = (s > 1) ? ((X + 64) & 127) - 64 : X;
+        X = (X - d) >> 7;
+        const float w = __int_as_float((127 - 7 * s) << 23);  // 2^(-7 s)
+        out[(size_t)(s - 1) * sstride] = __float2bfloat16_rn((float)d * w);
+      }
     }
   }
 }
@@ -344,10 +432,15 @@ int oz_split(const double *src, long long cstride, long long kstride, int K, int
              void *slices, long long ldk, long long sstride, int *e, const int *abort_flag,
              cudaStream_t s, const int *abort2) {
   if (ncols <= 0) return 0;
-  oz_split_kernel<<<ncols, 128, 0, s>>>(src, cstride, kstride, K, ncols, (__nv_bfloat16 *)slices,
-                                        ldk, sstride, e, abort_flag, abort2);
+  const dim3 blk(32, 8);
+  const int nv = (ncols + SPLIT_V - 1) / SPLIT_V;
+  oz_exp_kernel<<<nv, blk, 0, s>>>(src, cstride, kstride, K, ncols, e, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
-  count_launches(1);
+  const dim3 grid(nv, (unsigned)((ldk + SPLIT_K - 1) / SPLIT_K));
+  oz_slice_kernel<<<grid, blk, 0, s>>>(src, cstride, kstride, K, ncols, (__nv_bfloat16 *)slices,
+                                       ldk, sstride, e, abort_flag, abort2);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(2);
   return 0;
 }
 
@@ -446,4 +539,31 @@ extern "C" int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const 
                                bytes, nullptr, nullptr, s);
   cudaFreeAsync(buf, s);
   return rc;
+}
+
+// The two stages of dg_gemm_f64_emulated_tn as separate calls, for callers
+// that reuse the slices of one operand across many products (the tiles of a
+// factor, the matrix of a refinement residual).
+extern "C" int dg_f64_slices(int k, int ncols, const double *src, long long cstride,
+                             long long kstride, void *slices, int ldk, int *exps, void *stream) {
+  DG_CHECK_ARG(k > 0 && k <= 1024, 1);
+  DG_CHECK_ARG(ncols >= 0, 2);
+  DG_CHECK_ARG(ldk >= k && ldk % 8 == 0, 7);
+  DG_CHECK_ARG(((uintptr_t)slices & 15) == 0, 6);
+  return dg::oz_split(src, cstride, kstride, k, ncols, slices, ldk, (long long)ldk * ncols, exps,
+                      nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int dg_gemm_f64_slices(int m, int n, int k, double alpha, const void *a_slices,
+                                  int lda_k, const int *ea, const void *b_slices, int ldb_k,
+                                  const int *eb, double beta, double *C, int ldc, int *status,
+                                  void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(k > 0 && k <= 1024, 3);
+  DG_CHECK_ARG(lda_k >= k && lda_k % 8 == 0, 6);
+  DG_CHECK_ARG(ldb_k >= k && ldb_k % 8 == 0, 9);
+  DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 13);
+  return dg::oz_gemm(m, n, k, alpha, a_slices, lda_k, (long long)lda_k * m, ea, b_slices, ldb_k,
+                     (long long)ldb_k * n, eb, beta, C, ldc, 0, status, (cudaStream_t)stream);
 }

@@ -114,6 +114,7 @@ __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *
                                                          const int *a1, const int *a2) {
   if (aborted(info, a1) || aborted(a2, nullptr)) return;
   __shared__ T Ms[TB][TB + 1];
+  __shared__ T piv[2];  // sqrt of the pivot and its reciprocal, formed once
   __shared__ int fail_at;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < len * len; e += nt) {
@@ -124,16 +125,20 @@ __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *
   if (tid == 0) fail_at = -1;
   __syncthreads();
   for (int j = 0; j < len; j++) {
-    T d = Ms[j][j];
-    if (!(d > T(0))) {  // not positive, or NaN: LAPACK's test in dpotrf2/dpotf2
-      if (tid == 0) fail_at = j;
-      break;            // d is the same for every thread: uniform exit
+    if (tid == 0) {
+      const T d = Ms[j][j];
+      if (!(d > T(0))) {  // not positive, or NaN: LAPACK's test in dpotrf2/dpotf2
+        fail_at = j;
+      } else {
+        piv[0] = sqrt(d);
+        piv[1] = T(1) / piv[0];
+      }
     }
-    d = sqrt(d);
-    const T r = T(1) / d;
-    __syncthreads();    // every thread has read Ms[j][j]
+    __syncthreads();
+    if (fail_at >= 0) break;  // the same value for every thread: uniform exit
+    const T r = piv[1];
     for (int i = j + 1 + tid; i < len; i += nt) Ms[i][j] *= r;
-    if (tid == 0) Ms[j][j] = d;
+    if (tid == 0) Ms[j][j] = piv[0];
     __syncthreads();
     const int w = len - j - 1;
     for (int e = tid; e < w * w; e += nt) {

@@ -112,6 +112,11 @@ SIGNATURES = {
                               c_void_p]),
     "dg_gemm_f64_emulated_tn": (c_int, [c_int, c_int, c_int, c_double, c_void_p, c_int, c_void_p,
                                         c_int, c_double, c_void_p, c_int, c_void_p]),
+    "dg_f64_slices": (c_int, [c_int, c_int, c_void_p, ctypes.c_longlong, ctypes.c_longlong,
+                              c_void_p, c_int, c_void_p, c_void_p]),
+    "dg_gemm_f64_slices": (c_int, [c_int, c_int, c_int, c_double, c_void_p, c_int, c_void_p,
+                                   c_void_p, c_int, c_void_p, c_double, c_void_p, c_int, c_void_p,
+                                   c_void_p]),
     "dg_batched_potrs": (c_int, [c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int), c_void_p,
                                  c_void_p, c_void_p, c_int, c_double, c_int,
                                  ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int),

@@ -160,3 +160,31 @@ def test_engine2_cpu_config_4096(emulated):
     DB = d.DArray.from_array(B, d.Blocks(nb, nb))
     d.ldiv_(C, DB)
     assert rel_err(DB.numpy(), X) <= FP64_RTOL
+
+
+def test_slice_stages_match_one_call():
+    """dg_f64_slices + dg_gemm_f64_slices give the bits of the one-call form."""
+    import torch
+    import dagger_gb300 as d
+    L = d.lib()
+    r = np.random.default_rng(8)
+    k, m, n = 300, 200, 150
+    ldk = (k + 7) // 8 * 8
+    A = np.asfortranarray(r.standard_normal((k, m)))
+    B = np.asfortranarray(r.standard_normal((k, n)))
+    C0 = np.asfortranarray(r.standard_normal((m, n)))
+    Ad, Bd = dev_f(A), dev_f(B)
+    C1 = dev_f(C0)
+    d.gemm_f64_emulated_tn(-1.0, Ad, Bd, 1.0, C1)
+    sa = torch.empty(8 * ldk * m, dtype=torch.bfloat16, device="cuda")
+    sb = torch.empty(8 * ldk * n, dtype=torch.bfloat16, device="cuda")
+    ea = torch.empty(m, dtype=torch.int32, device="cuda")
+    eb = torch.empty(n, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    assert L.dg_f64_slices(k, m, Ad.data_ptr(), k, 1, sa.data_ptr(), ldk, ea.data_ptr(), s) == 0
+    assert L.dg_f64_slices(k, n, Bd.data_ptr(), k, 1, sb.data_ptr(), ldk, eb.data_ptr(), s) == 0
+    C2 = dev_f(C0)
+    assert L.dg_gemm_f64_slices(m, n, k, -1.0, sa.data_ptr(), ldk, ea.data_ptr(), sb.data_ptr(),
+                                ldk, eb.data_ptr(), 1.0, C2.data_ptr(), m, None, s) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(host_f(C1), host_f(C2))
