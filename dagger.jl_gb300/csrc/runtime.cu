@@ -790,9 +790,11 @@ extern "C" int dg_gemv(char trans, int m, int n, double alpha, const double *A, 
 // ---------------------------------------------------------------------------
 namespace dg {
 
+// The factorization's slots, plus one column of slots so that a following
+// solve with up to nb right-hand sides finds its ring in place.
 size_t oz_ring_bytes_for(int n, int nb) {
   const int mt = (n + nb - 1) / nb;
-  return (size_t)kOzRingDepth * mt * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+  return (size_t)kOzRingDepth * (mt + 1) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
 }
 
 // The emulated-FP64 form of the same task graph: after TRSM(k, j) a split
@@ -922,14 +924,31 @@ void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const
 
 // One left-side block solve of trsm.jl:89-140 (alpha = 1) over the factor's
 // tiles and the right-hand side's tiles.
+size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs) {
+  const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
+  return (size_t)kOzRingDepth * (mt + bnt) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+}
+
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
-                      int nrhs, double *const *btiles) {
+                      int nrhs, double *const *btiles, void *oz_ring, int step0) {
   const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
   auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
   auto cols = [&](int j) { return (j + 1) * nb <= nrhs ? nb : nrhs - j * nb; };
   auto A = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
   auto B = [&](int i, int j) { return btiles[i + (size_t)j * mt]; };
   const bool forward = (uplo == 'U') ? (trans != 'N') : (trans == 'N');
+  // emulated form: slots (step mod depth, m) hold the A-vectors of one
+  // update, slots depth*mt + (step mod depth)*bnt + c the solved block's
+  // columns; the datadeps rules order each slot's reuse after its readers
+  const int ldk = (nb + 7) / 8 * 8;
+  const size_t sb = oz_slot_bytes(ldk, nb);
+  auto aslot = [&](int step, int m) {
+    return (double *)((char *)oz_ring + ((size_t)(step % kOzRingDepth) * mt + m) * sb);
+  };
+  auto xslot = [&](int step, int c) {
+    return (double *)((char *)oz_ring +
+                      ((size_t)kOzRingDepth * mt + (size_t)(step % kOzRingDepth) * bnt + c) * sb);
+  };
   for (int s = 0; s < mt; s++) {
     int k = forward ? s : mt - 1 - s;
     for (int c = 0; c < bnt; c++) {
@@ -939,10 +958,32 @@ void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double
       t.m = rows(k); t.n = cols(c); t.alpha = 1.0; t.a = A(k, k); t.lda = rows(k);
       t.c = B(k, c); t.ldc = rows(k);
       dg_region_add(r, &t);
+      if (oz_ring && s + 1 < mt) {  // the solved block's columns, once per step
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_SPLIT; t.trans = 'N'; t.a = B(k, c); t.lda = rows(k); t.m = rows(k);
+        t.n = cols(c); t.c = xslot(step0 + s, c); t.ldc = ldk; t.k = nb;
+        dg_region_add(r, &t);
+      }
     }
     for (int s2 = s + 1; s2 < mt; s2++) {
       int m = forward ? s2 : mt - 1 - s2;
       int ai = (trans == 'N') ? m : k, aj = (trans == 'N') ? k : m;
+      if (oz_ring) {
+        // the rows of op(A(ai, aj)): rows of A(m, k) ('N'), columns of A(k, m) ('T')
+        dg_task t;
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_SPLIT; t.a = A(ai, aj); t.lda = rows(ai); t.m = rows(k); t.n = rows(m);
+        t.trans = (trans == 'N') ? 'T' : 'N'; t.c = aslot(step0 + s, m); t.ldc = ldk; t.k = nb;
+        dg_region_add(r, &t);
+        for (int c = 0; c < bnt; c++) {
+          memset(&t, 0, sizeof t);
+          t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = rows(m); t.n = cols(c); t.k = rows(k);
+          t.alpha = -1.0; t.beta = 1.0; t.a = aslot(step0 + s, m); t.b = xslot(step0 + s, c);
+          t.lda = ldk; t.ldb = nb; t.c = B(m, c); t.ldc = rows(m);
+          dg_region_add(r, &t);
+        }
+        continue;
+      }
       for (int c = 0; c < bnt; c++) {
         dg_task t;
         memset(&t, 0, sizeof t);
@@ -982,12 +1023,16 @@ extern "C" int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *
   DG_CHECK_ARG(btiles != nullptr, 6);
   dg_region r;
   const bool up = (uplo == 'U' || uplo == 'u');
+  void *ring = nullptr;
+  if (dg::get_f64_engine() == 2 && nb <= 1024)
+    DG_TRY(dg::device_state().oz_workspace(dg::oz_solve_ring_bytes_for(n, nb, nrhs), &ring));
+  const int mt = (n + nb - 1) / nb;
   if (up) {
-    dg::build_solve_pass(&r, 'U', 'T', n, nb, tiles, nrhs, btiles);
-    dg::build_solve_pass(&r, 'U', 'N', n, nb, tiles, nrhs, btiles);
+    dg::build_solve_pass(&r, 'U', 'T', n, nb, tiles, nrhs, btiles, ring, 0);
+    dg::build_solve_pass(&r, 'U', 'N', n, nb, tiles, nrhs, btiles, ring, mt);
   } else {
-    dg::build_solve_pass(&r, 'L', 'N', n, nb, tiles, nrhs, btiles);
-    dg::build_solve_pass(&r, 'L', 'T', n, nb, tiles, nrhs, btiles);
+    dg::build_solve_pass(&r, 'L', 'N', n, nb, tiles, nrhs, btiles, ring, 0);
+    dg::build_solve_pass(&r, 'L', 'T', n, nb, tiles, nrhs, btiles, ring, mt);
   }
   return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
 }

@@ -64,7 +64,10 @@ void clear_graphs();
 // oz_ring_bytes_for(n, nb) bytes of slice slots (nb <= 1024).
 void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
                            void *oz_ring = nullptr);
+// One block-triangular solve pass; oz_ring (oz_solve_ring_bytes_for bytes)
+// selects emulated updates, step0 numbers its steps within the ring.
+size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs);
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
-                      int nrhs, double *const *btiles);
+                      int nrhs, double *const *btiles, void *oz_ring = nullptr, int step0 = 0);
 
 }  // namespace dg

@@ -105,6 +105,113 @@ __global__ void __launch_bounds__(256) trsm_base_kernel(TriView<T> tv, int r0, i
   }
 }
 
+// Left-side solve M X = X of a few right-hand-side columns (one CTA per
+// column) for the whole triangle: the column lives in shared memory, blocks
+// of 64 rows are finished in order; each block first subtracts the solved
+// part (all 256 threads, reading M coalesced in either orientation), then
+// warp 0 substitutes through the 64 x 64 diagonal block staged in shared
+// memory.  Used for skinny right-hand sides (the solves of ldiv!), where the
+// recursive form has too little parallelism in its updates.
+constexpr int TC_MAX_LEN = 4096;
+constexpr int TC_MAX_RHS = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_cols_kernel(TriView<T> tv, int len, T *X,
+                                                        long long ldx, const int *a1,
+                                                        const int *a2) {
+  if (aborted(a1, a2)) return;
+  extern __shared__ unsigned char tc_smem[];
+  T (*D)[TB + 1] = (T (*)[TB + 1])tc_smem;              // diagonal block
+  T *x = (T *)(tc_smem + sizeof(T) * TB * (TB + 1));    // the column
+  __shared__ T part[4][TB];
+  const int tid = threadIdx.x;
+  T *xc = X + (size_t)blockIdx.x * ldx;
+  for (int i = tid; i < len; i += 256) x[i] = xc[i];
+  __syncthreads();
+  const int nblk = (len + TB - 1) / TB;
+  for (int bi = 0; bi < nblk; bi++) {
+    const int b = tv.lower ? bi : nblk - 1 - bi;
+    const int r0 = b * TB, rl = min(TB, len - r0);
+    const int p0 = tv.lower ? 0 : r0 + rl, p1 = tv.lower ? r0 : len;  // solved rows
+    // x[r0 + i] -= sum_{p0 <= p < p1} M(r0 + i, p) x[p]
+    if (!tv.trans) {  // M(i, p) = T_[i + p ld]: threads along i, 4 groups over p
+      const int i = tid & (TB - 1), g = tid >> 6;
+      T acc = T(0);
+      if (i < rl)
+        for (int p = p0 + g; p < p1; p += 4)
+          acc = fma(tv.T_[(size_t)(r0 + i) + (size_t)p * tv.ld], x[p], acc);
+      part[g][i] = acc;
+      __syncthreads();
+      if (tid < rl) x[r0 + tid] -= (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+    } else {          // M(i, p) = T_[p + i ld]: a warp per row, lanes along p
+      const int w = tid >> 5, lane = tid & 31;
+      for (int i = w; i < rl; i += 8) {
+        T acc = T(0);
+        for (int p = p0 + lane; p < p1; p += 32)
+          acc = fma(tv.T_[(size_t)p + (size_t)(r0 + i) * tv.ld], x[p], acc);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) x[r0 + i] -= acc;
+      }
+    }
+    // the diagonal block's triangle
+    for (int e = tid; e < rl * rl; e += 256) {
+      int i, j;
+      if (!tv.trans) { i = e % rl; j = e / rl; } else { j = e % rl; i = e / rl; }
+      if (tv.lower ? (j <= i) : (j >= i))
+        D[i][j] = tv.trans ? tv.T_[(size_t)(r0 + j) + (size_t)(r0 + i) * tv.ld]
+                           : tv.T_[(size_t)(r0 + i) + (size_t)(r0 + j) * tv.ld];
+    }
+    __syncthreads();
+    if (tid < 32) {
+      const int lane = tid;
+      const T d0 = tv.unit ? T(1) : (lane < rl ? T(1) / D[lane][lane] : T(1));
+      const T d1 = tv.unit ? T(1) : (lane + 32 < rl ? T(1) / D[lane + 32][lane + 32] : T(1));
+      T x0 = lane < rl ? x[r0 + lane] : T(0);
+      T x1 = lane + 32 < rl ? x[r0 + lane + 32] : T(0);
+      if (tv.lower) {
+        for (int i = 0; i < rl; i++) {
+          const T di = __shfl_sync(0xffffffffu, i < 32 ? d0 : d1, i & 31);
+          const T xi = __shfl_sync(0xffffffffu, i < 32 ? x0 : x1, i & 31) * di;
+          if (i < 32) { if (lane == i) x0 = xi; } else { if (lane == i - 32) x1 = xi; }
+          if (lane > i && lane < rl) x0 = fma(-D[lane][i], xi, x0);
+          if (lane + 32 > i && lane + 32 < rl) x1 = fma(-D[lane + 32][i], xi, x1);
+        }
+      } else {
+        for (int i = rl - 1; i >= 0; i--) {
+          const T di = __shfl_sync(0xffffffffu, i < 32 ? d0 : d1, i & 31);
+          const T xi = __shfl_sync(0xffffffffu, i < 32 ? x0 : x1, i & 31) * di;
+          if (i < 32) { if (lane == i) x0 = xi; } else { if (lane == i - 32) x1 = xi; }
+          if (lane < i) x0 = fma(-D[lane][i], xi, x0);
+          if (lane + 32 < i) x1 = fma(-D[lane + 32][i], xi, x1);
+        }
+      }
+      if (lane < rl) x[r0 + lane] = x0;
+      if (lane + 32 < rl) x[r0 + lane + 32] = x1;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < len; i += 256) xc[i] = x[i];
+}
+
+template <typename T>
+int trsm_cols(const TriView<T> &tv, int len, T *X, long long ldx, int nn, const int *a1,
+              const int *a2, cudaStream_t s) {
+  const size_t smem = sizeof(T) * (TB * (TB + 1) + (size_t)len);
+  static bool attr[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr[dev & 63]) {
+    DG_CUDA_TRY(cudaFuncSetAttribute(trsm_cols_kernel<T>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(T) * (TB * (TB + 1) + TC_MAX_LEN))));
+    attr[dev & 63] = true;
+  }
+  trsm_cols_kernel<T><<<nn, 256, smem, s>>>(tv, len, X, ldx, a1, a2);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return 0;
+}
+
 // Cholesky of one block of length len <= 64 at A (leading dimension lda).
 // Works on the lower triangle L; for uplo 'U' the block is staged transposed
 // (U' = L) and written back transposed, so only the uplo triangle is touched.
@@ -283,7 +390,10 @@ int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, 
       DG_TRY(scale_f32(m, n, (float)alpha, (float *)B, ldb, a1, s, a2));
     if (alpha == T(0)) return 0;
   }
-  return trsm_rec(p, 0, right ? n : m);
+  const int len = right ? n : m;
+  if (!right && p.nn <= TC_MAX_RHS && len > 2 * TB && len <= TC_MAX_LEN)
+    return trsm_cols<T>(p.tv, len, B, ldb, p.nn, a1, a2, s);
+  return trsm_rec(p, 0, len);
 }
 
 template <typename T>

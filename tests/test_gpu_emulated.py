@@ -114,10 +114,11 @@ def test_factor_engine2_vs_oracle(emulated, uplo, n, nb):
 
 
 @pytest.mark.parametrize("uplo", "UL")
-def test_solve_engine2_vs_oracle(emulated, uplo):
+@pytest.mark.parametrize("n,nb,nrhs", [(1000, 128, 16), (1500, 512, 64), (900, 300, 1),
+                                       (700, 100, 250), (2048, 1024, 130)])
+def test_solve_engine2_vs_oracle(emulated, uplo, n, nb, nrhs):
     d = emulated
     from oracle import tiled as o
-    n, nb, nrhs = 1000, 128, 16
     A = o.spd_uniform(n, 3 * n)
     B = o.rhs_normal(n, nrhs, n)
     F, _ = o.chol_tiled(A, nb, uplo)
