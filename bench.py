@@ -517,8 +517,8 @@ def roofline_emulated(L, nb, dev, stream, s):
     Tc = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
     sa = torch.empty(8 * ldk * nb, dtype=torch.bfloat16, device=dev)
     sb = torch.empty(8 * ldk * nb, dtype=torch.bfloat16, device=dev)
-    ea = torch.empty(nb, dtype=torch.int32, device=dev)
-    eb = torch.empty(nb, dtype=torch.int32, device=dev)
+    ea = torch.empty(nb, dtype=torch.int64, device=dev)
+    eb = torch.empty(nb, dtype=torch.int64, device=dev)
     L.dg_f64_slices(nb, nb, Ta.data_ptr(), nb, 1, sa.data_ptr(), ldk, ea.data_ptr(), s)
     L.dg_f64_slices(nb, nb, Tb.data_ptr(), nb, 1, sb.data_ptr(), ldk, eb.data_ptr(), s)
 

@@ -104,19 +104,21 @@ int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abo
 // FP64 GEMM emulated on the BF16 tensor cores (oz_gemm.cu).  oz_split cuts
 // ncols FP64 vectors of length K (element k of vector c at
 // src[c*cstride + k*kstride]) into 8 BF16 slices (slice s of vector c at
-// slices + s*sstride + c*ldk) and per-vector exponents e; oz_gemm computes
-// C(m x n) = alpha * sum_p A(p, i) B(p, j) + beta * C from the slices of the m
-// A-vectors and n B-vectors (K <= 1024, ldk a multiple of 8); tri 1 / 2
-// stores only the upper / lower triangle.  Kernels skip when *status or
-// *abort2 is non-zero; a timed-out wait records DG_ERR_TIMEOUT in *status.
+// slices + s*sstride + c*ldk) and one 8-byte scale word per vector; oz_gemm
+// computes C(m x n) = alpha * sum_p A(p, i) B(p, j) + beta * C from the
+// slices of the m A-vectors and n B-vectors (K <= 1024, ldk a multiple of 8);
+// tri 1 / 2 stores only the upper / lower triangle.  Kernels skip when
+// *status or *abort2 is non-zero; a timed-out wait records DG_ERR_TIMEOUT in
+// *status.
 constexpr int kOzSlices = 8;
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
-             void *slices, long long ldk, long long sstride, int *e, const int *abort_flag,
-             cudaStream_t s, const int *abort2 = nullptr);
+             void *slices, long long ldk, long long sstride, unsigned long long *scales,
+             const int *abort_flag, cudaStream_t s, const int *abort2 = nullptr);
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
-            long long a_sstride, const int *ea, const void *b_slices, long long ldb_k,
-            long long b_sstride, const int *eb, double beta, double *C, long long ldc, int tri,
-            int *status, cudaStream_t s, const int *abort2 = nullptr);
+            long long a_sstride, const unsigned long long *a_scales, const void *b_slices,
+            long long ldb_k, long long b_sstride, const unsigned long long *b_scales, double beta,
+            double *C, long long ldc, int tri, int *status, cudaStream_t s,
+            const int *abort2 = nullptr);
 // C = alpha op(A) op(B) + beta C (BLAS gemm / syrk arguments; tri as above)
 // through split + oz_gemm with the slices in caller scratch of `bytes`
 // (oz_scratch_bytes).  Returns 1 without work when k > 1024 or the scratch

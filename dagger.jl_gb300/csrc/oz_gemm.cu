@@ -1,16 +1,20 @@
 // FP64 GEMM emulated on the BF16 tensor cores (Ozaki's error-free splitting),
 // for the FP64 tile updates of the plain path and the FP64 residual of
-// refinement.  GB300 executes FP64 arithmetic at about 1.2 TFLOP/s, so the
-// FP64 products are carried out on tcgen05 exactly, and only a short FP64
-// accumulation per output element remains on the FP64 pipe.
+// refinement.  GB300 executes FP64 arithmetic at about 1.1 TFLOP/s, so the
+// FP64 products are carried out on tcgen05 exactly, the sums are formed in
+// 64-bit integers, and one FP64 operation per output element remains.
 //
-// Splitting (oz_split_kernel): each operand vector v (a row of op(A) or a
-// column of op(B), K values) is scaled by 2^-e with 2^(e-1) <= max|v| < 2^e,
-// and cut into S = 8 slices by rounding to nearest:
+// Splitting (oz_max_kernel, oz_slice_kernel): each operand vector v (a row of
+// op(A) or a column of op(B), K values) is scaled by 2^-e with
+// 2^(e-1) <= max|v| < 2^e and cut into S = 8 slices by rounding to nearest:
 //     v = 2^e * sum_{s=1..8} d_s 2^(-7 s) + r,   d_s integer,
 //     |d_1| <= 128, |d_s| <= 64 (s >= 2), |r| <= 2^(e-57).
 // Slice s is stored as the BF16 value d_s 2^(-7s): exact, since every
-// integer of magnitude <= 256 has at most 8 significant bits.
+// integer of magnitude <= 256 has at most 8 significant bits.  The split
+// runs on integer arithmetic: the per-vector scale word is max|v|'s bit
+// pattern (an atomic maximum over the vector), e follows from its exponent
+// field, and X = round(v 2^(56-e)) (|X| <= 2^56) is cut into base-128 digits.
+// A vector holding an infinity or a NaN makes every output that uses it NaN.
 //
 // Products (oz_gemm_kernel): C = alpha * 2^(ea_i + eb_j) * sum_{s+t<=9} A_s B_t'
 // + beta * C, K <= 1024.  A product A_s B_t' sums terms d_s d_t 2^(-7(s+t)).
@@ -19,11 +23,13 @@
 // 2^(-7L) (level 6: (2*128*64 + 2*64*64 + 64*64) * 512 < 2^24; levels 2 and
 // 3 within 2^24 over all 1024), so its FP32 accumulation in TMEM is exact.
 // Levels 2..6 are read exactly after each window and summed as 64-bit
-// integers in units of 2^-42 (|sum| < 2^53 over K = 1024, exact again in the
-// final conversion to FP64).  Levels 7..9 accumulate in FP32 over the whole
-// K; their rounding is below 2^-56 of |C|'s scale, and the dropped levels
-// (>= 10) and the slicing remainder are below 2^-55.  The result has an FP64
-// GEMM's accuracy relative to 2^(ea_i + eb_j) K.
+// integers in units of 2^-42 (|sum| < 2^53 over K = 1024).  Levels 7..9
+// accumulate in FP32 over the whole K (their rounding is below 2^-56 of
+// |C|'s scale; the dropped levels >= 10 and the slicing remainder are below
+// 2^-55) and join the integer sum at 2^-51.  The 62-bit total is rounded
+// once to FP64 by integer arithmetic, with 2^(ea_i + eb_j) folded into the
+// exponent, and added to beta C.  The result has an FP64 GEMM's accuracy
+// relative to 2^(ea_i + eb_j) K.
 //
 // TMEM holds one 64-column accumulator per level, level L at columns
 // 64 (L - 2) .. 64 (L - 1) - 1 (all 512 columns).  The B slices of a stage
@@ -34,10 +40,13 @@
 //
 // CTA tile: 128 rows (TMEM lanes) x 64 columns.  K advances in stages of 32:
 // one stage holds the 8 slices of the A tile and of the B tile (96 KiB, two
-// 3-D TMA loads with 64-byte swizzle), and two stages are in flight.  6
-// warps: warp 4 issues the TMA loads, warp 5 the MMAs (levels 7..9 first),
-// warps 0-3 read levels 2..6 at the end of each window (one row per thread,
-// 64 integers) while the next stage's MMAs onto levels 7..9 run.
+// 3-D TMA loads with 64-byte swizzle), and two stages are in flight.  18
+// warps: warp 16 issues the TMA loads, warp 17 the MMAs (levels 7..9 first),
+// warps 0-15 (four per TMEM lane quarter, 16 columns each) read levels 2..6
+// at the end of each window while the next stage's MMAs onto levels 7..9
+// run; at the start they prefetch the C tile into L2 and decode the column
+// exponents, at the end they form the outputs (several warps per scheduler,
+// so the integer epilogue's latency is hidden).
 // All waits are bounded (1 s): a timeout records DG_ERR_TIMEOUT and the CTA
 // drains and returns.
 #include <cuda_bf16.h>
@@ -59,11 +68,16 @@ constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB
 constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB
 constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 96 KiB
 constexpr int OZ_STAGES = 2;
-constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE + 1024 + 256;
+constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE + 1024 + 512;
+constexpr int OZ_GUARD = 9;                               // extra fraction bits of the sum
+constexpr int OZ_READERS = 16;                            // reader warps: 4 per TMEM lane quarter
+constexpr int OZ_RCOLS = OZ_BN / (OZ_READERS / 4);        // columns per reader thread (16)
+constexpr int OZ_PRODUCER = OZ_READERS, OZ_ISSUER = OZ_READERS + 1;
+constexpr int OZ_THREADS = 32 * (OZ_READERS + 2);
 
 struct OzParams {
-  CUtensorMap a, b;       // 3-D maps: {K, rows, slice}
-  const int *ea, *eb;     // exponents per A row / per B row
+  CUtensorMap a, b;                 // 3-D maps: {K, rows, slice}
+  const unsigned long long *ma, *mb;  // scale words per A row / per B row
   double *c;
   long long ldc;
   int m, n, k;
@@ -73,7 +87,51 @@ struct OzParams {
   const int *abort2;      // skip when non-zero (read only)
 };
 
-__global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__ OzParams p) {
+// frexp exponent of the non-negative double with bits b (0 for 0).
+__device__ __forceinline__ int exponent_of(unsigned long long b) {
+  const int eb = (int)(b >> 52);
+  if (eb >= 0x7FF) return kOzNonFinite;
+  if (eb) return eb - 1022;
+  if (b == 0) return 0;
+  return (63 - __clzll((long long)b)) + 1 - 1074;  // subnormal: b * 2^-1074
+}
+
+// Results outside the normal range (overflow, subnormal): the library's
+// scaling, kept out of line so that the common path stays integer-only.
+__device__ __noinline__ double scale_slow(unsigned long long sign, int p, unsigned long long mant,
+                                          int E) {
+  return ldexp(__longlong_as_double((long long)(sign | ((unsigned long long)(p + 1023) << 52) |
+                                                (mant & 0xFFFFFFFFFFFFFull))),
+               E);
+}
+
+// T * 2^E as a double, rounded to nearest even once (T < 2^63 in magnitude).
+__device__ __forceinline__ double int_to_double_scaled(long long T, int E) {
+  if (T == 0) return 0.0;
+  const unsigned long long sign = T < 0 ? (1ull << 63) : 0ull;
+  unsigned long long u = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
+  int p = 63 - __clzll((long long)u);  // leading bit
+  unsigned long long mant;
+  if (p <= 52) {
+    mant = u << (52 - p);
+  } else {
+    const int sh = p - 52;
+    mant = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1))) mant++;
+    if (mant >> 53) {
+      mant >>= 1;
+      p++;
+    }
+  }
+  const int biased = p + E + 1023;
+  if (biased >= 1 && biased <= 2046)
+    return __longlong_as_double(
+        (long long)(sign | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+  return scale_slow(sign, p, mant, E);
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_constant__ OzParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + OZ_STAGES * OZ_STAGE);
@@ -83,11 +141,12 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
   uint64_t *done = drained + 1;          // MMA -> readers: everything complete
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   int *abort_flag = (int *)(tmem_slot + 1);
+  int *eb_s = abort_flag + 1;            // the 64 column exponents
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i0 = blockIdx.x * OZ_BM, j0 = blockIdx.y * OZ_BN;
   if ((p.tri == 1 && i0 > j0 + OZ_BN - 1) || (p.tri == 2 && j0 > i0 + OZ_BM - 1)) return;
-  // one read of the status word decides for the whole CTA
+  // one read of the status words decides for the whole CTA
   if (threadIdx.x == 0)
     *abort_flag = aborted(p.status, p.abort2) ? 1 : 0;
   __syncthreads();
@@ -100,7 +159,7 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
       mbar_init(&empty[s], 1);
     }
     mbar_init(ready, 1);
-    mbar_init(drained, 128);
+    mbar_init(drained, 32 * OZ_READERS);
     mbar_init(done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -114,13 +173,15 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   }
+  if (threadIdx.x < OZ_BN)
+    eb_s[threadIdx.x] = (j0 + (int)threadIdx.x < p.n) ? exponent_of(p.mb[j0 + threadIdx.x]) : 0;
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const int nst = (p.k + OZ_BK - 1) / OZ_BK;  // stages
   const int nwin = (nst + OZ_WIN - 1) / OZ_WIN;
 
-  if (warp == 4) {
+  if (warp == OZ_PRODUCER) {
     if (lane == 0) {
       // ---------------- TMA producer ----------------
       int it = 0;
@@ -140,7 +201,7 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
         if (!mbar_wait(&full[q % OZ_STAGES], (q / OZ_STAGES) & 1)) atomicExch(abort_flag, 1);
     }
     __syncwarp();
-  } else if (warp == 5) {
+  } else if (warp == OZ_ISSUER) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
       const uint32_t idesc64 = idesc_f16kind(OZ_BM, OZ_BN, false);  // N = 64 c: + (8 (c-1)) << 17
@@ -189,29 +250,42 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
       mma_commit(done);
     }
     __syncwarp();
+  } else {
+    // ---------------- readers: C into L2 while the MMAs run ----------------
+    for (int line = threadIdx.x; line < OZ_BN * (OZ_BM / 16); line += 32 * OZ_READERS) {
+      const int col = j0 + line / (OZ_BM / 16), row = i0 + 16 * (line % (OZ_BM / 16));
+      if (col < p.n && row < p.m)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p.c + (size_t)row + (size_t)col * p.ldc));
+    }
   }
 
-  // ---------------- exact sums (warps 0-3) ----------------
-  long long acc[OZ_BN];
+  // ---------------- exact sums (reader warps) ----------------
+  // reader warp w: TMEM lanes 32 (w mod 4) .. + 31 (one output row per
+  // thread), columns cb .. cb + 15 with cb = 16 (w / 4)
+  const bool reader = warp < OZ_READERS;
+  const int cb = (warp >> 2) * OZ_RCOLS;
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+  long long acc[OZ_RCOLS];
 #pragma unroll
-  for (int c = 0; c < OZ_BN; c++) acc[c] = 0;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-  for (int w = 0; w < nwin && warp < 4; w++) {
+  for (int c = 0; c < OZ_RCOLS; c++) acc[c] = 0;
+  for (int w = 0; w < nwin && reader; w++) {
     if (!mbar_wait(ready, w & 1)) {
       atomicExch(abort_flag, 1);
       break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
+#pragma unroll
     for (int lvl = 2; lvl <= 6; lvl++) {
       const float up = __int_as_float((127 + 7 * lvl) << 23);  // 2^(7 lvl)
-      const long long unit = 1LL << (7 * (6 - lvl));           // 2^(7 (6 - lvl))
+      const int sh = 7 * (6 - lvl);                            // x 2^(7 (6 - lvl))
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        float v[32];
-        tmem_ld32(tmem + 64 * (lvl - 2) + h * 32 + lane_base, v);
+      for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
+        float v[16];
+        tmem_ld16(tmem + 64 * (lvl - 2) + cb + ch + lane_base, v);
 #pragma unroll
-        for (int c = 0; c < 32; c++) acc[h * 32 + c] += (long long)__float2int_rn(v[c] * up) * unit;
+        for (int c = 0; c < 16; c++)
+          acc[ch + c] +=
+              (long long)((unsigned long long)(long long)__float2int_rn(v[c] * up) << sh);
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -221,48 +295,57 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!ok) atomicExch(abort_flag, 1);
   __syncthreads();
-  const bool aborted = *(volatile int *)abort_flag != 0;
-  if (!aborted && nst > 0 && warp < 4) {
-    const int row = i0 + warp * 32 + lane;
-    const int ea = row < p.m ? p.ea[row] : 0;
+  const bool aborted_now = *(volatile int *)abort_flag != 0;
+  if (!aborted_now && nst > 0 && reader) {
+    const int row = i0 + (warp & 3) * 32 + lane;
+    const int ea = row < p.m ? exponent_of(p.ma[row]) : 0;
+    // levels 9, 8, 7 summed in FP32 (all lanes: the loads are warp-wide),
+    // joined to the integer sum at 2^-(42 + OZ_GUARD) (|v| < 2^-21)
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      // levels 9, 8, 7 summed in FP32 (all lanes: the loads are warp-wide)
-      float v[32], w[32];
-      tmem_ld32(tmem + 64 * 7 + h * 32 + lane_base, v);
-#pragma unroll 1
-      for (int lvl = 8; lvl >= 7; lvl--) {
-        tmem_ld32(tmem + 64 * (lvl - 2) + h * 32 + lane_base, w);
+    for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
+      float v[16], w[16];
+      tmem_ld16(tmem + 64 * 7 + cb + ch + lane_base, v);
+      tmem_ld16(tmem + 64 * 6 + cb + ch + lane_base, w);
 #pragma unroll
-        for (int c = 0; c < 32; c++) v[c] = w[c] + v[c];
+      for (int c = 0; c < 16; c++) v[c] = w[c] + v[c];
+      tmem_ld16(tmem + 64 * 5 + cb + ch + lane_base, w);
+#pragma unroll
+      for (int c = 0; c < 16; c++)
+        acc[ch + c] = (long long)((unsigned long long)acc[ch + c] << OZ_GUARD) +
+                      (long long)__float2int_rn((w[c] + v[c]) * 0x1p51f);
+    }
+    if (row < p.m) {
+      const bool fast = (p.alpha == -1.0 && p.beta == 1.0);
+#pragma unroll
+      for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
+      double old[16];
+#pragma unroll
+      for (int c = 0; c < 16; c++) {
+        const int col = j0 + cb + ch + c;
+        const bool in = col < p.n && !(p.tri == 1 && row > col) && !(p.tri == 2 && row < col);
+        old[c] = (in && p.beta != 0.0) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
       }
-      if (row >= p.m) continue;
-      // 8 columns at a time: their reads of C are issued before the writes
 #pragma unroll
-      for (int c0 = 0; c0 < 32; c0 += 8) {
-        double old[8];
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-          const int col = j0 + h * 32 + c0 + c;
-          const bool in = col < p.n && !(p.tri == 1 && row > col) && !(p.tri == 2 && row < col);
-          old[c] = (in && p.beta != 0.0) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
+      for (int c = 0; c < 16; c++) {
+        const int col = j0 + cb + ch + c;
+        if (col >= p.n || (p.tri == 1 && row > col) || (p.tri == 2 && row < col)) continue;
+        const int eb = eb_s[cb + ch + c];
+        double vout;
+        if (ea == kOzNonFinite || eb == kOzNonFinite) {
+          vout = __longlong_as_double(0x7FF8000000000000ll);
+        } else {
+          const double x = int_to_double_scaled(acc[ch + c], ea + eb - 42 - OZ_GUARD);
+          if (fast)
+            vout = old[c] - x;
+          else
+            vout = (p.beta != 0.0) ? fma(p.alpha, x, p.beta * old[c]) : p.alpha * x;
         }
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-          const int col = j0 + h * 32 + c0 + c;
-          if (col >= p.n || (p.tri == 1 && row > col) || (p.tri == 2 && row < col)) continue;
-          const double x = fma((double)acc[h * 32 + c0 + c], 0x1p-42, (double)v[c0 + c]);
-          const int eb = p.eb[col];
-          double vout = (ea == kOzNonFinite || eb == kOzNonFinite)
-                            ? __longlong_as_double(0x7FF8000000000000ll)
-                            : p.alpha * ldexp(x, ea + eb);
-          if (p.beta != 0.0) vout = fma(p.beta, old[c], vout);
-          p.c[(size_t)row + (size_t)col * p.ldc] = vout;
-        }
+        p.c[(size_t)row + (size_t)col * p.ldc] = vout;
+      }
       }
     }
   }
-  if (aborted && threadIdx.x == 0 && p.status) atomicCAS(p.status, 0, DG_ERR_TIMEOUT);
+  if (aborted_now && threadIdx.x == 0 && p.status) atomicCAS(p.status, 0, DG_ERR_TIMEOUT);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
@@ -270,26 +353,15 @@ __global__ void __launch_bounds__(192, 1) oz_gemm_kernel(const __grid_constant__
                  : "memory");
 }
 
-// Splitting runs on integer arithmetic (the FP64 pipe is slow on this
-// part): the exponent comes from the bits of max|v|, and the 56-bit integer
-// X = round(v * 2^(56 - e)) (|X| <= 2^56) is cut into base-128 digits
-// d_8 .. d_2 in [-64, 63] by rounding to nearest, leaving d_1 in [-128, 128].
-// A vector holding an infinity or a NaN gets the exponent kOzNonFinite, and
-// every output that uses it is NaN.
+// ---------------------------------------------------------------------------
+// splitting
+// ---------------------------------------------------------------------------
 constexpr int SPLIT_V = 32;    // vectors per CTA
+constexpr int MAX_K = 256;     // values of K per scale CTA
 constexpr int SPLIT_K = 128;   // values of K per slicing CTA
 
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-}
-
-// frexp exponent of the non-negative double with bits b (0 for 0).
-__device__ __forceinline__ int exponent_of(unsigned long long b) {
-  const int eb = (int)(b >> 52);
-  if (eb == 0x7FF) return kOzNonFinite;
-  if (eb) return eb - 1022;
-  if (b == 0) return 0;
-  return (63 - __clzll((long long)b)) + 1 - 1074;  // subnormal: b * 2^-1074
 }
 
 // round(v * 2^(56 - ex)) for |v| < 2^ex.
@@ -307,43 +379,54 @@ __device__ __forceinline__ long long scaled56(double v, int ex) {
   return (b >> 63) ? -r : r;
 }
 
-// Exponent of each of `ncols` vectors of length K (element k of vector c at
-// src[c*cstride + k*kstride]).  CTA: 32 x 8 threads over 32 vectors, reading
-// along whichever of k or c is contiguous.
-__global__ void __launch_bounds__(256) oz_exp_kernel(const double *src, long long cstride,
-                                                    long long kstride, int K, int ncols, int *e,
-                                                    const int *abort_flag, const int *abort2) {
+// Scale words of `ncols` vectors of length K (element k of vector c at
+// src[c*cstride + k*kstride]): the maximum of |v|'s bit pattern, by atomic
+// maximum over CTAs of 32 vectors x 256 values of K (the words start at 0).
+// CTA: 32 x 8 threads reading along whichever of k or c is contiguous.
+__global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long long cstride,
+                                                    long long kstride, int K, int ncols,
+                                                    unsigned long long *mb, const int *abort_flag,
+                                                    const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
   __shared__ unsigned long long red[8][SPLIT_V + 1];
-  const int tx = threadIdx.x, ty = threadIdx.y, c0 = blockIdx.x * SPLIT_V;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int c0 = blockIdx.x * SPLIT_V, k0 = blockIdx.y * MAX_K;
+  const int k1 = min(K, k0 + MAX_K);
   if (kstride == 1) {  // columns: lanes along k, warp ty over vectors ty, ty+8, ...
-    for (int vi = ty; vi < SPLIT_V; vi += 8) {
-      const int c = c0 + vi;
+#pragma unroll
+    for (int i = 0; i < SPLIT_V / 8; i++) {
+      const int c = c0 + ty + 8 * i;
       unsigned long long m = 0;
-      if (c < ncols)
-        for (int k = tx; k < K; k += 32) {
-          const unsigned long long a = abs_bits(src[(size_t)c * cstride + k]);
+      if (c < ncols) {
+        const double *v = src + (size_t)c * cstride;
+#pragma unroll
+        for (int j = 0; j < MAX_K / 32; j++) {
+          const int k = k0 + tx + 32 * j;
+          const unsigned long long a = k < k1 ? abs_bits(v[k]) : 0ull;
           m = a > m ? a : m;
         }
+      }
       for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long q = __shfl_xor_sync(0xffffffffu, m, o);
         m = q > m ? q : m;
       }
-      if (tx == 0 && c < ncols) e[c] = exponent_of(m);
+      if (tx == 0 && c < ncols && m) atomicMax(mb + c, m);
     }
-  } else {             // rows (or general strides): lanes along vectors
+  } else {             // rows (or general strides): lanes along vectors, warps along k
     const int c = c0 + tx;
     unsigned long long m = 0;
-    if (c < ncols)
-      for (int k = ty; k < K; k += 8) {
+    if (c < ncols) {
+#pragma unroll 8
+      for (int k = k0 + ty; k < k1; k += 8) {
         const unsigned long long a = abs_bits(src[(size_t)c * cstride + (size_t)k * kstride]);
         m = a > m ? a : m;
       }
+    }
     red[ty][tx] = m;
     __syncthreads();
     if (ty == 0 && c < ncols) {
       for (int y = 1; y < 8; y++) m = red[y][tx] > m ? red[y][tx] : m;
-      e[c] = exponent_of(m);
+      if (m) atomicMax(mb + c, m);
     }
   }
 }
@@ -355,13 +438,14 @@ __global__ void __launch_bounds__(256) oz_exp_kernel(const double *src, long lon
 __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long long cstride,
                                                       long long kstride, int K, int ncols,
                                                       __nv_bfloat16 *dst, long long ldk,
-                                                      long long sstride, const int *e,
+                                                      long long sstride,
+                                                      const unsigned long long *mb,
                                                       const int *abort_flag, const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
   __shared__ double tile[SPLIT_V][33];
   __shared__ int ex[SPLIT_V];
   const int tx = threadIdx.x, ty = threadIdx.y, c0 = blockIdx.x * SPLIT_V;
-  if (ty == 0) ex[tx] = (c0 + tx < ncols) ? e[c0 + tx] : 0;
+  if (ty == 0) ex[tx] = (c0 + tx < ncols) ? exponent_of(mb[c0 + tx]) : 0;
   for (int kc = blockIdx.y * SPLIT_K; kc < (blockIdx.y + 1) * SPLIT_K && kc < ldk; kc += 32) {
     __syncthreads();
     if (kstride == 1) {
@@ -429,36 +513,38 @@ bool oz_map(CUtensorMap *map, const void *base, long long ldk, long long rows, l
 }  // namespace
 
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
-             void *slices, long long ldk, long long sstride, int *e, const int *abort_flag,
-             cudaStream_t s, const int *abort2) {
+             void *slices, long long ldk, long long sstride, unsigned long long *scales,
+             const int *abort_flag, cudaStream_t s, const int *abort2) {
   if (ncols <= 0) return 0;
+  DG_CUDA_TRY(cudaMemsetAsync(scales, 0, sizeof(unsigned long long) * (size_t)ncols, s));
   const dim3 blk(32, 8);
   const int nv = (ncols + SPLIT_V - 1) / SPLIT_V;
-  oz_exp_kernel<<<nv, blk, 0, s>>>(src, cstride, kstride, K, ncols, e, abort_flag, abort2);
+  oz_max_kernel<<<dim3(nv, (K + MAX_K - 1) / MAX_K), blk, 0, s>>>(src, cstride, kstride, K, ncols,
+                                                                  scales, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   const dim3 grid(nv, (unsigned)((ldk + SPLIT_K - 1) / SPLIT_K));
   oz_slice_kernel<<<grid, blk, 0, s>>>(src, cstride, kstride, K, ncols, (__nv_bfloat16 *)slices,
-                                       ldk, sstride, e, abort_flag, abort2);
+                                       ldk, sstride, scales, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(2);
   return 0;
 }
 
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
-            long long a_sstride, const int *ea, const void *b_slices, long long ldb_k,
-            long long b_sstride, const int *eb, double beta, double *C, long long ldc, int tri,
-            int *status, cudaStream_t s, const int *abort2) {
+            long long a_sstride, const unsigned long long *ma, const void *b_slices,
+            long long ldb_k, long long b_sstride, const unsigned long long *mb, double beta,
+            double *C, long long ldc, int tri, int *status, cudaStream_t s, const int *abort2) {
   if (m <= 0 || n <= 0) return 0;
   if (k <= 0 || k > 1024 || lda_k % 8 || ldb_k % 8) return DG_ERR_UNSUPPORTED;
+  if (lda_k < k || ldb_k < k) return DG_ERR_UNSUPPORTED;
   OzParams p;
   memset(&p, 0, sizeof p);
-  if (lda_k < k || ldb_k < k) return DG_ERR_UNSUPPORTED;
   if (!oz_map(&p.a, a_slices, lda_k, m, a_sstride, OZ_BM) ||
       !oz_map(&p.b, b_slices, ldb_k, n, b_sstride, OZ_BN)) {
     dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
     return DG_ERR_CUDA;
   }
-  p.ea = ea; p.eb = eb; p.c = C; p.ldc = ldc;
+  p.ma = ma; p.mb = mb; p.c = C; p.ldc = ldc;
   p.m = m; p.n = n; p.k = k; p.alpha = alpha; p.beta = beta; p.tri = tri;
   p.status = status;
   p.abort2 = abort2;
@@ -471,7 +557,7 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
     attr[dev & 63] = true;
   }
   dim3 grid((m + OZ_BM - 1) / OZ_BM, (n + OZ_BN - 1) / OZ_BN);
-  oz_gemm_kernel<<<grid, 192, OZ_SMEM, s>>>(p);
+  oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(p);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -481,8 +567,8 @@ static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 size_t oz_scratch_bytes(int m, int n, int k, bool same) {
   const size_t ldk = (size_t)(k + 7) / 8 * 8;
-  size_t b = round256((size_t)OZ_S * ldk * m * 2) + round256((size_t)m * 4);
-  if (!same) b += round256((size_t)OZ_S * ldk * n * 2) + round256((size_t)n * 4);
+  size_t b = round256((size_t)OZ_S * ldk * m * 2) + round256((size_t)m * 8);
+  if (!same) b += round256((size_t)OZ_S * ldk * n * 2) + round256((size_t)n * 8);
   return b;
 }
 
@@ -499,20 +585,20 @@ int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const d
   char *q = (char *)scratch;
   void *sa = q;
   q += round256((size_t)OZ_S * ldk * m * 2);
-  int *ea = (int *)q;
-  q += round256((size_t)m * 4);
+  unsigned long long *ma = (unsigned long long *)q;
+  q += round256((size_t)m * 8);
   void *sb = sa;
-  int *eb = ea;
+  unsigned long long *mb = ma;
   // row i of op(A), element p: A[i + p lda] ('N') or A[p + i lda] ('T')
-  DG_TRY(oz_split(A, tA ? lda : 1, tA ? 1 : lda, k, m, sa, ldk, ldk * m, ea, status, s, abort2));
+  DG_TRY(oz_split(A, tA ? lda : 1, tA ? 1 : lda, k, m, sa, ldk, ldk * m, ma, status, s, abort2));
   if (!same) {
     sb = q;
     q += round256((size_t)OZ_S * ldk * n * 2);
-    eb = (int *)q;
+    mb = (unsigned long long *)q;
     // column j of op(B), element p: B[p + j ldb] ('N') or B[j + p ldb] ('T')
-    DG_TRY(oz_split(B, tB ? 1 : ldb, tB ? ldb : 1, k, n, sb, ldk, ldk * n, eb, status, s, abort2));
+    DG_TRY(oz_split(B, tB ? 1 : ldb, tB ? ldb : 1, k, n, sb, ldk, ldk * n, mb, status, s, abort2));
   }
-  return oz_gemm(m, n, k, alpha, sa, ldk, ldk * m, ea, sb, ldk, same ? ldk * m : ldk * n, eb, beta,
+  return oz_gemm(m, n, k, alpha, sa, ldk, ldk * m, ma, sb, ldk, same ? ldk * m : ldk * n, mb, beta,
                  C, ldc, tri, status, s, abort2);
 }
 
@@ -545,25 +631,29 @@ extern "C" int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const 
 // that reuse the slices of one operand across many products (the tiles of a
 // factor, the matrix of a refinement residual).
 extern "C" int dg_f64_slices(int k, int ncols, const double *src, long long cstride,
-                             long long kstride, void *slices, int ldk, int *exps, void *stream) {
+                             long long kstride, void *slices, int ldk, void *scales,
+                             void *stream) {
   DG_CHECK_ARG(k > 0 && k <= 1024, 1);
   DG_CHECK_ARG(ncols >= 0, 2);
   DG_CHECK_ARG(ldk >= k && ldk % 8 == 0, 7);
   DG_CHECK_ARG(((uintptr_t)slices & 15) == 0, 6);
-  return dg::oz_split(src, cstride, kstride, k, ncols, slices, ldk, (long long)ldk * ncols, exps,
-                      nullptr, (cudaStream_t)stream);
+  DG_CHECK_ARG(((uintptr_t)scales & 7) == 0, 8);
+  return dg::oz_split(src, cstride, kstride, k, ncols, slices, ldk, (long long)ldk * ncols,
+                      (unsigned long long *)scales, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int dg_gemm_f64_slices(int m, int n, int k, double alpha, const void *a_slices,
-                                  int lda_k, const int *ea, const void *b_slices, int ldb_k,
-                                  const int *eb, double beta, double *C, int ldc, int *status,
-                                  void *stream) {
+                                  int lda_k, const void *a_scales, const void *b_slices, int ldb_k,
+                                  const void *b_scales, double beta, double *C, int ldc,
+                                  int *status, void *stream) {
   DG_CHECK_ARG(m >= 0, 1);
   DG_CHECK_ARG(n >= 0, 2);
   DG_CHECK_ARG(k > 0 && k <= 1024, 3);
   DG_CHECK_ARG(lda_k >= k && lda_k % 8 == 0, 6);
   DG_CHECK_ARG(ldb_k >= k && ldb_k % 8 == 0, 9);
   DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 13);
-  return dg::oz_gemm(m, n, k, alpha, a_slices, lda_k, (long long)lda_k * m, ea, b_slices, ldb_k,
-                     (long long)ldb_k * n, eb, beta, C, ldc, 0, status, (cudaStream_t)stream);
+  return dg::oz_gemm(m, n, k, alpha, a_slices, lda_k, (long long)lda_k * m,
+                     (const unsigned long long *)a_scales, b_slices, ldb_k, (long long)ldb_k * n,
+                     (const unsigned long long *)b_scales, beta, C, ldc, 0, status,
+                     (cudaStream_t)stream);
 }

@@ -121,8 +121,10 @@ int DeviceState::oz_workspace(size_t bytes, void **p) {
   return 0;
 }
 
+// A slot: the 8 BF16 slices of up to `cap` vectors of padded length ldk,
+// then one 8-byte scale word per vector.
 size_t oz_slot_bytes(long long ldk, long long cap) {
-  size_t b = (size_t)kOzSlices * ldk * cap * 2 + (size_t)cap * 4;
+  size_t b = (size_t)kOzSlices * ldk * cap * 2 + (size_t)cap * 8;
   return (b + 255) & ~(size_t)255;
 }
 
@@ -369,14 +371,14 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case OP_OZ_SPLIT: {
       const bool cols = (t.trans == 'N');
       const long long sstride = (long long)t.ldc * t.k;
-      int *e = (int *)((char *)t.c + (size_t)kOzSlices * sstride * 2);
+      auto *e = (unsigned long long *)((char *)t.c + (size_t)kOzSlices * sstride * 2);
       return oz_split(t.a, cols ? t.lda : 1, cols ? 1 : t.lda, t.m, t.n, t.c, t.ldc, sstride, e,
                       info, s);
     }
     case OP_OZ_GEMM: {
       const long long sstride = (long long)t.lda * t.ldb;
-      const int *ea = (const int *)((const char *)t.a + (size_t)kOzSlices * sstride * 2);
-      const int *eb = (const int *)((const char *)t.b + (size_t)kOzSlices * sstride * 2);
+      auto *ea = (const unsigned long long *)((const char *)t.a + (size_t)kOzSlices * sstride * 2);
+      auto *eb = (const unsigned long long *)((const char *)t.b + (size_t)kOzSlices * sstride * 2);
       const int tri = (t.uplo == 'U' || t.uplo == 'u') ? 1 : (t.uplo == 'L' || t.uplo == 'l') ? 2 : 0;
       return oz_gemm(t.m, t.n, t.k, t.alpha, t.a, t.lda, sstride, ea, t.b, t.lda, sstride, eb,
                      t.beta, t.c, t.ldc, tri, info, s);

@@ -285,16 +285,18 @@ int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const double *A, 
  * ncols FP64 vectors of length k <= 1024 (element p of vector c at
  * src[c*cstride + p*kstride]) into 8 BF16 slices, slice s of vector c at
  * slices + 2*(s*ldk*ncols + c*ldk) bytes (ldk >= k, a multiple of 8; the
- * buffer 16-byte aligned, 16*ldk*ncols bytes), and one exponent per vector.
- * dg_gemm_f64_slices computes C = alpha A'B + beta C from the slices of the
- * m columns of A and the n columns of B (lda_k, ldb_k: their ldk).  status:
- * optional device word; the kernel skips when it is non-zero and records
- * DG_ERR_TIMEOUT there if a wait times out. */
+ * buffer 16-byte aligned, 16*ldk*ncols bytes), and one 8-byte scale word per
+ * vector in `scales` (8-byte aligned, 8*ncols bytes).  dg_gemm_f64_slices
+ * computes C = alpha A'B + beta C from the slices of the m columns of A and
+ * the n columns of B (lda_k, ldb_k: their ldk).  status: optional device
+ * word; the kernel skips when it is non-zero and records DG_ERR_TIMEOUT
+ * there if a wait times out. */
 int dg_f64_slices(int k, int ncols, const double *src, long long cstride, long long kstride,
-                  void *slices, int ldk, int *exps, void *stream);
+                  void *slices, int ldk, void *scales, void *stream);
 int dg_gemm_f64_slices(int m, int n, int k, double alpha, const void *a_slices, int lda_k,
-                       const int *ea, const void *b_slices, int ldb_k, const int *eb, double beta,
-                       double *C, int ldc, int *status, void *stream);
+                       const void *a_scales, const void *b_slices, int ldb_k,
+                       const void *b_scales, double beta, double *C, int ldc, int *status,
+                       void *stream);
 
 /* ---------------------------------------------------------------------------
  * Batched persistent launch (no counterpart in the reference, which would

@@ -179,8 +179,8 @@ def test_slice_stages_match_one_call():
     d.gemm_f64_emulated_tn(-1.0, Ad, Bd, 1.0, C1)
     sa = torch.empty(8 * ldk * m, dtype=torch.bfloat16, device="cuda")
     sb = torch.empty(8 * ldk * n, dtype=torch.bfloat16, device="cuda")
-    ea = torch.empty(m, dtype=torch.int32, device="cuda")
-    eb = torch.empty(n, dtype=torch.int32, device="cuda")
+    ea = torch.empty(m, dtype=torch.int64, device="cuda")
+    eb = torch.empty(n, dtype=torch.int64, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
     assert L.dg_f64_slices(k, m, Ad.data_ptr(), k, 1, sa.data_ptr(), ldk, ea.data_ptr(), s) == 0
     assert L.dg_f64_slices(k, n, Bd.data_ptr(), k, 1, sb.data_ptr(), ldk, eb.data_ptr(), s) == 0
