@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
 // ---------------------------------------------------------------------------
 constexpr int SPLIT_V = 32;    // vectors per CTA
 constexpr int MAX_K = 256;     // values of K per scale CTA
-constexpr int SPLIT_K = 128;   // values of K per slicing CTA
+constexpr int SPLIT_K = 64;    // values of K per slicing CTA
 
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
@@ -431,10 +431,11 @@ __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long lon
   }
 }
 
-// Slices of the vectors [32 bx, 32 bx + 32) over k in [128 by, 128 by + 128)
+// Slices of the vectors [32 bx, 32 bx + 32) over k in [64 by, 64 by + 64)
 // (k < ldk; zeros for k >= K): slice s (0-based) of vector c at
-// dst + s*sstride + c*ldk.  Tiles of 32 x 32 values pass through shared
-// memory so that both the reads and the writes are coalesced.
+// dst + s*sstride + c*ldk.  The 32 x 64 values pass through shared memory so
+// that the reads are coalesced in either orientation; each thread then cuts 8
+// consecutive values of one vector and writes 16 bytes per slice.
 __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long long cstride,
                                                       long long kstride, int K, int ncols,
                                                       __nv_bfloat16 *dst, long long ldk,
@@ -442,40 +443,58 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long l
                                                       const unsigned long long *mb,
                                                       const int *abort_flag, const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
-  __shared__ double tile[SPLIT_V][33];
+  __shared__ double tile[SPLIT_V][SPLIT_K + 1];
   __shared__ int ex[SPLIT_V];
-  const int tx = threadIdx.x, ty = threadIdx.y, c0 = blockIdx.x * SPLIT_V;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+  const int c0 = blockIdx.x * SPLIT_V, kc = blockIdx.y * SPLIT_K;
   if (ty == 0) ex[tx] = (c0 + tx < ncols) ? exponent_of(mb[c0 + tx]) : 0;
-  for (int kc = blockIdx.y * SPLIT_K; kc < (blockIdx.y + 1) * SPLIT_K && kc < ldk; kc += 32) {
-    __syncthreads();
-    if (kstride == 1) {
-      for (int vi = ty; vi < SPLIT_V; vi += 8) {
-        const int c = c0 + vi, k = kc + tx;
-        tile[vi][tx] = (c < ncols && k < K) ? src[(size_t)c * cstride + k] : 0.0;
-      }
-    } else {
-      for (int kk = ty; kk < 32; kk += 8) {
-        const int c = c0 + tx, k = kc + kk;
-        tile[tx][kk] = (c < ncols && k < K) ? src[(size_t)c * cstride + (size_t)k * kstride] : 0.0;
-      }
-    }
-    __syncthreads();
-    const int k = kc + tx;
-    if (k >= ldk) continue;
+  if (kstride == 1) {
     for (int vi = ty; vi < SPLIT_V; vi += 8) {
       const int c = c0 + vi;
-      if (c >= ncols) continue;
-      long long X = (ex[vi] == kOzNonFinite) ? 0 : scaled56(tile[vi][tx], ex[vi]);
-      __nv_bfloat16 *out = dst + (size_t)c * ldk + k;
 #pragma unroll
-      for (int s = OZ_S; s >= 1; s--) {
-        const long long d = (s > 1) ? ((X + 64) & 127) - 64 : X;
-        X = (X - d) >> 7;
-        const float w = __int_as_float((127 - 7 * s) << 23);  // 2^(-7 s)
-        out[(size_t)(s - 1) * sstride] = __float2bfloat16_rn((float)d * w);
+      for (int h = 0; h < SPLIT_K; h += 32) {
+        const int k = kc + h + tx;
+        tile[vi][h + tx] = (c < ncols && k < K) ? src[(size_t)c * cstride + k] : 0.0;
       }
     }
+  } else {
+    const int c = c0 + tx;
+#pragma unroll
+    for (int kk = ty; kk < SPLIT_K; kk += 8) {
+      const int k = kc + kk;
+      tile[tx][kk] = (c < ncols && k < K) ? src[(size_t)c * cstride + (size_t)k * kstride] : 0.0;
+    }
   }
+  __syncthreads();
+  const int vi = tid >> 3, k0 = 8 * (tid & 7);  // 8 values of one vector
+  const int c = c0 + vi;
+  if (c >= ncols || kc + k0 >= ldk) return;
+  const int e = ex[vi];
+  uint32_t packed[OZ_S][4];  // slice s: 8 BF16 values
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    uint32_t lo[OZ_S], hi[OZ_S];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      long long X = (e == kOzNonFinite) ? 0 : scaled56(tile[vi][k0 + j + h], e);
+#pragma unroll
+      for (int s_ = OZ_S; s_ >= 1; s_--) {
+        const long long d = (s_ > 1) ? ((X + 64) & 127) - 64 : X;
+        X = (X - d) >> 7;
+        // d 2^(-7 s) has at most 8 significant bits: its BF16 is the FP32's top half
+        const uint32_t b =
+            __float_as_uint((float)(int)d * __int_as_float((127 - 7 * s_) << 23)) >> 16;
+        if (h == 0) lo[s_ - 1] = b; else hi[s_ - 1] = b;
+      }
+    }
+#pragma unroll
+    for (int s_ = 0; s_ < OZ_S; s_++) packed[s_][j >> 1] = lo[s_] | (hi[s_] << 16);
+  }
+  __nv_bfloat16 *out = dst + (size_t)c * ldk + kc + k0;
+#pragma unroll
+  for (int s_ = 0; s_ < OZ_S; s_++)
+    *reinterpret_cast<uint4 *>(out + (size_t)s_ * sstride) =
+        make_uint4(packed[s_][0], packed[s_][1], packed[s_][2], packed[s_][3]);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,

@@ -247,10 +247,10 @@ __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *
     for (int i = j + 1 + tid; i < len; i += nt) Ms[i][j] *= r;
     if (tid == 0) Ms[j][j] = piv[0];
     __syncthreads();
-    const int w = len - j - 1;
-    for (int e = tid; e < w * w; e += nt) {
-      int i = j + 1 + e % w, k = j + 1 + e / w;
-      if (k <= i) Ms[i][k] = fma(-Ms[i][j], Ms[k][j], Ms[i][k]);
+    // the trailing triangle, threads on a 16 x 16 grid (no index division)
+    for (int i = j + 1 + (tid >> 4); i < len; i += nt >> 4) {
+      const T lij = Ms[i][j];
+      for (int k = j + 1 + (tid & 15); k <= i; k += 16) Ms[i][k] = fma(-lij, Ms[k][j], Ms[i][k]);
     }
     __syncthreads();
   }
