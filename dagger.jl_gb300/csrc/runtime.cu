@@ -69,17 +69,21 @@ DeviceState &device_state() {
   return *p;
 }
 
-// Per-thread pool of non-blocking streams (one pool per device).
-std::vector<cudaStream_t> &stream_pool(int want) {
-  static thread_local std::map<int, std::vector<cudaStream_t>> pools;
+// Per-thread pools of non-blocking streams (per device): the urgent pool at
+// the device's greatest stream priority, the normal pool at the least, so
+// that the CTAs of a region's critical-path tasks are scheduled first.
+std::vector<cudaStream_t> &stream_pool(int want, bool urgent) {
+  static thread_local std::map<std::pair<int, bool>, std::vector<cudaStream_t>> pools;
   int dev = 0;
   cudaGetDevice(&dev);
-  auto &v = pools[dev];
+  auto &v = pools[{dev, urgent}];
   while ((int)v.size() < want) {
     cudaStream_t s;
-    int lo = 0, hi = 0;
-    cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi) != cudaSuccess) break;
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, urgent ? greatest : least) !=
+        cudaSuccess)
+      break;
     v.push_back(s);
   }
   return v;
@@ -185,6 +189,7 @@ struct dg_region {
     std::vector<int> readers;
   };
   std::vector<dg_task> tasks;
+  std::vector<char> urgent;  // critical-path tasks (high-priority streams)
   std::vector<std::vector<int>> preds;
   std::vector<Ainfo> ainfos;
   std::multimap<uintptr_t, int> by_lo;
@@ -264,6 +269,7 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
+  r->urgent.push_back(0);
   hash_bytes(r->hash, &t, sizeof(dg_task));
   std::vector<dg_region::Access> acc;
   task_accesses(t, acc);
@@ -398,35 +404,46 @@ struct Plan {
   int nstreams = 0;
 };
 
+// Streams 0 .. kUrgentStreams-1 take the urgent tasks, the next `pool` the
+// others.  Within its class a task reuses the stream of its latest
+// predecessor when that predecessor is still the stream's tail, else the
+// least recently used stream.
 static Plan plan_streams(const dg_region &r, int pool) {
   Plan pl;
   const int n = (int)r.tasks.size();
+  const int total = kUrgentStreams + pool;
   pl.stream_of.assign(n, 0);
   pl.needs_event.assign(n, 0);
-  std::vector<int> tail(pool, -1);
-  std::vector<long> last_use(pool, -1);
-  int used = 0;
+  std::vector<int> tail(total, -1);
+  std::vector<long> last_use(total, -1);
   for (int t = 0; t < n; t++) {
+    const bool urg = r.urgent[t] != 0;
+    const int s0 = urg ? 0 : kUrgentStreams, s1 = urg ? kUrgentStreams : total;
     int best = -1, bestp = -1;
     for (int q : r.preds[t]) {
       int s = pl.stream_of[q];
-      if (tail[s] == q && q > bestp) { best = s; bestp = q; }
+      if (s >= s0 && s < s1 && tail[s] == q && q > bestp) { best = s; bestp = q; }
     }
     if (best < 0) {
-      // least recently used stream
-      best = 0;
-      for (int s = 1; s < pool; s++)
+      best = s0;
+      for (int s = s0 + 1; s < s1; s++)
         if (last_use[s] < last_use[best]) best = s;
     }
     pl.stream_of[t] = best;
     tail[best] = t;
     last_use[best] = t;
-    if (best + 1 > used) used = best + 1;
     for (int q : r.preds[t])
       if (pl.stream_of[q] != best) pl.needs_event[q] = 1;
   }
-  pl.nstreams = used;
+  pl.nstreams = total;
   return pl;
+}
+
+void mark_urgent(dg_region *r) {
+  if (r->urgent.empty()) return;
+  r->urgent.back() = 1;
+  const int id = (int)r->urgent.size() - 1;
+  hash_bytes(r->hash, &id, sizeof id);
 }
 
 struct GraphEntry {
@@ -452,8 +469,12 @@ static int issue(const dg_region &r, const Plan &pl, int *info, cudaStream_t ori
     }
     return 0;
   }
-  auto &pool = stream_pool(pl.nstreams);
-  if ((int)pool.size() < pl.nstreams) return DG_ERR_CUDA;
+  auto &upool = stream_pool(kUrgentStreams, true);
+  auto &npool = stream_pool(pl.nstreams - kUrgentStreams, false);
+  if ((int)upool.size() < kUrgentStreams || (int)npool.size() < pl.nstreams - kUrgentStreams)
+    return DG_ERR_CUDA;
+  std::vector<cudaStream_t> pool(upool.begin(), upool.end());
+  pool.insert(pool.end(), npool.begin(), npool.begin() + (pl.nstreams - kUrgentStreams));
   cudaEvent_t fork;
   DG_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   events.push_back(fork);
@@ -580,7 +601,8 @@ static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t o
       return rc;
     }
     DG_CUDA_TRY(e);
-    e = cudaGraphInstantiate(&entry.exec, graph, 0);
+    // kernel nodes keep the priority of the stream they were captured from
+    e = cudaGraphInstantiateWithFlags(&entry.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     DG_CUDA_TRY(e);
     std::lock_guard<std::mutex> g(g_graph_mu);
@@ -823,6 +845,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     t.op = OP_OZ_POTRF; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.c = T(k, k); t.ldc = rows(k);
     t.info_offset = k * nb; t.b = slot(k, k); t.ldb = slot_units;
     dg_region_add(r, &t);
+    mark_urgent(r);
     for (int j = k + 1; j < mt; j++) {
       memset(&t, 0, sizeof t);
       t.op = OP_OZ_TRSM; t.diag = 'N'; t.transa = 'T'; t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
@@ -833,6 +856,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
         t.side = 'R'; t.uplo = 'L'; t.m = rows(j); t.n = rows(k); t.c = T(j, k); t.ldc = rows(j);
       }
       dg_region_add(r, &t);
+      if (j == k + 1) mark_urgent(r);  // the next diagonal tile waits for this panel tile
       memset(&t, 0, sizeof t);
       t.op = OP_OZ_SPLIT; t.m = rows(k); t.n = rows(j); t.c = slot(k, j); t.ldc = ldk; t.k = nb;
       if (up) {  // columns of U(k, j)
@@ -841,6 +865,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
         t.trans = 'T'; t.a = T(j, k); t.lda = rows(j);
       }
       dg_region_add(r, &t);
+      if (j == k + 1) mark_urgent(r);
     }
     // cholesky.jl:43-52 (upper) / 88-97 (lower): C(m, j) -= V_m' V_j over the
     // vectors V of step k; the diagonal tiles keep one triangle (SYRK).
@@ -857,6 +882,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
           t.c = T(j, m); t.ldc = rows(j); t.uplo = (j == m) ? 'L' : 'N';
         }
         dg_region_add(r, &t);
+        if (m == k + 1) mark_urgent(r);  // the next panel
       }
     }
   }

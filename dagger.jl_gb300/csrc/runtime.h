@@ -12,6 +12,7 @@
 namespace dg {
 
 constexpr int kDefaultStreams = 16;
+constexpr int kUrgentStreams = 4;  // high-priority streams for critical-path tasks
 
 // Internal task kinds of the tiled Cholesky region with the emulated FP64
 // engine (not part of the public dg_op enumeration):
@@ -45,7 +46,8 @@ struct DeviceState {
 };
 
 DeviceState &device_state();
-std::vector<cudaStream_t> &stream_pool(int want);
+std::vector<cudaStream_t> &stream_pool(int want, bool urgent = false);
+void mark_urgent(dg_region *r);  // the last task added is on the critical path
 
 // Strided byte footprint of a column-major matrix argument.
 struct Footprint {

@@ -105,8 +105,9 @@ __global__ void __launch_bounds__(256) trsm_base_kernel(TriView<T> tv, int r0, i
   }
 }
 
-// Left-side solve M X = X of a few right-hand-side columns (one CTA per
-// column) for the whole triangle: the column lives in shared memory, blocks
+// Solve M X = X of a few right-hand-side columns (one CTA per column; for a
+// right-side solve the columns are B's rows) for the whole triangle: the
+// column lives in shared memory, blocks
 // of 64 rows are finished in order; each block first subtracts the solved
 // part (all 256 threads, reading M coalesced in either orientation), then
 // warp 0 substitutes through the 64 x 64 diagonal block staged in shared
@@ -114,19 +115,22 @@ __global__ void __launch_bounds__(256) trsm_base_kernel(TriView<T> tv, int r0, i
 // recursive form has too little parallelism in its updates.
 constexpr int TC_MAX_LEN = 4096;
 constexpr int TC_MAX_RHS = 128;
+// Inside POTRF the TRSM of each level is on the critical path: one
+// column-parallel launch replaces the recursion up to this width.
+constexpr int kPotrfColsMax = 512;
 
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_cols_kernel(TriView<T> tv, int len, T *X,
-                                                        long long ldx, const int *a1,
-                                                        const int *a2) {
+                                                        long long rs, long long cs,
+                                                        const int *a1, const int *a2) {
   if (aborted(a1, a2)) return;
   extern __shared__ unsigned char tc_smem[];
   T (*D)[TB + 1] = (T (*)[TB + 1])tc_smem;              // diagonal block
   T *x = (T *)(tc_smem + sizeof(T) * TB * (TB + 1));    // the column
   __shared__ T part[4][TB];
   const int tid = threadIdx.x;
-  T *xc = X + (size_t)blockIdx.x * ldx;
-  for (int i = tid; i < len; i += 256) x[i] = xc[i];
+  T *xc = X + (size_t)blockIdx.x * cs;  // element i of this column at xc[i * rs]
+  for (int i = tid; i < len; i += 256) x[i] = xc[(size_t)i * rs];
   __syncthreads();
   const int nblk = (len + TB - 1) / TB;
   for (int bi = 0; bi < nblk; bi++) {
@@ -190,12 +194,12 @@ __global__ void __launch_bounds__(256) trsm_cols_kernel(TriView<T> tv, int len, 
     }
     __syncthreads();
   }
-  for (int i = tid; i < len; i += 256) xc[i] = x[i];
+  for (int i = tid; i < len; i += 256) xc[(size_t)i * rs] = x[i];
 }
 
 template <typename T>
-int trsm_cols(const TriView<T> &tv, int len, T *X, long long ldx, int nn, const int *a1,
-              const int *a2, cudaStream_t s) {
+int trsm_cols(const TriView<T> &tv, int len, T *X, long long rs, long long cs, int nn,
+              const int *a1, const int *a2, cudaStream_t s) {
   const size_t smem = sizeof(T) * (TB * (TB + 1) + (size_t)len);
   static bool attr[64] = {false};
   int dev = 0;
@@ -206,7 +210,7 @@ int trsm_cols(const TriView<T> &tv, int len, T *X, long long ldx, int nn, const 
                                      (int)(sizeof(T) * (TB * (TB + 1) + TC_MAX_LEN))));
     attr[dev & 63] = true;
   }
-  trsm_cols_kernel<T><<<nn, 256, smem, s>>>(tv, len, X, ldx, a1, a2);
+  trsm_cols_kernel<T><<<nn, 256, smem, s>>>(tv, len, X, rs, cs, a1, a2);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -362,10 +366,12 @@ int trsm_rec(const TrsmPlan<T> &p, int r0, int len) {
   return trsm_rec(p, b0, blen);
 }
 
+// cols_max: widest right-hand side solved by the column-parallel kernel
+// (latency-bound callers raise it).
 template <typename T>
 int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, const T *A,
            long long lda, T *B, long long ldb, const int *a1, cudaStream_t s, const int *a2,
-           const OzScratch &oz = OzScratch()) {
+           const OzScratch &oz = OzScratch(), int cols_max = TC_MAX_RHS) {
   if (m <= 0 || n <= 0) return 0;
   const bool right = (side == 'R' || side == 'r');
   const bool tr = !(transa == 'N' || transa == 'n');
@@ -391,8 +397,8 @@ int trsm_t(char side, char uplo, char transa, char diag, int m, int n, T alpha, 
     if (alpha == T(0)) return 0;
   }
   const int len = right ? n : m;
-  if (!right && p.nn <= TC_MAX_RHS && len > 2 * TB && len <= TC_MAX_LEN)
-    return trsm_cols<T>(p.tv, len, B, ldb, p.nn, a1, a2, s);
+  if (p.nn <= cols_max && len > 2 * TB && len <= TC_MAX_LEN)
+    return trsm_cols<T>(p.tv, len, B, right ? ldb : 1, right ? 1 : ldb, p.nn, a1, a2, s);
   return trsm_rec(p, 0, len);
 }
 
@@ -417,12 +423,14 @@ int potrf_rec(bool upper, int n, T *A, long long lda, int *info, int off, cudaSt
   if (oz1.p) oz1.status = info;  // this factorization's word records a timeout
   if (upper) {
     T *A12 = A + (size_t)n1 * lda;
-    DG_TRY(trsm_t<T>('L', 'U', 'T', 'N', n1, n2, T(1), A, lda, A12, lda, k1, s, k2, oz1));
+    DG_TRY(trsm_t<T>('L', 'U', 'T', 'N', n1, n2, T(1), A, lda, A12, lda, k1, s, k2, oz1,
+                     kPotrfColsMax));
     DG_TRY(update_t<T>('T', 'N', n2, n2, n1, T(-1), A12, lda, A12, lda, T(1), A22, lda, TRI_UPPER,
                        k1, s, k2, oz1));
   } else {
     T *A21 = A + n1;
-    DG_TRY(trsm_t<T>('R', 'L', 'T', 'N', n2, n1, T(1), A, lda, A21, lda, k1, s, k2, oz1));
+    DG_TRY(trsm_t<T>('R', 'L', 'T', 'N', n2, n1, T(1), A, lda, A21, lda, k1, s, k2, oz1,
+                     kPotrfColsMax));
     DG_TRY(update_t<T>('N', 'T', n2, n2, n1, T(-1), A21, lda, A21, lda, T(1), A22, lda, TRI_LOWER,
                        k1, s, k2, oz1));
   }

@@ -79,7 +79,8 @@ def test_syrk(engine, uplo, trans, n, k):
 @pytest.mark.parametrize("uplo", "UL")
 @pytest.mark.parametrize("trans", "NT")
 @pytest.mark.parametrize("diag", "NU")
-@pytest.mark.parametrize("m,n", [(64, 64), (200, 70), (33, 129), (1, 3), (700, 5), (1030, 128)])
+@pytest.mark.parametrize("m,n", [(64, 64), (200, 70), (33, 129), (1, 3), (700, 5), (1030, 128),
+                                 (100, 300)])
 def test_trsm(engine, side, uplo, trans, diag, m, n):
     import dagger_gb300 as d
     from oracle import tiled as o
