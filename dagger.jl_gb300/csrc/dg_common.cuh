@@ -96,6 +96,8 @@ int potrf_f64(char uplo, int n, double *A, int lda, int *info_out, int info_offs
 int potrf_f32(char uplo, int n, float *A, long long lda, int *info_out, int info_offset,
               cudaStream_t s, const int *abort_flag = nullptr, const int *abort2 = nullptr);
 
+// W (n x n, ldw) = I.
+int eye_f64(int n, double *W, int ldw, const int *abort_flag, cudaStream_t s);
 int scale_f64(int m, int n, double alpha, double *B, int ldb, const int *abort_flag,
               cudaStream_t s, const int *abort2 = nullptr);
 int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abort_flag,

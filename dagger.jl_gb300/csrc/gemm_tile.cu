@@ -259,6 +259,13 @@ __global__ void scale_kernel(int m, int n, double alpha, T *B, long long ldb,
   }
 }
 
+__global__ void eye_kernel(int n, double *W, long long ldw, const int *abort_flag) {
+  if (aborted(abort_flag, nullptr)) return;
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    W[(size_t)i + (size_t)j * ldw] = (i == j) ? 1.0 : 0.0;
+}
+
 GemmArgs make_args(char ta, char tb, int m, int n, int k, double alpha, const void *A,
                    long long lda, const void *B, long long ldb, double beta, void *C, long long ldc,
                    Tri tri, const int *abort_flag, const int *abort2) {
@@ -351,6 +358,14 @@ int scale_f64(int m, int n, double alpha, double *B, int ldb, const int *abort_f
   int blocks = (int)((total + 255) / 256);
   if (blocks > 4 * dg_num_sms()) blocks = 4 * dg_num_sms();
   scale_kernel<double><<<blocks, 256, 0, s>>>(m, n, alpha, B, ldb, abort_flag, abort2);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return 0;
+}
+
+int eye_f64(int n, double *W, int ldw, const int *abort_flag, cudaStream_t s) {
+  if (n <= 0) return 0;
+  eye_kernel<<<n, 256, 0, s>>>(n, W, ldw, abort_flag);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;

@@ -217,6 +217,11 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
       if (t.op == dg::OP_OZ_POTRF)
         out.push_back({dg::footprint(t.b, t.ldb, 1, 1, 256), DG_OUT});  // slice scratch
       break;
+    case dg::OP_OZ_INV:
+      out.push_back({dg::footprint(t.a, t.n, t.n, t.lda, E), DG_IN});
+      out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), DG_OUT});
+      out.push_back({dg::footprint(t.b, t.ldb, 1, 1, 256), DG_OUT});  // slice scratch
+      break;
     case DG_OP_TRSM:
     case dg::OP_OZ_TRSM: {
       int ka = (t.side == 'L' || t.side == 'l') ? t.m : t.n;
@@ -265,7 +270,7 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
   DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) ||
-                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_OZ_POTRF),
+                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_OZ_INV),
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
@@ -362,6 +367,12 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case OP_OZ_POTRF:
       return potrf_f64_oz(t.uplo, t.n, t.c, t.ldc, info, t.info_offset, (void *)t.b,
                           (size_t)t.ldb * 256, s);
+    case OP_OZ_INV: {  // W = U^-T (upper) or L^-T (lower): the identity solved in place
+      const bool up = (t.uplo == 'U' || t.uplo == 'u');
+      DG_TRY(eye_f64(t.n, t.c, t.ldc, info, s));
+      return trsm_f64_oz(up ? 'L' : 'R', up ? 'U' : 'L', 'T', 'N', t.n, t.n, 1.0, t.a, t.lda, t.c,
+                         t.ldc, (void *)t.b, (size_t)t.ldb * 256, info, s);
+    }
     case OP_OZ_TRSM:
       return trsm_f64_oz(t.side, t.uplo, t.transa, t.diag, t.m, t.n, t.alpha, t.a, t.lda, t.c,
                          t.ldc, (void *)t.b, (size_t)t.ldb * 256, info, s);
@@ -815,10 +826,15 @@ extern "C" int dg_gemv(char trans, int m, int n, double alpha, const double *A, 
 namespace dg {
 
 // The factorization's slots, plus one column of slots so that a following
-// solve with up to nb right-hand sides finds its ring in place.
-size_t oz_ring_bytes_for(int n, int nb) {
+// solve with up to nb right-hand sides finds its ring in place, then the
+// FP64 inverses of the last kOzRingDepth diagonal tiles.
+static size_t oz_inv_offset(int n, int nb) {
   const int mt = (n + nb - 1) / nb;
   return (size_t)kOzRingDepth * (mt + 1) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+}
+static size_t oz_inv_bytes(int nb) { return ((size_t)nb * nb * 8 + 255) & ~(size_t)255; }
+size_t oz_ring_bytes_for(int n, int nb) {
+  return oz_inv_offset(n, nb) + (size_t)kOzRingDepth * oz_inv_bytes(nb);
 }
 
 // The emulated-FP64 form of the same task graph: after TRSM(k, j) a split
@@ -835,10 +851,17 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
   auto slot = [&](int k, int j) {
     return (double *)((char *)ring + ((size_t)(k % kOzRingDepth) * mt + j) * sb);
   };
-  // POTRF(k) and TRSM(k, j) cut their own recursion's operands into slices
-  // in slot (k, k) (unused by the splits of step k) and slot (k, j) (before
-  // the split of tile j fills it)
+  // The panel solve of step k (cholesky.jl:40-42 / 85-87) runs as emulated
+  // GEMMs with the inverse of the diagonal factor: W = U_kk^-T (upper) or
+  // L_kk^-T (lower) is formed once by substitution on the identity, and each
+  // panel tile becomes W A(k, j) (upper) or A(j, k) W (lower).  POTRF(k) and
+  // the inversion cut their recursions' operands into slices in slot (k, k),
+  // which then holds W's slices; slot (k, j) holds the panel tile's input
+  // slices, then its result's for the trailing update.
   const int slot_units = (int)(sb / 256);
+  auto W = [&](int k) {
+    return (double *)((char *)ring + oz_inv_offset(n, nb) + (size_t)(k % kOzRingDepth) * oz_inv_bytes(nb));
+  };
   for (int k = 0; k < mt; k++) {
     dg_task t;
     memset(&t, 0, sizeof t);
@@ -846,26 +869,42 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     t.info_offset = k * nb; t.b = slot(k, k); t.ldb = slot_units;
     dg_region_add(r, &t);
     mark_urgent(r);
+    if (k + 1 == mt) break;
+    memset(&t, 0, sizeof t);
+    t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.a = T(k, k); t.lda = rows(k);
+    t.c = W(k); t.ldc = rows(k); t.b = slot(k, k); t.ldb = slot_units;
+    dg_region_add(r, &t);
+    mark_urgent(r);
+    memset(&t, 0, sizeof t);  // rows of W (upper: A-vectors) / columns (lower: B-vectors)
+    t.op = OP_OZ_SPLIT; t.a = W(k); t.lda = rows(k); t.m = rows(k); t.n = rows(k);
+    t.trans = up ? 'T' : 'N'; t.c = slot(k, k); t.ldc = ldk; t.k = nb;
+    dg_region_add(r, &t);
+    mark_urgent(r);
     for (int j = k + 1; j < mt; j++) {
-      memset(&t, 0, sizeof t);
-      t.op = OP_OZ_TRSM; t.diag = 'N'; t.transa = 'T'; t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
-      t.b = slot(k, j); t.ldb = slot_units;
-      if (up) {  // cholesky.jl:40-42
-        t.side = 'L'; t.uplo = 'U'; t.m = rows(k); t.n = rows(j); t.c = T(k, j); t.ldc = rows(k);
-      } else {   // cholesky.jl:85-87
-        t.side = 'R'; t.uplo = 'L'; t.m = rows(j); t.n = rows(k); t.c = T(j, k); t.ldc = rows(j);
+      for (int pass = 0; pass < 2; pass++) {  // the tile's input, then its result
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_SPLIT; t.m = rows(k); t.n = rows(j); t.c = slot(k, j); t.ldc = ldk; t.k = nb;
+        if (up) {  // columns of A(k, j) / U(k, j)
+          t.trans = 'N'; t.a = T(k, j); t.lda = rows(k);
+        } else {   // rows of A(j, k) / L(j, k)
+          t.trans = 'T'; t.a = T(j, k); t.lda = rows(j);
+        }
+        dg_region_add(r, &t);
+        if (j == k + 1) mark_urgent(r);  // the next diagonal tile waits for this panel tile
+        if (pass == 1) break;
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_GEMM; t.uplo = 'N'; t.k = rows(k); t.alpha = 1.0; t.beta = 0.0;
+        t.lda = ldk; t.ldb = nb;
+        if (up) {  // U(k, j) = W A(k, j)
+          t.m = rows(k); t.n = rows(j); t.a = slot(k, k); t.b = slot(k, j);
+          t.c = T(k, j); t.ldc = rows(k);
+        } else {   // L(j, k) = A(j, k) W
+          t.m = rows(j); t.n = rows(k); t.a = slot(k, j); t.b = slot(k, k);
+          t.c = T(j, k); t.ldc = rows(j);
+        }
+        dg_region_add(r, &t);
+        if (j == k + 1) mark_urgent(r);
       }
-      dg_region_add(r, &t);
-      if (j == k + 1) mark_urgent(r);  // the next diagonal tile waits for this panel tile
-      memset(&t, 0, sizeof t);
-      t.op = OP_OZ_SPLIT; t.m = rows(k); t.n = rows(j); t.c = slot(k, j); t.ldc = ldk; t.k = nb;
-      if (up) {  // columns of U(k, j)
-        t.trans = 'N'; t.a = T(k, j); t.lda = rows(k);
-      } else {   // rows of L(j, k)
-        t.trans = 'T'; t.a = T(j, k); t.lda = rows(j);
-      }
-      dg_region_add(r, &t);
-      if (j == k + 1) mark_urgent(r);
     }
     // cholesky.jl:43-52 (upper) / 88-97 (lower): C(m, j) -= V_m' V_j over the
     // vectors V of step k; the diagonal tiles keep one triangle (SYRK).

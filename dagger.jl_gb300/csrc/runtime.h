@@ -24,10 +24,14 @@ constexpr int kUrgentStreams = 4;  // high-priority streams for critical-path ta
 //                stores one triangle
 //   OP_OZ_TRSM   DG_OP_TRSM whose recursion updates are emulated, with
 //   OP_OZ_POTRF  (likewise DG_OP_POTRF) b = slice scratch of ldb * 256 bytes
+//   OP_OZ_INV    c (n x n, ldc) = U^-T for uplo 'U' / L^-T for 'L' of the
+//                factor tile a (lda), by substitution on the identity; b, ldb
+//                slice scratch as above
 constexpr int OP_OZ_SPLIT = 100;
 constexpr int OP_OZ_GEMM = 101;
 constexpr int OP_OZ_TRSM = 102;
 constexpr int OP_OZ_POTRF = 103;
+constexpr int OP_OZ_INV = 104;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 size_t oz_slot_bytes(long long ldk, long long cap);
 size_t oz_ring_bytes_for(int n, int nb);
