@@ -113,14 +113,19 @@ int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abo
 // *status or *abort2 is non-zero; a timed-out wait records DG_ERR_TIMEOUT in
 // *status.
 constexpr int kOzSlices = 8;
+// diag_out (square operands): element c of vector c is written to diag_out[c]
+// and left out of the slices and the scale.  dscale: when set, the beta of
+// output row i (dmode 1) or column j (dmode 2) is dscale[i] / dscale[j]
+// (C = alpha A'B + diag(d) C, or C d), instead of the scalar beta.
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
              void *slices, long long ldk, long long sstride, unsigned long long *scales,
-             const int *abort_flag, cudaStream_t s, const int *abort2 = nullptr);
+             const int *abort_flag, cudaStream_t s, const int *abort2 = nullptr,
+             double *diag_out = nullptr);
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
             long long a_sstride, const unsigned long long *a_scales, const void *b_slices,
             long long ldb_k, long long b_sstride, const unsigned long long *b_scales, double beta,
             double *C, long long ldc, int tri, int *status, cudaStream_t s,
-            const int *abort2 = nullptr);
+            const int *abort2 = nullptr, const double *dscale = nullptr, int dmode = 0);
 // C = alpha op(A) op(B) + beta C (BLAS gemm / syrk arguments; tri as above)
 // through split + oz_gemm with the slices in caller scratch of `bytes`
 // (oz_scratch_bytes).  Returns 1 without work when k > 1024 or the scratch

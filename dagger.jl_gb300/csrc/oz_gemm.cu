@@ -85,6 +85,8 @@ struct OzParams {
   int tri;                // 1: store only i <= j, 2: only i >= j
   int *status;            // skip when non-zero; DG_ERR_TIMEOUT recorded here
   const int *abort2;      // skip when non-zero (read only)
+  const double *dscale;   // when set, beta of row i (dmode 1) / column j (dmode 2) is dscale[.]
+  int dmode;
 };
 
 // frexp exponent of the non-negative double with bits b (0 for 0).
@@ -323,7 +325,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
       for (int c = 0; c < 16; c++) {
         const int col = j0 + cb + ch + c;
         const bool in = col < p.n && !(p.tri == 1 && row > col) && !(p.tri == 2 && row < col);
-        old[c] = (in && p.beta != 0.0) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
+        old[c] = (in && (p.beta != 0.0 || p.dmode)) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
       }
 #pragma unroll
       for (int c = 0; c < 16; c++) {
@@ -337,6 +339,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
           const double x = int_to_double_scaled(acc[ch + c], ea + eb - 42 - OZ_GUARD);
           if (fast)
             vout = old[c] - x;
+          else if (p.dmode)
+            vout = fma(p.dscale[p.dmode == 1 ? row : col], old[c], p.alpha * x);
           else
             vout = (p.beta != 0.0) ? fma(p.alpha, x, p.beta * old[c]) : p.alpha * x;
         }
@@ -385,8 +389,8 @@ __device__ __forceinline__ long long scaled56(double v, int ex) {
 // CTA: 32 x 8 threads reading along whichever of k or c is contiguous.
 __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long long cstride,
                                                     long long kstride, int K, int ncols,
-                                                    unsigned long long *mb, const int *abort_flag,
-                                                    const int *abort2) {
+                                                    unsigned long long *mb, int zero_diag,
+                                                    const int *abort_flag, const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
   __shared__ unsigned long long red[8][SPLIT_V + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long lon
 #pragma unroll
         for (int j = 0; j < MAX_K / 32; j++) {
           const int k = k0 + tx + 32 * j;
-          const unsigned long long a = k < k1 ? abs_bits(v[k]) : 0ull;
+          const unsigned long long a = (k < k1 && !(zero_diag && k == c)) ? abs_bits(v[k]) : 0ull;
           m = a > m ? a : m;
         }
       }
@@ -418,7 +422,8 @@ __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long lon
     if (c < ncols) {
 #pragma unroll 8
       for (int k = k0 + ty; k < k1; k += 8) {
-        const unsigned long long a = abs_bits(src[(size_t)c * cstride + (size_t)k * kstride]);
+        const unsigned long long a =
+            (zero_diag && k == c) ? 0ull : abs_bits(src[(size_t)c * cstride + (size_t)k * kstride]);
         m = a > m ? a : m;
       }
     }
@@ -441,7 +446,8 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long l
                                                       __nv_bfloat16 *dst, long long ldk,
                                                       long long sstride,
                                                       const unsigned long long *mb,
-                                                      const int *abort_flag, const int *abort2) {
+                                                      double *diag_out, const int *abort_flag,
+                                                      const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
   __shared__ double tile[SPLIT_V][SPLIT_K + 1];
   __shared__ int ex[SPLIT_V];
@@ -469,6 +475,12 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long l
   const int vi = tid >> 3, k0 = 8 * (tid & 7);  // 8 values of one vector
   const int c = c0 + vi;
   if (c >= ncols || kc + k0 >= ldk) return;
+  // diag_out: element c of vector c goes there instead of into the slices
+  const int kd = (diag_out && c >= kc + k0 && c < kc + k0 + 8) ? c - kc - k0 : -1;
+  if (kd >= 0) {
+    diag_out[c] = tile[vi][k0 + kd];
+    tile[vi][k0 + kd] = 0.0;
+  }
   const int e = ex[vi];
   uint32_t packed[OZ_S][4];  // slice s: 8 BF16 values
 #pragma unroll
@@ -533,17 +545,17 @@ bool oz_map(CUtensorMap *map, const void *base, long long ldk, long long rows, l
 
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
              void *slices, long long ldk, long long sstride, unsigned long long *scales,
-             const int *abort_flag, cudaStream_t s, const int *abort2) {
+             const int *abort_flag, cudaStream_t s, const int *abort2, double *diag_out) {
   if (ncols <= 0) return 0;
   DG_CUDA_TRY(cudaMemsetAsync(scales, 0, sizeof(unsigned long long) * (size_t)ncols, s));
   const dim3 blk(32, 8);
   const int nv = (ncols + SPLIT_V - 1) / SPLIT_V;
-  oz_max_kernel<<<dim3(nv, (K + MAX_K - 1) / MAX_K), blk, 0, s>>>(src, cstride, kstride, K, ncols,
-                                                                  scales, abort_flag, abort2);
+  oz_max_kernel<<<dim3(nv, (K + MAX_K - 1) / MAX_K), blk, 0, s>>>(
+      src, cstride, kstride, K, ncols, scales, diag_out ? 1 : 0, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   const dim3 grid(nv, (unsigned)((ldk + SPLIT_K - 1) / SPLIT_K));
   oz_slice_kernel<<<grid, blk, 0, s>>>(src, cstride, kstride, K, ncols, (__nv_bfloat16 *)slices,
-                                       ldk, sstride, scales, abort_flag, abort2);
+                                       ldk, sstride, scales, diag_out, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(2);
   return 0;
@@ -552,7 +564,8 @@ int oz_split(const double *src, long long cstride, long long kstride, int K, int
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
             long long a_sstride, const unsigned long long *ma, const void *b_slices,
             long long ldb_k, long long b_sstride, const unsigned long long *mb, double beta,
-            double *C, long long ldc, int tri, int *status, cudaStream_t s, const int *abort2) {
+            double *C, long long ldc, int tri, int *status, cudaStream_t s, const int *abort2,
+            const double *dscale, int dmode) {
   if (m <= 0 || n <= 0) return 0;
   if (k <= 0 || k > 1024 || lda_k % 8 || ldb_k % 8) return DG_ERR_UNSUPPORTED;
   if (lda_k < k || ldb_k < k) return DG_ERR_UNSUPPORTED;
@@ -567,6 +580,8 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   p.m = m; p.n = n; p.k = k; p.alpha = alpha; p.beta = beta; p.tri = tri;
   p.status = status;
   p.abort2 = abort2;
+  p.dscale = dscale;
+  p.dmode = dscale ? dmode : 0;
   static bool attr[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);

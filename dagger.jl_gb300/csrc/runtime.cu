@@ -126,10 +126,14 @@ int DeviceState::oz_workspace(size_t bytes, void **p) {
 }
 
 // A slot: the 8 BF16 slices of up to `cap` vectors of padded length ldk,
-// then one 8-byte scale word per vector.
+// one 8-byte scale word per vector, then room for a square operand's
+// diagonal (kept in FP64 outside the slices).
 size_t oz_slot_bytes(long long ldk, long long cap) {
-  size_t b = (size_t)kOzSlices * ldk * cap * 2 + (size_t)cap * 8;
+  size_t b = (size_t)kOzSlices * ldk * cap * 2 + (size_t)cap * 16;
   return (b + 255) & ~(size_t)255;
+}
+static double *slot_diag(const void *slot, long long ldk, long long cap) {
+  return (double *)((char *)slot + (size_t)kOzSlices * ldk * cap * 2 + (size_t)cap * 8);
 }
 
 DeviceState::~DeviceState() {}
@@ -389,16 +393,21 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
       const bool cols = (t.trans == 'N');
       const long long sstride = (long long)t.ldc * t.k;
       auto *e = (unsigned long long *)((char *)t.c + (size_t)kOzSlices * sstride * 2);
+      // diag 'Z': the diagonal is kept apart in FP64 (the inverse of a triangle)
+      double *dg = (t.diag == 'Z') ? slot_diag(t.c, t.ldc, t.k) : nullptr;
       return oz_split(t.a, cols ? t.lda : 1, cols ? 1 : t.lda, t.m, t.n, t.c, t.ldc, sstride, e,
-                      info, s);
+                      info, s, nullptr, dg);
     }
     case OP_OZ_GEMM: {
       const long long sstride = (long long)t.lda * t.ldb;
       auto *ea = (const unsigned long long *)((const char *)t.a + (size_t)kOzSlices * sstride * 2);
       auto *eb = (const unsigned long long *)((const char *)t.b + (size_t)kOzSlices * sstride * 2);
       const int tri = (t.uplo == 'U' || t.uplo == 'u') ? 1 : (t.uplo == 'L' || t.uplo == 'l') ? 2 : 0;
+      // side 'A' / 'B': the A (rows) / B (columns) operand's FP64 diagonal scales C
+      const double *ds = (t.side == 'A') ? slot_diag(t.a, t.lda, t.ldb)
+                         : (t.side == 'B') ? slot_diag(t.b, t.lda, t.ldb) : nullptr;
       return oz_gemm(t.m, t.n, t.k, t.alpha, t.a, t.lda, sstride, ea, t.b, t.lda, sstride, eb,
-                     t.beta, t.c, t.ldc, tri, info, s);
+                     t.beta, t.c, t.ldc, tri, info, s, nullptr, ds, t.side == 'A' ? 1 : 2);
     }
     case DG_OP_COPY:
       if (t.m <= 0 || t.n <= 0) return 0;
@@ -875,9 +884,12 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     t.c = W(k); t.ldc = rows(k); t.b = slot(k, k); t.ldb = slot_units;
     dg_region_add(r, &t);
     mark_urgent(r);
-    memset(&t, 0, sizeof t);  // rows of W (upper: A-vectors) / columns (lower: B-vectors)
+    // rows of W (upper: A-vectors) / columns (lower: B-vectors); W's diagonal
+    // 1/u_ii dominates its vectors, so it stays FP64 and scales the panel
+    // tile exactly, and only the off-diagonal part is sliced
+    memset(&t, 0, sizeof t);
     t.op = OP_OZ_SPLIT; t.a = W(k); t.lda = rows(k); t.m = rows(k); t.n = rows(k);
-    t.trans = up ? 'T' : 'N'; t.c = slot(k, k); t.ldc = ldk; t.k = nb;
+    t.trans = up ? 'T' : 'N'; t.diag = 'Z'; t.c = slot(k, k); t.ldc = ldk; t.k = nb;
     dg_region_add(r, &t);
     mark_urgent(r);
     for (int j = k + 1; j < mt; j++) {
@@ -895,12 +907,12 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
         memset(&t, 0, sizeof t);
         t.op = OP_OZ_GEMM; t.uplo = 'N'; t.k = rows(k); t.alpha = 1.0; t.beta = 0.0;
         t.lda = ldk; t.ldb = nb;
-        if (up) {  // U(k, j) = W A(k, j)
+        if (up) {  // U(k, j) = diag(W) A(k, j) + offdiag(W) A(k, j)
           t.m = rows(k); t.n = rows(j); t.a = slot(k, k); t.b = slot(k, j);
-          t.c = T(k, j); t.ldc = rows(k);
-        } else {   // L(j, k) = A(j, k) W
+          t.c = T(k, j); t.ldc = rows(k); t.side = 'A';
+        } else {   // L(j, k) = A(j, k) diag(W) + A(j, k) offdiag(W)
           t.m = rows(j); t.n = rows(k); t.a = slot(k, j); t.b = slot(k, k);
-          t.c = T(j, k); t.ldc = rows(j);
+          t.c = T(j, k); t.ldc = rows(j); t.side = 'B';
         }
         dg_region_add(r, &t);
         if (j == k + 1) mark_urgent(r);
