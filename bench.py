@@ -596,8 +596,7 @@ def bench_mixed(args, d, DA, A, B, stream, world):
     rep, st = reports[-1]
     return {"precision": prec, "value": flops(n, r) * args.steps * world / t / 1e12,
             "unit": "TFLOP/s", "ms_per_step": 1e3 * t / args.steps,
-            "f64_engine": args.f64_engine, "dfma_engine": dfma,
-           "solves_per_s": r * args.steps * world / t,
+            "solves_per_s": r * args.steps * world / t,
             "factor_ms": st["factor_ms"], "refine_ms": rep["solve_ms"],
             "ir_iterations": rep["iterations"], "gmres_iterations": rep["gmres_iterations"],
             "fp64_retries": st["retries"],
