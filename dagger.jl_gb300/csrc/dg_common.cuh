@@ -108,7 +108,7 @@ int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abo
 // src[c*cstride + k*kstride]) into 8 BF16 slices (slice s of vector c at
 // slices + s*sstride + c*ldk) and one 8-byte scale word per vector; oz_gemm
 // computes C(m x n) = alpha * sum_p A(p, i) B(p, j) + beta * C from the
-// slices of the m A-vectors and n B-vectors (K <= 1024, ldk a multiple of 8);
+// slices of the m A-vectors and n B-vectors (K <= 131072, ldk a multiple of 8);
 // tri 1 / 2 stores only the upper / lower triangle.  Kernels skip when
 // *status or *abort2 is non-zero; a timed-out wait records DG_ERR_TIMEOUT in
 // *status.
@@ -126,9 +126,15 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
             long long ldb_k, long long b_sstride, const unsigned long long *b_scales, double beta,
             double *C, long long ldc, int tri, int *status, cudaStream_t s,
             const int *abort2 = nullptr, const double *dscale = nullptr, int dmode = 0);
+// The rows of the n x n matrix held as an nb x nb tile grid (tile (i, j) at
+// tiles_dev[i + j*mt], column-major, ld = its row count): vector c = row c,
+// K = n, into slices + s*ldk*n + c*ldk (n <= 131072).
+int oz_split_tile_rows(const double *const *tiles_dev, int n, int nb, void *slices, long long ldk,
+                       unsigned long long *scales, const int *abort_flag, cudaStream_t s);
+
 // C = alpha op(A) op(B) + beta C (BLAS gemm / syrk arguments; tri as above)
 // through split + oz_gemm with the slices in caller scratch of `bytes`
-// (oz_scratch_bytes).  Returns 1 without work when k > 1024 or the scratch
+// (oz_scratch_bytes).  Returns 1 without work when k > 131072 or the scratch
 // is too small, so the caller can use the FP64 kernels instead.
 size_t oz_scratch_bytes(int m, int n, int k, bool same_operand);
 int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const double *A,

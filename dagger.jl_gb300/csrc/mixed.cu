@@ -611,12 +611,27 @@ int correction(const dg_mixed *f, const double *R, long long ldr, double *X, lon
   return 0;
 }
 
+// With the emulated FP64 engine the residual's product runs on the tensor
+// cores: the rows of A (the caller's tile grid) are cut into BF16 slices once
+// per solve, X's columns every iteration, and R = B - A X is one emulated GEMM
+// with K = n and FP64 accuracy.
+struct OzResidual {
+  void *a = nullptr, *x = nullptr;          // slices of A's rows / X's columns
+  unsigned long long *as = nullptr, *xs = nullptr;
+  long long ldk = 0;
+};
+
 // R = B - A X (FP64, A from the caller's tiles)
 int residual(const dg_mixed *f, const double *B, long long ldb, const double *X, long long ldx,
-             double *R, int r, cudaStream_t s) {
+             double *R, int r, cudaStream_t s, const OzResidual *oz) {
   const int n = f->n;
   DG_CUDA_TRY(cudaMemcpy2DAsync(R, sizeof(double) * n, B, sizeof(double) * ldb,
                                 sizeof(double) * n, r, cudaMemcpyDeviceToDevice, s));
+  if (oz && oz->a) {
+    DG_TRY(dg::oz_split(X, ldx, 1, n, r, oz->x, oz->ldk, oz->ldk * r, oz->xs, nullptr, s));
+    return dg::oz_gemm(n, r, n, -1.0, oz->a, oz->ldk, oz->ldk * n, oz->as, oz->x, oz->ldk,
+                       oz->ldk * r, oz->xs, 1.0, R, n, 0, nullptr, s);
+  }
   return dg::gemm_tiles_f64(n, f->nb, r, -1.0, (const double *const *)f->tiles_dev, X, ldx, 1.0, R,
                             n, nullptr, s);
 }
@@ -836,6 +851,26 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
+  OzResidual oz;
+  if (dg::get_f64_engine() == 2 && n <= 131072) {
+    oz.ldk = ((long long)n + 7) / 8 * 8;
+    const size_t ba = 16 * (size_t)oz.ldk * n, bx = 16 * (size_t)oz.ldk * r;
+    if (cudaMallocAsync(&oz.a, ba + 8 * (size_t)n, s) != cudaSuccess ||
+        cudaMallocAsync(&oz.x, bx + 8 * (size_t)r, s) != cudaSuccess) {
+      cudaGetLastError();  // no room for the slices: the FP64 residual
+      if (oz.a) cudaFreeAsync(oz.a, s);
+      oz.a = oz.x = nullptr;
+    } else {
+      oz.as = (unsigned long long *)((char *)oz.a + ba);
+      oz.xs = (unsigned long long *)((char *)oz.x + bx);
+      if (dg::oz_split_tile_rows((const double *const *)f->tiles_dev, n, f->nb, oz.a, oz.ldk,
+                                 oz.as, nullptr, s)) {
+        cudaFreeAsync(oz.a, s);
+        cudaFreeAsync(oz.x, s);
+        oz.a = oz.x = nullptr;
+      }
+    }
+  }
   DG_CUDA_TRY(cudaMemset2DAsync(X, sizeof(double) * ldx, 0, sizeof(double) * n, r, s));
   DG_CUDA_TRY(cudaMemcpy2DAsync(R, sizeof(double) * n, B, sizeof(double) * ldb, sizeof(double) * n,
                                 r, cudaMemcpyDeviceToDevice, s));
@@ -852,7 +887,7 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
     }
     if (rc) break;
     outer++;
-    rc = residual(f, B, ldb, X, ldx, R, r, s);
+    rc = residual(f, B, ldb, X, ldx, R, r, s, &oz);
     if (rc) break;
     rc = backward_errors(f, B, ldb, X, ldx, R, r, cm, berr, s);
     if (rc) break;
@@ -879,6 +914,8 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
   cudaFreeAsync(R, s);
   cudaFreeAsync(cm, s);
   cudaFreeAsync(Z, s);
+  if (oz.a) cudaFreeAsync(oz.a, s);
+  if (oz.x) cudaFreeAsync(oz.x, s);
   if (rep) {
     rep->iterations = outer;
     rep->gmres_iterations = gm_iters;

@@ -17,16 +17,16 @@
 // A vector holding an infinity or a NaN makes every output that uses it NaN.
 //
 // Products (oz_gemm_kernel): C = alpha * 2^(ea_i + eb_j) * sum_{s+t<=9} A_s B_t'
-// + beta * C, K <= 1024.  A product A_s B_t' sums terms d_s d_t 2^(-7(s+t)).
+// + beta * C, K <= 131072.  A product A_s B_t' sums terms d_s d_t 2^(-7(s+t)).
 // Level L = s + t collects the L - 1 products of that weight.  Over a window
 // of 512 values of K the sum of level L <= 6 stays within 2^24 units of
 // 2^(-7L) (level 6: (2*128*64 + 2*64*64 + 64*64) * 512 < 2^24; levels 2 and
 // 3 within 2^24 over all 1024), so its FP32 accumulation in TMEM is exact.
 // Levels 2..6 are read exactly after each window and summed as 64-bit
-// integers in units of 2^-42 (|sum| < 2^53 over K = 1024).  Levels 7..9
+// integers in units of 2^-42 (|sum| < 2^53 K / 1024).  Levels 7..9
 // accumulate in FP32 over the whole K (their rounding is below 2^-56 of
 // |C|'s scale; the dropped levels >= 10 and the slicing remainder are below
-// 2^-55) and join the integer sum at 2^-51.  The 62-bit total is rounded
+// 2^-55) and join the integer sum at 2^-51 (2^-44 at the largest K).  The 62-bit total is rounded
 // once to FP64 by integer arithmetic, with 2^(ea_i + eb_j) folded into the
 // exponent, and added to beta C.  The result has an FP64 GEMM's accuracy
 // relative to 2^(ea_i + eb_j) K.
@@ -62,14 +62,21 @@ using namespace ptx;
 
 constexpr int OZ_S = 8;                                   // slices per operand
 constexpr int kOzNonFinite = 1 << 30;                     // exponent of a non-finite vector
-constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;        // K per stage
-constexpr int OZ_WIN = 16;                                // stages per exact window (K 512)
-constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB
-constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB
-constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 96 KiB
-constexpr int OZ_STAGES = 2;
+#ifndef OZ_STAGE_K
+#define OZ_STAGE_K 32
+#endif
+constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = OZ_STAGE_K;  // K per stage (16 or 32)
+constexpr int OZ_WIN = 512 / OZ_BK;                       // stages per exact window (K 512)
+constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB at K 32
+constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB at K 32
+constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 96 KiB at K 32
+constexpr int OZ_STAGES = (192 * 1024) / OZ_STAGE;        // 2 at K 32, 4 at K 16
+static_assert(OZ_BK == 16 || OZ_BK == 32, "stage K is 16 (32-byte swizzle) or 32 (64-byte)");
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE + 1024 + 512;
-constexpr int OZ_GUARD = 9;                               // extra fraction bits of the sum
+// Fraction bits kept below 2^-42 when levels 7..9 join the integer sum: 9 for
+// K <= 1024, one fewer per doubling of K, so |sum| * 2^guard stays below 2^62
+// (|sum| < 2^53 K / 1024).  K may reach kOzMaxK.
+constexpr int kOzMaxK = 131072;
 constexpr int OZ_READERS = 16;                            // reader warps: 4 per TMEM lane quarter
 constexpr int OZ_RCOLS = OZ_BN / (OZ_READERS / 4);        // columns per reader thread (16)
 constexpr int OZ_PRODUCER = OZ_READERS, OZ_ISSUER = OZ_READERS + 1;
@@ -87,6 +94,7 @@ struct OzParams {
   const int *abort2;      // skip when non-zero (read only)
   const double *dscale;   // when set, beta of row i (dmode 1) / column j (dmode 2) is dscale[.]
   int dmode;
+  int guard;              // fraction bits below 2^-42 of the integer sum
 };
 
 // frexp exponent of the non-negative double with bits b (0 for 0).
@@ -216,8 +224,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         // descriptors: base + (byte offset >> 4)
-        const uint64_t da = sw64_desc(sbase + st * OZ_STAGE);
-        const uint64_t db = sw64_desc(sbase + st * OZ_STAGE + OZ_S * OZ_A_SLICE);
+        const uint32_t sa = sbase + st * OZ_STAGE, sb = sa + OZ_S * OZ_A_SLICE;
+        const uint64_t da = OZ_BK == 32 ? sw64_desc(sa) : sw32_desc(sa);
+        const uint64_t db = OZ_BK == 32 ? sw64_desc(sb) : sw32_desc(sb);
         // A_s x [B_t .. B_u] onto levels s+t .. s+u (TMEM column 64 (s+t-2))
         auto mma_run = [&](int kk, int s_, int t, int u, uint32_t acc) {
           mma_bf16(tmem + 64 * (s_ + t - 2), da + (((s_ - 1) * OZ_A_SLICE + kk * 32) >> 4),
@@ -302,7 +311,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
     const int row = i0 + (warp & 3) * 32 + lane;
     const int ea = row < p.m ? exponent_of(p.ma[row]) : 0;
     // levels 9, 8, 7 summed in FP32 (all lanes: the loads are warp-wide),
-    // joined to the integer sum at 2^-(42 + OZ_GUARD) (|v| < 2^-21)
+    // joined to the integer sum at 2^-(42 + guard) (|v| < 2^-21 K / 1024)
+    const float unit7 = __int_as_float((127 + 42 + p.guard) << 23);
 #pragma unroll
     for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
       float v[16], w[16];
@@ -313,8 +323,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
       tmem_ld16(tmem + 64 * 5 + cb + ch + lane_base, w);
 #pragma unroll
       for (int c = 0; c < 16; c++)
-        acc[ch + c] = (long long)((unsigned long long)acc[ch + c] << OZ_GUARD) +
-                      (long long)__float2int_rn((w[c] + v[c]) * 0x1p51f);
+        acc[ch + c] = (long long)((unsigned long long)acc[ch + c] << p.guard) +
+                      (long long)__float2int_rn((w[c] + v[c]) * unit7);
     }
     if (row < p.m) {
       const bool fast = (p.alpha == -1.0 && p.beta == 1.0);
@@ -336,7 +346,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
         if (ea == kOzNonFinite || eb == kOzNonFinite) {
           vout = __longlong_as_double(0x7FF8000000000000ll);
         } else {
-          const double x = int_to_double_scaled(acc[ch + c], ea + eb - 42 - OZ_GUARD);
+          const double x = int_to_double_scaled(acc[ch + c], ea + eb - 42 - p.guard);
           if (fast)
             vout = old[c] - x;
           else if (p.dmode)
@@ -364,6 +374,24 @@ constexpr int SPLIT_V = 32;    // vectors per CTA
 constexpr int MAX_K = 256;     // values of K per scale CTA
 constexpr int SPLIT_K = 64;    // values of K per slicing CTA
 
+// Where the split reads: element k of vector c at p[c*cs + k*ks], or, for a
+// tile grid (tiles != nullptr), row c and column k of the n x n matrix whose
+// nb x nb tile (i, j) is tiles[i + j*mt] (column-major, ld = its row count).
+struct OzSrc {
+  const double *p;
+  long long cs, ks;
+  const double *const *tiles;
+  int nb, mt, n;
+  __device__ __forceinline__ double at(int c, int k) const {
+    if (!tiles) return p[(size_t)c * cs + (size_t)k * ks];
+    const int ti = c / nb, tj = k / nb;
+    const int ld = min(nb, n - ti * nb);
+    return tiles[ti + (size_t)tj * mt][(size_t)(c - ti * nb) + (size_t)(k - tj * nb) * ld];
+  }
+  // lanes along the contiguous direction: k for columns, c for rows and tiles
+  __device__ __forceinline__ bool k_contiguous() const { return !tiles && ks == 1; }
+};
+
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
 }
@@ -387,8 +415,7 @@ __device__ __forceinline__ long long scaled56(double v, int ex) {
 // src[c*cstride + k*kstride]): the maximum of |v|'s bit pattern, by atomic
 // maximum over CTAs of 32 vectors x 256 values of K (the words start at 0).
 // CTA: 32 x 8 threads reading along whichever of k or c is contiguous.
-__global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long long cstride,
-                                                    long long kstride, int K, int ncols,
+__global__ void __launch_bounds__(256) oz_max_kernel(OzSrc src, int K, int ncols,
                                                     unsigned long long *mb, int zero_diag,
                                                     const int *abort_flag, const int *abort2) {
   if (aborted(abort_flag, abort2)) return;
@@ -396,13 +423,13 @@ __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long lon
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int c0 = blockIdx.x * SPLIT_V, k0 = blockIdx.y * MAX_K;
   const int k1 = min(K, k0 + MAX_K);
-  if (kstride == 1) {  // columns: lanes along k, warp ty over vectors ty, ty+8, ...
+  if (src.k_contiguous()) {  // columns: lanes along k, warp ty over vectors ty, ty+8, ...
 #pragma unroll
     for (int i = 0; i < SPLIT_V / 8; i++) {
       const int c = c0 + ty + 8 * i;
       unsigned long long m = 0;
       if (c < ncols) {
-        const double *v = src + (size_t)c * cstride;
+        const double *v = src.p + (size_t)c * src.cs;
 #pragma unroll
         for (int j = 0; j < MAX_K / 32; j++) {
           const int k = k0 + tx + 32 * j;
@@ -422,8 +449,7 @@ __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long lon
     if (c < ncols) {
 #pragma unroll 8
       for (int k = k0 + ty; k < k1; k += 8) {
-        const unsigned long long a =
-            (zero_diag && k == c) ? 0ull : abs_bits(src[(size_t)c * cstride + (size_t)k * kstride]);
+        const unsigned long long a = (zero_diag && k == c) ? 0ull : abs_bits(src.at(c, k));
         m = a > m ? a : m;
       }
     }
@@ -441,8 +467,7 @@ __global__ void __launch_bounds__(256) oz_max_kernel(const double *src, long lon
 // dst + s*sstride + c*ldk.  The 32 x 64 values pass through shared memory so
 // that the reads are coalesced in either orientation; each thread then cuts 8
 // consecutive values of one vector and writes 16 bytes per slice.
-__global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long long cstride,
-                                                      long long kstride, int K, int ncols,
+__global__ void __launch_bounds__(256) oz_slice_kernel(OzSrc src, int K, int ncols,
                                                       __nv_bfloat16 *dst, long long ldk,
                                                       long long sstride,
                                                       const unsigned long long *mb,
@@ -454,13 +479,13 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long l
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const int c0 = blockIdx.x * SPLIT_V, kc = blockIdx.y * SPLIT_K;
   if (ty == 0) ex[tx] = (c0 + tx < ncols) ? exponent_of(mb[c0 + tx]) : 0;
-  if (kstride == 1) {
+  if (src.k_contiguous()) {
     for (int vi = ty; vi < SPLIT_V; vi += 8) {
       const int c = c0 + vi;
 #pragma unroll
       for (int h = 0; h < SPLIT_K; h += 32) {
         const int k = kc + h + tx;
-        tile[vi][h + tx] = (c < ncols && k < K) ? src[(size_t)c * cstride + k] : 0.0;
+        tile[vi][h + tx] = (c < ncols && k < K) ? src.p[(size_t)c * src.cs + k] : 0.0;
       }
     }
   } else {
@@ -468,7 +493,7 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const double *src, long l
 #pragma unroll
     for (int kk = ty; kk < SPLIT_K; kk += 8) {
       const int k = kc + kk;
-      tile[tx][kk] = (c < ncols && k < K) ? src[(size_t)c * cstride + (size_t)k * kstride] : 0.0;
+      tile[tx][kk] = (c < ncols && k < K) ? src.at(c, k) : 0.0;
     }
   }
   __syncthreads();
@@ -537,28 +562,45 @@ bool oz_map(CUtensorMap *map, const void *base, long long ldk, long long rows, l
   cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, (cuuint32_t)OZ_S};
   cuuint32_t estr[3] = {1, 1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)base, dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+             CU_TENSOR_MAP_INTERLEAVE_NONE,
+             OZ_BK == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace
 
-int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
-             void *slices, long long ldk, long long sstride, unsigned long long *scales,
-             const int *abort_flag, cudaStream_t s, const int *abort2, double *diag_out) {
+static int split_from(const OzSrc &src, int K, int ncols, void *slices, long long ldk,
+                      long long sstride, unsigned long long *scales, const int *abort_flag,
+                      cudaStream_t s, const int *abort2, double *diag_out) {
   if (ncols <= 0) return 0;
   DG_CUDA_TRY(cudaMemsetAsync(scales, 0, sizeof(unsigned long long) * (size_t)ncols, s));
   const dim3 blk(32, 8);
   const int nv = (ncols + SPLIT_V - 1) / SPLIT_V;
   oz_max_kernel<<<dim3(nv, (K + MAX_K - 1) / MAX_K), blk, 0, s>>>(
-      src, cstride, kstride, K, ncols, scales, diag_out ? 1 : 0, abort_flag, abort2);
+      src, K, ncols, scales, diag_out ? 1 : 0, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   const dim3 grid(nv, (unsigned)((ldk + SPLIT_K - 1) / SPLIT_K));
-  oz_slice_kernel<<<grid, blk, 0, s>>>(src, cstride, kstride, K, ncols, (__nv_bfloat16 *)slices,
-                                       ldk, sstride, scales, diag_out, abort_flag, abort2);
+  oz_slice_kernel<<<grid, blk, 0, s>>>(src, K, ncols, (__nv_bfloat16 *)slices, ldk, sstride,
+                                       scales, diag_out, abort_flag, abort2);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(2);
   return 0;
+}
+
+int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
+             void *slices, long long ldk, long long sstride, unsigned long long *scales,
+             const int *abort_flag, cudaStream_t s, const int *abort2, double *diag_out) {
+  OzSrc q;
+  q.p = src; q.cs = cstride; q.ks = kstride; q.tiles = nullptr; q.nb = q.mt = q.n = 0;
+  return split_from(q, K, ncols, slices, ldk, sstride, scales, abort_flag, s, abort2, diag_out);
+}
+
+int oz_split_tile_rows(const double *const *tiles_dev, int n, int nb, void *slices, long long ldk,
+                       unsigned long long *scales, const int *abort_flag, cudaStream_t s) {
+  if (n > kOzMaxK) return DG_ERR_UNSUPPORTED;
+  OzSrc q;
+  q.p = nullptr; q.cs = q.ks = 0; q.tiles = tiles_dev; q.nb = nb; q.mt = (n + nb - 1) / nb; q.n = n;
+  return split_from(q, n, n, slices, ldk, ldk * n, scales, abort_flag, s, nullptr, nullptr);
 }
 
 int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long lda_k,
@@ -567,7 +609,7 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
             double *C, long long ldc, int tri, int *status, cudaStream_t s, const int *abort2,
             const double *dscale, int dmode) {
   if (m <= 0 || n <= 0) return 0;
-  if (k <= 0 || k > 1024 || lda_k % 8 || ldb_k % 8) return DG_ERR_UNSUPPORTED;
+  if (k <= 0 || k > kOzMaxK || lda_k % 8 || ldb_k % 8) return DG_ERR_UNSUPPORTED;
   if (lda_k < k || ldb_k < k) return DG_ERR_UNSUPPORTED;
   OzParams p;
   memset(&p, 0, sizeof p);
@@ -582,6 +624,8 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   p.abort2 = abort2;
   p.dscale = dscale;
   p.dmode = dscale ? dmode : 0;
+  p.guard = 9;
+  for (long long kk = 1024; kk < k; kk *= 2) p.guard--;
   static bool attr[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -614,7 +658,7 @@ int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const d
   const bool tA = !(ta == 'N' || ta == 'n'), tB = !(tb == 'N' || tb == 'n');
   // the rows of op(A) are the columns of op(B): one set of slices (SYRK)
   const bool same = (A == B && lda == ldb && m == n && tA != tB);
-  if (k <= 0 || k > 1024 || !scratch || oz_scratch_bytes(m, n, k, same) > bytes) return 1;
+  if (k <= 0 || k > kOzMaxK || !scratch || oz_scratch_bytes(m, n, k, same) > bytes) return 1;
   const long long ldk = (k + 7) / 8 * 8;
   char *q = (char *)scratch;
   void *sa = q;
@@ -640,13 +684,13 @@ int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const d
 
 // Building block exposed for tests: C = alpha op(A) op(B) + beta C in FP64
 // through the emulated path, with op(A) = A' (A is k x m) and op(B) = B
-// (k x n), both column-major, k <= 1024.  Uses stream-ordered scratch.
+// (k x n), both column-major, k <= 131072.  Uses stream-ordered scratch.
 extern "C" int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const double *A, int lda,
                                        const double *B, int ldb, double beta, double *C, int ldc,
                                        void *stream) {
   DG_CHECK_ARG(m >= 0, 1);
   DG_CHECK_ARG(n >= 0, 2);
-  DG_CHECK_ARG(k > 0 && k <= 1024, 3);
+  DG_CHECK_ARG(k > 0 && k <= dg::kOzMaxK, 3);
   DG_CHECK_ARG(lda >= k, 6);
   DG_CHECK_ARG(ldb >= k, 8);
   DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 11);
@@ -667,7 +711,7 @@ extern "C" int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const 
 extern "C" int dg_f64_slices(int k, int ncols, const double *src, long long cstride,
                              long long kstride, void *slices, int ldk, void *scales,
                              void *stream) {
-  DG_CHECK_ARG(k > 0 && k <= 1024, 1);
+  DG_CHECK_ARG(k > 0 && k <= dg::kOzMaxK, 1);
   DG_CHECK_ARG(ncols >= 0, 2);
   DG_CHECK_ARG(ldk >= k && ldk % 8 == 0, 7);
   DG_CHECK_ARG(((uintptr_t)slices & 15) == 0, 6);
@@ -682,7 +726,7 @@ extern "C" int dg_gemm_f64_slices(int m, int n, int k, double alpha, const void 
                                   int *status, void *stream) {
   DG_CHECK_ARG(m >= 0, 1);
   DG_CHECK_ARG(n >= 0, 2);
-  DG_CHECK_ARG(k > 0 && k <= 1024, 3);
+  DG_CHECK_ARG(k > 0 && k <= dg::kOzMaxK, 3);
   DG_CHECK_ARG(lda_k >= k && lda_k % 8 == 0, 6);
   DG_CHECK_ARG(ldb_k >= k && ldb_k % 8 == 0, 9);
   DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 13);

@@ -83,6 +83,16 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t addr) {
   return d;
 }
 
+// ... and a 32-byte swizzle: rows of 16 BF16 (32 B), 8-row atoms of 256 B.
+__device__ __forceinline__ uint64_t sw32_desc(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(256 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)6 << 61;                           // 32-byte swizzle
+  return d;
+}
+
 // Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B
 // both BF16 (bits 7-9, 10-12 = 1) or both FP16 (= 0), both K-major (bits
 // 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.

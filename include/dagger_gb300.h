@@ -273,7 +273,7 @@ int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const void *a_hi, co
                   float *C, int ldc, int bn, int *status, void *stream);
 
 /* FP64 GEMM emulated on the BF16 tensor cores: C = alpha A'B + beta C with
- * A k x m, B k x n and C m x n column-major FP64 on the device, k <= 1024.
+ * A k x m, B k x n and C m x n column-major FP64 on the device, k <= 131072.
  * The building block of engine 2's trailing updates (BLAS.gemm!('T', 'N')
  * of src/array/cholesky.jl:50); its error is that of an FP64 GEMM relative
  * to max|A(:, i)| max|B(:, j)| k.  Allocates stream-ordered scratch. */
@@ -282,7 +282,7 @@ int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const double *A, 
                             void *stream);
 
 /* Its two stages, for operands reused across products.  dg_f64_slices cuts
- * ncols FP64 vectors of length k <= 1024 (element p of vector c at
+ * ncols FP64 vectors of length k <= 131072 (element p of vector c at
  * src[c*cstride + p*kstride]) into 8 BF16 slices, slice s of vector c at
  * slices + 2*(s*ldk*ncols + c*ldk) bytes (ldk >= k, a multiple of 8; the
  * buffer 16-byte aligned, 16*ldk*ncols bytes), and one 8-byte scale word per

@@ -49,7 +49,8 @@ def _emulated_gemm_error(m, n, k, alpha, beta, seed, scale_rows=False):
 
 
 @pytest.mark.parametrize("m,n,k", [(128, 64, 64), (1, 1, 1), (257, 129, 100), (1000, 700, 1024),
-                                   (130, 70, 513), (64, 300, 8), (1024, 1024, 1024)])
+                                   (130, 70, 513), (64, 300, 8), (1024, 1024, 1024),
+                                   (256, 64, 4096), (300, 100, 33000)])
 def test_emulated_gemm_vs_fp64(m, n, k):
     assert _emulated_gemm_error(m, n, k, -1.0, 1.0, m + n + k) <= 1.0
 
@@ -88,11 +89,11 @@ def test_emulated_gemm_zero_vectors():
 def test_emulated_gemm_argument_errors():
     import dagger_gb300 as d
     r = np.random.default_rng(5)
-    A = dev_f(r.standard_normal((1025, 4)))
-    B = dev_f(r.standard_normal((1025, 4)))
-    C = dev_f(np.zeros((4, 4), order='F'))
+    A = dev_f(r.standard_normal((131073, 2)))
+    B = dev_f(r.standard_normal((131073, 2)))
+    C = dev_f(np.zeros((2, 2), order='F'))
     with pytest.raises(ValueError):
-        d.gemm_f64_emulated_tn(1.0, A, B, 0.0, C)   # k > 1024
+        d.gemm_f64_emulated_tn(1.0, A, B, 0.0, C)   # k > 131072
 
 
 @pytest.mark.parametrize("uplo", "UL")

@@ -88,6 +88,32 @@ def test_mixed_solve(precision, n, nb, cond, nrhs):
     F.close()
 
 
+@pytest.mark.parametrize("precision", ["bf16", "bf16x3"])
+@pytest.mark.parametrize("n,nb,cond,nrhs", [(1536, 256, 1e4, 5), (1000, 128, 1e6, 2),
+                                            (700, 100, None, 64)])
+def test_mixed_solve_emulated_residual(precision, n, nb, cond, nrhs):
+    """With the emulated FP64 engine the refinement's residual runs on the
+    tensor cores (K = n): the same targets as the FP64-pipe residual."""
+    import torch
+    import dagger_gb300 as d
+    from oracle import tiled as o
+    A = _spd(n, cond, 13)
+    B = o.rhs_normal(n, nrhs, 6)
+    old = d.set_f64_engine("emulated")
+    try:
+        F = d.cholesky_mixed(d.DArray.from_array(A, d.Blocks(nb, nb)), precision)
+        X, rep = F.solve(torch.from_numpy(B).cuda(), tol=1e-12, gmres="auto", max_iter=40)
+        F.close()
+    finally:
+        d.set_f64_engine(old)
+    Xh = X.cpu().numpy()
+    berr = o.backward_error(A, Xh, B)
+    assert rep["converged"] == 1 and berr.max() <= 1e-12, (rep, berr.max())
+    Xr = o.lapack_solve(A, B)
+    kappa = np.linalg.cond(A, np.inf)
+    assert np.abs(Xh - Xr).max() / np.abs(Xr).max() <= 10 * kappa * 1e-12
+
+
 @pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
 def test_gmres_ir_ill_conditioned(precision):
     """kappa = 1e8: refinement with GMRES-IR still reaches 1e-12."""
