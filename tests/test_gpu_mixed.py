@@ -90,7 +90,7 @@ def test_mixed_solve(precision, n, nb, cond, nrhs):
 
 @pytest.mark.parametrize("precision", ["bf16", "bf16x3"])
 @pytest.mark.parametrize("n,nb,cond,nrhs", [(1536, 256, 1e4, 5), (1000, 128, 1e6, 2),
-                                            (700, 100, None, 64)])
+                                            (700, 128, None, 64)])
 def test_mixed_solve_emulated_residual(precision, n, nb, cond, nrhs):
     """With the emulated FP64 engine the refinement's residual runs on the
     tensor cores (K = n): the same targets as the FP64-pipe residual."""
