@@ -51,6 +51,7 @@ struct dg_mixed {
   float *panel_max = nullptr;    // per-step |panel| maximum (FP16 scaling)
   float *alpha_dev = nullptr;    // per-step -1/scale^2 of the trailing update
   float *Vinv = nullptr;         // inverses of the diagonal blocks (mt x nb x nb)
+  float *Lp = nullptr;           // block columns of the factor, transposed (backward solves)
   int *words = nullptr;          // [0] status, [1] retries, [2] first bad diagonal, [3..] info_k
   double normA = 0.0;            // ||A||_inf
   size_t bytes = 0;
@@ -102,6 +103,34 @@ __global__ void row_abs_sum_kernel(const double *const *tiles, int n, int nb, in
 
 __host__ __device__ inline long long panel_base(long long r, long long n, long long nb) {
   return nb * (r * n - nb * r * (r - 1) / 2);
+}
+
+// Block column k of the factor (rows 0 .. (k+1) nb - 1), transposed: an
+// nb x (k+1) nb matrix with leading dimension nb at Lp + lp_base(k).
+__host__ __device__ inline long long lp_base(long long k, long long nb) {
+  return nb * nb * (k * (k + 1) / 2);
+}
+
+// Lp_k(:, j nb + i) = U(j nb + i, k nb + :) for the block (j, k), j <= k, in
+// 32 x 32 tiles through shared memory; blockIdx.z enumerates the blocks.
+__global__ void transpose_blocks_kernel(const float *W, float *Lp, int n, int nb,
+                                        const int2 *blocks) {
+  __shared__ float t[32][33];
+  const int2 b = blocks[blockIdx.z];
+  const int j = b.x, k = b.y;
+  const float *P = W + panel_base(j, n, nb) + (long long)(k - j) * nb * nb;  // U(j, k), ld nb
+  float *L = Lp + lp_base(k, nb) + (long long)j * nb * nb;                   // its transpose
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int cols = min(nb, n - k * nb);  // columns of block column k
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int c = c0 + y, r = r0 + threadIdx.x;
+    t[y][threadIdx.x] = (c < cols) ? P[r + (long long)c * nb] : 0.f;
+  }
+  __syncthreads();
+  for (int y = threadIdx.y; y < 32; y += blockDim.y) {
+    const int r = r0 + y, c = c0 + threadIdx.x;
+    L[c + (long long)r * nb] = t[threadIdx.x][y];
+  }
 }
 
 // W = float(S A S) on the upper row panels; the strict lower part of each
@@ -442,18 +471,35 @@ int mixed_tri_solve(const dg_mixed *f, float *Z, float *Z2, long long ldz, int r
       DG_TRY(gemm_f32('T', 'N', (int)T, r, nbk, -1.f, Pk + (size_t)nb * nb, nb, Z2 + (size_t)k * nb,
                       ldz, 1.f, Z + (size_t)(k + 1) * nb, ldz, TRI_NONE, nullptr, s));
   }
+  // backward, right-looking: Z_k = Vinv_k Z2_k, then every block above it
+  // takes its share, Z2_(0:k) -= U~_(0:k, k) Z_k, as one tall GEMM on the
+  // transposed block column
   for (int k = mt - 1; k >= 0; k--) {
-    const float *Pk = f->W + panel_base(k, n, nb);
     const float *V = f->Vinv + (size_t)k * nb * nb;
     const int nbk = std::min(nb, n - k * nb);
-    const long long T = (long long)n - (long long)(k + 1) * nb;
-    if (T > 0)
-      DG_TRY(gemm_f32('N', 'N', nbk, r, (int)T, -1.f, Pk + (size_t)nb * nb, nb,
-                      Z + (size_t)(k + 1) * nb, ldz, 1.f, Z2 + (size_t)k * nb, ldz, TRI_NONE,
-                      nullptr, s));
     DG_TRY(gemm_f32('N', 'N', nbk, r, nbk, 1.f, V, nb, Z2 + (size_t)k * nb, ldz, 0.f,
                     Z + (size_t)k * nb, ldz, TRI_NONE, nullptr, s));
+    if (k > 0)
+      DG_TRY(gemm_f32('T', 'N', k * nb, r, nbk, -1.f, f->Lp + lp_base(k, nb), nb,
+                      Z + (size_t)k * nb, ldz, 1.f, Z2, ldz, TRI_NONE, nullptr, s));
   }
+  return 0;
+}
+
+// Fills Lp from the finished panels (one launch over every block j <= k).
+int mixed_transpose_columns(dg_mixed *f, cudaStream_t s) {
+  const int mt = f->mt, nb = f->nb;
+  std::vector<int2> hb;
+  for (int k = 0; k < mt; k++)
+    for (int j = 0; j <= k; j++) hb.push_back(make_int2(j, k));
+  int2 *db = nullptr;
+  DG_CUDA_TRY(cudaMallocAsync((void **)&db, sizeof(int2) * hb.size(), s));
+  DG_CUDA_TRY(cudaMemcpyAsync(db, hb.data(), sizeof(int2) * hb.size(), cudaMemcpyHostToDevice, s));
+  dim3 grid((nb + 31) / 32, (nb + 31) / 32, (unsigned)hb.size());
+  transpose_blocks_kernel<<<grid, dim3(32, 8), 0, s>>>(f->W, f->Lp, f->n, nb, db);
+  count_launches(1);
+  DG_CUDA_TRY(cudaGetLastError());
+  cudaFreeAsync(db, s);  // (a copy from pageable memory is staged before the call returns)
   return 0;
 }
 
@@ -505,6 +551,7 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
       {(void **)&f->alpha_dev, sizeof(float) * (size_t)mt},
       {(void **)&f->words, sizeof(int) * (size_t)(3 + mt)},
       {(void **)&f->Vinv, sizeof(float) * (size_t)mt * nb * nb},
+      {(void **)&f->Lp, sizeof(float) * (size_t)dg::lp_base(mt, nb)},
   };
   f->stream = s;
   for (auto &a : allocs) {
@@ -533,6 +580,7 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   int rc = dg::mixed_factor_run(f, s);
+  if (!rc) rc = dg::mixed_transpose_columns(f, s);
   cudaEventRecord(e1, s);
   if (rc) {
     cudaEventDestroy(e0);
@@ -564,7 +612,7 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
 extern "C" void dg_mixed_destroy(dg_mixed *f) {
   if (!f) return;
   void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
-                f->panel_max, f->alpha_dev, f->words, f->Vinv};
+                f->panel_max, f->alpha_dev, f->words, f->Vinv, f->Lp};
   for (void *p : ps)
     if (p) cudaFreeAsync(p, f->stream);  // stream-ordered: no device-wide synchronisation
   if (f->ev_next) cudaEventDestroy(f->ev_next);
