@@ -382,9 +382,10 @@ struct OzSrc {
   long long cs, ks;
   const double *const *tiles;
   int nb, mt, n;
+  int lg;  // log2(nb) when nb is a power of two (the tile index is a shift), else -1
   __device__ __forceinline__ double at(int c, int k) const {
     if (!tiles) return p[(size_t)c * cs + (size_t)k * ks];
-    const int ti = c / nb, tj = k / nb;
+    const int ti = lg >= 0 ? c >> lg : c / nb, tj = lg >= 0 ? k >> lg : k / nb;
     const int ld = min(nb, n - ti * nb);
     return tiles[ti + (size_t)tj * mt][(size_t)(c - ti * nb) + (size_t)(k - tj * nb) * ld];
   }
@@ -591,7 +592,7 @@ int oz_split(const double *src, long long cstride, long long kstride, int K, int
              void *slices, long long ldk, long long sstride, unsigned long long *scales,
              const int *abort_flag, cudaStream_t s, const int *abort2, double *diag_out) {
   OzSrc q;
-  q.p = src; q.cs = cstride; q.ks = kstride; q.tiles = nullptr; q.nb = q.mt = q.n = 0;
+  q.p = src; q.cs = cstride; q.ks = kstride; q.tiles = nullptr; q.nb = q.mt = q.n = 0; q.lg = -1;
   return split_from(q, K, ncols, slices, ldk, sstride, scales, abort_flag, s, abort2, diag_out);
 }
 
@@ -600,6 +601,9 @@ int oz_split_tile_rows(const double *const *tiles_dev, int n, int nb, void *slic
   if (n > kOzMaxK) return DG_ERR_UNSUPPORTED;
   OzSrc q;
   q.p = nullptr; q.cs = q.ks = 0; q.tiles = tiles_dev; q.nb = nb; q.mt = (n + nb - 1) / nb; q.n = n;
+  q.lg = -1;
+  for (int l = 0; l < 31; l++)
+    if ((1 << l) == nb) q.lg = l;
   return split_from(q, n, n, slices, ldk, ldk * n, scales, abort_flag, s, nullptr, nullptr);
 }
 
