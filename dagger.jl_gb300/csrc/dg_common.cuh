@@ -87,6 +87,12 @@ int trsm_f64_oz(char side, char uplo, char transa, char diag, int m, int n, doub
 int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_offset,
                  void *scratch, size_t bytes, cudaStream_t s);
 
+// W (n x n, ldw) = U^-T for uplo 'U', L^-T for 'L', of the triangular factor
+// A (lda), by column-parallel forward substitution on the unit vectors
+// (n <= 4096).  Kernels skip when *abort_flag is set.
+int trinv_t_f64(char uplo, int n, const double *A, int lda, double *W, int ldw,
+                const int *abort_flag, cudaStream_t s);
+
 // Cholesky of one tile.  info_out receives offset + local pivot index of
 // the first failure (written once); kernels skip when info_out, abort_flag
 // or abort2 is already non-zero.  The plain FP64 path passes its info word

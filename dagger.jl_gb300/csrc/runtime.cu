@@ -371,12 +371,8 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case OP_OZ_POTRF:
       return potrf_f64_oz(t.uplo, t.n, t.c, t.ldc, info, t.info_offset, (void *)t.b,
                           (size_t)t.ldb * 256, s);
-    case OP_OZ_INV: {  // W = U^-T (upper) or L^-T (lower): the identity solved in place
-      const bool up = (t.uplo == 'U' || t.uplo == 'u');
-      DG_TRY(eye_f64(t.n, t.c, t.ldc, info, s));
-      return trsm_f64_oz(up ? 'L' : 'R', up ? 'U' : 'L', 'T', 'N', t.n, t.n, 1.0, t.a, t.lda, t.c,
-                         t.ldc, (void *)t.b, (size_t)t.ldb * 256, info, s);
-    }
+    case OP_OZ_INV:  // W = U^-T (upper) or L^-T (lower), one column per CTA
+      return trinv_t_f64(t.uplo, t.n, t.a, t.lda, t.c, t.ldc, info, s);
     case OP_OZ_TRSM:
       return trsm_f64_oz(t.side, t.uplo, t.transa, t.diag, t.m, t.n, t.alpha, t.a, t.lda, t.c,
                          t.ldc, (void *)t.b, (size_t)t.ldb * 256, info, s);

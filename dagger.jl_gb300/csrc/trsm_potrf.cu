@@ -119,9 +119,12 @@ constexpr int TC_MAX_RHS = 128;
 // column-parallel launch replaces the recursion up to this width.
 constexpr int kPotrfColsMax = 512;
 
+// eye (forward solves only): column c starts as e_c instead of being read, so
+// its first c entries stay zero and the blocks above c are skipped (the
+// columns of a triangular inverse).
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_cols_kernel(TriView<T> tv, int len, T *X,
-                                                        long long rs, long long cs,
+                                                        long long rs, long long cs, int eye,
                                                         const int *a1, const int *a2) {
   if (aborted(a1, a2)) return;
   extern __shared__ unsigned char tc_smem[];
@@ -129,14 +132,16 @@ __global__ void __launch_bounds__(256) trsm_cols_kernel(TriView<T> tv, int len, 
   T *x = (T *)(tc_smem + sizeof(T) * TB * (TB + 1));    // the column
   __shared__ T part[4][TB];
   const int tid = threadIdx.x;
-  T *xc = X + (size_t)blockIdx.x * cs;  // element i of this column at xc[i * rs]
-  for (int i = tid; i < len; i += 256) x[i] = xc[(size_t)i * rs];
+  const int col = blockIdx.x;
+  T *xc = X + (size_t)col * cs;  // element i of this column at xc[i * rs]
+  for (int i = tid; i < len; i += 256) x[i] = eye ? T(i == col ? 1 : 0) : xc[(size_t)i * rs];
   __syncthreads();
   const int nblk = (len + TB - 1) / TB;
-  for (int bi = 0; bi < nblk; bi++) {
+  const int b_first = (eye && tv.lower) ? col / TB : 0;
+  for (int bi = b_first; bi < nblk; bi++) {
     const int b = tv.lower ? bi : nblk - 1 - bi;
     const int r0 = b * TB, rl = min(TB, len - r0);
-    const int p0 = tv.lower ? 0 : r0 + rl, p1 = tv.lower ? r0 : len;  // solved rows
+    const int p0 = tv.lower ? b_first * TB : r0 + rl, p1 = tv.lower ? r0 : len;  // solved rows
     // x[r0 + i] -= sum_{p0 <= p < p1} M(r0 + i, p) x[p]
     if (!tv.trans) {  // M(i, p) = T_[i + p ld]: threads along i, 4 groups over p
       const int i = tid & (TB - 1), g = tid >> 6;
@@ -199,7 +204,7 @@ __global__ void __launch_bounds__(256) trsm_cols_kernel(TriView<T> tv, int len, 
 
 template <typename T>
 int trsm_cols(const TriView<T> &tv, int len, T *X, long long rs, long long cs, int nn,
-              const int *a1, const int *a2, cudaStream_t s) {
+              const int *a1, const int *a2, cudaStream_t s, int eye = 0) {
   const size_t smem = sizeof(T) * (TB * (TB + 1) + (size_t)len);
   static bool attr[64] = {false};
   int dev = 0;
@@ -210,7 +215,7 @@ int trsm_cols(const TriView<T> &tv, int len, T *X, long long rs, long long cs, i
                                      (int)(sizeof(T) * (TB * (TB + 1) + TC_MAX_LEN))));
     attr[dev & 63] = true;
   }
-  trsm_cols_kernel<T><<<nn, 256, smem, s>>>(tv, len, X, rs, cs, a1, a2);
+  trsm_cols_kernel<T><<<nn, 256, smem, s>>>(tv, len, X, rs, cs, eye, a1, a2);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -465,6 +470,22 @@ int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_o
   oz.status = info_out;
   return potrf_rec<double>(uplo == 'U' || uplo == 'u', n, A, lda, info_out, info_offset, s,
                            nullptr, nullptr, oz);
+}
+
+int trinv_t_f64(char uplo, int n, const double *A, int lda, double *W, int ldw,
+                const int *abort_flag, cudaStream_t s) {
+  if (n <= 0) return 0;
+  if (n > TC_MAX_LEN) return DG_ERR_UNSUPPORTED;
+  // W = U^-T: U' W = I, left side; W = L^-T: W L' = I, right side.  Both are
+  // forward substitutions whose right-hand sides are the unit vectors.
+  const bool up = (uplo == 'U' || uplo == 'u');
+  TriView<double> tv;
+  tv.T_ = A;
+  tv.ld = lda;
+  tv.trans = up;   // left, 'T' -> M = U'; right, 'T' -> M = L (canonical forward)
+  tv.lower = true;
+  tv.unit = false;
+  return trsm_cols<double>(tv, n, W, up ? 1 : ldw, up ? ldw : 1, n, abort_flag, nullptr, s, 1);
 }
 
 int trsm_f32(char side, char uplo, char transa, char diag, int m, int n, float alpha,
