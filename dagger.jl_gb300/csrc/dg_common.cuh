@@ -123,6 +123,9 @@ constexpr int kOzSlices = 8;
 // and left out of the slices and the scale.  dscale: when set, the beta of
 // output row i (dmode 1) or column j (dmode 2) is dscale[i] / dscale[j]
 // (C = alpha A'B + diag(d) C, or C d), instead of the scalar beta.
+// blocks_per_cta > 1: each CTA computes that many 128 x 64 output blocks in
+// turn, forming one block's outputs while the next one's products run (for
+// launches that share the GPU with others); 0: ceil(blocks / SMs), one wave.
 int oz_split(const double *src, long long cstride, long long kstride, int K, int ncols,
              void *slices, long long ldk, long long sstride, unsigned long long *scales,
              const int *abort_flag, cudaStream_t s, const int *abort2 = nullptr,
@@ -131,7 +134,8 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
             long long a_sstride, const unsigned long long *a_scales, const void *b_slices,
             long long ldb_k, long long b_sstride, const unsigned long long *b_scales, double beta,
             double *C, long long ldc, int tri, int *status, cudaStream_t s,
-            const int *abort2 = nullptr, const double *dscale = nullptr, int dmode = 0);
+            const int *abort2 = nullptr, const double *dscale = nullptr, int dmode = 0,
+            int blocks_per_cta = 1);
 // The rows of the n x n matrix held as an nb x nb tile grid (tile (i, j) at
 // tiles_dev[i + j*mt], column-major, ld = its row count): vector c = row c,
 // K = n, into slices + s*ldk*n + c*ldk (n <= 131072).

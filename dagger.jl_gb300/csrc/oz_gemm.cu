@@ -44,12 +44,15 @@
 // warps: warp 16 issues the TMA loads, warp 17 the MMAs (levels 7..9 first),
 // warps 0-15 (four per TMEM lane quarter, 16 columns each) read levels 2..6
 // at the end of each window while the next stage's MMAs onto levels 7..9
-// run; at the start they prefetch the C tile into L2 and decode the column
-// exponents, at the end they form the outputs (several warps per scheduler,
-// so the integer epilogue's latency is hidden).
+// run, and at the end of a block they form its outputs (several warps per
+// scheduler, so the integer epilogue's latency is hidden).  A CTA may own
+// several output blocks: the producer and the issuer then run on into the
+// next block as soon as the readers have emptied TMEM, so that one block's
+// outputs are formed while the next block's products run.
 // All waits are bounded (1 s): a timeout records DG_ERR_TIMEOUT and the CTA
 // drains and returns.
 #include <cuda_bf16.h>
+#include <limits.h>
 
 #include "dg_common.cuh"
 #include "runtime.h"
@@ -95,6 +98,7 @@ struct OzParams {
   const double *dscale;   // when set, beta of row i (dmode 1) / column j (dmode 2) is dscale[.]
   int dmode;
   int guard;              // fraction bits below 2^-42 of the integer sum
+  int blocks;             // 128 x 64 output blocks of the stored part
 };
 
 // frexp exponent of the non-negative double with bits b (0 for 0).
@@ -141,21 +145,66 @@ __device__ __forceinline__ double int_to_double_scaled(long long T, int E) {
   return scale_slow(sign, p, mant, E);
 }
 
+// Output blocks (128 x 64) that hold part of the stored triangle in block
+// column bj: row blocks lo .. lo + count - 1 (all mblk of them when tri = 0).
+__host__ __device__ __forceinline__ int oz_col_blocks(int tri, int bj, int mblk, int &lo) {
+  int hi = mblk;
+  lo = 0;
+  if (tri == 1) {  // i <= j: rows below (64 bj + 63) only
+    const int h = (bj * OZ_BN + OZ_BN - 1) / OZ_BM + 1;
+    hi = h < mblk ? h : mblk;
+  } else if (tri == 2) {  // i >= j: rows from 64 bj on
+    lo = (bj * OZ_BN) / OZ_BM;
+  }
+  return hi > lo ? hi - lo : 0;
+}
+
+// Origin of the v-th output block of the stored part, row blocks fastest.
+__device__ __forceinline__ void oz_block(const OzParams &p, int v, int mblk, int nblk, int &i0,
+                                         int &j0) {
+  if (p.tri == 0) {
+    i0 = (v % mblk) * OZ_BM;
+    j0 = (v / mblk) * OZ_BN;
+    return;
+  }
+  i0 = j0 = 0;
+  for (int bj = 0; bj < nblk; bj++) {
+    int lo;
+    const int c = oz_col_blocks(p.tri, bj, mblk, lo);
+    if (v < c) {
+      i0 = (lo + v) * OZ_BM;
+      j0 = bj * OZ_BN;
+      return;
+    }
+    v -= c;
+  }
+}
+
+// The same decision in every lane of a warp (the TMEM loads are warp-wide).
+__device__ __forceinline__ bool warp_aborted(const int *flag) {
+  return __any_sync(0xffffffffu, *(const volatile int *)flag != 0);
+}
+
+// One CTA computes the output blocks v = blockIdx.x, + gridDim.x, ... of
+// the stored part (p.blocks of them).  Its TMA producer and MMA issuer run
+// ahead across block boundaries: the next block's stages are loaded while
+// the current block's last MMAs run, and its MMAs start as soon as the
+// readers have taken the current block's accumulators out of TMEM, so that
+// the outputs are formed (C read, integer sum rounded, C written) while the
+// tensor cores work on the next block.
 __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_constant__ OzParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + OZ_STAGES * OZ_STAGE);
   uint64_t *empty = full + OZ_STAGES;
   uint64_t *ready = empty + OZ_STAGES;   // MMA -> readers: a window's exact sums complete
-  uint64_t *drained = ready + 1;         // readers -> MMA: exact accumulators read
-  uint64_t *done = drained + 1;          // MMA -> readers: everything complete
+  uint64_t *drained = ready + 1;         // readers -> MMA: a window's accumulators read
+  uint64_t *done = drained + 1;          // MMA -> readers: every MMA of the CTA complete
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   int *abort_flag = (int *)(tmem_slot + 1);
-  int *eb_s = abort_flag + 1;            // the 64 column exponents
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i0 = blockIdx.x * OZ_BM, j0 = blockIdx.y * OZ_BN;
-  if ((p.tri == 1 && i0 > j0 + OZ_BN - 1) || (p.tri == 2 && j0 > i0 + OZ_BM - 1)) return;
+  const int mblk = (p.m + OZ_BM - 1) / OZ_BM, nblk = (p.n + OZ_BN - 1) / OZ_BN;
   // one read of the status words decides for the whole CTA
   if (threadIdx.x == 0)
     *abort_flag = aborted(p.status, p.abort2) ? 1 : 0;
@@ -183,31 +232,36 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   }
-  if (threadIdx.x < OZ_BN)
-    eb_s[threadIdx.x] = (j0 + (int)threadIdx.x < p.n) ? exponent_of(p.mb[j0 + threadIdx.x]) : 0;
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const int nst = (p.k + OZ_BK - 1) / OZ_BK;  // stages
+  const int nst = (p.k + OZ_BK - 1) / OZ_BK;  // stages per block
   const int nwin = (nst + OZ_WIN - 1) / OZ_WIN;
 
   if (warp == OZ_PRODUCER) {
     if (lane == 0) {
       // ---------------- TMA producer ----------------
-      int it = 0;
-      for (; it < nst && !*(volatile int *)abort_flag; it++) {
-        const int st = it % OZ_STAGES;
-        if (it >= OZ_STAGES && !mbar_wait(&empty[st], ((it / OZ_STAGES) - 1) & 1)) {
-          atomicExch(abort_flag, 1);
-          break;
+      int g = 0;  // stages loaded, over all blocks
+      bool stop = false;
+      for (int v = blockIdx.x; v < p.blocks && !stop; v += gridDim.x) {
+        int i0, j0;
+        oz_block(p, v, mblk, nblk, i0, j0);
+        for (int it = 0; it < nst; it++, g++) {
+          const int st = g % OZ_STAGES;
+          if (*(volatile int *)abort_flag ||
+              (g >= OZ_STAGES && !mbar_wait(&empty[st], ((g / OZ_STAGES) - 1) & 1))) {
+            atomicExch(abort_flag, 1);
+            stop = true;
+            break;
+          }
+          uint8_t *dst = smem + st * OZ_STAGE;
+          mbar_expect_tx(&full[st], OZ_STAGE);
+          tma_load_3d(dst, &p.a, &full[st], it * OZ_BK, i0, 0);
+          tma_load_3d(dst + OZ_S * OZ_A_SLICE, &p.b, &full[st], it * OZ_BK, j0, 0);
         }
-        uint8_t *dst = smem + st * OZ_STAGE;
-        mbar_expect_tx(&full[st], OZ_STAGE);
-        tma_load_3d(dst, &p.a, &full[st], it * OZ_BK, i0, 0);
-        tma_load_3d(dst + OZ_S * OZ_A_SLICE, &p.b, &full[st], it * OZ_BK, j0, 0);
       }
       // drain the loads in flight
-      for (int q = (it > OZ_STAGES ? it - OZ_STAGES : 0); q < it; q++)
+      for (int q = (g > OZ_STAGES ? g - OZ_STAGES : 0); q < g; q++)
         if (!mbar_wait(&full[q % OZ_STAGES], (q / OZ_STAGES) & 1)) atomicExch(abort_flag, 1);
     }
     __syncwarp();
@@ -216,150 +270,179 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
       // ---------------- MMA issuer ----------------
       const uint32_t idesc64 = idesc_f16kind(OZ_BM, OZ_BN, false);  // N = 64 c: + (8 (c-1)) << 17
       const uint32_t sbase = smem_u32(smem);
-      for (int it = 0; it < nst; it++) {
-        const int st = it % OZ_STAGES, w = it / OZ_WIN, wpos = it % OZ_WIN;
-        if (!mbar_wait(&full[st], (it / OZ_STAGES) & 1)) {
-          atomicExch(abort_flag, 1);
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // descriptors: base + (byte offset >> 4)
-        const uint32_t sa = sbase + st * OZ_STAGE, sb = sa + OZ_S * OZ_A_SLICE;
-        const uint64_t da = OZ_BK == 32 ? sw64_desc(sa) : sw32_desc(sa);
-        const uint64_t db = OZ_BK == 32 ? sw64_desc(sb) : sw32_desc(sb);
-        // A_s x [B_t .. B_u] onto levels s+t .. s+u (TMEM column 64 (s+t-2))
-        auto mma_run = [&](int kk, int s_, int t, int u, uint32_t acc) {
-          mma_bf16(tmem + 64 * (s_ + t - 2), da + (((s_ - 1) * OZ_A_SLICE + kk * 32) >> 4),
-                   db + (((t - 1) * OZ_B_SLICE + kk * 32) >> 4),
-                   idesc64 + ((uint32_t)(8 * (u - t)) << 17), acc);
-        };
-        // levels 7..9: t from max(1, 7 - s) to 9 - s; the first MMA sets them
+      int g = 0, gw = 0;  // stages and windows issued, over all blocks
+      bool stop = false, any = false;
+      for (int v = blockIdx.x; v < p.blocks && !stop; v += gridDim.x) {
+        for (int it = 0; it < nst; it++, g++) {
+          const int st = g % OZ_STAGES, wpos = it % OZ_WIN;
+          if (!mbar_wait(&full[st], (g / OZ_STAGES) & 1)) {
+            atomicExch(abort_flag, 1);
+            stop = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          // descriptors: base + (byte offset >> 4)
+          const uint32_t sa = sbase + st * OZ_STAGE, sb = sa + OZ_S * OZ_A_SLICE;
+          const uint64_t da = OZ_BK == 32 ? sw64_desc(sa) : sw32_desc(sa);
+          const uint64_t db = OZ_BK == 32 ? sw64_desc(sb) : sw32_desc(sb);
+          // A_s x [B_t .. B_u] onto levels s+t .. s+u (TMEM column 64 (s+t-2))
+          auto mma_run = [&](int kk, int s_, int t, int u, uint32_t acc) {
+            mma_bf16(tmem + 64 * (s_ + t - 2), da + (((s_ - 1) * OZ_A_SLICE + kk * 32) >> 4),
+                     db + (((t - 1) * OZ_B_SLICE + kk * 32) >> 4),
+                     idesc64 + ((uint32_t)(8 * (u - t)) << 17), acc);
+          };
+          // a new block resets levels 7..9 too: the previous block's sums
+          // (all levels) must have been read
+          if (it == 0 && gw > 0) {
+            if (!mbar_wait(drained, (gw - 1) & 1)) {
+              atomicExch(abort_flag, 1);
+              stop = true;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          }
+          any = true;
+          // levels 7..9: t from max(1, 7 - s) to 9 - s; the block's first MMA sets them
 #pragma unroll 1
-        for (int kk = 0; kk < OZ_BK / 16; kk++)
+          for (int kk = 0; kk < OZ_BK / 16; kk++)
 #pragma unroll 1
-          for (int s_ = 1; s_ <= OZ_S; s_++)
-            mma_run(kk, s_, 7 - s_ > 1 ? 7 - s_ : 1, 9 - s_, (it == 0 && kk == 0 && s_ == 1) ? 0u : 1u);
-        // levels 2..6: the previous window's sums must have been read
-        if (wpos == 0 && w > 0 && !mbar_wait(drained, (w - 1) & 1)) {
-          atomicExch(abort_flag, 1);
-          break;
-        }
-        const uint32_t first = (wpos == 0) ? 0u : 1u;
+            for (int s_ = 1; s_ <= OZ_S; s_++)
+              mma_run(kk, s_, 7 - s_ > 1 ? 7 - s_ : 1, 9 - s_,
+                      (it == 0 && kk == 0 && s_ == 1) ? 0u : 1u);
+          // levels 2..6: the previous window's sums must have been read
+          if (wpos == 0 && it > 0) {
+            if (!mbar_wait(drained, (gw - 1) & 1)) {
+              atomicExch(abort_flag, 1);
+              stop = true;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          }
+          const uint32_t first = (wpos == 0) ? 0u : 1u;
 #pragma unroll 1
-        for (int kk = 0; kk < OZ_BK / 16; kk++) {
-          const uint32_t a0 = (kk == 0) ? first : 1u;
-          mma_run(kk, 1, 1, 4, a0);   // levels 2..5
-          mma_run(kk, 1, 5, 5, a0);   // level 6
-          mma_run(kk, 2, 1, 4, 1u);   // levels 3..6
-          mma_run(kk, 3, 1, 3, 1u);   // levels 4..6
-          mma_run(kk, 4, 1, 2, 1u);   // levels 5..6
-          mma_run(kk, 5, 1, 1, 1u);   // level 6
+          for (int kk = 0; kk < OZ_BK / 16; kk++) {
+            const uint32_t a0 = (kk == 0) ? first : 1u;
+            mma_run(kk, 1, 1, 4, a0);   // levels 2..5
+            mma_run(kk, 1, 5, 5, a0);   // level 6
+            mma_run(kk, 2, 1, 4, 1u);   // levels 3..6
+            mma_run(kk, 3, 1, 3, 1u);   // levels 4..6
+            mma_run(kk, 4, 1, 2, 1u);   // levels 5..6
+            mma_run(kk, 5, 1, 1, 1u);   // level 6
+          }
+          mma_commit(&empty[st]);
+          if (wpos == OZ_WIN - 1 || it == nst - 1) {
+            mma_commit(ready);
+            gw++;
+          }
         }
-        mma_commit(&empty[st]);
-        if (wpos == OZ_WIN - 1 || it == nst - 1) mma_commit(ready);
       }
-      mma_commit(done);
+      if (any)
+        mma_commit(done);
+      else
+        mbar_arrive(done);
     }
     __syncwarp();
   } else {
-    // ---------------- readers: C into L2 while the MMAs run ----------------
-    for (int line = threadIdx.x; line < OZ_BN * (OZ_BM / 16); line += 32 * OZ_READERS) {
-      const int col = j0 + line / (OZ_BM / 16), row = i0 + 16 * (line % (OZ_BM / 16));
-      if (col < p.n && row < p.m)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(p.c + (size_t)row + (size_t)col * p.ldc));
+    // ---------------- readers ----------------
+    // reader warp w: TMEM lanes 32 (w mod 4) .. + 31 (one output row per
+    // thread), columns cb .. cb + 15 with cb = 16 (w / 4)
+    const int cb = (warp >> 2) * OZ_RCOLS;
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    // levels 9, 8, 7 summed in FP32 join the integer sum at 2^-(42 + guard)
+    // (|v| < 2^-21 K / 1024)
+    const float unit7 = __int_as_float((127 + 42 + p.guard) << 23);
+    int gw = 0;  // windows read, over all blocks
+    for (int v = blockIdx.x; v < p.blocks; v += gridDim.x) {
+      int i0, j0;
+      oz_block(p, v, mblk, nblk, i0, j0);
+      long long acc[OZ_RCOLS];
+#pragma unroll
+      for (int c = 0; c < OZ_RCOLS; c++) acc[c] = 0;
+      bool ok = !warp_aborted(abort_flag);
+      for (int w = 0; w < nwin; w++, gw++) {
+        if (ok) {
+          ok = __all_sync(0xffffffffu, mbar_wait(ready, gw & 1));
+          if (!ok) atomicExch(abort_flag, 1);
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (ok) {
+#pragma unroll
+          for (int lvl = 2; lvl <= 6; lvl++) {
+            const float up = __int_as_float((127 + 7 * lvl) << 23);  // 2^(7 lvl)
+            const int sh = 7 * (6 - lvl);                            // x 2^(7 (6 - lvl))
+#pragma unroll
+            for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
+              float x[16];
+              tmem_ld16(tmem + 64 * (lvl - 2) + cb + ch + lane_base, x);
+#pragma unroll
+              for (int c = 0; c < 16; c++)
+                acc[ch + c] +=
+                    (long long)((unsigned long long)(long long)__float2int_rn(x[c] * up) << sh);
+            }
+          }
+          if (w == nwin - 1) {
+#pragma unroll
+            for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
+              float x[16], y[16];
+              tmem_ld16(tmem + 64 * 7 + cb + ch + lane_base, x);
+              tmem_ld16(tmem + 64 * 6 + cb + ch + lane_base, y);
+#pragma unroll
+              for (int c = 0; c < 16; c++) x[c] = y[c] + x[c];
+              tmem_ld16(tmem + 64 * 5 + cb + ch + lane_base, y);
+#pragma unroll
+              for (int c = 0; c < 16; c++)
+                acc[ch + c] = (long long)((unsigned long long)acc[ch + c] << p.guard) +
+                              (long long)__float2int_rn((y[c] + x[c]) * unit7);
+            }
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(drained);
+      }
+      const int row = i0 + (warp & 3) * 32 + lane;
+      if (!ok || row >= p.m) continue;
+      // the block's outputs, while the tensor cores run the next block
+      const int ea = exponent_of(p.ma[row]);
+      const bool fast = (p.alpha == -1.0 && p.beta == 1.0);
+#pragma unroll
+      for (int ch = 0; ch < OZ_RCOLS; ch += 8) {
+        double old[8];
+        int eb[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          const int col = j0 + cb + ch + c;
+          const bool in = col < p.n && !(p.tri == 1 && row > col) && !(p.tri == 2 && row < col);
+          old[c] = (in && (p.beta != 0.0 || p.dmode)) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
+          eb[c] = col < p.n ? exponent_of(p.mb[col]) : 0;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          const int col = j0 + cb + ch + c;
+          if (col >= p.n || (p.tri == 1 && row > col) || (p.tri == 2 && row < col)) continue;
+          double vout;
+          if (ea == kOzNonFinite || eb[c] == kOzNonFinite) {
+            vout = __longlong_as_double(0x7FF8000000000000ll);
+          } else {
+            const double x = int_to_double_scaled(acc[ch + c], ea + eb[c] - 42 - p.guard);
+            if (fast)
+              vout = old[c] - x;
+            else if (p.dmode)
+              vout = fma(p.dscale[p.dmode == 1 ? row : col], old[c], p.alpha * x);
+            else
+              vout = (p.beta != 0.0) ? fma(p.alpha, x, p.beta * old[c]) : p.alpha * x;
+          }
+          p.c[(size_t)row + (size_t)col * p.ldc] = vout;
+        }
+      }
     }
   }
 
-  // ---------------- exact sums (reader warps) ----------------
-  // reader warp w: TMEM lanes 32 (w mod 4) .. + 31 (one output row per
-  // thread), columns cb .. cb + 15 with cb = 16 (w / 4)
-  const bool reader = warp < OZ_READERS;
-  const int cb = (warp >> 2) * OZ_RCOLS;
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  long long acc[OZ_RCOLS];
-#pragma unroll
-  for (int c = 0; c < OZ_RCOLS; c++) acc[c] = 0;
-  for (int w = 0; w < nwin && reader; w++) {
-    if (!mbar_wait(ready, w & 1)) {
-      atomicExch(abort_flag, 1);
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-    for (int lvl = 2; lvl <= 6; lvl++) {
-      const float up = __int_as_float((127 + 7 * lvl) << 23);  // 2^(7 lvl)
-      const int sh = 7 * (6 - lvl);                            // x 2^(7 (6 - lvl))
-#pragma unroll
-      for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
-        float v[16];
-        tmem_ld16(tmem + 64 * (lvl - 2) + cb + ch + lane_base, v);
-#pragma unroll
-        for (int c = 0; c < 16; c++)
-          acc[ch + c] +=
-              (long long)((unsigned long long)(long long)__float2int_rn(v[c] * up) << sh);
-      }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    mbar_arrive(drained);
-  }
-  const bool ok = mbar_wait(done, 0);
+  // every MMA complete before TMEM is freed
+  if (threadIdx.x == 0 && !mbar_wait(done, 0)) atomicExch(abort_flag, 1);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (!ok) atomicExch(abort_flag, 1);
   __syncthreads();
-  const bool aborted_now = *(volatile int *)abort_flag != 0;
-  if (!aborted_now && nst > 0 && reader) {
-    const int row = i0 + (warp & 3) * 32 + lane;
-    const int ea = row < p.m ? exponent_of(p.ma[row]) : 0;
-    // levels 9, 8, 7 summed in FP32 (all lanes: the loads are warp-wide),
-    // joined to the integer sum at 2^-(42 + guard) (|v| < 2^-21 K / 1024)
-    const float unit7 = __int_as_float((127 + 42 + p.guard) << 23);
-#pragma unroll
-    for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
-      float v[16], w[16];
-      tmem_ld16(tmem + 64 * 7 + cb + ch + lane_base, v);
-      tmem_ld16(tmem + 64 * 6 + cb + ch + lane_base, w);
-#pragma unroll
-      for (int c = 0; c < 16; c++) v[c] = w[c] + v[c];
-      tmem_ld16(tmem + 64 * 5 + cb + ch + lane_base, w);
-#pragma unroll
-      for (int c = 0; c < 16; c++)
-        acc[ch + c] = (long long)((unsigned long long)acc[ch + c] << p.guard) +
-                      (long long)__float2int_rn((w[c] + v[c]) * unit7);
-    }
-    if (row < p.m) {
-      const bool fast = (p.alpha == -1.0 && p.beta == 1.0);
-#pragma unroll
-      for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
-      double old[16];
-#pragma unroll
-      for (int c = 0; c < 16; c++) {
-        const int col = j0 + cb + ch + c;
-        const bool in = col < p.n && !(p.tri == 1 && row > col) && !(p.tri == 2 && row < col);
-        old[c] = (in && (p.beta != 0.0 || p.dmode)) ? p.c[(size_t)row + (size_t)col * p.ldc] : 0.0;
-      }
-#pragma unroll
-      for (int c = 0; c < 16; c++) {
-        const int col = j0 + cb + ch + c;
-        if (col >= p.n || (p.tri == 1 && row > col) || (p.tri == 2 && row < col)) continue;
-        const int eb = eb_s[cb + ch + c];
-        double vout;
-        if (ea == kOzNonFinite || eb == kOzNonFinite) {
-          vout = __longlong_as_double(0x7FF8000000000000ll);
-        } else {
-          const double x = int_to_double_scaled(acc[ch + c], ea + eb - 42 - p.guard);
-          if (fast)
-            vout = old[c] - x;
-          else if (p.dmode)
-            vout = fma(p.dscale[p.dmode == 1 ? row : col], old[c], p.alpha * x);
-          else
-            vout = (p.beta != 0.0) ? fma(p.alpha, x, p.beta * old[c]) : p.alpha * x;
-        }
-        p.c[(size_t)row + (size_t)col * p.ldc] = vout;
-      }
-      }
-    }
-  }
-  if (aborted_now && threadIdx.x == 0 && p.status) atomicCAS(p.status, 0, DG_ERR_TIMEOUT);
+  if (*(volatile int *)abort_flag != 0 && threadIdx.x == 0 && p.status)
+    atomicCAS(p.status, 0, DG_ERR_TIMEOUT);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
@@ -611,7 +694,7 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
             long long a_sstride, const unsigned long long *ma, const void *b_slices,
             long long ldb_k, long long b_sstride, const unsigned long long *mb, double beta,
             double *C, long long ldc, int tri, int *status, cudaStream_t s, const int *abort2,
-            const double *dscale, int dmode) {
+            const double *dscale, int dmode, int blocks_per_cta) {
   if (m <= 0 || n <= 0) return 0;
   if (k <= 0 || k > kOzMaxK || lda_k % 8 || ldb_k % 8) return DG_ERR_UNSUPPORTED;
   if (lda_k < k || ldb_k < k) return DG_ERR_UNSUPPORTED;
@@ -638,8 +721,25 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
                                      OZ_SMEM));
     attr[dev & 63] = true;
   }
-  dim3 grid((m + OZ_BM - 1) / OZ_BM, (n + OZ_BN - 1) / OZ_BN);
-  oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(p);
+  const int mblk = (m + OZ_BM - 1) / OZ_BM, nblk = (n + OZ_BN - 1) / OZ_BN;
+  long long blocks = 0;
+  for (int bj = 0; bj < nblk; bj++) {
+    int lo;
+    blocks += oz_col_blocks(tri, bj, mblk, lo);
+  }
+  if (blocks == 0) return 0;
+  if (blocks > INT_MAX) return DG_ERR_UNSUPPORTED;
+  p.blocks = (int)blocks;
+  int per = blocks_per_cta;
+  if (per <= 0) {  // one wave: ceil(blocks / SMs) blocks per CTA
+    static int sms[64] = {0};
+    if (!sms[dev & 63]) {
+      DG_CUDA_TRY(cudaDeviceGetAttribute(&sms[dev & 63], cudaDevAttrMultiProcessorCount, dev));
+    }
+    per = (int)((blocks + sms[dev & 63] - 1) / sms[dev & 63]);
+  }
+  const long long ctas = (blocks + per - 1) / per;
+  oz_gemm_kernel<<<(unsigned)ctas, OZ_THREADS, OZ_SMEM, s>>>(p);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -681,7 +781,7 @@ int oz_gemm_general(char ta, char tb, int m, int n, int k, double alpha, const d
     DG_TRY(oz_split(B, tB ? 1 : ldb, tB ? ldb : 1, k, n, sb, ldk, ldk * n, mb, status, s, abort2));
   }
   return oz_gemm(m, n, k, alpha, sa, ldk, ldk * m, ma, sb, ldk, same ? ldk * m : ldk * n, mb, beta,
-                 C, ldc, tri, status, s, abort2);
+                 C, ldc, tri, status, s, abort2, nullptr, 0, 0);
 }
 
 }  // namespace dg
@@ -737,5 +837,5 @@ extern "C" int dg_gemm_f64_slices(int m, int n, int k, double alpha, const void 
   return dg::oz_gemm(m, n, k, alpha, a_slices, lda_k, (long long)lda_k * m,
                      (const unsigned long long *)a_scales, b_slices, ldb_k, (long long)ldb_k * n,
                      (const unsigned long long *)b_scales, beta, C, ldc, 0, status,
-                     (cudaStream_t)stream);
+                     (cudaStream_t)stream, nullptr, nullptr, 0, 0);
 }

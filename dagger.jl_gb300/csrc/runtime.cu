@@ -403,7 +403,8 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
       const double *ds = (t.side == 'A') ? slot_diag(t.a, t.lda, t.ldb)
                          : (t.side == 'B') ? slot_diag(t.b, t.lda, t.ldb) : nullptr;
       return oz_gemm(t.m, t.n, t.k, t.alpha, t.a, t.lda, sstride, ea, t.b, t.lda, sstride, eb,
-                     t.beta, t.c, t.ldc, tri, info, s, nullptr, ds, t.side == 'A' ? 1 : 2);
+                     t.beta, t.c, t.ldc, tri, info, s, nullptr, ds, t.side == 'A' ? 1 : 2,
+                     t.diag == 'P' ? kOzBlocksPerCta : 1);
     }
     case DG_OP_COPY:
       if (t.m <= 0 || t.n <= 0) return 0;
@@ -928,8 +929,11 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
           t.m = rows(j); t.n = rows(m); t.a = slot(k, j); t.b = slot(k, m);
           t.c = T(j, m); t.ldc = rows(j); t.uplo = (j == m) ? 'L' : 'N';
         }
+        // the next panel is urgent; the others share the GPU, one CTA per
+        // several output blocks
+        if (m != k + 1) t.diag = 'P';
         dg_region_add(r, &t);
-        if (m == k + 1) mark_urgent(r);  // the next panel
+        if (m == k + 1) mark_urgent(r);
       }
     }
   }

@@ -21,7 +21,8 @@ constexpr int kUrgentStreams = 4;  // high-priority streams for critical-path ta
 //                ldc = ldk, k = slot capacity in vectors
 //   OP_OZ_GEMM   a, b = slice slots (lda = ldk, ldb = slot capacity), c = FP64
 //                tile (ldc), m x n output, k = K, alpha, beta; uplo 'U' / 'L'
-//                stores one triangle
+//                stores one triangle; diag 'P' (off the critical path): each
+//                CTA computes kOzBlocksPerCta output blocks in turn
 //   OP_OZ_TRSM   DG_OP_TRSM whose recursion updates are emulated, with
 //   OP_OZ_POTRF  (likewise DG_OP_POTRF) b = slice scratch of ldb * 256 bytes
 //   OP_OZ_INV    c (n x n, ldc) = U^-T for uplo 'U' / L^-T for 'L' of the
@@ -33,6 +34,7 @@ constexpr int OP_OZ_TRSM = 102;
 constexpr int OP_OZ_POTRF = 103;
 constexpr int OP_OZ_INV = 104;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
+constexpr int kOzBlocksPerCta = 4;
 size_t oz_slot_bytes(long long ldk, long long cap);
 size_t oz_ring_bytes_for(int n, int nb);
 

@@ -50,7 +50,9 @@ def _emulated_gemm_error(m, n, k, alpha, beta, seed, scale_rows=False):
 
 @pytest.mark.parametrize("m,n,k", [(128, 64, 64), (1, 1, 1), (257, 129, 100), (1000, 700, 1024),
                                    (130, 70, 513), (64, 300, 8), (1024, 1024, 1024),
-                                   (256, 64, 4096), (300, 100, 33000)])
+                                   (256, 64, 4096), (300, 100, 33000),
+                                   # several output blocks per CTA (one wave over the SMs)
+                                   (4096, 1024, 256), (3000, 2000, 100), (2500, 700, 1500)])
 def test_emulated_gemm_vs_fp64(m, n, k):
     assert _emulated_gemm_error(m, n, k, -1.0, 1.0, m + n + k) <= 1.0
 
