@@ -355,6 +355,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
     for (int v = blockIdx.x; v < p.blocks; v += gridDim.x) {
       int i0, j0;
       oz_block(p, v, mblk, nblk, i0, j0);
+      // the block's C into L2 while its products run
+      for (int line = threadIdx.x; line < OZ_BN * (OZ_BM / 16); line += 32 * OZ_READERS) {
+        const int col = j0 + line / (OZ_BM / 16), row = i0 + 16 * (line % (OZ_BM / 16));
+        if (col < p.n && row < p.m)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(p.c + (size_t)row + (size_t)col * p.ldc));
+      }
       long long acc[OZ_RCOLS];
 #pragma unroll
       for (int c = 0; c < OZ_RCOLS; c++) acc[c] = 0;

@@ -911,6 +911,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
           t.m = rows(j); t.n = rows(k); t.a = slot(k, j); t.b = slot(k, k);
           t.c = T(j, k); t.ldc = rows(j); t.side = 'B';
         }
+        if (j != k + 1) t.diag = 'P';  // off the critical path
         dg_region_add(r, &t);
         if (j == k + 1) mark_urgent(r);
       }
