@@ -731,6 +731,8 @@ extern "C" int dg_set_f64_engine(int engine) {
   return old;
 }
 
+extern "C" int dg_get_f64_engine(void) { return dg::get_f64_engine(); }
+
 extern "C" int dg_potrf_async(char uplo, int n, double *A, int lda, int *info_dev, void *stream) {
   DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
   DG_CHECK_ARG(n >= 0, 2);
@@ -831,12 +833,13 @@ extern "C" int dg_gemv(char trans, int m, int n, double alpha, const double *A, 
 // ---------------------------------------------------------------------------
 namespace dg {
 
-// The factorization's slots, plus one column of slots so that a following
-// solve with up to nb right-hand sides finds its ring in place, then the
-// FP64 inverses of the last kOzRingDepth diagonal tiles.
+// The factorization's slots, plus three columns of slots so that a following
+// solve with up to nb right-hand sides finds its ring in place (with the
+// inverses: oz_solve_ring_bytes_for(n, nb, nb, true)), then the FP64
+// inverses of the last kOzRingDepth diagonal tiles.
 static size_t oz_inv_offset(int n, int nb) {
   const int mt = (n + nb - 1) / nb;
-  return (size_t)kOzRingDepth * (mt + 1) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+  return (size_t)kOzRingDepth * (mt + 3) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
 }
 static size_t oz_inv_bytes(int nb) { return ((size_t)nb * nb * 8 + 255) & ~(size_t)255; }
 size_t oz_ring_bytes_for(int n, int nb) {
@@ -848,7 +851,7 @@ size_t oz_ring_bytes_for(int n, int nb) {
 // (k mod depth, j), and every SYRK/GEMM of step k reads its operands from the
 // slots.  The datadeps rules order a slot's reuse after its last reader.
 static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, double *const *tiles,
-                                     void *ring) {
+                                     void *ring, double *winv) {
   const int mt = (n + nb - 1) / nb;
   auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
   auto T = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
@@ -866,6 +869,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
   // slices, then its result's for the trailing update.
   const int slot_units = (int)(sb / 256);
   auto W = [&](int k) {
+    if (winv) return winv + (size_t)k * nb * nb;
     return (double *)((char *)ring + oz_inv_offset(n, nb) + (size_t)(k % kOzRingDepth) * oz_inv_bytes(nb));
   };
   for (int k = 0; k < mt; k++) {
@@ -875,7 +879,15 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     t.info_offset = k * nb; t.b = slot(k, k); t.ldb = slot_units;
     dg_region_add(r, &t);
     mark_urgent(r);
-    if (k + 1 == mt) break;
+    if (k + 1 == mt) {
+      if (winv) {  // kept for the solves: the last tile's inverse too
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.a = T(k, k); t.lda = rows(k);
+        t.c = W(k); t.ldc = rows(k); t.b = slot(k, k); t.ldb = slot_units;
+        dg_region_add(r, &t);
+      }
+      break;
+    }
     memset(&t, 0, sizeof t);
     t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.a = T(k, k); t.lda = rows(k);
     t.c = W(k); t.ldc = rows(k); t.b = slot(k, k); t.ldb = slot_units;
@@ -941,13 +953,13 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
 }
 
 void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
-                           void *oz_ring) {
+                           void *oz_ring, double *winv) {
   const int mt = (n + nb - 1) / nb;
   auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
   auto T = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
   const bool up = (uplo == 'U' || uplo == 'u');
   if (oz_ring) {
-    build_cholesky_region_oz(r, up, n, nb, tiles, oz_ring);
+    build_cholesky_region_oz(r, up, n, nb, tiles, oz_ring, winv);
     return;
   }
   for (int k = 0; k < mt; k++) {
@@ -1004,13 +1016,15 @@ void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const
 
 // One left-side block solve of trsm.jl:89-140 (alpha = 1) over the factor's
 // tiles and the right-hand side's tiles.
-size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs) {
+size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs, bool inv) {
   const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
-  return (size_t)kOzRingDepth * (mt + bnt) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+  return (size_t)kOzRingDepth * (mt + bnt + (inv ? 1 + bnt : 0)) *
+         oz_slot_bytes((nb + 7) / 8 * 8, nb);
 }
 
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
-                      int nrhs, double *const *btiles, void *oz_ring, int step0) {
+                      int nrhs, double *const *btiles, void *oz_ring, int step0,
+                      const double *winv) {
   const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
   auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
   auto cols = [&](int j) { return (j + 1) * nb <= nrhs ? nb : nrhs - j * nb; };
@@ -1029,20 +1043,56 @@ void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double
     return (double *)((char *)oz_ring +
                       ((size_t)kOzRingDepth * mt + (size_t)(step % kOzRingDepth) * bnt + c) * sb);
   };
+  // with the inverses: slots after those hold the inverse's vectors and the
+  // block's columns before its solve
+  const size_t inv0 = (size_t)kOzRingDepth * (mt + bnt);
+  auto wslot = [&](int step) {
+    return (double *)((char *)oz_ring + (inv0 + (size_t)(step % kOzRingDepth)) * sb);
+  };
+  auto bslot = [&](int step, int c) {
+    return (double *)((char *)oz_ring +
+                      (inv0 + kOzRingDepth + (size_t)(step % kOzRingDepth) * bnt + c) * sb);
+  };
+  const bool inv = (oz_ring != nullptr && winv != nullptr);
   for (int s = 0; s < mt; s++) {
     int k = forward ? s : mt - 1 - s;
+    if (inv) {
+      // op(A(k, k))^-1 is W_k (trans 'T') or W_k' ('N'), W_k = U_kk^-T or
+      // L_kk^-T: its rows are W_k's rows or columns, its diagonal stays FP64
+      dg_task t;
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_SPLIT; t.a = winv + (size_t)k * nb * nb; t.lda = rows(k); t.m = rows(k);
+      t.n = rows(k); t.trans = (trans == 'N') ? 'N' : 'T'; t.diag = 'Z';
+      t.c = wslot(step0 + s); t.ldc = ldk; t.k = nb;
+      dg_region_add(r, &t);
+    }
     for (int c = 0; c < bnt; c++) {
       dg_task t;
       memset(&t, 0, sizeof t);
-      t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = uplo; t.transa = trans; t.diag = 'N';
-      t.m = rows(k); t.n = cols(c); t.alpha = 1.0; t.a = A(k, k); t.lda = rows(k);
-      t.c = B(k, c); t.ldc = rows(k);
-      dg_region_add(r, &t);
+      if (inv) {
+        // B(k, c) = op(A(k, k))^-1 B(k, c) as one emulated product
+        t.op = OP_OZ_SPLIT; t.trans = 'N'; t.a = B(k, c); t.lda = rows(k); t.m = rows(k);
+        t.n = cols(c); t.c = bslot(step0 + s, c); t.ldc = ldk; t.k = nb;
+        dg_region_add(r, &t);
+        mark_urgent(r);
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = rows(k); t.n = cols(c); t.k = rows(k);
+        t.alpha = 1.0; t.beta = 0.0; t.a = wslot(step0 + s); t.b = bslot(step0 + s, c);
+        t.lda = ldk; t.ldb = nb; t.c = B(k, c); t.ldc = rows(k); t.side = 'A';
+        dg_region_add(r, &t);
+        mark_urgent(r);
+      } else {
+        t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = uplo; t.transa = trans; t.diag = 'N';
+        t.m = rows(k); t.n = cols(c); t.alpha = 1.0; t.a = A(k, k); t.lda = rows(k);
+        t.c = B(k, c); t.ldc = rows(k);
+        dg_region_add(r, &t);
+      }
       if (oz_ring && s + 1 < mt) {  // the solved block's columns, once per step
         memset(&t, 0, sizeof t);
         t.op = OP_OZ_SPLIT; t.trans = 'N'; t.a = B(k, c); t.lda = rows(k); t.m = rows(k);
         t.n = cols(c); t.c = xslot(step0 + s, c); t.ldc = ldk; t.k = nb;
         dg_region_add(r, &t);
+        if (inv) mark_urgent(r);
       }
     }
     for (int s2 = s + 1; s2 < mt; s2++) {
@@ -1061,6 +1111,7 @@ void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double
           t.alpha = -1.0; t.beta = 1.0; t.a = aslot(step0 + s, m); t.b = xslot(step0 + s, c);
           t.lda = ldk; t.ldb = nb; t.c = B(m, c); t.ldc = rows(m);
           dg_region_add(r, &t);
+          if (inv && s2 == s + 1) mark_urgent(r);  // the next diagonal block
         }
         continue;
       }
@@ -1089,6 +1140,46 @@ extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles,
   if (dg::get_f64_engine() == 2 && nb <= 1024)
     DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
   dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring);
+  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+}
+
+extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *tiles,
+                                      double *winv, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(nb > 0, 3);
+  DG_CHECK_ARG(tiles != nullptr || n == 0, 4);
+  DG_CHECK_ARG(winv != nullptr || n == 0, 5);
+  if (dg::get_f64_engine() != 2 || nb > 1024) return DG_ERR_UNSUPPORTED;
+  if (n == 0) return 0;
+  dg_region r;
+  void *ring = nullptr;
+  DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+  dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring, winv);
+  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+}
+
+extern "C" int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *const *tiles,
+                                            const double *winv, int nrhs,
+                                            double *const *btiles, void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(nb > 0, 3);
+  DG_CHECK_ARG(nrhs >= 0, 6);
+  if (dg::get_f64_engine() != 2 || nb > 1024) return DG_ERR_UNSUPPORTED;
+  if (n == 0 || nrhs == 0) return 0;
+  DG_CHECK_ARG(tiles != nullptr, 4);
+  DG_CHECK_ARG(winv != nullptr, 5);
+  DG_CHECK_ARG(btiles != nullptr, 7);
+  dg_region r;
+  const bool up = (uplo == 'U' || uplo == 'u');
+  void *ring = nullptr;
+  DG_TRY(dg::device_state().oz_workspace(dg::oz_solve_ring_bytes_for(n, nb, nrhs, true), &ring));
+  const int mt = (n + nb - 1) / nb;
+  dg::build_solve_pass(&r, up ? 'U' : 'L', up ? 'T' : 'N', n, nb, tiles, nrhs, btiles, ring, 0,
+                       winv);
+  dg::build_solve_pass(&r, up ? 'U' : 'L', up ? 'N' : 'T', n, nb, tiles, nrhs, btiles, ring, mt,
+                       winv);
   return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
 }
 

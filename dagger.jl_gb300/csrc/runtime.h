@@ -69,13 +69,18 @@ int region_run(dg_region *r, int use_graph, int serial, cudaStream_t origin, int
 void clear_graphs();
 
 // oz_ring != nullptr selects the emulated-FP64 trailing updates, with
-// oz_ring_bytes_for(n, nb) bytes of slice slots (nb <= 1024).
+// oz_ring_bytes_for(n, nb) bytes of slice slots (nb <= 1024).  winv (with
+// oz_ring): the transposed inverses of the diagonal factor tiles are kept
+// there, tile k at winv + k nb^2 (ld = its row count), all mt of them.
 void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
-                           void *oz_ring = nullptr);
+                           void *oz_ring = nullptr, double *winv = nullptr);
 // One block-triangular solve pass; oz_ring (oz_solve_ring_bytes_for bytes)
-// selects emulated updates, step0 numbers its steps within the ring.
-size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs);
+// selects emulated updates, step0 numbers its steps within the ring; winv
+// (with oz_ring, the factorization's inverses) turns each diagonal block
+// solve into one emulated product.
+size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs, bool inv = false);
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
-                      int nrhs, double *const *btiles, void *oz_ring = nullptr, int step0 = 0);
+                      int nrhs, double *const *btiles, void *oz_ring = nullptr, int step0 = 0,
+                      const double *winv = nullptr);
 
 }  // namespace dg

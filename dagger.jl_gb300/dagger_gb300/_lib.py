@@ -95,7 +95,11 @@ SIGNATURES = {
     "dg_cholesky_tiled": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p]),
     "dg_cholesky_solve_tiled": (c_int, [c_char, c_int, c_int, c_void_p, c_int, c_void_p,
                                         c_void_p]),
+    "dg_cholesky_tiled_winv": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "dg_cholesky_solve_tiled_winv": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p, c_int,
+                                             c_void_p, c_void_p]),
     "dg_set_f64_engine": (c_int, [c_int]),
+    "dg_get_f64_engine": (c_int, []),
     "dg_ishermitian_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
     "dg_chkfinite_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
     "dg_probe_fp64_fma_tflops": (c_int, [c_int, ctypes.POINTER(c_double), c_void_p]),

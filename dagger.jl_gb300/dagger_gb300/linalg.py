@@ -122,6 +122,11 @@ def set_f64_engine(engine) -> str:
     return {v: k for k, v in F64_ENGINES.items()}[old]
 
 
+def get_f64_engine() -> str:
+    """The current engine of the FP64 tile updates (see set_f64_engine)."""
+    return {v: k for k, v in F64_ENGINES.items()}[lib().dg_get_f64_engine()]
+
+
 def trsv_(uplo, trans, diag, A, x, stream=None):
     """BLAS.trsv!(uplo, trans, diag, A, x) -> x."""
     pa, n, _, lda = _colmajor(A, "A")
@@ -145,12 +150,18 @@ def gemv_(trans, alpha, A, x, beta, y, stream=None):
 # ---------------------------------------------------------------------------
 
 class Cholesky:
-    """LinearAlgebra.Cholesky{T,<:DMatrix}: the factor tiles and uplo."""
+    """LinearAlgebra.Cholesky{T,<:DMatrix}: the factor tiles and uplo.
 
-    def __init__(self, factors: DArray, uplo: str, info: int):
+    With the emulated FP64 engine the factorization also keeps the
+    transposed inverses of its diagonal tiles (winv, formed for the panel
+    products anyway), which ldiv_ applies as emulated products; a Cholesky
+    built from factors alone solves by substitution."""
+
+    def __init__(self, factors: DArray, uplo: str, info: int, winv=None):
         self.factors = factors
         self.uplo = uplo
         self.info = info
+        self.winv = winv
 
     @property
     def U(self) -> torch.Tensor:
@@ -181,12 +192,22 @@ def cholesky_(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> C
     if uplo not in ('U', 'L'):
         raise ValueError("uplo must be 'U' or 'L'")
     nb = _square_blocks(A)
-    rc = lib().dg_cholesky_tiled(ch(uplo), A.shape[0], nb, A.tile_ptrs(), _stream(stream))
+    n = A.shape[0]
+    winv = None
+    if n > 0 and nb <= 1024 and lib().dg_get_f64_engine() == F64_ENGINES["emulated"]:
+        mt = (n + nb - 1) // nb
+        winv = torch.empty(mt * nb * nb, dtype=torch.float64, device=A.storage.device)
+        rc = lib().dg_cholesky_tiled_winv(ch(uplo), n, nb, A.tile_ptrs(), winv.data_ptr(),
+                                          _stream(stream))
+    else:
+        rc = lib().dg_cholesky_tiled(ch(uplo), n, nb, A.tile_ptrs(), _stream(stream))
     if rc < 0:
         check(rc)
-    if rc > 0 and check_:
-        raise PosDefException(rc)
-    return Cholesky(A, uplo, rc)
+    if rc > 0:
+        winv = None
+        if check_:
+            raise PosDefException(rc)
+    return Cholesky(A, uplo, rc, winv)
 
 
 def cholesky(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Cholesky:
@@ -207,8 +228,13 @@ def ldiv_(C: Cholesky, B: DArray, stream=None) -> DArray:
     if B.partitioning.blocksize[0] != nb or (B.ndim == 2 and B.partitioning.blocksize[1] != nb):
         raise ValueError("B must be blocked Blocks(nb, nb) (or Blocks(nb)) like the factor")
     nrhs = 1 if B.ndim == 1 else B.shape[1]
-    rc = lib().dg_cholesky_solve_tiled(ch(C.uplo), F.shape[0], nb, F.tile_ptrs(), nrhs,
-                                       B.tile_ptrs(), _stream(stream))
+    if C.winv is not None and lib().dg_get_f64_engine() == F64_ENGINES["emulated"]:
+        rc = lib().dg_cholesky_solve_tiled_winv(ch(C.uplo), F.shape[0], nb, F.tile_ptrs(),
+                                                C.winv.data_ptr(), nrhs, B.tile_ptrs(),
+                                                _stream(stream))
+    else:
+        rc = lib().dg_cholesky_solve_tiled(ch(C.uplo), F.shape[0], nb, F.tile_ptrs(), nrhs,
+                                           B.tile_ptrs(), _stream(stream))
     check(rc)
     return B
 

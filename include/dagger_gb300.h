@@ -181,6 +181,22 @@ int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles, void *stre
 int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *tiles, int nrhs,
                             double *const *btiles, void *stream);
 
+/* Extension of the two calls above for the emulated FP64 engine (engine 2,
+ * nb <= 1024; DG_ERR_UNSUPPORTED otherwise, without work): the factorization
+ * forms W_k = U_kk^-T (uplo 'U') or L_kk^-T ('L') of every diagonal factor
+ * tile for its panel products anyway; dg_cholesky_tiled_winv keeps all mt of
+ * them in winv (device, mt * nb * nb doubles: W_k at winv + k*nb*nb,
+ * column-major, ld = the tile's row count), and dg_cholesky_solve_tiled_winv
+ * then applies each diagonal block's solve as one emulated product with W_k
+ * (or W_k') instead of a substitution on the FP64 pipe.  winv belongs to the
+ * factor it was made with: the solve reads both.  Results satisfy the same
+ * bounds as dg_cholesky_tiled / dg_cholesky_solve_tiled. */
+int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *tiles, double *winv,
+                           void *stream);
+int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *const *tiles,
+                                 const double *winv, int nrhs, double *const *btiles,
+                                 void *stream);
+
 /* ishermitian(::DArray) (src/array/linalg.jl:90-124; pair test
  * is_cross_hermitian, linalg.jl:43-48) over the same tile grid.  Returns 1
  * (Hermitian), 0 (not), or a negative status.  Synchronises `stream`. */
@@ -198,6 +214,8 @@ int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream);
  * dg_gemm_f64_emulated_tn).  Returns the previous setting.  The setting is
  * process-wide. */
 int dg_set_f64_engine(int engine);
+/* The current setting of dg_set_f64_engine. */
+int dg_get_f64_engine(void);
 
 /* ---------------------------------------------------------------------------
  * Mixed-precision form (no counterpart in the reference: a faster path beside

@@ -192,3 +192,63 @@ def test_slice_stages_match_one_call():
                                 ldk, eb.data_ptr(), 1.0, C2.data_ptr(), m, None, s) == 0
     torch.cuda.synchronize()
     assert np.array_equal(host_f(C1), host_f(C2))
+
+
+@pytest.mark.parametrize("uplo", "UL")
+@pytest.mark.parametrize("n,nb,nrhs", [(1000, 128, 16), (2048, 1024, 64), (700, 100, 250)])
+def test_solve_engine2_inverse_and_substitution_agree(emulated, uplo, n, nb, nrhs):
+    """The solve with the kept inverses and the one by substitution (a
+    Cholesky built from the factor alone) both meet the oracle's bar."""
+    d = emulated
+    from oracle import tiled as o
+    A = o.spd_uniform(n, 3 * n + 1)
+    B = o.rhs_normal(n, nrhs, n + 1)
+    F, _ = o.chol_tiled(A, nb, uplo)
+    X = B.copy(order='F')
+    o.ldiv_cholesky(F, uplo, X, nb)
+    C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), uplo)
+    assert C.winv is not None
+    for chol in (C, d.Cholesky(C.factors, uplo, 0)):
+        DB = d.DArray.from_array(B, d.Blocks(nb, nb))
+        d.ldiv_(chol, DB)
+        assert rel_err(DB.numpy(), X) <= FP64_RTOL
+        assert o.backward_error(A, DB.numpy(), B).max() < 1e-14
+
+
+@pytest.mark.parametrize("uplo", "UL")
+def test_factor_keeps_diagonal_inverses(emulated, uplo):
+    """winv holds W_k = U_kk^-T (L_kk^-T) of every diagonal tile, the ragged
+    last one included, column-major with ld = the tile's rows."""
+    d = emulated
+    import torch
+    from oracle import tiled as o
+    n, nb = 1000, 128
+    A = o.spd_uniform(n, 11)
+    C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), uplo)
+    G = C.factors.numpy()
+    W = C.winv.cpu().numpy()
+    mt = (n + nb - 1) // nb
+    for k in range(mt):
+        r = min(nb, n - k * nb)
+        T = G[k * nb:k * nb + r, k * nb:k * nb + r]
+        T = np.triu(T) if uplo == 'U' else np.tril(T)
+        Wk = W[k * nb * nb:k * nb * nb + r * r].reshape(r, r, order='F')
+        ref = np.linalg.inv(T).T
+        assert np.abs(Wk - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_winv_calls_need_the_emulated_engine():
+    import torch
+    import dagger_gb300 as d
+    from oracle import tiled as o
+    L = d.lib()
+    old = d.set_f64_engine("dfma")
+    try:
+        A = d.DArray.from_array(o.spd_uniform(256, 3), d.Blocks(64, 64))
+        w = torch.empty(4 * 64 * 64, dtype=torch.float64, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+        assert L.dg_cholesky_tiled_winv(b'U', 256, 64, A.tile_ptrs(), w.data_ptr(), s) == -1003
+        C = d.cholesky(A, 'U')
+        assert C.winv is None
+    finally:
+        d.set_f64_engine(old)
