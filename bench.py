@@ -503,11 +503,17 @@ def _measured_bf16_peak():
         return 1900.0, "fallback 1.9 PFLOP/s"
 
 
+# The emulated FP64 GEMM cuts each operand vector into 7 BF16 slices and
+# multiplies the 28 slice pairs (s, t) with s + t <= 8.
+EMULATED_SLICES = 7
+EMULATED_PRODUCTS = 28
+
+
 def roofline_emulated(L, nb, dev, stream, s):
     """The emulated FP64 tile GEMM (oz_gemm_kernel) of the trailing update,
     C(nb x nb) -= A'B with both operands already cut into slices, timed alone
-    with CUDA events on the launching stream: 36 BF16 products of 2 nb^3
-    flops per launch against the measured BF16 tensor peak."""
+    with CUDA events on the launching stream: EMULATED_PRODUCTS BF16 products
+    of 2 nb^3 flops per launch against the measured BF16 tensor peak."""
     import torch
     ldk = (nb + 7) // 8 * 8
     g = torch.Generator(device=dev)
@@ -515,8 +521,8 @@ def roofline_emulated(L, nb, dev, stream, s):
     Ta = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
     Tb = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
     Tc = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
-    sa = torch.empty(8 * ldk * nb, dtype=torch.bfloat16, device=dev)
-    sb = torch.empty(8 * ldk * nb, dtype=torch.bfloat16, device=dev)
+    sa = torch.empty(EMULATED_SLICES * ldk * nb, dtype=torch.bfloat16, device=dev)
+    sb = torch.empty(EMULATED_SLICES * ldk * nb, dtype=torch.bfloat16, device=dev)
     ea = torch.empty(nb, dtype=torch.int64, device=dev)
     eb = torch.empty(nb, dtype=torch.int64, device=dev)
     L.dg_f64_slices(nb, nb, Ta.data_ptr(), nb, 1, sa.data_ptr(), ldk, ea.data_ptr(), s)
@@ -537,12 +543,12 @@ def roofline_emulated(L, nb, dev, stream, s):
     torch.cuda.synchronize()
     tg = g0.elapsed_time(g1) / 1e3 / reps
     peak, src = _measured_bf16_peak()
-    achieved = 36 * 2.0 * nb ** 3 / tg / 1e12
+    achieved = EMULATED_PRODUCTS * 2.0 * nb ** 3 / tg / 1e12
     return {"bound": "tensor", "kernel": "oz_gemm_kernel (emulated FP64 tile GEMM of the "
                                           "trailing update, BF16 tcgen05)",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": src,
-            "per_launch": f"36 x 2*{nb}^3 BF16 flops (= 2*{nb}^3 FP64-equivalent), "
+            "per_launch": f"{EMULATED_PRODUCTS} x 2*{nb}^3 BF16 flops (= 2*{nb}^3 FP64-equivalent), "
                           f"{1e6 * tg:.0f} us, {nb // 128} x {nb // 64} CTAs",
             "fp64_equivalent_tflops": 2.0 * nb ** 3 / tg / 1e12,
             "traffic": None}

@@ -111,14 +111,14 @@ int scale_f32(int m, int n, float alpha, float *B, long long ldb, const int *abo
 
 // FP64 GEMM emulated on the BF16 tensor cores (oz_gemm.cu).  oz_split cuts
 // ncols FP64 vectors of length K (element k of vector c at
-// src[c*cstride + k*kstride]) into 8 BF16 slices (slice s of vector c at
+// src[c*cstride + k*kstride]) into 7 BF16 slices (slice s of vector c at
 // slices + s*sstride + c*ldk) and one 8-byte scale word per vector; oz_gemm
 // computes C(m x n) = alpha * sum_p A(p, i) B(p, j) + beta * C from the
 // slices of the m A-vectors and n B-vectors (K <= 131072, ldk a multiple of 8);
 // tri 1 / 2 stores only the upper / lower triangle.  Kernels skip when
 // *status or *abort2 is non-zero; a timed-out wait records DG_ERR_TIMEOUT in
 // *status.
-constexpr int kOzSlices = 8;
+constexpr int kOzSlices = 7;
 // diag_out (square operands): element c of vector c is written to diag_out[c]
 // and left out of the slices and the scale.  dscale: when set, the beta of
 // output row i (dmode 1) or column j (dmode 2) is dscale[i] / dscale[j]

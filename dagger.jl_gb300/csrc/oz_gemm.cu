@@ -6,44 +6,45 @@
 //
 // Splitting (oz_max_kernel, oz_slice_kernel): each operand vector v (a row of
 // op(A) or a column of op(B), K values) is scaled by 2^-e with
-// 2^(e-1) <= max|v| < 2^e and cut into S = 8 slices by rounding to nearest:
-//     v = 2^e * sum_{s=1..8} d_s 2^(-7 s) + r,   d_s integer,
-//     |d_1| <= 128, |d_s| <= 64 (s >= 2), |r| <= 2^(e-57).
-// Slice s is stored as the BF16 value d_s 2^(-7s): exact, since every
-// integer of magnitude <= 256 has at most 8 significant bits.  The split
-// runs on integer arithmetic: the per-vector scale word is max|v|'s bit
-// pattern (an atomic maximum over the vector), e follows from its exponent
-// field, and X = round(v 2^(56-e)) (|X| <= 2^56) is cut into base-128 digits.
+// 2^(e-1) <= max|v| < 2^e and cut into S = 7 slices by rounding to nearest:
+//     v = 2^e * sum_{s=1..7} d_s 2^(-8 s) + r,   d_s integer,
+//     |d_1| <= 256, |d_s| <= 128 (s >= 2), |r| <= 2^(e-57).
+// Slice s is stored as the BF16 value d_s 2^(-8s): exact, since every
+// integer of magnitude <= 256 has at most 8 significant bits (the digits use
+// the whole BF16 significand).  The split runs on integer arithmetic: the
+// per-vector scale word is max|v|'s bit pattern (an atomic maximum over the
+// vector), e follows from its exponent field, and X = round(v 2^(56-e))
+// (|X| <= 2^56) is cut into balanced base-256 digits.
 // A vector holding an infinity or a NaN makes every output that uses it NaN.
 //
-// Products (oz_gemm_kernel): C = alpha * 2^(ea_i + eb_j) * sum_{s+t<=9} A_s B_t'
-// + beta * C, K <= 131072.  A product A_s B_t' sums terms d_s d_t 2^(-7(s+t)).
-// Level L = s + t collects the L - 1 products of that weight.  Over a window
-// of 512 values of K the sum of level L <= 6 stays within 2^24 units of
-// 2^(-7L) (level 6: (2*128*64 + 2*64*64 + 64*64) * 512 < 2^24; levels 2 and
-// 3 within 2^24 over all 1024), so its FP32 accumulation in TMEM is exact.
-// Levels 2..6 are read exactly after each window and summed as 64-bit
-// integers in units of 2^-42 (|sum| < 2^53 K / 1024).  Levels 7..9
-// accumulate in FP32 over the whole K (their rounding is below 2^-56 of
-// |C|'s scale; the dropped levels >= 10 and the slicing remainder are below
-// 2^-55) and join the integer sum at 2^-51 (2^-44 at the largest K).  The 62-bit total is rounded
-// once to FP64 by integer arithmetic, with 2^(ea_i + eb_j) folded into the
+// Products (oz_gemm_kernel): C = alpha * 2^(ea_i + eb_j) * sum_{s+t<=8} A_s B_t'
+// + beta * C, K <= 131072: 28 slice products.  A product A_s B_t' sums terms
+// d_s d_t 2^(-8(s+t)).  Level L = s + t collects the L - 1 products of that
+// weight.  Over a window of 128 values of K the sum of level L <= 5 stays
+// within 2^24 units of 2^(-8L) (level 5: (2*256*128 + 2*128*128) * 128 < 2^24),
+// so its FP32 accumulation in TMEM is exact.  Levels 2..5 are read exactly
+// after each window and summed as 64-bit integers in units of 2^-40
+// (|sum| < 2^50 K / 1024).  Levels 6..8 accumulate in FP32 over the whole K
+// (their rounding is below 2^-55 K of |C|'s scale, the dropped levels >= 9
+// below 2^-55 K, the slicing remainders below 2^-56 K) and join the integer
+// sum at 2^-51 (2^-44 at the largest K).  The 62-bit total is rounded once
+// to FP64 by integer arithmetic, with 2^(ea_i + eb_j) folded into the
 // exponent, and added to beta C.  The result has an FP64 GEMM's accuracy
 // relative to 2^(ea_i + eb_j) K.
 //
 // TMEM holds one 64-column accumulator per level, level L at columns
-// 64 (L - 2) .. 64 (L - 1) - 1 (all 512 columns).  The B slices of a stage
-// are stored one after the other, so B_t .. B_u form one operand of
+// 64 (L - 2) .. 64 (L - 1) - 1 (448 columns).  The B slices of a stage are
+// stored one after the other, so B_t .. B_u form one operand of
 // 64 (u - t + 1) rows, and A_s x [B_t .. B_u] is ONE MMA whose output
 // columns fall exactly on levels s + t .. s + u.  Per 16 values of K that is
-// 14 MMAs of N = 64..256: 8 onto levels 7..9 and 6 onto levels 2..6.
+// 11 MMAs of N = 64..256: 7 onto levels 6..8 and 4 onto levels 2..5.
 //
 // CTA tile: 128 rows (TMEM lanes) x 64 columns.  K advances in stages of 32:
-// one stage holds the 8 slices of the A tile and of the B tile (96 KiB, two
+// one stage holds the 7 slices of the A tile and of the B tile (84 KiB, two
 // 3-D TMA loads with 64-byte swizzle), and two stages are in flight.  18
-// warps: warp 16 issues the TMA loads, warp 17 the MMAs (levels 7..9 first),
-// warps 0-15 (four per TMEM lane quarter, 16 columns each) read levels 2..6
-// at the end of each window while the next stage's MMAs onto levels 7..9
+// warps: warp 16 issues the TMA loads, warp 17 the MMAs (levels 6..8 first),
+// warps 0-15 (four per TMEM lane quarter, 16 columns each) read levels 2..5
+// at the end of each window while the next stage's MMAs onto levels 6..8
 // run, and at the end of a block they form its outputs (several warps per
 // scheduler, so the integer epilogue's latency is hidden).  A CTA may own
 // several output blocks: the producer and the issuer then run on into the
@@ -63,22 +64,22 @@ namespace {
 
 using namespace ptx;
 
-constexpr int OZ_S = 8;                                   // slices per operand
+constexpr int OZ_S = kOzSlices;                           // slices per operand (7)
 constexpr int kOzNonFinite = 1 << 30;                     // exponent of a non-finite vector
 #ifndef OZ_STAGE_K
 #define OZ_STAGE_K 32
 #endif
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = OZ_STAGE_K;  // K per stage (16 or 32)
-constexpr int OZ_WIN = 512 / OZ_BK;                       // stages per exact window (K 512)
+constexpr int OZ_WIN = 128 / OZ_BK;                       // stages per exact window (K 128)
 constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB at K 32
 constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB at K 32
-constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 96 KiB at K 32
+constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 84 KiB at K 32
 constexpr int OZ_STAGES = (192 * 1024) / OZ_STAGE;        // 2 at K 32, 4 at K 16
 static_assert(OZ_BK == 16 || OZ_BK == 32, "stage K is 16 (32-byte swizzle) or 32 (64-byte)");
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE + 1024 + 512;
-// Fraction bits kept below 2^-42 when levels 7..9 join the integer sum: 9 for
-// K <= 1024, one fewer per doubling of K, so |sum| * 2^guard stays below 2^62
-// (|sum| < 2^53 K / 1024).  K may reach kOzMaxK.
+// Fraction bits kept below 2^-40 when levels 6..8 join the integer sum: 11
+// for K <= 1024, one fewer per doubling of K, so |sum| * 2^guard stays below
+// 2^62 (|sum| < 2^50 K / 1024).  K may reach kOzMaxK.
 constexpr int kOzMaxK = 131072;
 constexpr int OZ_READERS = 16;                            // reader warps: 4 per TMEM lane quarter
 constexpr int OZ_RCOLS = OZ_BN / (OZ_READERS / 4);        // columns per reader thread (16)
@@ -97,7 +98,7 @@ struct OzParams {
   const int *abort2;      // skip when non-zero (read only)
   const double *dscale;   // when set, beta of row i (dmode 1) / column j (dmode 2) is dscale[.]
   int dmode;
-  int guard;              // fraction bits below 2^-42 of the integer sum
+  int guard;              // fraction bits below 2^-40 of the integer sum
   int blocks;             // 128 x 64 output blocks of the stored part
 };
 
@@ -302,14 +303,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           }
           any = true;
-          // levels 7..9: t from max(1, 7 - s) to 9 - s; the block's first MMA sets them
+          // levels 6..8: t from max(1, 6 - s) to 8 - s; the block's first MMA
+          // (s = 1, levels 6..8) sets them
 #pragma unroll 1
           for (int kk = 0; kk < OZ_BK / 16; kk++)
 #pragma unroll 1
             for (int s_ = 1; s_ <= OZ_S; s_++)
-              mma_run(kk, s_, 7 - s_ > 1 ? 7 - s_ : 1, 9 - s_,
+              mma_run(kk, s_, 6 - s_ > 1 ? 6 - s_ : 1, 8 - s_,
                       (it == 0 && kk == 0 && s_ == 1) ? 0u : 1u);
-          // levels 2..6: the previous window's sums must have been read
+          // levels 2..5: the previous window's sums must have been read
           if (wpos == 0 && it > 0) {
             if (!mbar_wait(drained, (gw - 1) & 1)) {
               atomicExch(abort_flag, 1);
@@ -323,11 +325,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
           for (int kk = 0; kk < OZ_BK / 16; kk++) {
             const uint32_t a0 = (kk == 0) ? first : 1u;
             mma_run(kk, 1, 1, 4, a0);   // levels 2..5
-            mma_run(kk, 1, 5, 5, a0);   // level 6
-            mma_run(kk, 2, 1, 4, 1u);   // levels 3..6
-            mma_run(kk, 3, 1, 3, 1u);   // levels 4..6
-            mma_run(kk, 4, 1, 2, 1u);   // levels 5..6
-            mma_run(kk, 5, 1, 1, 1u);   // level 6
+            mma_run(kk, 2, 1, 3, 1u);   // levels 3..5
+            mma_run(kk, 3, 1, 2, 1u);   // levels 4..5
+            mma_run(kk, 4, 1, 1, 1u);   // level 5
           }
           mma_commit(&empty[st]);
           if (wpos == OZ_WIN - 1 || it == nst - 1) {
@@ -348,9 +348,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
     // thread), columns cb .. cb + 15 with cb = 16 (w / 4)
     const int cb = (warp >> 2) * OZ_RCOLS;
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-    // levels 9, 8, 7 summed in FP32 join the integer sum at 2^-(42 + guard)
-    // (|v| < 2^-21 K / 1024)
-    const float unit7 = __int_as_float((127 + 42 + p.guard) << 23);
+    // levels 8, 7, 6 summed in FP32 join the integer sum at 2^-(40 + guard)
+    // (|v| < 2^-21 K / 1024, so |v| 2^(40 + guard) < 2^30)
+    const float unit6 = __int_as_float((127 + 40 + p.guard) << 23);
     int gw = 0;  // windows read, over all blocks
     for (int v = blockIdx.x; v < p.blocks; v += gridDim.x) {
       int i0, j0;
@@ -373,9 +373,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (ok) {
 #pragma unroll
-          for (int lvl = 2; lvl <= 6; lvl++) {
-            const float up = __int_as_float((127 + 7 * lvl) << 23);  // 2^(7 lvl)
-            const int sh = 7 * (6 - lvl);                            // x 2^(7 (6 - lvl))
+          for (int lvl = 2; lvl <= 5; lvl++) {
+            const float up = __int_as_float((127 + 8 * lvl) << 23);  // 2^(8 lvl)
+            const int sh = 8 * (5 - lvl);                            // x 2^(8 (5 - lvl))
 #pragma unroll
             for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
               float x[16];
@@ -390,15 +390,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
 #pragma unroll
             for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
               float x[16], y[16];
-              tmem_ld16(tmem + 64 * 7 + cb + ch + lane_base, x);
-              tmem_ld16(tmem + 64 * 6 + cb + ch + lane_base, y);
+              tmem_ld16(tmem + 64 * 6 + cb + ch + lane_base, x);
+              tmem_ld16(tmem + 64 * 5 + cb + ch + lane_base, y);
 #pragma unroll
               for (int c = 0; c < 16; c++) x[c] = y[c] + x[c];
-              tmem_ld16(tmem + 64 * 5 + cb + ch + lane_base, y);
+              tmem_ld16(tmem + 64 * 4 + cb + ch + lane_base, y);
 #pragma unroll
               for (int c = 0; c < 16; c++)
                 acc[ch + c] = (long long)((unsigned long long)acc[ch + c] << p.guard) +
-                              (long long)__float2int_rn((y[c] + x[c]) * unit7);
+                              (long long)__float2int_rn((y[c] + x[c]) * unit6);
             }
           }
         }
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
           if (ea == kOzNonFinite || eb[c] == kOzNonFinite) {
             vout = __longlong_as_double(0x7FF8000000000000ll);
           } else {
-            const double x = int_to_double_scaled(acc[ch + c], ea + eb[c] - 42 - p.guard);
+            const double x = int_to_double_scaled(acc[ch + c], ea + eb[c] - 40 - p.guard);
             if (fast)
               vout = old[c] - x;
             else if (p.dmode)
@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(256) oz_max_kernel(OzSrc src, int K, int ncols
 // (k < ldk; zeros for k >= K): slice s (0-based) of vector c at
 // dst + s*sstride + c*ldk.  The 32 x 64 values pass through shared memory so
 // that the reads are coalesced in either orientation; each thread then cuts 8
-// consecutive values of one vector and writes 16 bytes per slice.
+// consecutive values of one vector into 7 slices and writes 16 bytes per slice.
 __global__ void __launch_bounds__(256) oz_slice_kernel(OzSrc src, int K, int ncols,
                                                       __nv_bfloat16 *dst, long long ldk,
                                                       long long sstride,
@@ -606,11 +606,11 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzSrc src, int K, int nco
       long long X = (e == kOzNonFinite) ? 0 : scaled56(tile[vi][k0 + j + h], e);
 #pragma unroll
       for (int s_ = OZ_S; s_ >= 1; s_--) {
-        const long long d = (s_ > 1) ? ((X + 64) & 127) - 64 : X;
-        X = (X - d) >> 7;
-        // d 2^(-7 s) has at most 8 significant bits: its BF16 is the FP32's top half
+        const long long d = (s_ > 1) ? ((X + 128) & 255) - 128 : X;
+        X = (X - d) >> 8;
+        // d 2^(-8 s) has at most 8 significant bits: its BF16 is the FP32's top half
         const uint32_t b =
-            __float_as_uint((float)(int)d * __int_as_float((127 - 7 * s_) << 23)) >> 16;
+            __float_as_uint((float)(int)d * __int_as_float((127 - 8 * s_) << 23)) >> 16;
         if (h == 0) lo[s_ - 1] = b; else hi[s_ - 1] = b;
       }
     }
@@ -717,7 +717,7 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   p.abort2 = abort2;
   p.dscale = dscale;
   p.dmode = dscale ? dmode : 0;
-  p.guard = 9;
+  p.guard = 11;
   for (long long kk = 1024; kk < k; kk *= 2) p.guard--;
   static bool attr[64] = {false};
   int dev = 0;

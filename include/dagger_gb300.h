@@ -209,7 +209,7 @@ int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream);
 /* Selects the FP64 tile engine: 0 = DFMA register tiles, 1 = DMMA
  * (mma.sync.m8n8k4.f64), 2 = DFMA for POTRF/TRSM plus, inside
  * dg_cholesky_tiled with nb <= 1024, the trailing SYRK/GEMM tile updates
- * emulated on the BF16 tensor cores with FP64 accuracy (8 slices of 7 bits
+ * emulated on the BF16 tensor cores with FP64 accuracy (7 slices of 8 bits
  * per operand vector, exact products, FP64 sum; see
  * dg_gemm_f64_emulated_tn).  Returns the previous setting.  The setting is
  * process-wide. */
@@ -301,9 +301,9 @@ int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const double *A, 
 
 /* Its two stages, for operands reused across products.  dg_f64_slices cuts
  * ncols FP64 vectors of length k <= 131072 (element p of vector c at
- * src[c*cstride + p*kstride]) into 8 BF16 slices, slice s of vector c at
+ * src[c*cstride + p*kstride]) into 7 BF16 slices, slice s of vector c at
  * slices + 2*(s*ldk*ncols + c*ldk) bytes (ldk >= k, a multiple of 8; the
- * buffer 16-byte aligned, 16*ldk*ncols bytes), and one 8-byte scale word per
+ * buffer 16-byte aligned, 14*ldk*ncols bytes), and one 8-byte scale word per
  * vector in `scales` (8-byte aligned, 8*ncols bytes).  dg_gemm_f64_slices
  * computes C = alpha A'B + beta C from the slices of the m columns of A and
  * the n columns of B (lda_k, ldb_k: their ldk).  status: optional device

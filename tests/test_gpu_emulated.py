@@ -1,5 +1,5 @@
 """FP64 engine 2: the trailing SYRK/GEMM tile updates emulated on the BF16
-tensor cores (8 slices of 7 bits per vector, exact products, FP64 sum).
+tensor cores (7 slices of 8 bits per vector, exact products, FP64 sum).
 
 The building block is checked against numpy's FP64 GEMM with the bound of an
 FP64 GEMM taken over each output's vectors:
@@ -180,8 +180,8 @@ def test_slice_stages_match_one_call():
     Ad, Bd = dev_f(A), dev_f(B)
     C1 = dev_f(C0)
     d.gemm_f64_emulated_tn(-1.0, Ad, Bd, 1.0, C1)
-    sa = torch.empty(8 * ldk * m, dtype=torch.bfloat16, device="cuda")
-    sb = torch.empty(8 * ldk * n, dtype=torch.bfloat16, device="cuda")
+    sa = torch.empty(7 * ldk * m, dtype=torch.bfloat16, device="cuda")
+    sb = torch.empty(7 * ldk * n, dtype=torch.bfloat16, device="cuda")
     ea = torch.empty(m, dtype=torch.int64, device="cuda")
     eb = torch.empty(n, dtype=torch.int64, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
