@@ -74,7 +74,7 @@ constexpr int OZ_WIN = 128 / OZ_BK;                       // stages per exact wi
 constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB at K 32
 constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB at K 32
 constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 84 KiB at K 32
-constexpr int OZ_STAGES = (192 * 1024) / OZ_STAGE;        // 2 at K 32, 4 at K 16
+constexpr int OZ_STAGES = (220 * 1024 - 1536) / OZ_STAGE;  // 2 at K 32, 5 at K 16
 static_assert(OZ_BK == 16 || OZ_BK == 32, "stage K is 16 (32-byte swizzle) or 32 (64-byte)");
 constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE + 1024 + 512;
 // Fraction bits kept below 2^-40 when levels 6..8 join the integer sum: 11

@@ -69,21 +69,21 @@ DeviceState &device_state() {
   return *p;
 }
 
-// Per-thread pools of non-blocking streams (per device): the urgent pool at
-// the device's greatest stream priority, the normal pool at the least, so
-// that the CTAs of a region's critical-path tasks are scheduled first.
-std::vector<cudaStream_t> &stream_pool(int want, bool urgent) {
-  static thread_local std::map<std::pair<int, bool>, std::vector<cudaStream_t>> pools;
+// Per-thread pools of non-blocking streams (per device and priority level):
+// level 0 at the device's greatest stream priority, each further level one
+// step lower down to the least, so that the CTAs of the tasks needed soonest
+// are scheduled first.
+std::vector<cudaStream_t> &stream_pool(int want, int level) {
+  static thread_local std::map<std::pair<int, int>, std::vector<cudaStream_t>> pools;
   int dev = 0;
   cudaGetDevice(&dev);
-  auto &v = pools[{dev, urgent}];
+  auto &v = pools[{dev, level}];
   while ((int)v.size() < want) {
     cudaStream_t s;
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
-    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, urgent ? greatest : least) !=
-        cudaSuccess)
-      break;
+    const int prio = (level >= kPrioLevels - 1 || greatest + level > least) ? least : greatest + level;
+    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio) != cudaSuccess) break;
     v.push_back(s);
   }
   return v;
@@ -193,7 +193,7 @@ struct dg_region {
     std::vector<int> readers;
   };
   std::vector<dg_task> tasks;
-  std::vector<char> urgent;  // critical-path tasks (high-priority streams)
+  std::vector<char> level;  // priority level, 0 = critical path (kPrioLevels - 1 by default)
   std::vector<std::vector<int>> preds;
   std::vector<Ainfo> ainfos;
   std::multimap<uintptr_t, int> by_lo;
@@ -278,7 +278,7 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
-  r->urgent.push_back(0);
+  r->level.push_back((char)(dg::kPrioLevels - 1));
   hash_bytes(r->hash, &t, sizeof(dg_task));
   std::vector<dg_region::Access> acc;
   task_accesses(t, acc);
@@ -419,23 +419,33 @@ struct Plan {
   std::vector<int> stream_of;
   std::vector<char> needs_event;
   int nstreams = 0;
+  std::vector<std::pair<int, int>> classes;  // (priority level, streams), in stream order
 };
 
-// Streams 0 .. kUrgentStreams-1 take the urgent tasks, the next `pool` the
-// others.  Within its class a task reuses the stream of its latest
-// predecessor when that predecessor is still the stream's tail, else the
-// least recently used stream.
+// One class of streams per priority level in use: kUrgentStreams streams for
+// each level above the lowest, `pool` for the lowest.  Within its class a
+// task reuses the stream of its latest predecessor when that predecessor is
+// still the stream's tail, else the least recently used stream.
 static Plan plan_streams(const dg_region &r, int pool) {
   Plan pl;
   const int n = (int)r.tasks.size();
-  const int total = kUrgentStreams + pool;
+  std::vector<int> first(kPrioLevels, -1), count(kPrioLevels, 0);
+  std::vector<char> used(kPrioLevels, 0);
+  for (int t = 0; t < n; t++) used[r.level[t]] = 1;
+  int total = 0;
+  for (int l = 0; l < kPrioLevels; l++) {
+    if (!used[l]) continue;
+    first[l] = total;
+    count[l] = (l == kPrioLevels - 1) ? pool : kUrgentStreams;
+    total += count[l];
+    pl.classes.push_back({l, count[l]});
+  }
   pl.stream_of.assign(n, 0);
   pl.needs_event.assign(n, 0);
   std::vector<int> tail(total, -1);
   std::vector<long> last_use(total, -1);
   for (int t = 0; t < n; t++) {
-    const bool urg = r.urgent[t] != 0;
-    const int s0 = urg ? 0 : kUrgentStreams, s1 = urg ? kUrgentStreams : total;
+    const int s0 = first[r.level[t]], s1 = s0 + count[r.level[t]];
     int best = -1, bestp = -1;
     for (int q : r.preds[t]) {
       int s = pl.stream_of[q];
@@ -456,12 +466,16 @@ static Plan plan_streams(const dg_region &r, int pool) {
   return pl;
 }
 
-void mark_urgent(dg_region *r) {
-  if (r->urgent.empty()) return;
-  r->urgent.back() = 1;
-  const int id = (int)r->urgent.size() - 1;
+void mark_level(dg_region *r, int level) {
+  if (r->level.empty()) return;
+  level = level < 0 ? 0 : level > kPrioLevels - 1 ? kPrioLevels - 1 : level;
+  r->level.back() = (char)level;
+  const int id = (int)r->level.size() - 1;
   hash_bytes(r->hash, &id, sizeof id);
+  hash_bytes(r->hash, &level, sizeof level);
 }
+
+void mark_urgent(dg_region *r) { mark_level(r, 0); }
 
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
@@ -486,12 +500,12 @@ static int issue(const dg_region &r, const Plan &pl, int *info, cudaStream_t ori
     }
     return 0;
   }
-  auto &upool = stream_pool(kUrgentStreams, true);
-  auto &npool = stream_pool(pl.nstreams - kUrgentStreams, false);
-  if ((int)upool.size() < kUrgentStreams || (int)npool.size() < pl.nstreams - kUrgentStreams)
-    return DG_ERR_CUDA;
-  std::vector<cudaStream_t> pool(upool.begin(), upool.end());
-  pool.insert(pool.end(), npool.begin(), npool.begin() + (pl.nstreams - kUrgentStreams));
+  std::vector<cudaStream_t> pool;
+  for (const auto &c : pl.classes) {
+    auto &v = stream_pool(c.second, c.first);
+    if ((int)v.size() < c.second) return DG_ERR_CUDA;
+    pool.insert(pool.end(), v.begin(), v.begin() + c.second);
+  }
   cudaEvent_t fork;
   DG_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
   events.push_back(fork);
@@ -901,7 +915,11 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     t.trans = up ? 'T' : 'N'; t.diag = 'Z'; t.c = slot(k, k); t.ldc = ldk; t.k = nb;
     dg_region_add(r, &t);
     mark_urgent(r);
+    // Priority of a tile of column j (row j for 'L') at step k: j - k - 1,
+    // the number of steps before POTRF(j) needs it, so the work needed soonest
+    // runs first; a task's level is never above those of its inputs.
     for (int j = k + 1; j < mt; j++) {
+      const int lvl = j - k - 1;
       for (int pass = 0; pass < 2; pass++) {  // the tile's input, then its result
         memset(&t, 0, sizeof t);
         t.op = OP_OZ_SPLIT; t.m = rows(k); t.n = rows(j); t.c = slot(k, j); t.ldc = ldk; t.k = nb;
@@ -911,7 +929,7 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
           t.trans = 'T'; t.a = T(j, k); t.lda = rows(j);
         }
         dg_region_add(r, &t);
-        if (j == k + 1) mark_urgent(r);  // the next diagonal tile waits for this panel tile
+        mark_level(r, lvl);
         if (pass == 1) break;
         memset(&t, 0, sizeof t);
         t.op = OP_OZ_GEMM; t.uplo = 'N'; t.k = rows(k); t.alpha = 1.0; t.beta = 0.0;
@@ -923,9 +941,9 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
           t.m = rows(j); t.n = rows(k); t.a = slot(k, j); t.b = slot(k, k);
           t.c = T(j, k); t.ldc = rows(j); t.side = 'B';
         }
-        if (j != k + 1) t.diag = 'P';  // off the critical path
+        if (lvl > 0) t.diag = 'P';  // off the critical path: one CTA per several blocks
         dg_region_add(r, &t);
-        if (j == k + 1) mark_urgent(r);
+        mark_level(r, lvl);
       }
     }
     // cholesky.jl:43-52 (upper) / 88-97 (lower): C(m, j) -= V_m' V_j over the
@@ -942,11 +960,12 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
           t.m = rows(j); t.n = rows(m); t.a = slot(k, j); t.b = slot(k, m);
           t.c = T(j, m); t.ldc = rows(j); t.uplo = (j == m) ? 'L' : 'N';
         }
-        // the next panel is urgent; the others share the GPU, one CTA per
-        // several output blocks
-        if (m != k + 1) t.diag = 'P';
+        // level j - k - 1 as for the panel tiles; off the critical path the
+        // tiles share the GPU, one CTA per several output blocks
+        const int lvl = j - k - 1;
+        if (lvl > 0) t.diag = 'P';
         dg_region_add(r, &t);
-        if (m == k + 1) mark_urgent(r);
+        mark_level(r, lvl);
       }
     }
   }

@@ -12,7 +12,8 @@
 namespace dg {
 
 constexpr int kDefaultStreams = 16;
-constexpr int kUrgentStreams = 4;  // high-priority streams for critical-path tasks
+constexpr int kUrgentStreams = 4;  // streams per priority level above the lowest
+constexpr int kPrioLevels = 6;     // stream priority levels used (fewer on the device collapse)
 
 // Internal task kinds of the tiled Cholesky region with the emulated FP64
 // engine (not part of the public dg_op enumeration):
@@ -52,8 +53,11 @@ struct DeviceState {
 };
 
 DeviceState &device_state();
-std::vector<cudaStream_t> &stream_pool(int want, bool urgent = false);
-void mark_urgent(dg_region *r);  // the last task added is on the critical path
+std::vector<cudaStream_t> &stream_pool(int want, int level = kPrioLevels - 1);
+// The priority level of the last task added: 0 = on the critical path, up to
+// kPrioLevels - 1 (the default) for work needed last.
+void mark_level(dg_region *r, int level);
+void mark_urgent(dg_region *r);  // mark_level(r, 0)
 
 // Strided byte footprint of a column-major matrix argument.
 struct Footprint {
