@@ -224,13 +224,41 @@ int trsm_cols(const TriView<T> &tv, int len, T *X, long long rs, long long cs, i
 // Cholesky of one block of length len <= 64 at A (leading dimension lda).
 // Works on the lower triangle L; for uplo 'U' the block is staged transposed
 // (U' = L) and written back transposed, so only the uplo triangle is touched.
+// Right-looking with the column scaling deferred: step j subtracts
+// M(i, j) M(k, j) / d_j (d_j the pivot) from the trailing triangle, and each
+// column is scaled by 1 / sqrt(d_j) once at the end (square roots and
+// divisions for all columns at once, off the sequential path), so one
+// barrier per column suffices.  Warps 0-6 update the trailing triangle of
+// step j while warp 7 updates element (j+1, j+1) first and forms 1 / d_{j+1}
+// by Newton's iteration for the reciprocal (x <- x + x (1 - d x), quadratic
+// convergence from the hardware's approximate reciprocal, two steps to FP64
+// precision), so the sequential path per column is a few FMAs.  A pivot that
+// is not positive (or NaN) stops the factorization at that column,
+// info = column + 1 (LAPACK's dpotf2 test); the columns before it are
+// factored.
+template <typename T>
+__device__ __forceinline__ T recip_newton(T d);
+template <>
+__device__ __forceinline__ double recip_newton<double>(double d) {
+  double x;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(d));
+  x = fma(x, fma(-d, x, 1.0), x);
+  return fma(x, fma(-d, x, 1.0), x);
+}
+template <>
+__device__ __forceinline__ float recip_newton<float>(float d) {
+  float x;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(x) : "f"(d));
+  return fmaf(x, fmaf(-d, x, 1.0f), x);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *A, long long lda,
                                                          int *info, int info_offset,
                                                          const int *a1, const int *a2) {
   if (aborted(info, a1) || aborted(a2, nullptr)) return;
   __shared__ T Ms[TB][TB + 1];
-  __shared__ T piv[2];  // sqrt of the pivot and its reciprocal, formed once
+  __shared__ T dinv[TB];  // 1 / d_j
   __shared__ int fail_at;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < len * len; e += nt) {
@@ -238,30 +266,52 @@ __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *
     if (!upper) { i = e % len; j = e / len; } else { j = e % len; i = e / len; }
     if (j <= i) Ms[i][j] = upper ? A[(size_t)j + (size_t)i * lda] : A[(size_t)i + (size_t)j * lda];
   }
-  if (tid == 0) fail_at = -1;
   __syncthreads();
+  // the approximate reciprocal flushes subnormals: extreme pivots divide
+  const T lo = sizeof(T) == 8 ? T(1e-300) : T(1e-36), hi = sizeof(T) == 8 ? T(1e300) : T(1e36);
+  auto pivot = [&](int j, T d) {
+    if (!(d > T(0)))  // not positive, or NaN
+      fail_at = j;
+    else
+      dinv[j] = (d > lo && d < hi) ? recip_newton<T>(d) : T(1) / d;
+  };
+  if (tid == 0) {
+    fail_at = -1;
+    pivot(0, Ms[0][0]);
+  }
+  __syncthreads();
+  int done = 0;  // columns factored
+  constexpr int kRowLanes = 14;  // warps 0-6: a 14 x 16 grid over the trailing triangle
   for (int j = 0; j < len; j++) {
-    if (tid == 0) {
-      const T d = Ms[j][j];
-      if (!(d > T(0))) {  // not positive, or NaN: LAPACK's test in dpotrf2/dpotf2
-        fail_at = j;
-      } else {
-        piv[0] = sqrt(d);
-        piv[1] = T(1) / piv[0];
+    if (fail_at >= 0 && fail_at <= j) break;  // the same value for every thread
+    done = j + 1;
+    const T r2 = dinv[j];
+    if (tid == 7 * 32) {
+      if (j + 1 < len) {
+        const T a = Ms[j + 1][j];
+        const T d = fma(-a * r2, a, Ms[j + 1][j + 1]);
+        Ms[j + 1][j + 1] = d;
+        pivot(j + 1, d);
+      }
+    } else if (tid < 7 * 32) {
+      for (int i = j + 1 + (tid >> 4); i < len; i += kRowLanes) {
+        const T lij = Ms[i][j] * r2;
+        for (int k = j + 1 + (tid & 15); k <= i; k += 16)
+          if (k != j + 1 || i != j + 1) Ms[i][k] = fma(-lij, Ms[k][j], Ms[i][k]);
       }
     }
     __syncthreads();
-    if (fail_at >= 0) break;  // the same value for every thread: uniform exit
-    const T r = piv[1];
-    for (int i = j + 1 + tid; i < len; i += nt) Ms[i][j] *= r;
-    if (tid == 0) Ms[j][j] = piv[0];
-    __syncthreads();
-    // the trailing triangle, threads on a 16 x 16 grid (no index division)
-    for (int i = j + 1 + (tid >> 4); i < len; i += nt >> 4) {
-      const T lij = Ms[i][j];
-      for (int k = j + 1 + (tid & 15); k <= i; k += 16) Ms[i][k] = fma(-lij, Ms[k][j], Ms[i][k]);
-    }
-    __syncthreads();
+  }
+  // scale the factored columns: L(j, j) = sqrt(d_j), L(i, j) = M(i, j) / sqrt(d_j)
+  __shared__ T sq[TB], rs[TB];
+  for (int j = tid; j < done; j += nt) {
+    sq[j] = sqrt(Ms[j][j]);
+    rs[j] = T(1) / sq[j];
+  }
+  __syncthreads();
+  for (int e = tid; e < len * len; e += nt) {
+    const int i = e % len, j = e / len;
+    if (j < done && i >= j) Ms[i][j] = (i == j) ? sq[j] : Ms[i][j] * rs[j];
   }
   __syncthreads();
   if (fail_at >= 0 && tid == 0) atomicCAS(info, 0, info_offset + fail_at + 1);
