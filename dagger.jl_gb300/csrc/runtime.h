@@ -35,7 +35,7 @@ constexpr int OP_OZ_TRSM = 102;
 constexpr int OP_OZ_POTRF = 103;
 constexpr int OP_OZ_INV = 104;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
-constexpr int kOzBlocksPerCta = 4;
+constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);
 size_t oz_ring_bytes_for(int n, int nb);
 
