@@ -11,7 +11,8 @@
 #     BLAS.trsm!, syrk!, gemm!, trsv!, gemv!: each returns a ccall wrapper, so
 #     Dagger's unchanged _chol! (src/array/cholesky.jl) and trsm!/trsv!
 #     (src/array/trsm.jl) run their tile tasks on the GB300 kernels;
-#   * cholesky_gb300! / ldiv_gb300!: the whole datadeps region of a DArray
+#   * cholesky_gb300! / ldiv_gb300! (and the engine-2 forms cholesky_gb300_winv!
+#     / ldiv_gb300!(C, winv, B)): the whole datadeps region of a DArray
 #     handed to the library in one call (dg_cholesky_tiled /
 #     dg_cholesky_solve_tiled), issued as one cached multi-stream CUDA graph.
 #
@@ -216,6 +217,38 @@ function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, B::DArray{Float64})
     dgcheck(ccall((:dg_cholesky_solve_tiled, libdg), Cint,
                   (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
                   C.uplo, n, nb, tile_pointers(F), nrhs, tile_pointers(B), C_NULL))
+    return B
+end
+
+"""
+    cholesky_gb300_winv!(A::DArray{Float64,2}, uplo='U') -> (Cholesky, winv)
+
+cholesky_gb300! with the emulated FP64 engine (engine 2), also keeping the
+transposed inverses of the diagonal factor tiles the factorization forms for
+its panel products (winv: mt * nb * nb doubles on the device), so that
+ldiv_gb300!(C, winv, B) solves each diagonal block as one product.
+"""
+function cholesky_gb300_winv!(A::DArray{Float64,2}, uplo::Char='U')
+    n = size(A, 1)
+    nb = A.partitioning.blocksize[1]
+    mt = cld(n, nb)
+    winv = GB300Array{Float64,1}(undef, (mt * nb * nb,))
+    info = ccall((:dg_cholesky_tiled_winv, libdg), Cint,
+                 (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Cvoid}),
+                 uplo, n, nb, tile_pointers(A), pointer(winv), C_NULL)
+    dgcheck(info)
+    info > 0 && throw(PosDefException(Int(info)))
+    return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0)), winv
+end
+
+function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, winv::GB300Array{Float64,1}, B::DArray{Float64})
+    F = C.factors
+    n = size(F, 1)
+    nb = F.partitioning.blocksize[1]
+    nrhs = ndims(B) == 1 ? 1 : size(B, 2)
+    dgcheck(ccall((:dg_cholesky_solve_tiled_winv, libdg), Cint,
+                  (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Float64}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
+                  C.uplo, n, nb, tile_pointers(F), pointer(winv), nrhs, tile_pointers(B), C_NULL))
     return B
 end
 
