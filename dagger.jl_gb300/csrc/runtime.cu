@@ -221,6 +221,9 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
       if (t.op == dg::OP_OZ_POTRF)
         out.push_back({dg::footprint(t.b, t.ldb, 1, 1, 256), DG_OUT});  // slice scratch
       break;
+    case dg::OP_OZ_ZERO:
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_OUT});
+      break;
     case dg::OP_OZ_INV:
       out.push_back({dg::footprint(t.a, t.n, t.n, t.lda, E), DG_IN});
       out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), DG_OUT});
@@ -274,7 +277,7 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
   DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) ||
-                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_OZ_INV),
+                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_OZ_ZERO),
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
@@ -371,6 +374,10 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case OP_OZ_POTRF:
       return potrf_f64_oz(t.uplo, t.n, t.c, t.ldc, info, t.info_offset, (void *)t.b,
                           (size_t)t.ldb * 256, s);
+    case OP_OZ_ZERO:
+      if (t.m <= 0 || t.n <= 0) return 0;
+      DG_CUDA_TRY(cudaMemset2DAsync(t.c, (size_t)t.ldc * 8, 0, (size_t)t.m * 8, t.n, s));
+      return 0;
     case OP_OZ_INV:  // W = U^-T (upper) or L^-T (lower), one column per CTA
       return trinv_t_f64(t.uplo, t.n, t.a, t.lda, t.c, t.ldc, info, s);
     case OP_OZ_TRSM:
@@ -886,6 +893,75 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     if (winv) return winv + (size_t)k * nb * nb;
     return (double *)((char *)ring + oz_inv_offset(n, nb) + (size_t)(k % kOzRingDepth) * oz_inv_bytes(nb));
   };
+  // W_k of an n x n tile with n >= 256 by halves (h + n2 = n): the two
+  // diagonal inverses by substitution, side by side, and the off-diagonal
+  // block as two emulated products,
+  //   upper: W = [W11 0; -W22 (U12' W11)  W22],
+  //   lower: W = [W11 -W11 (L21' W22); 0  W22],
+  // the product's operands cut into three sub-slots of slot (k, k) (the slot
+  // then receives W's own slices).  A quarter of the substitution's FP64 work.
+  auto add_inv = [&](int k) {
+    const int nk = rows(k);
+    double *Wk = W(k);
+    const double *Uk = T(k, k);
+    dg_task t;
+    const int h0 = ((nk / 2) + 63) / 64 * 64, cap0 = h0 > nk - h0 ? h0 : nk - h0;
+    if (nk < 256 || 3 * oz_slot_bytes((cap0 + 7) / 8 * 8, cap0) > sb) {
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = nk; t.a = Uk; t.lda = nk;
+      t.c = Wk; t.ldc = nk; t.b = slot(k, k); t.ldb = slot_units;
+      dg_region_add(r, &t);
+      mark_urgent(r);
+      return;
+    }
+    const int h = h0, n2 = nk - h;
+    const int cap = cap0, ldh = (cap + 7) / 8 * 8;
+    const size_t subb = oz_slot_bytes(ldh, cap);
+    auto sub = [&](int i) { return (double *)((char *)slot(k, k) + (size_t)i * subb); };
+    auto add = [&]() { dg_region_add(r, &t); mark_urgent(r); };
+    // the zero block: upper W12 (rows 0..h-1, columns h..), lower W21
+    memset(&t, 0, sizeof t);
+    t.op = OP_OZ_ZERO; t.c = up ? Wk + (size_t)h * nk : Wk + h; t.ldc = nk;
+    t.m = up ? h : n2; t.n = up ? n2 : h;
+    add();
+    for (int half = 0; half < 2; half++) {  // W11, W22
+      const size_t off = half ? (size_t)h + (size_t)h * nk : 0;
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = half ? n2 : h; t.a = Uk + off; t.lda = nk;
+      t.c = Wk + off; t.ldc = nk;
+      add();
+    }
+    auto split = [&](const double *src, int K, int nv, char trans, double *dst) {
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_SPLIT; t.a = src; t.lda = nk; t.m = K; t.n = nv; t.trans = trans;
+      t.c = dst; t.ldc = ldh; t.k = cap;
+      add();
+    };
+    auto gemm = [&](int m, int nn, int K, double alpha, double *a, double *b, double *c) {
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = m; t.n = nn; t.k = K; t.alpha = alpha; t.beta = 0.0;
+      t.a = a; t.b = b; t.lda = ldh; t.ldb = cap; t.c = c; t.ldc = nk;
+      add();
+    };
+    const double *W11 = Wk, *W22 = Wk + (size_t)h + (size_t)h * nk;
+    if (up) {
+      double *W21 = Wk + h;  // T = U12' W11 there first
+      split(Uk + (size_t)h * nk, h, n2, 'N', sub(0));  // columns of U12
+      split(W11, h, h, 'N', sub(1));                    // columns of W11
+      gemm(n2, h, h, 1.0, sub(0), sub(1), W21);
+      split(W22, n2, n2, 'T', sub(2));                  // rows of W22
+      split(W21, n2, h, 'N', sub(0));                   // columns of T
+      gemm(n2, h, n2, -1.0, sub(2), sub(0), W21);
+    } else {
+      double *W12 = Wk + (size_t)h * nk;  // T = L21' W22 there first
+      split(Uk + h, n2, h, 'N', sub(0));                // columns of L21
+      split(W22, n2, n2, 'N', sub(1));                  // columns of W22
+      gemm(h, n2, n2, 1.0, sub(0), sub(1), W12);
+      split(W11, h, h, 'T', sub(2));                    // rows of W11
+      split(W12, h, n2, 'N', sub(0));                   // columns of T
+      gemm(h, n2, h, -1.0, sub(2), sub(0), W12);
+    }
+  };
   for (int k = 0; k < mt; k++) {
     dg_task t;
     memset(&t, 0, sizeof t);
@@ -894,19 +970,10 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
     dg_region_add(r, &t);
     mark_urgent(r);
     if (k + 1 == mt) {
-      if (winv) {  // kept for the solves: the last tile's inverse too
-        memset(&t, 0, sizeof t);
-        t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.a = T(k, k); t.lda = rows(k);
-        t.c = W(k); t.ldc = rows(k); t.b = slot(k, k); t.ldb = slot_units;
-        dg_region_add(r, &t);
-      }
+      if (winv) add_inv(k);  // kept for the solves: the last tile's inverse too
       break;
     }
-    memset(&t, 0, sizeof t);
-    t.op = OP_OZ_INV; t.uplo = up ? 'U' : 'L'; t.n = rows(k); t.a = T(k, k); t.lda = rows(k);
-    t.c = W(k); t.ldc = rows(k); t.b = slot(k, k); t.ldb = slot_units;
-    dg_region_add(r, &t);
-    mark_urgent(r);
+    add_inv(k);
     // rows of W (upper: A-vectors) / columns (lower: B-vectors); W's diagonal
     // 1/u_ii dominates its vectors, so it stays FP64 and scales the panel
     // tile exactly, and only the off-diagonal part is sliced

@@ -26,6 +26,7 @@ constexpr int kPrioLevels = 6;     // stream priority levels used (fewer on the 
 //                CTA computes kOzBlocksPerCta output blocks in turn
 //   OP_OZ_TRSM   DG_OP_TRSM whose recursion updates are emulated, with
 //   OP_OZ_POTRF  (likewise DG_OP_POTRF) b = slice scratch of ldb * 256 bytes
+//   OP_OZ_ZERO   c (m x n, ldc) = 0
 //   OP_OZ_INV    c (n x n, ldc) = U^-T for uplo 'U' / L^-T for 'L' of the
 //                factor tile a (lda), by substitution on the identity; b, ldb
 //                slice scratch as above
@@ -34,6 +35,7 @@ constexpr int OP_OZ_GEMM = 101;
 constexpr int OP_OZ_TRSM = 102;
 constexpr int OP_OZ_POTRF = 103;
 constexpr int OP_OZ_INV = 104;
+constexpr int OP_OZ_ZERO = 105;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);

@@ -216,13 +216,14 @@ def test_solve_engine2_inverse_and_substitution_agree(emulated, uplo, n, nb, nrh
 
 
 @pytest.mark.parametrize("uplo", "UL")
-def test_factor_keeps_diagonal_inverses(emulated, uplo):
+@pytest.mark.parametrize("n,nb", [(1000, 128), (1800, 1024), (2048, 512)])
+def test_factor_keeps_diagonal_inverses(emulated, uplo, n, nb):
     """winv holds W_k = U_kk^-T (L_kk^-T) of every diagonal tile, the ragged
-    last one included, column-major with ld = the tile's rows."""
+    last one included, column-major with ld = the tile's rows (tiles of 256
+    rows or more are inverted by halves, the off-diagonal block emulated)."""
     d = emulated
     import torch
     from oracle import tiled as o
-    n, nb = 1000, 128
     A = o.spd_uniform(n, 11)
     C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), uplo)
     G = C.factors.numpy()
