@@ -14,7 +14,8 @@ Reported:
                in HBM (CUDA events on the launching stream, max over ranks)
   e2e          the same through the public API from pinned host buffers:
                host->device copy of A and B and device->host copy of X inside
-               every timed step
+               every timed step (A's tiles are uploaded by tasks of the
+               factorization's graph, cholesky_distribute)
   solves_per_s right-hand sides solved per second (factor included)
   roofline     the dominant kernel (the FP64 tile GEMM of the trailing
                update, 2 nb^3 flops per launch) timed alone with CUDA events,
@@ -373,8 +374,9 @@ def run_ours(args):
         DBh = d.DArray(DB0.shape, part, device=dev)
 
         def e2e_step():
-            DAh.copy_from(A_h)                         # host -> device + tiling
-            C = d.cholesky_(DAh, 'U', stream=stream)
+            # cholesky(distribute(A_h, Blocks)): the tiles' uploads are tasks of
+            # the factorization's graph, overlapping its first steps
+            C = d.cholesky_distribute(A_h, part, 'U', stream=stream, out=DAh)
             DBh.copy_from(B_h)
             d.ldiv_(C, DBh, stream=stream)
             X_h.copy_(DBh.collect(), non_blocking=True)

@@ -93,6 +93,13 @@ int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_o
 int trinv_t_f64(char uplo, int n, const double *A, int lda, double *W, int ldw,
                 const int *abort_flag, cudaStream_t s);
 
+// Tile upload (upload.cu): the rows x cols block at host (row-major, row
+// stride ldh, page-locked host or device memory) into a column-major tile
+// (ld = rows).  device_readable: whether a kernel may read p.
+int upload_tile(const double *host, long long ldh, int rows, int cols, double *tile,
+                cudaStream_t s);
+bool device_readable(const void *p);
+
 // Cholesky of one tile.  info_out receives offset + local pivot index of
 // the first failure (written once); kernels skip when info_out, abort_flag
 // or abort2 is already non-zero.  The plain FP64 path passes its info word

@@ -224,6 +224,10 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
     case dg::OP_OZ_ZERO:
       out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_OUT});
       break;
+    case dg::OP_UPLOAD:  // the source is row-major: n contiguous values per row
+      out.push_back({dg::footprint(t.a, t.n, t.m, t.lda, E), DG_IN});
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_OUT});
+      break;
     case dg::OP_OZ_INV:
       out.push_back({dg::footprint(t.a, t.n, t.n, t.lda, E), DG_IN});
       out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), DG_OUT});
@@ -277,7 +281,7 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
   DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) ||
-                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_OZ_ZERO),
+                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_UPLOAD),
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
@@ -374,6 +378,8 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
     case OP_OZ_POTRF:
       return potrf_f64_oz(t.uplo, t.n, t.c, t.ldc, info, t.info_offset, (void *)t.b,
                           (size_t)t.ldb * 256, s);
+    case OP_UPLOAD:
+      return upload_tile(t.a, t.lda, t.m, t.n, t.c, s);
     case OP_OZ_ZERO:
       if (t.m <= 0 || t.n <= 0) return 0;
       DG_CUDA_TRY(cudaMemset2DAsync(t.c, (size_t)t.ldc * 8, 0, (size_t)t.m * 8, t.n, s));
@@ -436,14 +442,15 @@ struct Plan {
 static Plan plan_streams(const dg_region &r, int pool) {
   Plan pl;
   const int n = (int)r.tasks.size();
-  std::vector<int> first(kPrioLevels, -1), count(kPrioLevels, 0);
-  std::vector<char> used(kPrioLevels, 0);
+  std::vector<int> first(kPrioLevels + 1, -1), count(kPrioLevels + 1, 0);
+  std::vector<char> used(kPrioLevels + 1, 0);
   for (int t = 0; t < n; t++) used[r.level[t]] = 1;
   int total = 0;
-  for (int l = 0; l < kPrioLevels; l++) {
+  for (int l = 0; l <= kPrioLevels; l++) {
     if (!used[l]) continue;
     first[l] = total;
-    count[l] = (l == kPrioLevels - 1) ? pool : kUrgentStreams;
+    count[l] = (l == kTransferLevel) ? kTransferStreams
+               : (l == kPrioLevels - 1) ? pool : kUrgentStreams;
     total += count[l];
     pl.classes.push_back({l, count[l]});
   }
@@ -483,6 +490,14 @@ void mark_level(dg_region *r, int level) {
 }
 
 void mark_urgent(dg_region *r) { mark_level(r, 0); }
+
+void mark_transfer(dg_region *r) {
+  if (r->level.empty()) return;
+  r->level.back() = (char)kTransferLevel;
+  const int id = (int)r->level.size() - 1;
+  hash_bytes(r->hash, &id, sizeof id);
+  hash_bytes(r->hash, &kTransferLevel, sizeof kTransferLevel);
+}
 
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
@@ -1038,6 +1053,29 @@ static void build_cholesky_region_oz(dg_region *r, bool up, int n, int nb, doubl
   }
 }
 
+void build_upload_tasks(dg_region *r, char uplo, int n, int nb, double *const *tiles,
+                        const double *host, long long ldh) {
+  const int mt = (n + nb - 1) / nb;
+  const bool up = (uplo == 'U' || uplo == 'u');
+  auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
+  // on the transfer streams in the order of first use: the factor's
+  // triangle by column (row for 'L'), then the other triangle
+  for (int pass = 0; pass < 2; pass++)
+    for (int j = 0; j < mt; j++)
+      for (int i = 0; i < mt; i++) {
+        const int a = up ? i : j, b = up ? j : i;  // row and column of the upper form
+        const bool mine = a <= b;
+        if (mine != (pass == 0)) continue;
+        dg_task t;
+        memset(&t, 0, sizeof t);
+        t.op = OP_UPLOAD; t.m = rows(i); t.n = rows(j);
+        t.a = host + (size_t)i * nb * ldh + (size_t)j * nb; t.lda = (int)ldh;
+        t.c = tiles[i + (size_t)j * mt]; t.ldc = rows(i);
+        dg_region_add(r, &t);
+        mark_transfer(r);
+      }
+}
+
 void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
                            void *oz_ring, double *winv) {
   const int mt = (n + nb - 1) / nb;
@@ -1241,6 +1279,29 @@ extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *t
   dg_region r;
   void *ring = nullptr;
   DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+  dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring, winv);
+  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+}
+
+extern "C" int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *host,
+                                      long long ldh, double *const *tiles, double *winv,
+                                      void *stream) {
+  DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(nb > 0, 3);
+  if (n == 0) return 0;
+  DG_CHECK_ARG(ldh >= n && ldh <= 2147483647LL, 5);
+  // the kernels read the source directly: page-locked host or device memory
+  DG_CHECK_ARG(host != nullptr && dg::device_readable(host) &&
+                   dg::device_readable(host + (size_t)(n - 1) * ldh + (n - 1)),
+               4);
+  DG_CHECK_ARG(tiles != nullptr, 6);
+  const bool emulated = dg::get_f64_engine() == 2 && nb <= 1024;
+  if (winv && !emulated) return DG_ERR_UNSUPPORTED;
+  dg_region r;
+  void *ring = nullptr;
+  if (emulated) DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+  dg::build_upload_tasks(&r, uplo, n, nb, tiles, host, ldh);
   dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring, winv);
   return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
 }

@@ -14,6 +14,9 @@ namespace dg {
 constexpr int kDefaultStreams = 16;
 constexpr int kUrgentStreams = 4;  // streams per priority level above the lowest
 constexpr int kPrioLevels = 6;     // stream priority levels used (fewer on the device collapse)
+// Host-to-device uploads get their own class of streams (at the least
+// priority), so that no compute task queues behind a transfer it does not need.
+constexpr int kTransferLevel = kPrioLevels, kTransferStreams = 4;
 
 // Internal task kinds of the tiled Cholesky region with the emulated FP64
 // engine (not part of the public dg_op enumeration):
@@ -27,6 +30,8 @@ constexpr int kPrioLevels = 6;     // stream priority levels used (fewer on the 
 //   OP_OZ_TRSM   DG_OP_TRSM whose recursion updates are emulated, with
 //   OP_OZ_POTRF  (likewise DG_OP_POTRF) b = slice scratch of ldb * 256 bytes
 //   OP_OZ_ZERO   c (m x n, ldc) = 0
+//   OP_UPLOAD    c (m x n tile, ldc = m) = the row-major block at a (row
+//                stride lda) in page-locked host or device memory
 //   OP_OZ_INV    c (n x n, ldc) = U^-T for uplo 'U' / L^-T for 'L' of the
 //                factor tile a (lda), by substitution on the identity; b, ldb
 //                slice scratch as above
@@ -36,6 +41,7 @@ constexpr int OP_OZ_TRSM = 102;
 constexpr int OP_OZ_POTRF = 103;
 constexpr int OP_OZ_INV = 104;
 constexpr int OP_OZ_ZERO = 105;
+constexpr int OP_UPLOAD = 106;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);
@@ -60,6 +66,7 @@ std::vector<cudaStream_t> &stream_pool(int want, int level = kPrioLevels - 1);
 // kPrioLevels - 1 (the default) for work needed last.
 void mark_level(dg_region *r, int level);
 void mark_urgent(dg_region *r);  // mark_level(r, 0)
+void mark_transfer(dg_region *r);  // the last task added is an upload
 
 // Strided byte footprint of a column-major matrix argument.
 struct Footprint {
@@ -80,6 +87,12 @@ void clear_graphs();
 // there, tile k at winv + k nb^2 (ld = its row count), all mt of them.
 void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
                            void *oz_ring = nullptr, double *winv = nullptr);
+// Upload tasks for every tile from a row-major source (element (r, c) at
+// host[r*ldh + c]), ranked like the factorization's first use of the tile;
+// added before build_cholesky_region, its tasks then wait only for the
+// tiles they touch.
+void build_upload_tasks(dg_region *r, char uplo, int n, int nb, double *const *tiles,
+                        const double *host, long long ldh);
 // One block-triangular solve pass; oz_ring (oz_solve_ring_bytes_for bytes)
 // selects emulated updates, step0 numbers its steps within the ring; winv
 // (with oz_ring, the factorization's inverses) turns each diagonal block

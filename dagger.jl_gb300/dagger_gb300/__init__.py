@@ -10,13 +10,14 @@ tile calls).
 from ._lib import DaggerGB300Error, PosDefException, lib
 from .darray import Blocks, DArray, distribute
 from .datadeps import In, InOut, Out, copyto_, spawn, spawn_datadeps
-from .linalg import (Cholesky, cholesky, cholesky_, gemm_, gemm_f64_emulated_tn, gemv_,
+from .linalg import (Cholesky, cholesky, cholesky_, cholesky_distribute, gemm_, gemm_f64_emulated_tn, gemv_,
                      get_f64_engine, ishermitian, issymmetric, ldiv_, potrf_, set_f64_engine,
                      syrk_, trsm_, trsv_)
 from .mixed import MixedCholesky, cholesky_mixed
 
 __all__ = [
-    "Blocks", "DArray", "distribute", "Cholesky", "cholesky", "cholesky_", "ldiv_",
+    "Blocks", "DArray", "distribute", "Cholesky", "cholesky", "cholesky_", "cholesky_distribute",
+    "ldiv_",
     "ishermitian", "issymmetric", "potrf_", "trsm_", "syrk_", "gemm_", "trsv_", "gemv_",
     "gemm_f64_emulated_tn", "set_f64_engine", "get_f64_engine", "spawn_datadeps", "spawn", "In", "Out", "InOut", "copyto_", "PosDefException",
     "DaggerGB300Error", "lib",

@@ -96,6 +96,8 @@ SIGNATURES = {
     "dg_cholesky_solve_tiled": (c_int, [c_char, c_int, c_int, c_void_p, c_int, c_void_p,
                                         c_void_p]),
     "dg_cholesky_tiled_winv": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "dg_cholesky_tiled_host": (c_int, [c_char, c_int, c_int, c_void_p, ctypes.c_longlong, c_void_p,
+                                       c_void_p, c_void_p]),
     "dg_cholesky_solve_tiled_winv": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p, c_int,
                                              c_void_p, c_void_p]),
     "dg_set_f64_engine": (c_int, [c_int]),

@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -208,6 +209,52 @@ def cholesky_(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> C
         if check_:
             raise PosDefException(rc)
     return Cholesky(A, uplo, rc, winv)
+
+
+def cholesky_distribute(A, part: Blocks, uplo: str = 'U', check_: bool = True, stream=None,
+                        out: DArray | None = None) -> Cholesky:
+    """cholesky(distribute(A, Blocks(nb, nb))) for a square array A on the host.
+
+    The tiles move to the device inside the factorization's graph, one upload
+    task per tile, so each tile's first task waits only for its own transfer
+    and the transfers overlap the first steps' updates; Dagger moves a CPU
+    chunk to the GPU processor when the first task that needs it runs
+    (ext/CUDAExt.jl:329-348).  A: numpy array or torch tensor (host or device),
+    read C-contiguous in FP64; a Cholesky's input is symmetric, so the row-major
+    layout reads the same as Julia's column-major one.  A host tensor that is
+    not page-locked is first copied into page-locked memory.  out: a DArray of
+    A's shape and Blocks(nb, nb) to receive the tiles (allocated if None).
+    Returns the Cholesky of the tiles, as cholesky_ does."""
+    if uplo not in ('U', 'L'):
+        raise ValueError("uplo must be 'U' or 'L'")
+    t = torch.from_numpy(np.ascontiguousarray(A, dtype=np.float64)) if isinstance(A, np.ndarray) else A
+    if t.ndim != 2 or t.shape[0] != t.shape[1]:
+        raise ValueError(f"matrix is not square: dimensions are {tuple(t.shape)}")
+    t = t.to(torch.float64).contiguous()
+    if not t.is_cuda and not t.is_pinned():
+        t = t.pin_memory()
+    n = t.shape[0]
+    if len(part.blocksize) != 2 or part.blocksize[0] != part.blocksize[1]:
+        raise ValueError("the Cholesky path needs square blocks Blocks(nb, nb)")
+    nb = part.blocksize[0]
+    D = out if out is not None else DArray((n, n), part,
+                                           device=t.device if t.is_cuda else None)
+    if D.shape != (n, n) or D.partitioning != part:
+        raise ValueError("out must have A's shape and the same Blocks")
+    winv = None
+    if n > 0 and nb <= 1024 and lib().dg_get_f64_engine() == F64_ENGINES["emulated"]:
+        mt = (n + nb - 1) // nb
+        winv = torch.empty(mt * nb * nb, dtype=torch.float64, device=D.storage.device)
+    rc = lib().dg_cholesky_tiled_host(ch(uplo), n, nb, t.data_ptr(), t.stride(0), D.tile_ptrs(),
+                                      winv.data_ptr() if winv is not None else None,
+                                      _stream(stream))
+    if rc < 0:
+        check(rc)
+    if rc > 0:
+        winv = None
+        if check_:
+            raise PosDefException(rc)
+    return Cholesky(D, uplo, rc, winv)
 
 
 def cholesky(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Cholesky:

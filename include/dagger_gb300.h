@@ -193,6 +193,18 @@ int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *tiles, int 
  * bounds as dg_cholesky_tiled / dg_cholesky_solve_tiled. */
 int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *tiles, double *winv,
                            void *stream);
+/* cholesky(distribute(A, Blocks(nb, nb))) with A on the host: the factor's
+ * graph also moves the tiles to the device, one upload task per tile
+ * (element (r, c) of A at host[r*ldh + c], row-major, so a C-contiguous or
+ * symmetric array; page-locked host memory or device memory, argument 4
+ * otherwise), so each tile's first task waits only for its own transfer and
+ * the transfers overlap the first steps' updates (Dagger moves CPU chunks to
+ * the GPU processor when the first task needs them, ext/CUDAExt.jl:329-348).
+ * tiles receive the whole matrix as dg_cholesky_tiled expects it, then the
+ * factor; winv (engine 2 only, else DG_ERR_UNSUPPORTED; may be NULL) as in
+ * dg_cholesky_tiled_winv.  Returns info. */
+int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *host, long long ldh,
+                           double *const *tiles, double *winv, void *stream);
 int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *const *tiles,
                                  const double *winv, int nrhs, double *const *btiles,
                                  void *stream);
