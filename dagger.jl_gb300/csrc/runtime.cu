@@ -734,6 +734,23 @@ extern "C" int dg_device_free(void *p) {
   return 0;
 }
 
+extern "C" int dg_host_alloc(size_t bytes, void **out) {
+  DG_CHECK_ARG(out != nullptr, 2);
+  *out = nullptr;
+  if (bytes == 0) return 0;
+  if (cudaHostAlloc(out, bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    dg_set_last_error(__FILE__, __LINE__, "cudaHostAlloc failed");
+    return DG_ERR_NOMEM;
+  }
+  return 0;
+}
+
+extern "C" int dg_host_free(void *p) {
+  if (p) DG_CUDA_TRY(cudaFreeHost(p));
+  return 0;
+}
+
 extern "C" int dg_copy(void *dst, const void *src, size_t bytes, int kind, void *stream) {
   DG_CHECK_ARG(kind >= 0 && kind <= 2, 4);
   static const cudaMemcpyKind kinds[3] = {cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost,

@@ -71,6 +71,8 @@ SIGNATURES = {
     "dg_set_device": (c_int, [c_int]),
     "dg_device_alloc": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
     "dg_device_free": (c_int, [c_void_p]),
+    "dg_host_alloc": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
+    "dg_host_free": (c_int, [c_void_p]),
     "dg_copy": (c_int, [c_void_p, c_void_p, ctypes.c_size_t, c_int, c_void_p]),
     "dg_stream_create": (c_int, [ctypes.POINTER(c_void_p)]),
     "dg_stream_destroy": (c_int, [c_void_p]),

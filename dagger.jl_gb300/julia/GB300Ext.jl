@@ -241,6 +241,34 @@ function cholesky_gb300_winv!(A::DArray{Float64,2}, uplo::Char='U')
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0)), winv
 end
 
+"""
+    cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo='U') -> Cholesky
+
+cholesky(distribute(H, Blocks(nb, nb))) for a host matrix H (symmetric, so
+its column-major storage reads the same as the row-major source the library
+expects), with the chunks' moves to the device as tasks of the factor's graph.
+dg_cholesky_tiled_host reads page-locked memory only, so H is copied into a
+buffer from dg_host_alloc for the call.  A receives the tiles and then the
+factor.
+"""
+function cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo::Char='U')
+    n = size(A, 1)
+    nb = A.partitioning.blocksize[1]
+    buf = Ref{Ptr{Cvoid}}(C_NULL)
+    dgcheck(ccall((:dg_host_alloc, libdg), Cint, (Csize_t, Ptr{Ptr{Cvoid}}), sizeof(H), buf))
+    info = try
+        unsafe_copyto!(Ptr{Float64}(buf[]), pointer(H), length(H))
+        ccall((:dg_cholesky_tiled_host, libdg), Cint,
+              (Cchar, Cint, Cint, Ptr{Float64}, Clonglong, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Cvoid}),
+              uplo, n, nb, Ptr{Float64}(buf[]), stride(H, 2), tile_pointers(A), C_NULL, C_NULL)
+    finally
+        ccall((:dg_host_free, libdg), Cint, (Ptr{Cvoid},), buf[])
+    end
+    dgcheck(info)
+    info > 0 && throw(PosDefException(Int(info)))
+    return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0))
+end
+
 function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, winv::GB300Array{Float64,1}, B::DArray{Float64})
     F = C.factors
     n = size(F, 1)

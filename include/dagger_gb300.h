@@ -63,6 +63,10 @@ int dg_finalize(void);
 int dg_set_device(int device);
 int dg_device_alloc(size_t bytes, void **out);
 int dg_device_free(void *p);
+/* Page-locked host memory the device can read directly (the source of
+ * dg_cholesky_tiled_host). */
+int dg_host_alloc(size_t bytes, void **out);
+int dg_host_free(void *p);
 int dg_copy(void *dst, const void *src, size_t bytes, int kind, void *stream);
 int dg_stream_create(void **out);
 int dg_stream_destroy(void *stream);

@@ -91,3 +91,26 @@ def test_upload_rejects_pageable_memory():
     assert rc == -4
     rc = d.lib().dg_cholesky_tiled_host(b'U', n, nb, A.ctypes.data, n - 1, D.tile_ptrs(), None, s)
     assert rc == -5
+
+
+def test_upload_from_library_host_buffer():
+    """A source in dg_host_alloc memory (what a binding without torch uses)."""
+    import ctypes
+    import dagger_gb300 as d
+    from oracle import tiled as o
+    n, nb = 640, 128
+    L = d.lib()
+    A = np.ascontiguousarray(o.spd_uniform(n, 21))
+    p = ctypes.c_void_p()
+    assert L.dg_host_alloc(A.nbytes, ctypes.byref(p)) == 0
+    try:
+        H = np.ctypeslib.as_array((ctypes.c_double * (n * n)).from_address(p.value)).reshape(n, n)
+        H[:] = A
+        D = d.DArray((n, n), d.Blocks(nb, nb))
+        import torch
+        s = torch.cuda.current_stream().cuda_stream
+        assert L.dg_cholesky_tiled_host(b'L', n, nb, p.value, n, D.tile_ptrs(), None, s) == 0
+        C = d.cholesky(d.DArray.from_array(A, d.Blocks(nb, nb)), 'L')
+        assert torch.equal(D.collect(), C.factors.collect())
+    finally:
+        assert L.dg_host_free(p) == 0
