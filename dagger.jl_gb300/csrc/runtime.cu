@@ -19,6 +19,7 @@
 // task list (same tasks, same pointers -> same graph), and replayed.
 #include <atomic>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -675,6 +676,99 @@ static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t o
   return sync ? read_info(entry.info, origin) : 0;
 }
 
+// Launches the cached graph of `key` on origin (a legacy stream bridged to
+// the private capture stream as region_run does); false when it is not cached
+// (never built, evicted, or cleared when the workspace grew).
+static bool launch_cached(uint64_t key, cudaStream_t origin, bool sync, int *rc) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  GraphEntry entry;
+  {
+    std::lock_guard<std::mutex> g(g_graph_mu);
+    auto it = g_graphs.find({dev, key});
+    if (it == g_graphs.end()) return false;
+    it->second.last_used = ++g_graph_clock;
+    entry = it->second;
+  }
+  const bool legacy = origin == nullptr || origin == cudaStreamLegacy || origin == cudaStreamPerThread;
+  cudaStream_t s = origin;
+  cudaEvent_t in = nullptr, out = nullptr;
+  if (legacy) {
+    s = private_stream();
+    if (!s || cudaEventCreateWithFlags(&in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&out, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      if (in) cudaEventDestroy(in);
+      return false;
+    }
+    cudaEventRecord(in, origin);
+    cudaStreamWaitEvent(s, in, 0);
+  }
+  *rc = 0;
+  if (cudaGraphLaunch(entry.exec, s) != cudaSuccess) {
+    cudaGetLastError();
+    dg_set_last_error(__FILE__, __LINE__, "cudaGraphLaunch failed");
+    *rc = DG_ERR_CUDA;
+  } else {
+    count_launches(entry.nodes);
+  }
+  if (legacy) {
+    cudaEventRecord(out, s);
+    cudaStreamWaitEvent(origin, out, 0);
+    cudaEventDestroy(in);
+    cudaEventDestroy(out);
+  }
+  if (*rc == 0 && sync) *rc = read_info(entry.info, s);
+  return true;
+}
+
+// Whole-call cache: the hashed arguments of a region-building entry point ->
+// the key of its graph, so that a repeated call (same tiles, sizes, engine,
+// workspace) launches the graph without rebuilding the region and its stream
+// plan (about 8 ms of host time for the 7 k tasks of N = 32768, during which
+// the GPU would idle).
+static std::mutex g_call_mu;
+static std::unordered_map<uint64_t, uint64_t> g_calls;
+
+int region_run_cached(uint64_t call, const std::function<void(dg_region *)> &build,
+                      cudaStream_t origin, bool sync) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int engine = get_f64_engine();
+  hash_bytes(call, &dev, sizeof dev);
+  hash_bytes(call, &engine, sizeof engine);
+  uint64_t key = 0;
+  bool known = false;
+  {
+    std::lock_guard<std::mutex> g(g_call_mu);
+    auto it = g_calls.find(call);
+    if (it != g_calls.end()) {
+      key = it->second;
+      known = true;
+    }
+  }
+  int rc = 0;
+  if (known && launch_cached(key, origin, sync, &rc)) return rc;
+  dg_region r;
+  build(&r);
+  rc = region_run(&r, 1, 0, origin, kDefaultStreams, sync);
+  if (rc >= 0) {
+    std::lock_guard<std::mutex> g(g_call_mu);
+    if (g_calls.size() > 4096) g_calls.clear();
+    g_calls[call] = r.hash ^ ((uint64_t)kDefaultStreams << 40);
+  }
+  return rc;
+}
+
+// The hash of a call's arguments (region_run_cached).
+uint64_t call_hash(int fn, const void *args, size_t bytes, const void *const *ptrs, size_t nptrs) {
+  uint64_t h = 1469598103934665603ull;
+  hash_bytes(h, &fn, sizeof fn);
+  hash_bytes(h, args, bytes);
+  if (nptrs) hash_bytes(h, ptrs, nptrs * sizeof(void *));
+  return h;
+}
+
 void clear_graphs() {
   std::lock_guard<std::mutex> g(g_graph_mu);
   int dev = 0;
@@ -1270,18 +1364,43 @@ void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double
 
 }  // namespace dg
 
+namespace {
+// The arguments that decide a whole-call region, zero-padded for hashing.
+struct CallArgs {
+  int64_t n, nb, nrhs, ldh;
+  const void *ring, *winv, *host;
+  char uplo;
+};
+uint64_t call_key(int fn, char uplo, int n, int nb, int nrhs, long long ldh, const void *ring,
+                  const void *winv, const void *host, double *const *tiles,
+                  double *const *btiles) {
+  CallArgs a;
+  memset(&a, 0, sizeof a);
+  a.n = n; a.nb = nb; a.nrhs = nrhs; a.ldh = ldh;
+  a.ring = ring; a.winv = winv; a.host = host; a.uplo = uplo;
+  const size_t mt = (size_t)(n + nb - 1) / nb;
+  uint64_t h = dg::call_hash(fn, &a, sizeof a, (const void *const *)tiles, mt * mt);
+  if (btiles) {
+    const size_t bnt = (size_t)(nrhs + nb - 1) / nb;
+    h = dg::call_hash(fn, &h, sizeof h, (const void *const *)btiles, mt * bnt);
+  }
+  return h;
+}
+}  // namespace
+
 extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles, void *stream) {
   DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
   DG_CHECK_ARG(n >= 0, 2);
   DG_CHECK_ARG(nb > 0, 3);
   DG_CHECK_ARG(tiles != nullptr || n == 0, 4);
   if (n == 0) return 0;
-  dg_region r;
   void *ring = nullptr;
   if (dg::get_f64_engine() == 2 && nb <= 1024)
     DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
-  dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring);
-  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+  return dg::region_run_cached(
+      call_key(1, uplo, n, nb, 0, 0, ring, nullptr, nullptr, tiles, nullptr),
+      [&](dg_region *r) { dg::build_cholesky_region(r, uplo, n, nb, tiles, ring); },
+      (cudaStream_t)stream, true);
 }
 
 extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *tiles,
@@ -1293,11 +1412,12 @@ extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *t
   DG_CHECK_ARG(winv != nullptr || n == 0, 5);
   if (dg::get_f64_engine() != 2 || nb > 1024) return DG_ERR_UNSUPPORTED;
   if (n == 0) return 0;
-  dg_region r;
   void *ring = nullptr;
   DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
-  dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring, winv);
-  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+  return dg::region_run_cached(
+      call_key(2, uplo, n, nb, 0, 0, ring, winv, nullptr, tiles, nullptr),
+      [&](dg_region *r) { dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, winv); },
+      (cudaStream_t)stream, true);
 }
 
 extern "C" int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *host,
@@ -1315,12 +1435,15 @@ extern "C" int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *ho
   DG_CHECK_ARG(tiles != nullptr, 6);
   const bool emulated = dg::get_f64_engine() == 2 && nb <= 1024;
   if (winv && !emulated) return DG_ERR_UNSUPPORTED;
-  dg_region r;
   void *ring = nullptr;
   if (emulated) DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
-  dg::build_upload_tasks(&r, uplo, n, nb, tiles, host, ldh);
-  dg::build_cholesky_region(&r, uplo, n, nb, tiles, ring, winv);
-  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+  return dg::region_run_cached(
+      call_key(3, uplo, n, nb, 0, ldh, ring, winv, host, tiles, nullptr),
+      [&](dg_region *r) {
+        dg::build_upload_tasks(r, uplo, n, nb, tiles, host, ldh);
+        dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, winv);
+      },
+      (cudaStream_t)stream, true);
 }
 
 extern "C" int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *const *tiles,
@@ -1335,16 +1458,19 @@ extern "C" int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *co
   DG_CHECK_ARG(tiles != nullptr, 4);
   DG_CHECK_ARG(winv != nullptr, 5);
   DG_CHECK_ARG(btiles != nullptr, 7);
-  dg_region r;
   const bool up = (uplo == 'U' || uplo == 'u');
   void *ring = nullptr;
   DG_TRY(dg::device_state().oz_workspace(dg::oz_solve_ring_bytes_for(n, nb, nrhs, true), &ring));
   const int mt = (n + nb - 1) / nb;
-  dg::build_solve_pass(&r, up ? 'U' : 'L', up ? 'T' : 'N', n, nb, tiles, nrhs, btiles, ring, 0,
-                       winv);
-  dg::build_solve_pass(&r, up ? 'U' : 'L', up ? 'N' : 'T', n, nb, tiles, nrhs, btiles, ring, mt,
-                       winv);
-  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+  return dg::region_run_cached(
+      call_key(4, uplo, n, nb, nrhs, 0, ring, winv, nullptr, tiles, btiles),
+      [&](dg_region *r) {
+        dg::build_solve_pass(r, up ? 'U' : 'L', up ? 'T' : 'N', n, nb, tiles, nrhs, btiles, ring,
+                             0, winv);
+        dg::build_solve_pass(r, up ? 'U' : 'L', up ? 'N' : 'T', n, nb, tiles, nrhs, btiles, ring,
+                             mt, winv);
+      },
+      (cudaStream_t)stream, true);
 }
 
 extern "C" int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *tiles, int nrhs,
@@ -1356,18 +1482,16 @@ extern "C" int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *
   if (n == 0 || nrhs == 0) return 0;
   DG_CHECK_ARG(tiles != nullptr, 4);
   DG_CHECK_ARG(btiles != nullptr, 6);
-  dg_region r;
   const bool up = (uplo == 'U' || uplo == 'u');
   void *ring = nullptr;
   if (dg::get_f64_engine() == 2 && nb <= 1024)
     DG_TRY(dg::device_state().oz_workspace(dg::oz_solve_ring_bytes_for(n, nb, nrhs), &ring));
   const int mt = (n + nb - 1) / nb;
-  if (up) {
-    dg::build_solve_pass(&r, 'U', 'T', n, nb, tiles, nrhs, btiles, ring, 0);
-    dg::build_solve_pass(&r, 'U', 'N', n, nb, tiles, nrhs, btiles, ring, mt);
-  } else {
-    dg::build_solve_pass(&r, 'L', 'N', n, nb, tiles, nrhs, btiles, ring, 0);
-    dg::build_solve_pass(&r, 'L', 'T', n, nb, tiles, nrhs, btiles, ring, mt);
-  }
-  return dg::region_run(&r, 1, 0, (cudaStream_t)stream, dg::kDefaultStreams, true);
+  return dg::region_run_cached(
+      call_key(5, uplo, n, nb, nrhs, 0, ring, nullptr, nullptr, tiles, btiles),
+      [&](dg_region *r) {
+        dg::build_solve_pass(r, up ? 'U' : 'L', up ? 'T' : 'N', n, nb, tiles, nrhs, btiles, ring, 0);
+        dg::build_solve_pass(r, up ? 'U' : 'L', up ? 'N' : 'T', n, nb, tiles, nrhs, btiles, ring, mt);
+      },
+      (cudaStream_t)stream, true);
 }

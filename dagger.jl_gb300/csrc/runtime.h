@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <functional>
 #include <vector>
 
 #include "../../include/dagger_gb300.h"
@@ -80,6 +81,13 @@ int run_task(const dg_task &t, int *info, cudaStream_t s);
 int region_run(dg_region *r, int use_graph, int serial, cudaStream_t origin, int stream_pool_size,
                bool sync);
 void clear_graphs();
+// A whole-call region: `call` hashes the entry point's arguments
+// (call_hash); when a graph for the same call is cached it is launched
+// without building the region, else build(r) fills a region that is run and
+// remembered.  The f64 engine and the device join the key.
+int region_run_cached(uint64_t call, const std::function<void(dg_region *)> &build,
+                      cudaStream_t origin, bool sync);
+uint64_t call_hash(int fn, const void *args, size_t bytes, const void *const *ptrs, size_t nptrs);
 
 // oz_ring != nullptr selects the emulated-FP64 trailing updates, with
 // oz_ring_bytes_for(n, nb) bytes of slice slots (nb <= 1024).  winv (with
