@@ -305,9 +305,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
           any = true;
           // levels 6..8: t from max(1, 6 - s) to 8 - s; the block's first MMA
           // (s = 1, levels 6..8) sets them
-#pragma unroll 1
+#pragma unroll
           for (int kk = 0; kk < OZ_BK / 16; kk++)
-#pragma unroll 1
+#pragma unroll
             for (int s_ = 1; s_ <= OZ_S; s_++)
               mma_run(kk, s_, 6 - s_ > 1 ? 6 - s_ : 1, 8 - s_,
                       (it == 0 && kk == 0 && s_ == 1) ? 0u : 1u);
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           }
           const uint32_t first = (wpos == 0) ? 0u : 1u;
-#pragma unroll 1
+#pragma unroll
           for (int kk = 0; kk < OZ_BK / 16; kk++) {
             const uint32_t a0 = (kk == 0) ? first : 1u;
             mma_run(kk, 1, 1, 4, a0);   // levels 2..5
