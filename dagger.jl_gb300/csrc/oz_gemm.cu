@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
                      db + (((t - 1) * OZ_B_SLICE + kk * 32) >> 4),
                      idesc64 + ((uint32_t)(8 * (u - t)) << 17), acc);
           };
-          // a new block resets levels 7..9 too: the previous block's sums
+          // a new block resets levels 6..8 too: the previous block's sums
           // (all levels) must have been read
           if (it == 0 && gw > 0) {
             if (!mbar_wait(drained, (gw - 1) & 1)) {
@@ -373,17 +373,23 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) oz_gemm_kernel(const __grid_con
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (ok) {
 #pragma unroll
-          for (int lvl = 2; lvl <= 5; lvl++) {
+          // level L holds an integer below 2^24 in units of 2^(-8L): to 32
+          // bits, then shifted to units of 2^-40 (two levels per TMEM wait)
+#pragma unroll
+          for (int lvl = 2; lvl <= 5; lvl += 2) {
             const float up = __int_as_float((127 + 8 * lvl) << 23);  // 2^(8 lvl)
             const int sh = 8 * (5 - lvl);                            // x 2^(8 (5 - lvl))
 #pragma unroll
             for (int ch = 0; ch < OZ_RCOLS; ch += 16) {
-              float x[16];
-              tmem_ld16(tmem + 64 * (lvl - 2) + cb + ch + lane_base, x);
+              float x[16], y[16];
+              tmem_ld16x2(tmem + 64 * (lvl - 2) + cb + ch + lane_base,
+                          tmem + 64 * (lvl - 1) + cb + ch + lane_base, x, y);
 #pragma unroll
               for (int c = 0; c < 16; c++)
                 acc[ch + c] +=
-                    (long long)((unsigned long long)(long long)__float2int_rn(x[c] * up) << sh);
+                    (long long)((unsigned long long)(long long)__float2int_rn(x[c] * up) << sh) +
+                    (long long)((unsigned long long)(long long)__float2int_rn(y[c] * (up * 256.0f))
+                                << (sh - 8));
             }
           }
           if (w == nwin - 1) {
