@@ -20,8 +20,8 @@
 // Products (oz_gemm_kernel): C = alpha * 2^(ea_i + eb_j) * sum_{s+t<=8} A_s B_t'
 // + beta * C, K <= 131072: 28 slice products.  A product A_s B_t' sums terms
 // d_s d_t 2^(-8(s+t)).  Level L = s + t collects the L - 1 products of that
-// weight.  Over a window of 128 values of K the sum of level L <= 5 stays
-// within 2^24 units of 2^(-8L) (level 5: (2*256*128 + 2*128*128) * 128 < 2^24),
+// weight.  Over a window of 160 values of K the sum of level L <= 5 stays
+// within 2^24 units of 2^(-8L) (level 5: (2*256*128 + 2*128*128) * 160 < 2^24),
 // so its FP32 accumulation in TMEM is exact.  Levels 2..5 are read exactly
 // after each window and summed as 64-bit integers in units of 2^-40
 // (|sum| < 2^50 K / 1024).  Levels 6..8 accumulate in FP32 over the whole K
@@ -70,7 +70,7 @@ constexpr int kOzNonFinite = 1 << 30;                     // exponent of a non-f
 #define OZ_STAGE_K 32
 #endif
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = OZ_STAGE_K;  // K per stage (16 or 32)
-constexpr int OZ_WIN = 128 / OZ_BK;                       // stages per exact window (K 128)
+constexpr int OZ_WIN = 160 / OZ_BK;                       // stages per exact window (K 160)
 constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;             // 8 KiB at K 32
 constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;             // 4 KiB at K 32
 constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 84 KiB at K 32
