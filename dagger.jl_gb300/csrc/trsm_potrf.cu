@@ -227,9 +227,12 @@ int trsm_cols(const TriView<T> &tv, int len, T *X, long long rs, long long cs, i
 // Right-looking with the column scaling deferred: step j subtracts
 // M(i, j) M(k, j) / d_j (d_j the pivot) from the trailing triangle, and each
 // column is scaled by 1 / sqrt(d_j) once at the end (square roots and
-// divisions for all columns at once, off the sequential path), so one
-// barrier per column suffices.  Warps 0-6 update the trailing triangle of
-// step j while warp 7 updates element (j+1, j+1) first and forms 1 / d_{j+1}
+// divisions for all columns at once, off the sequential path).  Each step
+// stages M(i, j) / d_j once, then warps 0-6 update the trailing triangle,
+// its elements handed out densely from a table (on GB300 a warp's FP64
+// instruction costs the same with idle lanes, so a rectangular thread grid
+// over the shrinking triangle wasted most of them), while warp 7 updates
+// element (j+1, j+1) first and forms 1 / d_{j+1}
 // by Newton's iteration for the reciprocal (x <- x + x (1 - d x), quadratic
 // convergence from the hardware's approximate reciprocal, two steps to FP64
 // precision), so the sequential path per column is a few FMAs.  A pivot that
@@ -259,12 +262,21 @@ __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *
   if (aborted(info, a1) || aborted(a2, nullptr)) return;
   __shared__ T Ms[TB][TB + 1];
   __shared__ T dinv[TB];  // 1 / d_j
+  __shared__ T S[TB];     // M(i, j) / d_j of the current column
+  // the lower triangle's elements (i << 8 | k), columns in decreasing order:
+  // the elements of columns > j, step j's update, are its first
+  // (len-1-j)(len-j)/2 entries, handed out densely to the threads
+  __shared__ uint32_t tri[TB * (TB + 1) / 2];
   __shared__ int fail_at;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < len * len; e += nt) {
     int i, j;
     if (!upper) { i = e % len; j = e / len; } else { j = e % len; i = e / len; }
     if (j <= i) Ms[i][j] = upper ? A[(size_t)j + (size_t)i * lda] : A[(size_t)i + (size_t)j * lda];
+  }
+  for (int k = tid; k < len; k += nt) {
+    const int off = (len - 1 - k) * (len - k) / 2;
+    for (int i = k; i < len; i++) tri[off + i - k] = ((uint32_t)i << 8) | (uint32_t)k;
   }
   __syncthreads();
   // the approximate reciprocal flushes subnormals: extreme pivots divide
@@ -281,23 +293,26 @@ __global__ void __launch_bounds__(256) potrf_base_kernel(int upper, int len, T *
   }
   __syncthreads();
   int done = 0;  // columns factored
-  constexpr int kRowLanes = 14;  // warps 0-6: a 14 x 16 grid over the trailing triangle
   for (int j = 0; j < len; j++) {
     if (fail_at >= 0 && fail_at <= j) break;  // the same value for every thread
     done = j + 1;
     const T r2 = dinv[j];
+    for (int i = j + 1 + tid; i < len; i += nt) S[i] = Ms[i][j] * r2;
+    __syncthreads();
     if (tid == 7 * 32) {
       if (j + 1 < len) {
-        const T a = Ms[j + 1][j];
-        const T d = fma(-a * r2, a, Ms[j + 1][j + 1]);
+        const T d = fma(-S[j + 1], Ms[j + 1][j], Ms[j + 1][j + 1]);
         Ms[j + 1][j + 1] = d;
         pivot(j + 1, d);
       }
-    } else if (tid < 7 * 32) {
-      for (int i = j + 1 + (tid >> 4); i < len; i += kRowLanes) {
-        const T lij = Ms[i][j] * r2;
-        for (int k = j + 1 + (tid & 15); k <= i; k += 16)
-          if (k != j + 1 || i != j + 1) Ms[i][k] = fma(-lij, Ms[k][j], Ms[i][k]);
+    } else if (tid < 7 * 32) {  // warps 0-6: every other element of columns > j
+      const int P = (len - 1 - j) * (len - j) / 2;
+      const int skip = (len - 2 - j) * (len - 1 - j) / 2;  // (j+1, j+1), warp 7's
+      for (int e = tid; e < P; e += 7 * 32) {
+        if (e == skip) continue;
+        const uint32_t ik = tri[e];
+        const int i = (int)(ik >> 8), k = (int)(ik & 255u);
+        Ms[i][k] = fma(-S[i], Ms[k][j], Ms[i][k]);
       }
     }
     __syncthreads();
