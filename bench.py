@@ -509,6 +509,9 @@ def _measured_bf16_peak():
 # multiplies the 28 slice pairs (s, t) with s + t <= 8.
 EMULATED_SLICES = 7
 EMULATED_PRODUCTS = 28
+# DRAM bytes (read + write) of one 1024^3 emulated tile launch, ncu capture:
+# the 29 MiB of slices mostly hit L2 and C's write-back stays in L2.
+OZ_TILE_DRAM_BYTES = 23160576 + 0
 
 
 def roofline_emulated(L, nb, dev, stream, s):
@@ -553,7 +556,10 @@ def roofline_emulated(L, nb, dev, stream, s):
             "per_launch": f"{EMULATED_PRODUCTS} x 2*{nb}^3 BF16 flops (= 2*{nb}^3 FP64-equivalent), "
                           f"{1e6 * tg:.0f} us, {nb // 128} x {nb // 64} CTAs",
             "fp64_equivalent_tflops": 2.0 * nb ** 3 / tg / 1e12,
-            "traffic": None}
+            # dram__bytes_read.sum + dram__bytes_write.sum of one launch at
+            # nb = 1024 from an ncu capture of the same launch (profiles/)
+            "traffic": OZ_TILE_DRAM_BYTES if nb == 1024 else None,
+            "traffic_unit": "bytes per launch"}
 
 
 def choose_precision(cond):
