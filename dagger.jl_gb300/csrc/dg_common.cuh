@@ -100,6 +100,12 @@ int upload_tile(const double *host, long long ldh, int rows, int cols, double *t
                 cudaStream_t s);
 bool device_readable(const void *p);
 
+// Tile copies of copytri! (tiles.cu): dst (cols x rows, ldd) = src (rows x
+// cols, lds)'; the upper triangle of the n x n tile A mirrored into the lower.
+int tile_transpose(const double *src, long long lds, int rows, int cols, double *dst,
+                   long long ldd, cudaStream_t s);
+int tile_mirror_upper(double *A, long long lda, int n, cudaStream_t s);
+
 // Cholesky of one tile.  info_out receives offset + local pivot index of
 // the first failure (written once); kernels skip when info_out, abort_flag
 // or abort2 is already non-zero.  The plain FP64 path passes its info word

@@ -225,6 +225,13 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
     case dg::OP_OZ_ZERO:
       out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_OUT});
       break;
+    case dg::OP_TILE_T:
+      out.push_back({dg::footprint(t.a, t.m, t.n, t.lda, E), DG_IN});
+      out.push_back({dg::footprint(t.c, t.n, t.m, t.ldc, E), DG_OUT});
+      break;
+    case dg::OP_TILE_MIRROR:
+      out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), DG_INOUT});
+      break;
     case dg::OP_UPLOAD:  // the source is row-major: n contiguous values per row
       out.push_back({dg::footprint(t.a, t.n, t.m, t.lda, E), DG_IN});
       out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_OUT});
@@ -282,7 +289,7 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
   DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) ||
-                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_UPLOAD),
+                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_TILE_MIRROR),
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
@@ -381,6 +388,10 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
                           (size_t)t.ldb * 256, s);
     case OP_UPLOAD:
       return upload_tile(t.a, t.lda, t.m, t.n, t.c, s);
+    case OP_TILE_T:
+      return tile_transpose(t.a, t.lda, t.m, t.n, t.c, t.ldc, s);
+    case OP_TILE_MIRROR:
+      return tile_mirror_upper(t.c, t.ldc, t.n, s);
     case OP_OZ_ZERO:
       if (t.m <= 0 || t.n <= 0) return 0;
       DG_CUDA_TRY(cudaMemset2DAsync(t.c, (size_t)t.ldc * 8, 0, (size_t)t.m * 8, t.n, s));
@@ -1187,6 +1198,167 @@ void build_upload_tasks(dg_region *r, char uplo, int n, int nb, double *const *t
       }
 }
 
+// ---------------------------------------------------------------------------
+// gemm_dagger! / syrk_dagger! + copytri! (src/array/mul.jl:133-425)
+// ---------------------------------------------------------------------------
+size_t mul_ring_bytes_for(int m, int n, int nb) {
+  const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb;
+  return (size_t)kOzRingDepth * (mt + nt) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+}
+
+namespace {
+struct MulGrid {
+  int nb;
+  int len(int i, int total) const { return (i + 1) * nb <= total ? nb : total - i * nb; }
+};
+}  // namespace
+
+// The rows of op(X) block (i, p) of a tile grid holding X (op = 'N': X is
+// rows x K with tile (i, p); 'T': X is K x rows with tile (p, i)) cut into
+// slot `dst` as vectors of length K.
+static void add_row_split(dg_region *r, const MulGrid &g, bool tr, double *const *X, int rows,
+                          int K, int i, int p, double *dst, int ldk) {
+  const int mt = (rows + g.nb - 1) / g.nb, kt = (K + g.nb - 1) / g.nb;
+  dg_task t;
+  memset(&t, 0, sizeof t);
+  t.op = OP_OZ_SPLIT; t.m = g.len(p, K); t.n = g.len(i, rows);
+  if (!tr) {  // rows of X(i, p)
+    t.a = X[i + (size_t)p * mt]; t.lda = g.len(i, rows); t.trans = 'T';
+  } else {    // columns of X(p, i)
+    t.a = X[p + (size_t)i * kt]; t.lda = g.len(p, K); t.trans = 'N';
+  }
+  t.c = dst; t.ldc = ldk; t.k = g.nb;
+  dg_region_add(r, &t);
+}
+
+// The transposes of copytri!: tile (j, i) = tile (i, j)' for i < j, the
+// diagonal tiles' upper triangles mirrored.
+static void add_copytri(dg_region *r, const MulGrid &g, int n, double *const *C) {
+  const int nt = (n + g.nb - 1) / g.nb;
+  for (int i = 0; i < nt; i++)
+    for (int j = i; j < nt; j++) {
+      dg_task t;
+      memset(&t, 0, sizeof t);
+      if (i == j) {
+        t.op = OP_TILE_MIRROR; t.n = g.len(i, n); t.c = C[i + (size_t)i * nt]; t.ldc = g.len(i, n);
+      } else {
+        t.op = OP_TILE_T; t.m = g.len(i, n); t.n = g.len(j, n);
+        t.a = C[i + (size_t)j * nt]; t.lda = g.len(i, n);
+        t.c = C[j + (size_t)i * nt]; t.ldc = g.len(j, n);
+      }
+      dg_region_add(r, &t);
+    }
+}
+
+void build_gemm_region(dg_region *r, char ta, char tb, int m, int n, int k, int nb, double alpha,
+                       double *const *A, double *const *B, double beta, double *const *C,
+                       void *oz_ring) {
+  const MulGrid g{nb};
+  const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb, kt = (k + nb - 1) / nb;
+  const bool tA = !(ta == 'N' || ta == 'n'), tB = !(tb == 'N' || tb == 'n');
+  auto Ct = [&](int i, int j) { return C[i + (size_t)j * mt]; };
+  if (!oz_ring) {
+    // mul.jl:154-212: for each C tile, the k loop of gemm! with beta on the first
+    for (int i = 0; i < mt; i++)
+      for (int j = 0; j < nt; j++)
+        for (int p = 0; p < kt; p++) {
+          dg_task t;
+          memset(&t, 0, sizeof t);
+          t.op = DG_OP_GEMM; t.transa = tA ? 'T' : 'N'; t.transb = tB ? 'T' : 'N';
+          t.m = g.len(i, m); t.n = g.len(j, n); t.k = g.len(p, k);
+          t.alpha = alpha; t.beta = (p == 0) ? beta : 1.0;
+          t.a = tA ? A[p + (size_t)i * kt] : A[i + (size_t)p * mt];
+          t.lda = tA ? g.len(p, k) : g.len(i, m);
+          t.b = tB ? B[j + (size_t)p * nt] : B[p + (size_t)j * kt];
+          t.ldb = tB ? g.len(j, n) : g.len(p, k);
+          t.c = Ct(i, j); t.ldc = g.len(i, m);
+          dg_region_add(r, &t);
+        }
+    return;
+  }
+  // emulated: step p cuts op(A)'s block column p and op(B)'s block row p into
+  // slices once, then every C tile takes its product (the same order of the
+  // k accumulation per tile)
+  const int ldk = (nb + 7) / 8 * 8;
+  const size_t sb = oz_slot_bytes(ldk, nb);
+  auto slot = [&](int p, int q) {
+    return (double *)((char *)oz_ring + ((size_t)(p % kOzRingDepth) * (mt + nt) + q) * sb);
+  };
+  for (int p = 0; p < kt; p++) {
+    for (int i = 0; i < mt; i++) add_row_split(r, g, tA, A, m, k, i, p, slot(p, i), ldk);
+    // the columns of op(B) block (p, j) are the rows of op(B)' block (j, p)
+    for (int j = 0; j < nt; j++) add_row_split(r, g, !tB, B, n, k, j, p, slot(p, mt + j), ldk);
+    for (int i = 0; i < mt; i++)
+      for (int j = 0; j < nt; j++) {
+        dg_task t;
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_GEMM; t.uplo = 'N'; t.diag = 'P';
+        t.m = g.len(i, m); t.n = g.len(j, n); t.k = g.len(p, k);
+        t.alpha = alpha; t.beta = (p == 0) ? beta : 1.0;
+        t.a = slot(p, i); t.b = slot(p, mt + j); t.lda = ldk; t.ldb = nb;
+        t.c = Ct(i, j); t.ldc = g.len(i, m);
+        dg_region_add(r, &t);
+      }
+  }
+}
+
+void build_syrk_region(dg_region *r, char trans, int n, int k, int nb, double alpha,
+                       double *const *A, double beta, double *const *C, void *oz_ring) {
+  const MulGrid g{nb};
+  const int nt = (n + nb - 1) / nb, kt = (k + nb - 1) / nb;
+  const bool tr = !(trans == 'N' || trans == 'n');
+  auto Ct = [&](int i, int j) { return C[i + (size_t)j * nt]; };
+  // op(A) block (i, p): A(i, p) ('N', A is n x k) or A(p, i)' ('T', A is k x n)
+  auto At = [&](int i, int p) { return tr ? A[p + (size_t)i * kt] : A[i + (size_t)p * nt]; };
+  auto Ald = [&](int i, int p) { return tr ? g.len(p, k) : g.len(i, n); };
+  if (!oz_ring) {
+    // mul.jl:244-361 with uplo = 'U': syrk! on the diagonal tiles, gemm! on
+    // the upper ones, beta on the first term of each
+    for (int j = 0; j < nt; j++) {
+      for (int p = 0; p < kt; p++) {
+        dg_task t;
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_SYRK; t.uplo = 'U'; t.trans = tr ? 'T' : 'N';
+        t.n = g.len(j, n); t.k = g.len(p, k); t.alpha = alpha; t.beta = (p == 0) ? beta : 1.0;
+        t.a = At(j, p); t.lda = Ald(j, p); t.c = Ct(j, j); t.ldc = g.len(j, n);
+        dg_region_add(r, &t);
+      }
+      for (int m2 = j + 1; m2 < nt; m2++)
+        for (int p = 0; p < kt; p++) {
+          dg_task t;
+          memset(&t, 0, sizeof t);
+          t.op = DG_OP_GEMM; t.transa = tr ? 'T' : 'N'; t.transb = tr ? 'N' : 'T';
+          t.m = g.len(j, n); t.n = g.len(m2, n); t.k = g.len(p, k);
+          t.alpha = alpha; t.beta = (p == 0) ? beta : 1.0;
+          t.a = At(j, p); t.lda = Ald(j, p); t.b = At(m2, p); t.ldb = Ald(m2, p);
+          t.c = Ct(j, m2); t.ldc = g.len(j, n);
+          dg_region_add(r, &t);
+        }
+    }
+  } else {
+    const int ldk = (nb + 7) / 8 * 8;
+    const size_t sb = oz_slot_bytes(ldk, nb);
+    auto slot = [&](int p, int q) {
+      return (double *)((char *)oz_ring + ((size_t)(p % kOzRingDepth) * (nt + 0) + q) * sb);
+    };
+    for (int p = 0; p < kt; p++) {
+      for (int i = 0; i < nt; i++) add_row_split(r, g, tr, A, n, k, i, p, slot(p, i), ldk);
+      for (int i = 0; i < nt; i++)
+        for (int j = i; j < nt; j++) {
+          dg_task t;
+          memset(&t, 0, sizeof t);
+          t.op = OP_OZ_GEMM; t.uplo = (i == j) ? 'U' : 'N'; t.diag = 'P';
+          t.m = g.len(i, n); t.n = g.len(j, n); t.k = g.len(p, k);
+          t.alpha = alpha; t.beta = (p == 0) ? beta : 1.0;
+          t.a = slot(p, i); t.b = slot(p, j); t.lda = ldk; t.ldb = nb;
+          t.c = Ct(i, j); t.ldc = g.len(i, n);
+          dg_region_add(r, &t);
+        }
+    }
+  }
+  add_copytri(r, g, n, C);  // mul.jl:363
+}
+
 void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const *tiles,
                            void *oz_ring, double *winv) {
   const int mt = (n + nb - 1) / nb;
@@ -1387,6 +1559,89 @@ uint64_t call_key(int fn, char uplo, int n, int nb, int nrhs, long long ldh, con
   return h;
 }
 }  // namespace
+
+// C = beta C over a tile grid (the empty contraction).
+static int scale_tiles(int m, int n, int nb, double beta, double *const *C, cudaStream_t s) {
+  const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb;
+  for (int j = 0; j < nt; j++)
+    for (int i = 0; i < mt; i++) {
+      const int r = (i + 1) * nb <= m ? nb : m - i * nb, c = (j + 1) * nb <= n ? nb : n - j * nb;
+      DG_TRY(dg::scale_f64(r, c, beta, C[i + (size_t)j * mt], r, nullptr, s));
+    }
+  return 0;
+}
+
+extern "C" int dg_gemm_tiled(char transa, char transb, int m, int n, int k, int nb, double alpha,
+                             double *const *atiles, double *const *btiles, double beta,
+                             double *const *ctiles, void *stream) {
+  DG_CHECK_ARG(is_one_of(transa, "NnTtCc"), 1);
+  DG_CHECK_ARG(is_one_of(transb, "NnTtCc"), 2);
+  DG_CHECK_ARG(m >= 0, 3);
+  DG_CHECK_ARG(n >= 0, 4);
+  DG_CHECK_ARG(k >= 0, 5);
+  DG_CHECK_ARG(nb > 0, 6);
+  if (m == 0 || n == 0) return 0;
+  DG_CHECK_ARG(ctiles != nullptr, 11);
+  if (k == 0 || alpha == 0.0) return scale_tiles(m, n, nb, beta, ctiles, (cudaStream_t)stream);
+  DG_CHECK_ARG(atiles != nullptr, 8);
+  DG_CHECK_ARG(btiles != nullptr, 9);
+  const char ta = is_one_of(transa, "Nn") ? 'N' : 'T', tb = is_one_of(transb, "Nn") ? 'N' : 'T';
+  void *ring = nullptr;
+  if (dg::get_f64_engine() == 2 && nb <= 1024)
+    DG_TRY(dg::device_state().oz_workspace(dg::mul_ring_bytes_for(m, n, nb), &ring));
+  const size_t mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb, kt = (k + nb - 1) / nb;
+  struct { int64_t m, n, k, nb; double alpha, beta; const void *ring; char ta, tb; } a;
+  memset(&a, 0, sizeof a);
+  a.m = m; a.n = n; a.k = k; a.nb = nb; a.alpha = alpha; a.beta = beta; a.ring = ring;
+  a.ta = ta; a.tb = tb;
+  uint64_t key = dg::call_hash(6, &a, sizeof a, (const void *const *)atiles, mt * kt);
+  key = dg::call_hash(6, &key, sizeof key, (const void *const *)btiles, kt * nt);
+  key = dg::call_hash(6, &key, sizeof key, (const void *const *)ctiles, mt * nt);
+  return dg::region_run_cached(
+      key,
+      [&](dg_region *r) {
+        dg::build_gemm_region(r, ta, tb, m, n, k, nb, alpha, atiles, btiles, beta, ctiles, ring);
+      },
+      (cudaStream_t)stream, true);
+}
+
+extern "C" int dg_syrk_tiled(char trans, int n, int k, int nb, double alpha,
+                             double *const *atiles, double beta, double *const *ctiles,
+                             void *stream) {
+  DG_CHECK_ARG(is_one_of(trans, "NnTtCc"), 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(k >= 0, 3);
+  DG_CHECK_ARG(nb > 0, 4);
+  if (n == 0) return 0;
+  DG_CHECK_ARG(ctiles != nullptr, 8);
+  const char tr = is_one_of(trans, "Nn") ? 'N' : 'T';
+  const size_t nt = (n + nb - 1) / nb, kt = (k + nb - 1) / nb;
+  if (k == 0 || alpha == 0.0) {
+    DG_TRY(scale_tiles(n, n, nb, beta, ctiles, (cudaStream_t)stream));
+    return dg::region_run_cached(
+        dg::call_hash(8, &nb, sizeof nb, (const void *const *)ctiles, nt * nt),
+        [&](dg_region *r) {
+          const int nn = n;
+          dg::build_syrk_region(r, tr, nn, 0, nb, 0.0, nullptr, 1.0, ctiles, nullptr);
+        },
+        (cudaStream_t)stream, true);
+  }
+  DG_CHECK_ARG(atiles != nullptr, 6);
+  void *ring = nullptr;
+  if (dg::get_f64_engine() == 2 && nb <= 1024)
+    DG_TRY(dg::device_state().oz_workspace(dg::mul_ring_bytes_for(n, 0, nb), &ring));
+  struct { int64_t n, k, nb; double alpha, beta; const void *ring; char tr; } a;
+  memset(&a, 0, sizeof a);
+  a.n = n; a.k = k; a.nb = nb; a.alpha = alpha; a.beta = beta; a.ring = ring; a.tr = tr;
+  uint64_t key = dg::call_hash(7, &a, sizeof a, (const void *const *)atiles, nt * kt);
+  key = dg::call_hash(7, &key, sizeof key, (const void *const *)ctiles, nt * nt);
+  return dg::region_run_cached(
+      key,
+      [&](dg_region *r) {
+        dg::build_syrk_region(r, tr, n, k, nb, alpha, atiles, beta, ctiles, ring);
+      },
+      (cudaStream_t)stream, true);
+}
 
 extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles, void *stream) {
   DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);

@@ -33,6 +33,8 @@ constexpr int kTransferLevel = kPrioLevels, kTransferStreams = 4;
 //   OP_OZ_ZERO   c (m x n, ldc) = 0
 //   OP_UPLOAD    c (m x n tile, ldc = m) = the row-major block at a (row
 //                stride lda) in page-locked host or device memory
+//   OP_TILE_T    c (n x m, ldc) = a (m x n, lda)'
+//   OP_TILE_MIRROR  c (n x n, ldc): the upper triangle copied to the lower
 //   OP_OZ_INV    c (n x n, ldc) = U^-T for uplo 'U' / L^-T for 'L' of the
 //                factor tile a (lda), by substitution on the identity; b, ldb
 //                slice scratch as above
@@ -43,6 +45,8 @@ constexpr int OP_OZ_POTRF = 103;
 constexpr int OP_OZ_INV = 104;
 constexpr int OP_OZ_ZERO = 105;
 constexpr int OP_UPLOAD = 106;
+constexpr int OP_TILE_T = 107;
+constexpr int OP_TILE_MIRROR = 108;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);
@@ -101,6 +105,17 @@ void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const
 // tiles they touch.
 void build_upload_tasks(dg_region *r, char uplo, int n, int nb, double *const *tiles,
                         const double *host, long long ldh);
+// The datadeps regions of gemm_dagger! and syrk_dagger! + copytri!
+// (src/array/mul.jl:133-425) over square nb x nb tile grids (column-major
+// grids, ragged last row/column).  oz_ring (mul_ring_bytes_for bytes) selects
+// the emulated FP64 products: each step of the contraction cuts its tiles'
+// vectors into slices once, into a ring of kOzRingDepth steps.
+size_t mul_ring_bytes_for(int m, int n, int nb);
+void build_gemm_region(dg_region *r, char ta, char tb, int m, int n, int k, int nb, double alpha,
+                       double *const *A, double *const *B, double beta, double *const *C,
+                       void *oz_ring);
+void build_syrk_region(dg_region *r, char trans, int n, int k, int nb, double alpha,
+                       double *const *A, double beta, double *const *C, void *oz_ring);
 // One block-triangular solve pass; oz_ring (oz_solve_ring_bytes_for bytes)
 // selects emulated updates, step0 numbers its steps within the ring; winv
 // (with oz_ring, the factorization's inverses) turns each diagonal block

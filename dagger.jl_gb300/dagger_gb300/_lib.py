@@ -102,6 +102,10 @@ SIGNATURES = {
                                        c_void_p, c_void_p]),
     "dg_cholesky_solve_tiled_winv": (c_int, [c_char, c_int, c_int, c_void_p, c_void_p, c_int,
                                              c_void_p, c_void_p]),
+    "dg_gemm_tiled": (c_int, [c_char, c_char, c_int, c_int, c_int, c_int, c_double, c_void_p,
+                              c_void_p, c_double, c_void_p, c_void_p]),
+    "dg_syrk_tiled": (c_int, [c_char, c_int, c_int, c_int, c_double, c_void_p, c_double,
+                              c_void_p, c_void_p]),
     "dg_set_f64_engine": (c_int, [c_int]),
     "dg_get_f64_engine": (c_int, []),
     "dg_ishermitian_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),

@@ -286,6 +286,71 @@ def ldiv_(C: Cholesky, B: DArray, stream=None) -> DArray:
     return B
 
 
+def _mul_blocks(*arrays):
+    nb = None
+    for X in arrays:
+        if X.ndim != 2 or len(X.partitioning.blocksize) != 2:
+            raise ValueError("mul needs 2-D DArrays")
+        b0, b1 = X.partitioning.blocksize
+        if b0 != b1 or (nb is not None and b0 != nb):
+            raise ValueError("mul needs every operand blocked Blocks(nb, nb) with the same nb "
+                             "(maybe_copy_buffered re-blocks in the reference)")
+        nb = b0
+    return nb
+
+
+def _trans(t: str) -> bytes:
+    if t not in ('N', 'T', 'C'):
+        raise ValueError(f"transpose flag must be 'N', 'T' or 'C', got {t!r}")
+    return b'N' if t == 'N' else b'T'
+
+
+def gemm_dagger_(C: DArray, transA: str, transB: str, A: DArray, B: DArray, alpha=1.0,
+                 beta=0.0, stream=None) -> DArray:
+    """gemm_dagger!(C, transA, transB, A, B, alpha, beta) (src/array/mul.jl:133-215):
+    C = alpha op(A) op(B) + beta C over the tiles, one cached graph."""
+    nb = _mul_blocks(A, B, C)
+    m, k = (A.shape if transA == 'N' else A.shape[::-1])
+    k2, n = (B.shape if transB == 'N' else B.shape[::-1])
+    if k != k2 or C.shape != (m, n):
+        raise ValueError(f"DimensionMismatch: op(A) {m}x{k}, op(B) {k2}x{n}, C {C.shape}")
+    check(lib().dg_gemm_tiled(_trans(transA), _trans(transB), m, n, k, nb, float(alpha),
+                              A.tile_ptrs(), B.tile_ptrs(), float(beta), C.tile_ptrs(),
+                              _stream(stream)))
+    return C
+
+
+def syrk_dagger_(C: DArray, trans: str, A: DArray, alpha=1.0, beta=0.0, stream=None) -> DArray:
+    """syrk_dagger!(C, trans, A, alpha, beta) (src/array/mul.jl:230-365):
+    C = alpha op(A) op(A)' + beta C; the upper tiles are computed and copied
+    to the lower ones (copytri!, mul.jl:368-425), so C is fully symmetric."""
+    nb = _mul_blocks(A, C)
+    n, k = (A.shape if trans == 'N' else A.shape[::-1])
+    if C.shape != (n, n):
+        raise ValueError(f"DimensionMismatch: op(A) {n}x{k}, C {C.shape}")
+    check(lib().dg_syrk_tiled(_trans(trans), n, k, nb, float(alpha), A.tile_ptrs(), float(beta),
+                              C.tile_ptrs(), _stream(stream)))
+    return C
+
+
+def mul_(C: DArray, A: DArray, B: DArray, alpha=1.0, beta=0.0, transA: str = 'N',
+         transB: str = 'N', stream=None) -> DArray:
+    """mul!(C, op(A), op(B), alpha, beta) on DArrays (generic_matmatmul!,
+    src/array/mul.jl:11-41): A is B with exactly one of them transposed takes
+    syrk_dagger!, everything else gemm_dagger!."""
+    if A is B and (transA == 'N') != (transB == 'N'):
+        return syrk_dagger_(C, transA if transA == 'N' else 'T', A, alpha, beta, stream)
+    return gemm_dagger_(C, transA, transB, A, B, alpha, beta, stream)
+
+
+def matmul(A: DArray, B: DArray, transA: str = 'N', transB: str = 'N', stream=None) -> DArray:
+    """op(A) * op(B) as a new DArray with the operands' Blocks (A * B, A' * A, ...)."""
+    m = A.shape[0] if transA == 'N' else A.shape[1]
+    n = B.shape[1] if transB == 'N' else B.shape[0]
+    C = DArray((m, n), A.partitioning, device=A.storage.device)
+    return mul_(C, A, B, 1.0, 0.0, transA, transB, stream)
+
+
 def _herm_pairs(A: DArray):
     nb = _square_blocks(A)
     return nb

@@ -213,6 +213,25 @@ int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *const *tiles,
                                  const double *winv, int nrhs, double *const *btiles,
                                  void *stream);
 
+/* LinearAlgebra.mul! on DArrays (src/array/mul.jl): the datadeps regions of
+ * gemm_dagger! (mul.jl:133-215) and syrk_dagger! + copytri! (mul.jl:230-425)
+ * as one cached graph each.  Square Blocks(nb, nb) tile grids (column-major
+ * grids of column-major tiles, ld = a tile's row count, ragged last
+ * row/column), the layout of dg_cholesky_tiled.
+ * dg_gemm_tiled: C (m x n) = alpha op(A) op(B) + beta C, op(A) m x k, op(B)
+ * k x n; transa/transb 'N' or 'T' ('C' reads as 'T' for real data).
+ * dg_syrk_tiled: C (n x n) = alpha op(A) op(A)' + beta C, op(A) n x k
+ * ('N': A is n x k, 'T': A is k x n): the upper tiles are computed (syrk! on
+ * the diagonal, gemm! above it) and copied to the lower ones, so C is the
+ * full symmetric result, as syrk_dagger! leaves it.
+ * With dg_set_f64_engine(2) and nb <= 1024 every tile product is the emulated
+ * FP64 GEMM (each tile's vectors cut into slices once per contraction step). */
+int dg_gemm_tiled(char transa, char transb, int m, int n, int k, int nb, double alpha,
+                  double *const *atiles, double *const *btiles, double beta,
+                  double *const *ctiles, void *stream);
+int dg_syrk_tiled(char trans, int n, int k, int nb, double alpha, double *const *atiles,
+                  double beta, double *const *ctiles, void *stream);
+
 /* ishermitian(::DArray) (src/array/linalg.jl:90-124; pair test
  * is_cross_hermitian, linalg.jl:43-48) over the same tile grid.  Returns 1
  * (Hermitian), 0 (not), or a negative status.  Synchronises `stream`. */

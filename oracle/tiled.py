@@ -19,6 +19,7 @@ Reference files (paths within JuliaParallel/Dagger.jl v0.22.0):
   src/array/linalg.jl:90-124    ishermitian(::DArray)
   src/array/linalg.jl:352-405   ldiv!(::Cholesky{T,<:DMatrix}, B)
   src/array/darray.jl:107-117   Blocks partitioning (ragged last block)
+  src/array/mul.jl:133-425      gemm_dagger!, syrk_dagger!, copytri!
 
 Tiles are views into one column-major (Fortran-order) matrix: tile (i, j)
 covers rows i*nb : min((i+1)*nb, m) and columns j*nb : min((j+1)*nb, n),
@@ -421,6 +422,59 @@ def ishermitian_tiled(A: np.ndarray, nb: int) -> bool:
             if np.linalg.norm(a1 - a2) > rtol * max(np.linalg.norm(a1), np.linalg.norm(a2)):
                 return False
     return True
+
+
+# --------------------------------------------------------------------------
+# DArray multiplication (src/array/mul.jl)
+# --------------------------------------------------------------------------
+
+def gemm_dagger(C: np.ndarray, transA: str, transB: str, A: np.ndarray, B: np.ndarray,
+                alpha: float, beta: float, nb: int) -> np.ndarray:
+    """gemm_dagger! (mul.jl:133-215): for every C tile (m, n), the k loop of
+    gemm!(transA, transB, alpha, op(A) tile, op(B) tile, k == 1 ? beta : 1)."""
+    Cf = np.asfortranarray(C.copy())
+    TA = TileView(np.asfortranarray(A), nb, nb)
+    TB = TileView(np.asfortranarray(B), nb, nb)
+    TC = TileView(Cf, nb, nb)
+    kt = TA.nt if transA == 'N' else TA.mt
+    for m in range(TC.mt):
+        for n in range(TC.nt):
+            for k in range(kt):
+                a = TA.get(m, k) if transA == 'N' else TA.get(k, m)
+                b = TB.get(k, n) if transB == 'N' else TB.get(n, k)
+                TC.set(m, n, _gemm(transA, transB, alpha, a, b, beta if k == 0 else 1.0,
+                                   np.asfortranarray(TC.get(m, n))))
+    return Cf
+
+
+def syrk_dagger(C: np.ndarray, trans: str, A: np.ndarray, alpha: float, beta: float,
+                nb: int) -> np.ndarray:
+    """syrk_dagger! (mul.jl:230-365) with uplo = 'U', then copytri! (mul.jl:368-425):
+    syrk! on the diagonal tiles and gemm! above them, each with beta on its
+    first term, then the upper tiles transposed into the lower ones."""
+    Cf = np.asfortranarray(C.copy())
+    TA = TileView(np.asfortranarray(A), nb, nb)
+    TC = TileView(Cf, nb, nb)
+    kt = TA.nt if trans == 'N' else TA.mt
+    tile = (lambda i, k: TA.get(i, k)) if trans == 'N' else (lambda i, k: TA.get(k, i))
+    other = 'T' if trans == 'N' else 'N'
+    for n in range(TC.nt):
+        for k in range(kt):
+            TC.set(n, n, _syrk('U', trans, alpha, tile(n, k), beta if k == 0 else 1.0,
+                               np.asfortranarray(TC.get(n, n))))
+        for m in range(n + 1, TC.mt):
+            for k in range(kt):
+                ta, tb = (trans, other)
+                TC.set(n, m, _gemm(ta, tb, alpha, tile(n, k), tile(m, k), beta if k == 0 else 1.0,
+                                   np.asfortranarray(TC.get(n, m))))
+    for i in range(TC.mt):  # copytri!(C, 'U')
+        for j in range(i, TC.mt):
+            if i == j:
+                d = TC.get(i, i)
+                TC.set(i, i, np.triu(d) + np.triu(d, 1).T)
+            else:
+                TC.set(j, i, TC.get(i, j).T)
+    return Cf
 
 
 # --------------------------------------------------------------------------
