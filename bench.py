@@ -25,6 +25,8 @@ Reported:
                bounded sample (N = 16384, same tiling and RHS count)
   accuracy     normwise backward error of every RHS (inf-norms) and a
                probed ||A - U'U|| / ||A|| for the factor
+  mul          G G' on the same tiling (syrk_dagger! + copytri!), the
+               reference benchmark's input construction, TFLOP/s (n^3)
 
 `--impl reference` times only the CPU baseline (the reference's algorithm
 restated in C, run with all host threads) on the same metric.
@@ -64,6 +66,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-mul", action="store_true",
+                    help="skip the DArray syrk (G G', the reference benchmark's input) line")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--mixed-precision", default="auto")
     ap.add_argument("--batch-count", type=int, default=10000)
@@ -463,6 +467,9 @@ def run_ours(args):
         del W, DBw
         torch.cuda.empty_cache()
         mixed = bench_mixed(args, d, DA, A, B, stream, world)
+    mul = None
+    if not args.no_mul:
+        mul = bench_mul(args, d, dev, stream)
     batched = None
     if not args.no_batched:
         batched = bench_batched(args, d, dev, rank)
@@ -490,7 +497,7 @@ def run_ours(args):
                         "factor_residual_probe": fres},
            "roofline": roof, "gpu_launches": int(launches),
            "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
-           "mixed": mixed, "batched": batched, "serving": serving}
+           "mixed": mixed, "mul": mul, "batched": batched, "serving": serving}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -567,6 +574,42 @@ def choose_precision(cond):
     to 1e6, FP32 updates beyond (the factor must stay usable as a
     preconditioner for GMRES-IR)."""
     return "bf16x3" if cond <= 1e6 else "fp32"
+
+
+def bench_mul(args, d, dev, stream):
+    """The reference benchmark's input construction, G G' (syrk_dagger! +
+    copytri!, src/array/mul.jl:230-425; benchmark/suites/linalg.jl:15), on
+    N x N tiles of the headline's Blocks with the headline's FP64 engine:
+    n^2 k flops per call (k = n), the upper tiles' products plus the copies.
+    Checked on a probe: C v against G (G' v) in FP64."""
+    import torch
+    n, nb = args.n, args.nb
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 17)
+    G = torch.rand(n, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1
+    part = d.Blocks(nb, nb)
+    DG = d.DArray.from_array(G, part)
+    C = d.DArray(DG.shape, part, device=dev)
+    d.syrk_dagger_(C, 'N', DG, 1.0, 0.0, stream=stream)           # warm-up (graph capture)
+    reps = 2
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        d.syrk_dagger_(C, 'N', DG, 1.0, 0.0, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    v = torch.randn(n, 2, generator=g, device=dev, dtype=torch.float64)
+    Cv = C.collect() @ v
+    ref = G @ (G.T @ v)
+    err = float(((Cv - ref).abs().max() / ref.abs().max()).item())
+    del DG, C, G
+    torch.cuda.empty_cache()
+    return {"op": "syrk_dagger! + copytri!, C = G G'", "value": float(n) * n * n / t / 1e12,
+            "unit": "TFLOP/s", "ms": 1e3 * t, "n": n, "nb": nb, "engine": args.f64_engine,
+            "probe_rel_error": err}
 
 
 def bench_mixed(args, d, DA, A, B, stream, world):
