@@ -280,4 +280,33 @@ function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, winv::GB300Array{Float64,1},
     return B
 end
 
+"""
+    mul_gb300!(C::DArray, A::DArray, B::DArray, alpha=1, beta=0, tA='N', tB='N') -> C
+
+mul!(C, op(A), op(B), alpha, beta) on Blocks(nb, nb) DArrays of GB300Arrays,
+dispatched as generic_matmatmul! does (src/array/mul.jl:11-41): A === B with
+exactly one transposed is syrk_dagger! + copytri!, anything else
+gemm_dagger!; each is one library graph (dg_syrk_tiled / dg_gemm_tiled).
+"""
+function mul_gb300!(C::DArray{Float64,2}, A::DArray{Float64,2}, B::DArray{Float64,2},
+                    alpha::Real=1.0, beta::Real=0.0, tA::Char='N', tB::Char='N')
+    nb = C.partitioning.blocksize[1]
+    m, n = size(C)
+    k = tA == 'N' ? size(A, 2) : size(A, 1)
+    if A === B && (tA == 'N') != (tB == 'N')
+        dgcheck(ccall((:dg_syrk_tiled, libdg), Cint,
+                      (Cchar, Cint, Cint, Cint, Cdouble, Ptr{Ptr{Float64}}, Cdouble,
+                       Ptr{Ptr{Float64}}, Ptr{Cvoid}),
+                      tA == 'N' ? 'N' : 'T', n, k, nb, alpha, tile_pointers(A), beta,
+                      tile_pointers(C), C_NULL))
+    else
+        dgcheck(ccall((:dg_gemm_tiled, libdg), Cint,
+                      (Cchar, Cchar, Cint, Cint, Cint, Cint, Cdouble, Ptr{Ptr{Float64}},
+                       Ptr{Ptr{Float64}}, Cdouble, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
+                      tA, tB, m, n, k, nb, alpha, tile_pointers(A), tile_pointers(B), beta,
+                      tile_pointers(C), C_NULL))
+    end
+    return C
+end
+
 end # module
