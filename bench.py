@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-mul", action="store_true",
                     help="skip the DArray syrk (G G', the reference benchmark's input) line")
+    ap.add_argument("--no-lu", action="store_true",
+                    help="skip the tiled LU line (lu(A, RowMaximum()) and lu(A) \\ b)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--mixed-precision", default="auto")
     ap.add_argument("--batch-count", type=int, default=10000)
@@ -470,6 +472,9 @@ def run_ours(args):
     mul = None
     if not args.no_mul:
         mul = bench_mul(args, d, dev, stream)
+    lu = None
+    if not args.no_lu:
+        lu = bench_lu(args, d, dev, stream)
     batched = None
     if not args.no_batched:
         batched = bench_batched(args, d, dev, rank)
@@ -497,7 +502,7 @@ def run_ours(args):
                         "factor_residual_probe": fres},
            "roofline": roof, "gpu_launches": int(launches),
            "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
-           "mixed": mixed, "mul": mul, "batched": batched, "serving": serving}
+           "mixed": mixed, "mul": mul, "lu": lu, "batched": batched, "serving": serving}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -610,6 +615,66 @@ def bench_mul(args, d, dev, stream):
     return {"op": "syrk_dagger! + copytri!, C = G G'", "value": float(n) * n * n / t / 1e12,
             "unit": "TFLOP/s", "ms": 1e3 * t, "n": n, "nb": nb, "engine": args.f64_engine,
             "probe_rel_error": err}
+
+
+def bench_lu(args, d, dev, stream):
+    """lu(A, RowMaximum()) and lu(A) \\ b, the reference benchmark's "lu" and
+    "solve (A\\b via lu)" (benchmark/suites/linalg.jl), on N x N tiles of the
+    headline's Blocks with the headline's FP64 engine; A = rand(N, N)
+    (uniform [0, 1), seeded).  2/3 N^3 flops per factorization, 2 N^2 per
+    vector solve.  Checked on the GPU: P A v against L (U v) for two probe
+    vectors, and the solve's normwise backward error."""
+    import torch
+    n, nb = args.n, args.nb
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 29)
+    A0 = torch.rand(n, n, generator=g, device=dev, dtype=torch.float64)
+    part = d.Blocks(nb, nb)
+    D0 = d.DArray.from_array(A0, part)
+    DA = D0.copy()
+    d.lu_(DA, stream=stream)                          # warm-up (graph capture)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    times = []
+    for _ in range(2):
+        DA.storage.copy_(D0.storage)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        F = d.lu_(DA, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = sum(times) / len(times)
+    b = torch.rand(n, generator=g, device=dev, dtype=torch.float64)
+    Db = d.DArray.from_array(b, d.Blocks(nb))
+    d.ldiv_(F, Db, stream=stream)                     # warm-up
+    st = []
+    for _ in range(3):
+        Db.copy_from(b)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        d.ldiv_(F, Db, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        st.append(e0.elapsed_time(e1) / 1e3)
+    ts = sum(st) / len(st)
+    x = Db.collect()
+    berr = float(((b - A0 @ x).abs().max() /
+                  (A0.abs().sum(1).max() * x.abs().max() + b.abs().max())).item())
+    Fd = F.factors.collect()
+    v = torch.randn(n, 2, generator=g, device=dev, dtype=torch.float64)
+    Uv = torch.triu(Fd) @ v
+    LUv = torch.tril(Fd, -1) @ Uv + Uv
+    PAv = A0[F.p.to(dev)] @ v
+    res = float(((PAv - LUv).abs().max() / PAv.abs().max()).item())
+    del Fd, DA, D0, A0, Db, F
+    torch.cuda.empty_cache()
+    flops = 2.0 * n ** 3 / 3.0
+    return {"op": "lu(A, RowMaximum()) and lu(A) \\ b, A = rand(N, N)",
+            "value": flops / t / 1e12, "unit": "TFLOP/s", "ms": 1e3 * t,
+            "solve_ms": 1e3 * ts, "factor_and_solve_tflops": (flops + 2.0 * n * n) / (t + ts) / 1e12,
+            "n": n, "nb": nb, "engine": args.f64_engine, "probe_rel_residual": res,
+            "solve_backward_error": berr}
 
 
 def bench_mixed(args, d, DA, A, B, stream, world):

@@ -87,6 +87,39 @@ int trsm_f64_oz(char side, char uplo, char transa, char diag, int m, int n, doub
 int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_offset,
                  void *scratch, size_t bytes, cudaStream_t s);
 
+// C = alpha op(A) op(B) + beta C: emulated (scratch of `bytes`, see
+// oz_gemm_general) when the scratch allows, else on the FP64 tile kernels.
+// Kernels skip when *status is non-zero; a timeout records DG_ERR_TIMEOUT.
+int gemm_update_f64(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                    long long lda, const double *B, long long ldb, double beta, double *C,
+                    long long ldc, void *scratch, size_t bytes, int *status, cudaStream_t s);
+
+// Tiled LU pieces (lu.cu).  lu_panel_f64 factors the mrows x wcols panel P
+// (ld) in place: with pivoting like LAPACK getrf (lpiv[p] = panel row of
+// column p's pivot; ipiv_out[p] = info_offset + lpiv[p] + 1; lists = the
+// rows the interchanges move, see lu_laswp_tiles), without it like
+// generic_lufact!(NoPivot); lists may be null (ipiv only, any width).
+// info: atomicMin with info_offset + the 1-based
+// column of an exactly zero pivot.  oz (bytes): scratch of the emulated
+// updates, or null for the FP64 kernels.  leaf_scratch: lu_leaf_scratch_bytes().
+constexpr int kMaxTileRows = 256;  // tile rows of one block column a kernel addresses
+size_t lu_leaf_scratch_bytes();
+// Sets the LU kernels' shared-memory attributes (once; call before a capture).
+void lu_prepare();
+int lu_panel_f64(double *P, long long ld, int mrows, int wcols, bool pivot, int *lpiv, int *info,
+                 int info_offset, void *leaf_scratch, int *status, void *oz, size_t oz_bytes,
+                 long long *ipiv_out, int *lists, int list_cap, cudaStream_t s);
+// The (destination, source) row list of one panel applied to a block column
+// of ntiles tiles (rows in total, nb per tile, ld = the tile's rows).
+int lu_laswp_tiles(double *const *tiles, int ntiles, int nb, int rows, int ncols, const int *lists,
+                   int list_cap, cudaStream_t s);
+// perm = the composite of npiv interchanges (ipiv, 1-based) on n rows;
+// lu_rows_tiles permutes a tiled block column by it through X (n x ncols).
+int lu_perm(const long long *ipiv, int npiv, int n, int *perm, cudaStream_t s);
+int lu_rows_tiles(double *const *tiles, int ntiles, int nb, int n, int ncols, const int *perm,
+                  double *X, cudaStream_t s);
+int lu_iota(long long *ipiv, int n, cudaStream_t s);
+
 // W (n x n, ldw) = U^-T for uplo 'U', L^-T for 'L', of the triangular factor
 // A (lda), by column-parallel forward substitution on the unit vectors
 // (n <= 4096).  Kernels skip when *abort_flag is set.

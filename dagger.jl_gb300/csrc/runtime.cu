@@ -19,6 +19,7 @@
 // task list (same tasks, same pointers -> same graph), and replayed.
 #include <atomic>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <map>
 #include <memory>
@@ -201,6 +202,7 @@ struct dg_region {
   uint64_t max_len = 0;
   uint64_t hash = 1469598103934665603ull;
   int nedges = 0;
+  std::deque<std::vector<double *>> tables;  // tile lists of OP_LU_LASWP / OP_LU_ROWS
 };
 
 static void hash_bytes(uint64_t &h, const void *p, size_t n) {
@@ -278,6 +280,44 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
       out.push_back({dg::footprint(t.b, (int)dg::oz_slot_bytes(t.lda, t.ldb), 1, 1, 1), DG_IN});
       out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_INOUT});
       break;
+    case dg::OP_LU_PANEL: {
+      out.push_back({dg::footprint(t.c, t.m, t.n, t.ldc, E), DG_INOUT});
+      const bool piv = (t.transa == 'P');
+      const dg::LuLayout L = dg::lu_layout(t.lda, t.k, t.ldb, piv, t.diag == 'E');
+      const char *ws = (const char *)t.b;
+      const int step = t.info_offset / t.ldb;
+      // the leaf scratch and the panel's emulated-update scratch
+      out.push_back({dg::footprint(ws + L.leaf, (int)(L.lpiv - L.leaf), 1, 1, 1), DG_OUT});
+      if (L.ozp_bytes)
+        out.push_back({dg::footprint(ws + L.ozp, (int)(L.ozp_bytes / 256), 1, 1, 256), DG_OUT});
+      if (piv) {
+        const int npiv = t.m < t.n ? t.m : t.n;
+        out.push_back({dg::footprint(ws + L.lists + (size_t)step * L.list_stride * 4,
+                                     (int)L.list_stride, 1, 1, 4), DG_OUT});
+        out.push_back({dg::footprint((const long long *)t.a + t.info_offset, npiv, 1, 1, 8),
+                       DG_OUT});
+      }
+      break;
+    }
+    case dg::OP_LU_LASWP:
+    case dg::OP_LU_ROWS: {
+      double *const *tl = (double *const *)t.a;
+      for (int i = 0; i < t.k; i++) {
+        const int rows = (i == t.k - 1) ? t.m - i * t.ldb : t.ldb;
+        out.push_back({dg::footprint(tl[i], rows, t.n, rows, E), DG_INOUT});
+      }
+      if (t.op == dg::OP_LU_LASWP) {
+        out.push_back({dg::footprint(t.b, 1 + 2 * t.ldc, 1, 1, 4), DG_IN});
+      } else {
+        out.push_back({dg::footprint(t.b, t.m, 1, 1, 4), DG_IN});
+        out.push_back({dg::footprint(t.c, t.m, t.n, t.m, E), DG_OUT});
+      }
+      break;
+    }
+    case dg::OP_LU_PERM:
+      out.push_back({dg::footprint(t.a, t.k, 1, 1, 8), DG_IN});
+      out.push_back({dg::footprint(t.c, t.n, 1, 1, 4), DG_OUT});
+      break;
   }
 }
 
@@ -289,12 +329,14 @@ extern "C" int dg_region_add(dg_region *r, const dg_task *tp) {
   DG_CHECK_ARG(tp != nullptr, 2);
   const dg_task &t = *tp;
   DG_CHECK_ARG((t.op >= DG_OP_POTRF && t.op <= DG_OP_COPY) ||
-                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::OP_TILE_MIRROR),
+                   (t.op >= dg::OP_OZ_SPLIT && t.op <= dg::kOpLast),
                2);
   const int id = (int)r->tasks.size();
   r->tasks.push_back(t);
   r->level.push_back((char)(dg::kPrioLevels - 1));
   hash_bytes(r->hash, &t, sizeof(dg_task));
+  if (t.op == dg::OP_LU_LASWP || t.op == dg::OP_LU_ROWS)  // the tiles, not the list's address
+    hash_bytes(r->hash, t.a, sizeof(double *) * (size_t)t.k);
   std::vector<dg_region::Access> acc;
   task_accesses(t, acc);
   std::vector<int> p;
@@ -436,6 +478,23 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
       DG_CUDA_TRY(cudaMemcpy2DAsync(t.c, (size_t)t.ldc * 8, t.a, (size_t)t.lda * 8, (size_t)t.m * 8,
                                     t.n, cudaMemcpyDeviceToDevice, s));
       return 0;
+    case OP_LU_PANEL: {
+      const bool piv = (t.transa == 'P');
+      const LuLayout L = lu_layout(t.lda, t.k, t.ldb, piv, t.diag == 'E');
+      char *ws = (char *)t.b;
+      const int step = t.info_offset / t.ldb;
+      return lu_panel_f64(t.c, t.ldc, t.m, t.n, piv, (int *)(ws + L.lpiv) + t.info_offset,
+                          (int *)(ws + L.info), t.info_offset, ws + L.leaf, (int *)(ws + L.status),
+                          L.ozp_bytes ? ws + L.ozp : nullptr, L.ozp_bytes,
+                          (long long *)t.a + t.info_offset,
+                          (int *)(ws + L.lists) + (size_t)step * L.list_stride, L.list_cap, s);
+    }
+    case OP_LU_LASWP:
+      return lu_laswp_tiles((double *const *)t.a, t.k, t.ldb, t.m, t.n, (const int *)t.b, t.ldc, s);
+    case OP_LU_PERM:
+      return lu_perm((const long long *)t.a, t.k, t.n, (int *)t.c, s);
+    case OP_LU_ROWS:
+      return lu_rows_tiles((double *const *)t.a, t.k, t.ldb, t.m, t.n, (const int *)t.b, t.c, s);
   }
   return DG_ERR_UNSUPPORTED;
 }
@@ -1431,7 +1490,7 @@ size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs, bool inv) {
 
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
                       int nrhs, double *const *btiles, void *oz_ring, int step0,
-                      const double *winv) {
+                      const double *winv, char diag) {
   const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
   auto rows = [&](int i) { return (i + 1) * nb <= n ? nb : n - i * nb; };
   auto cols = [&](int j) { return (j + 1) * nb <= nrhs ? nb : nrhs - j * nb; };
@@ -1489,7 +1548,7 @@ void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double
         dg_region_add(r, &t);
         mark_urgent(r);
       } else {
-        t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = uplo; t.transa = trans; t.diag = 'N';
+        t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = uplo; t.transa = trans; t.diag = diag;
         t.m = rows(k); t.n = cols(c); t.alpha = 1.0; t.a = A(k, k); t.lda = rows(k);
         t.c = B(k, c); t.ldc = rows(k);
         dg_region_add(r, &t);
@@ -1532,6 +1591,208 @@ void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double
       }
     }
   }
+}
+
+double *const *region_table(dg_region *r, const std::vector<double *> &ptrs) {
+  r->tables.push_back(ptrs);
+  return r->tables.back().data();
+}
+
+static size_t r256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated) {
+  LuLayout L;
+  const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb;
+  const int steps = mt < nt ? mt : nt, mn = m < n ? m : n;
+  size_t off = 256;
+  L.leaf = off;
+  off += r256(lu_leaf_scratch_bytes());
+  L.lpiv = off;
+  off += r256((size_t)mn * 4);
+  L.list_cap = 2 * nb;
+  L.list_stride = 1 + 2 * (size_t)L.list_cap;
+  L.lists = off;
+  off += r256((size_t)steps * L.list_stride * 4);
+  if (pivot) {
+    L.panel_bytes = r256((size_t)m * nb * 8);
+    L.panel = off;
+    off += 2 * L.panel_bytes;
+  }
+  if (emulated) {
+    // the panel recursion's largest update: (rows) x (nb/2) x (nb/2 rounded up to 32)
+    const int h = nb / 2 + 32;
+    L.ozp_bytes = r256(oz_scratch_bytes(pivot ? m : nb, h, h, false));
+    L.ozp = off;
+    off += L.ozp_bytes;
+    L.ring = off;
+    off += (size_t)kOzRingDepth * (mt + nt) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+  }
+  L.total = off;
+  return L;
+}
+
+// lu.jl:306-410 (RowMaximum) / 5-54 (NoPivot).  Step k: the block column's
+// tiles from the diagonal down are gathered into a panel buffer, factored
+// (OP_LU_PANEL) and scattered back; its interchanges go to every other block
+// column (swaprows_trail!, one task per block column); then TRSM('L', 'L',
+// 'N', 'U') of the row panel and GEMM('N', 'N', -1) of the trailing tiles.
+// Without pivoting the diagonal tile is factored in place and the column
+// panel solved with TRSM('R', 'U', 'N', 'N').  With the emulated engine the
+// rows of L(i, k) and the columns of U(k, j) are cut into slices once per
+// step (ring slots (k mod depth, i) and (k mod depth, mt + j)) and every
+// trailing tile takes one emulated product; the row panel's TRSMs run their
+// recursion's updates emulated, with the slot of U(k, j) as scratch.
+void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, bool pivot,
+                     void *ws, long long *ipiv, bool emulated) {
+  const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb, steps = mt < nt ? mt : nt;
+  auto rows = [&](int i) { return (i + 1) * nb <= m ? nb : m - i * nb; };
+  auto cols = [&](int j) { return (j + 1) * nb <= n ? nb : n - j * nb; };
+  auto T = [&](int i, int j) { return tiles[i + (size_t)j * mt]; };
+  const LuLayout L = lu_layout(m, n, nb, pivot, emulated);
+  char *w = (char *)ws;
+  const int ldk = (nb + 7) / 8 * 8;
+  const size_t sb = oz_slot_bytes(ldk, nb);
+  const int slot_units = (int)(sb / 256);
+  auto slot = [&](int k, int q) {
+    return (double *)(w + L.ring + ((size_t)(k % kOzRingDepth) * (mt + nt) + q) * sb);
+  };
+  dg_task t;
+  auto add = [&](int lvl) {
+    dg_region_add(r, &t);
+    mark_level(r, lvl);
+  };
+  for (int k = 0; k < steps; k++) {
+    const int mk = m - k * nb, wk = cols(k);
+    const int kk = rows(k) < wk ? rows(k) : wk;  // order of L(k, k) and U(k, k)
+    double *P;
+    int ldp;
+    if (pivot) {
+      P = (double *)(w + L.panel + (size_t)(k % 2) * L.panel_bytes);
+      ldp = mk;
+      for (int i = k; i < mt; i++) {
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_COPY; t.m = rows(i); t.n = wk; t.a = T(i, k); t.lda = rows(i);
+        t.c = P + (size_t)(i - k) * nb; t.ldc = ldp;
+        add(0);
+      }
+    } else {
+      P = T(k, k);
+      ldp = rows(k);
+    }
+    memset(&t, 0, sizeof t);
+    t.op = OP_LU_PANEL; t.c = P; t.ldc = ldp; t.m = pivot ? mk : rows(k); t.n = wk;
+    t.lda = m; t.k = n; t.ldb = nb; t.info_offset = k * nb; t.b = (const double *)ws;
+    t.a = (const double *)ipiv; t.transa = pivot ? 'P' : 'N'; t.diag = emulated ? 'E' : 'N';
+    add(0);
+    if (pivot) {
+      for (int i = k; i < mt; i++) {
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_COPY; t.m = rows(i); t.n = wk; t.a = P + (size_t)(i - k) * nb; t.lda = ldp;
+        t.c = T(i, k); t.ldc = rows(i);
+        add(0);
+      }
+      const int *lists = (const int *)(w + L.lists) + (size_t)k * L.list_stride;
+      for (int j = 0; j < nt; j++) {
+        if (j == k) continue;
+        std::vector<double *> col;
+        for (int i = k; i < mt; i++) col.push_back(T(i, j));
+        memset(&t, 0, sizeof t);
+        t.op = OP_LU_LASWP; t.a = (const double *)region_table(r, col); t.k = mt - k; t.m = mk;
+        t.n = cols(j); t.ldb = nb; t.b = (const double *)lists; t.ldc = L.list_cap;
+        add(j > k ? j - k - 1 : kPrioLevels - 1);
+      }
+    } else {
+      for (int i = k + 1; i < mt; i++) {  // L(i, k) = A(i, k) U(k, k)^-1
+        memset(&t, 0, sizeof t);
+        t.op = emulated ? OP_OZ_TRSM : DG_OP_TRSM; t.side = 'R'; t.uplo = 'U'; t.transa = 'N';
+        t.diag = 'N'; t.m = rows(i); t.n = kk; t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
+        t.c = T(i, k); t.ldc = rows(i);
+        if (emulated) { t.b = slot(k, i); t.ldb = slot_units; }
+        add(0);
+      }
+    }
+    if (k + 1 >= nt) continue;
+    if (emulated)
+      for (int i = k + 1; i < mt; i++) {  // the rows of L(i, k): A-vectors of length kk
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_SPLIT; t.trans = 'T'; t.a = T(i, k); t.lda = rows(i); t.m = kk;
+        t.n = rows(i); t.c = slot(k, i); t.ldc = ldk; t.k = nb;
+        add(0);
+      }
+    for (int j = k + 1; j < nt; j++) {
+      const int lvl = j - k - 1;
+      memset(&t, 0, sizeof t);  // U(k, j) = L(k, k)^-1 A(k, j)
+      t.op = emulated ? OP_OZ_TRSM : DG_OP_TRSM; t.side = 'L'; t.uplo = 'L'; t.transa = 'N';
+      t.diag = 'U'; t.m = kk; t.n = cols(j); t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
+      t.c = T(k, j); t.ldc = rows(k);
+      if (emulated) { t.b = slot(k, mt + j); t.ldb = slot_units; }
+      add(lvl);
+      if (k + 1 >= mt) continue;
+      if (emulated) {  // the columns of U(k, j): B-vectors of length kk
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_SPLIT; t.trans = 'N'; t.a = T(k, j); t.lda = rows(k); t.m = kk;
+        t.n = cols(j); t.c = slot(k, mt + j); t.ldc = ldk; t.k = nb;
+        add(lvl);
+      }
+      for (int i = k + 1; i < mt; i++) {  // A(i, j) -= L(i, k) U(k, j)
+        memset(&t, 0, sizeof t);
+        if (emulated) {
+          t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = rows(i); t.n = cols(j); t.k = kk;
+          t.alpha = -1.0; t.beta = 1.0; t.a = slot(k, i); t.b = slot(k, mt + j);
+          t.lda = ldk; t.ldb = nb; t.c = T(i, j); t.ldc = rows(i);
+          if (lvl > 0) t.diag = 'P';
+        } else {
+          t.op = DG_OP_GEMM; t.transa = 'N'; t.transb = 'N'; t.m = rows(i); t.n = cols(j);
+          t.k = kk; t.alpha = -1.0; t.beta = 1.0; t.a = T(i, k); t.lda = rows(i);
+          t.b = T(k, j); t.ldb = rows(k); t.c = T(i, j); t.ldc = rows(i);
+        }
+        add(lvl);
+      }
+    }
+  }
+}
+
+size_t lu_solve_bytes(int n, int nb, int nrhs, bool emulated) {
+  const int bnt = (nrhs + nb - 1) / nb;
+  size_t b = emulated ? r256(oz_solve_ring_bytes_for(n, nb, nrhs)) : 0;
+  b += r256((size_t)n * 4);
+  for (int c = 0; c < bnt; c++) {
+    const int w = (c + 1) * nb <= nrhs ? nb : nrhs - c * nb;
+    b += r256((size_t)n * w * 8);
+  }
+  return b;
+}
+
+// linalg.jl:264-308: B's rows permuted by the pivots (one permutation
+// applied per block column of B), then ldiv!(UnitLowerTriangular) and
+// ldiv!(UpperTriangular) as the two block solve passes.
+void build_lu_solve_region(dg_region *r, int n, int nb, double *const *tiles,
+                           const long long *ipiv, int nrhs, double *const *btiles, void *ws,
+                           bool emulated) {
+  const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
+  char *w = (char *)ws;
+  void *ring = emulated ? w : nullptr;
+  size_t off = emulated ? r256(oz_solve_ring_bytes_for(n, nb, nrhs)) : 0;
+  int *perm = (int *)(w + off);
+  off += r256((size_t)n * 4);
+  dg_task t;
+  memset(&t, 0, sizeof t);
+  t.op = OP_LU_PERM; t.a = (const double *)ipiv; t.k = n; t.n = n; t.c = (double *)perm;
+  dg_region_add(r, &t);
+  mark_urgent(r);
+  for (int c = 0; c < bnt; c++) {
+    const int wc = (c + 1) * nb <= nrhs ? nb : nrhs - c * nb;
+    std::vector<double *> col;
+    for (int i = 0; i < mt; i++) col.push_back(btiles[i + (size_t)c * mt]);
+    memset(&t, 0, sizeof t);
+    t.op = OP_LU_ROWS; t.a = (const double *)region_table(r, col); t.k = mt; t.m = n; t.n = wc;
+    t.ldb = nb; t.b = (const double *)perm; t.c = (double *)(w + off);
+    dg_region_add(r, &t);
+    mark_urgent(r);
+    off += r256((size_t)n * wc * 8);
+  }
+  build_solve_pass(r, 'L', 'N', n, nb, tiles, nrhs, btiles, ring, 0, nullptr, 'U');
+  build_solve_pass(r, 'U', 'N', n, nb, tiles, nrhs, btiles, ring, mt, nullptr, 'N');
 }
 
 }  // namespace dg
@@ -1747,6 +2008,126 @@ extern "C" int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *
       [&](dg_region *r) {
         dg::build_solve_pass(r, up ? 'U' : 'L', up ? 'T' : 'N', n, nb, tiles, nrhs, btiles, ring, 0);
         dg::build_solve_pass(r, up ? 'U' : 'L', up ? 'N' : 'T', n, nb, tiles, nrhs, btiles, ring, mt);
+      },
+      (cudaStream_t)stream, true);
+}
+
+// ---------------------------------------------------------------------------
+// Tiled LU (src/array/lu.jl, linalg.jl:264-308).
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kLuNoInfo = 0x7f7f7f7f;  // the info word before a zero pivot lowers it
+
+struct LuCallArgs {
+  int64_t m, n, nb, nrhs, pivot, emulated;
+  const void *ws, *ipiv;
+};
+
+uint64_t lu_key(int fn, int64_t m, int64_t n, int64_t nb, int64_t nrhs, int64_t pivot,
+                int64_t emulated, const void *ws, const void *ipiv, double *const *tiles,
+                size_t ntiles, double *const *btiles, size_t nbtiles) {
+  LuCallArgs a;
+  memset(&a, 0, sizeof a);
+  a.m = m; a.n = n; a.nb = nb; a.nrhs = nrhs; a.pivot = pivot; a.emulated = emulated;
+  a.ws = ws; a.ipiv = ipiv;
+  uint64_t h = dg::call_hash(fn, &a, sizeof a, (const void *const *)tiles, ntiles);
+  if (btiles) h = dg::call_hash(fn, &h, sizeof h, (const void *const *)btiles, nbtiles);
+  return h;
+}
+
+// The status word (a timed-out wait) and the info word after the work queued
+// on s: DG_ERR_TIMEOUT, else the first zero pivot's column (1-based) or 0.
+int lu_words_reset(void *ws, cudaStream_t s) {
+  DG_CUDA_TRY(cudaMemsetAsync(ws, 0, 4, s));
+  DG_CUDA_TRY(cudaMemsetAsync((char *)ws + 4, 0x7f, 4, s));
+  return 0;
+}
+int lu_words_read(const void *ws, cudaStream_t s) {
+  int v[2] = {0, 0};
+  DG_CUDA_TRY(cudaMemcpyAsync(v, ws, sizeof v, cudaMemcpyDeviceToHost, s));
+  DG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (v[0]) return DG_ERR_TIMEOUT;
+  return v[1] == kLuNoInfo ? 0 : v[1];
+}
+}  // namespace
+
+extern "C" int dg_getrf(int m, int n, double *A, int lda, long long *ipiv, int *info_host,
+                        void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(lda >= (m > 1 ? m : 1), 4);
+  DG_CHECK_ARG(info_host != nullptr, 6);
+  *info_host = 0;
+  if (m == 0 || n == 0) return 0;
+  DG_CHECK_ARG(A != nullptr, 3);
+  DG_CHECK_ARG(ipiv != nullptr, 5);
+  const bool emulated = dg::get_f64_engine() == 2;
+  auto r256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t leaf = r256(dg::lu_leaf_scratch_bytes());
+  const size_t lpiv = r256((size_t)(m < n ? m : n) * 4);
+  const int h = n / 2 + 32;
+  const size_t ozp = emulated ? r256(dg::oz_scratch_bytes(m, h, h, false)) : 0;
+  dg::lu_prepare();
+  void *ws = nullptr;
+  DG_TRY(dg::device_state().oz_workspace(256 + leaf + lpiv + ozp, &ws));
+  char *w = (char *)ws;
+  cudaStream_t s = (cudaStream_t)stream;
+  DG_TRY(lu_words_reset(ws, s));
+  DG_TRY(dg::lu_panel_f64(A, lda, m, n, true, (int *)(w + 256 + leaf), (int *)(w + 4), 0,
+                          w + 256, (int *)w, ozp ? w + 256 + leaf + lpiv : nullptr, ozp, ipiv,
+                          nullptr, 0, s));
+  const int rc = lu_words_read(ws, s);
+  if (rc >= 0) *info_host = rc;
+  return rc;
+}
+
+extern "C" int dg_lu_tiled(int m, int n, int nb, double *const *tiles, int pivot,
+                           long long *ipiv, void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(nb > 0, 3);
+  DG_CHECK_ARG(pivot == 0 || pivot == 1, 5);
+  if (m == 0 || n == 0) return 0;
+  DG_CHECK_ARG(tiles != nullptr, 4);
+  DG_CHECK_ARG(ipiv != nullptr, 6);
+  const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb;
+  if (nb > 1024 || mt > dg::kMaxTileRows) return DG_ERR_UNSUPPORTED;
+  const bool emulated = dg::get_f64_engine() == 2;
+  const dg::LuLayout L = dg::lu_layout(m, n, nb, pivot != 0, emulated);
+  dg::lu_prepare();
+  void *ws = nullptr;
+  DG_TRY(dg::device_state().oz_workspace(L.total, &ws));
+  cudaStream_t s = (cudaStream_t)stream;
+  DG_TRY(lu_words_reset(ws, s));
+  const int rc = dg::region_run_cached(
+      lu_key(30, m, n, nb, 0, pivot, emulated, ws, ipiv, tiles, (size_t)mt * nt, nullptr, 0),
+      [&](dg_region *r) { dg::build_lu_region(r, m, n, nb, tiles, pivot != 0, ws, ipiv, emulated); },
+      s, true);
+  if (rc) return rc;
+  if (!pivot) DG_TRY(dg::lu_iota(ipiv, m < n ? m : n, s));
+  return lu_words_read(ws, s);
+}
+
+extern "C" int dg_lu_solve_tiled(int n, int nb, double *const *tiles, const long long *ipiv,
+                                 int nrhs, double *const *btiles, void *stream) {
+  DG_CHECK_ARG(n >= 0, 1);
+  DG_CHECK_ARG(nb > 0, 2);
+  DG_CHECK_ARG(nrhs >= 0, 5);
+  if (n == 0 || nrhs == 0) return 0;
+  DG_CHECK_ARG(tiles != nullptr, 3);
+  DG_CHECK_ARG(ipiv != nullptr, 4);
+  DG_CHECK_ARG(btiles != nullptr, 6);
+  const int mt = (n + nb - 1) / nb, bnt = (nrhs + nb - 1) / nb;
+  if (mt > dg::kMaxTileRows) return DG_ERR_UNSUPPORTED;
+  const bool emulated = dg::get_f64_engine() == 2 && nb <= 1024;
+  dg::lu_prepare();
+  void *ws = nullptr;
+  DG_TRY(dg::device_state().oz_workspace(dg::lu_solve_bytes(n, nb, nrhs, emulated), &ws));
+  return dg::region_run_cached(
+      lu_key(31, n, n, nb, nrhs, 1, emulated, ws, ipiv, tiles, (size_t)mt * mt, btiles,
+             (size_t)mt * bnt),
+      [&](dg_region *r) {
+        dg::build_lu_solve_region(r, n, nb, tiles, ipiv, nrhs, btiles, ws, emulated);
       },
       (cudaStream_t)stream, true);
 }

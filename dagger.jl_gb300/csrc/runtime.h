@@ -47,6 +47,23 @@ constexpr int OP_OZ_ZERO = 105;
 constexpr int OP_UPLOAD = 106;
 constexpr int OP_TILE_T = 107;
 constexpr int OP_TILE_MIRROR = 108;
+// Tiled LU (lu.cu):
+//   OP_LU_PANEL  the m x n panel c (ldc) factored in place, transa 'P' with
+//                row interchanges, 'N' without; diag 'E': emulated updates;
+//                lda x k = the whole matrix, ldb = nb, info_offset = the
+//                panel's first row; b = the LU workspace (lu_layout), a = ipiv
+//   OP_LU_LASWP  a panel's row list (b, int, ldc = its capacity) applied to
+//                a block column: a = host array of its k tile pointers (m rows
+//                in all, ldb = nb per tile), n columns
+//   OP_LU_PERM   c (int, n) = the composite of k interchanges a (int64 ipiv)
+//   OP_LU_ROWS   a block column of k tiles (a = host array of tile pointers,
+//                m rows, n columns, ldb = nb) permuted by b (OP_LU_PERM's
+//                result) through c (m x n doubles)
+constexpr int OP_LU_PANEL = 109;
+constexpr int OP_LU_LASWP = 110;
+constexpr int OP_LU_PERM = 111;
+constexpr int OP_LU_ROWS = 112;
+constexpr int kOpLast = OP_LU_ROWS;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);
@@ -103,6 +120,37 @@ void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const
 // host[r*ldh + c]), ranked like the factorization's first use of the tile;
 // added before build_cholesky_region, its tasks then wait only for the
 // tiles they touch.
+// Workspace of the tiled LU of an m x n matrix in nb x nb tiles (byte
+// offsets from its base): the status and info words, the leaf launches'
+// scratch, every panel's pivots (panel rows) and interchange row list, two
+// panel buffers, the panel's emulated-update scratch and (emulated engine)
+// the slice slots of the trailing updates.
+struct LuLayout {
+  size_t status = 0, info = 4, leaf = 256, lpiv = 0, lists = 0, panel = 0, panel_bytes = 0,
+         ozp = 0, ozp_bytes = 0, ring = 0, total = 0;
+  int list_cap = 0;        // entries of one step's destination (and source) list
+  size_t list_stride = 0;  // ints per step
+};
+LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated);
+// The datadeps region of lu!(A, RowMaximum()) (pivot) or lu!(A, NoPivot())
+// (src/array/lu.jl:5-54, 306-410) over the mt x nt tile grid; ws holds
+// lu_layout(m, n, nb, pivot, emulated).total bytes; ipiv (device, min(m, n)
+// int64) receives the global 1-based pivots.
+void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, bool pivot,
+                     void *ws, long long *ipiv, bool emulated);
+// ldiv!(F::LU, B) (linalg.jl:264-308): B's rows permuted by ipiv, then the
+// unit-lower and the upper block solves.  ws: lu_solve_bytes(n, nb, nrhs,
+// emulated) bytes (the permutation, the permuted block columns, the slice
+// slots of the emulated updates).
+size_t lu_solve_bytes(int n, int nb, int nrhs, bool emulated);
+void build_lu_solve_region(dg_region *r, int n, int nb, double *const *tiles,
+                           const long long *ipiv, int nrhs, double *const *btiles, void *ws,
+                           bool emulated);
+
+// A copy of `ptrs` owned by the region (alive until it is destroyed), for
+// tasks that address a list of tiles.
+double *const *region_table(dg_region *r, const std::vector<double *> &ptrs);
+
 void build_upload_tasks(dg_region *r, char uplo, int n, int nb, double *const *tiles,
                         const double *host, long long ldh);
 // The datadeps regions of gemm_dagger! and syrk_dagger! + copytri!
@@ -123,6 +171,6 @@ void build_syrk_region(dg_region *r, char trans, int n, int k, int nb, double al
 size_t oz_solve_ring_bytes_for(int n, int nb, int nrhs, bool inv = false);
 void build_solve_pass(dg_region *r, char uplo, char trans, int n, int nb, double *const *tiles,
                       int nrhs, double *const *btiles, void *oz_ring = nullptr, int step0 = 0,
-                      const double *winv = nullptr);
+                      const double *winv = nullptr, char diag = 'N');
 
 }  // namespace dg

@@ -537,6 +537,17 @@ int potrf_f64_oz(char uplo, int n, double *A, int lda, int *info_out, int info_o
                            nullptr, nullptr, oz);
 }
 
+int gemm_update_f64(char ta, char tb, int m, int n, int k, double alpha, const double *A,
+                    long long lda, const double *B, long long ldb, double beta, double *C,
+                    long long ldc, void *scratch, size_t bytes, int *status, cudaStream_t s) {
+  OzScratch oz;
+  oz.p = scratch;
+  oz.bytes = bytes;
+  oz.status = status;
+  return update_t<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, TRI_NONE, status,
+                          s, nullptr, oz);
+}
+
 int trinv_t_f64(char uplo, int n, const double *A, int lda, double *W, int ldw,
                 const int *abort_flag, cudaStream_t s) {
   if (n <= 0) return 0;

@@ -7,13 +7,13 @@ mirror of the reference's interface (DArray/Blocks, cholesky, cholesky!,
 ldiv!, ishermitian, spawn_datadeps with In/Out/InOut and the BLAS/LAPACK
 tile calls).
 """
-from ._lib import DaggerGB300Error, PosDefException, lib
+from ._lib import DaggerGB300Error, PosDefException, SingularException, lib
 from .darray import Blocks, DArray, distribute
 from .datadeps import In, InOut, Out, copyto_, spawn, spawn_datadeps
 from .linalg import (Cholesky, cholesky, cholesky_, cholesky_distribute, gemm_, gemm_dagger_,
                      matmul, mul_, syrk_dagger_, gemm_f64_emulated_tn, gemv_,
-                     get_f64_engine, ishermitian, issymmetric, ldiv_, potrf_, set_f64_engine,
-                     syrk_, trsm_, trsv_)
+                     get_f64_engine, getrf_, ishermitian, issymmetric, LU, ldiv, ldiv_, lu, lu_,
+                     potrf_, set_f64_engine, syrk_, trsm_, trsv_)
 from .mixed import MixedCholesky, cholesky_mixed
 
 __all__ = [
@@ -21,5 +21,5 @@ __all__ = [
     "ldiv_", "gemm_dagger_", "syrk_dagger_", "mul_", "matmul",
     "ishermitian", "issymmetric", "potrf_", "trsm_", "syrk_", "gemm_", "trsv_", "gemv_",
     "gemm_f64_emulated_tn", "set_f64_engine", "get_f64_engine", "spawn_datadeps", "spawn", "In", "Out", "InOut", "copyto_", "PosDefException",
-    "DaggerGB300Error", "lib",
+    "DaggerGB300Error", "lib", "LU", "lu", "lu_", "ldiv", "getrf_", "SingularException",
 ]

@@ -106,6 +106,9 @@ SIGNATURES = {
                               c_void_p, c_double, c_void_p, c_void_p]),
     "dg_syrk_tiled": (c_int, [c_char, c_int, c_int, c_int, c_double, c_void_p, c_double,
                               c_void_p, c_void_p]),
+    "dg_getrf": (c_int, [c_int, c_int, c_dp, c_int, c_void_p, ctypes.POINTER(c_int), c_void_p]),
+    "dg_lu_tiled": (c_int, [c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "dg_lu_solve_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "dg_set_f64_engine": (c_int, [c_int]),
     "dg_get_f64_engine": (c_int, []),
     "dg_ishermitian_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
@@ -173,6 +176,15 @@ class PosDefException(Exception):
 
     def __init__(self, info: int):
         super().__init__(f"matrix is not positive definite; Cholesky factorization failed (info={info})")
+        self.info = info
+
+
+class SingularException(Exception):
+    """LinearAlgebra.SingularException(info): U[info, info] of an LU is
+    exactly zero."""
+
+    def __init__(self, info: int):
+        super().__init__(f"SingularException({info})")
         self.info = info
 
 

@@ -6,6 +6,9 @@ argument meanings and error behaviour:
   cholesky(DA, uplo)   LinearAlgebra.cholesky on a DArray: cholcopy then the
                        tiled factor (src/array/cholesky.jl:1,19-108)
   cholesky_(DA, uplo)  cholesky! (in place)
+  lu(DA, pivot) / lu_  LinearAlgebra.lu / lu! with RowMaximum or NoPivot
+                       (src/array/lu.jl); ldiv(F, B) / ldiv_(F, B) with an LU
+                       (linalg.jl:221-308); getrf_ the panel's LAPACK call
   ldiv_(C, B)          ldiv!(C::Cholesky{T,<:DMatrix}, B) (src/array/linalg.jl:352-405)
   ishermitian / issymmetric on a DArray (linalg.jl:43-124)
   potrf_, trsm_, syrk_, gemm_, trsv_, gemv_
@@ -63,6 +66,20 @@ def potrf_(uplo: str, A: torch.Tensor, stream=None):
     if rc < 0:
         check(rc)
     return A, info.value
+
+
+def getrf_(A: torch.Tensor, stream=None):
+    """LAPACK.getrf!(A) -> (A, ipiv, info) on a column-major CUDA tensor: the
+    pivoted LU in place, ipiv a 1-based int64 CUDA tensor of min(m, n) rows;
+    synchronises like the reference's getrf!.  The panel task of
+    lu!(A, RowMaximum()) (factor_panel_lapack!, lu.jl:263-304)."""
+    p, r, c, ld = _colmajor(A, "A")
+    ipiv = torch.empty(max(min(r, c), 1), dtype=torch.int64, device=A.device)
+    info = ctypes.c_int(0)
+    rc = lib().dg_getrf(r, c, p, ld, ipiv.data_ptr(), ctypes.byref(info), _stream(stream))
+    if rc < 0:
+        check(rc)
+    return A, ipiv[:min(r, c)], info.value
 
 
 def trsm_(side, uplo, transa, diag, alpha, A, B, stream=None):
@@ -262,12 +279,15 @@ def cholesky(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Ch
     return cholesky_(A.copy(), uplo, check_, stream)
 
 
-def ldiv_(C: Cholesky, B: DArray, stream=None) -> DArray:
-    """ldiv!(C, B): B <- A^-1 B with A = U'U or LL' (linalg.jl:352-405).
+def ldiv_(C, B: DArray, stream=None) -> DArray:
+    """ldiv!(C, B): B <- A^-1 B with A = U'U or LL' (linalg.jl:352-405), or
+    with A = P' L U for an LU (linalg.jl:264-278).
 
     B is an N-vector or an N x r matrix; its row blocking must equal the
     factor's block size (ldiv! re-blocks B to Blocks(min_bsa, min_bsa),
     linalg.jl:362-364)."""
+    if isinstance(C, LU):
+        return _ldiv_lu(C, B, stream)
     F = C.factors
     nb = F.partitioning.blocksize[0]
     if B.shape[0] != F.shape[0]:
@@ -284,6 +304,142 @@ def ldiv_(C: Cholesky, B: DArray, stream=None) -> DArray:
                                            B.tile_ptrs(), _stream(stream))
     check(rc)
     return B
+
+
+class LU:
+    """LinearAlgebra.LU{T,DMatrix{T},DVector{Int}}: factors (L unit lower
+    below the diagonal, U on and above it), ipiv (the 1-based global row
+    interchanges, an int64 CUDA tensor of min(m, n) rows) and info."""
+
+    def __init__(self, factors: DArray, ipiv: torch.Tensor, info: int):
+        self.factors = factors
+        self.ipiv = ipiv
+        self.info = info
+
+    @property
+    def L(self) -> torch.Tensor:
+        F = self.factors.collect()
+        m, n = F.shape
+        k = min(m, n)
+        return torch.tril(F[:, :k], -1) + torch.eye(m, k, dtype=F.dtype, device=F.device)
+
+    @property
+    def U(self) -> torch.Tensor:
+        F = self.factors.collect()
+        k = min(F.shape)
+        return torch.triu(F[:k, :])
+
+    @property
+    def p(self) -> torch.Tensor:
+        """The row permutation (0-based): row t of P A is row p[t] of A."""
+        m = self.factors.shape[0]
+        perm = list(range(m))
+        for i, g in enumerate(self.ipiv.tolist()):
+            r = g - 1
+            perm[i], perm[r] = perm[r], perm[i]
+        return torch.tensor(perm, dtype=torch.int64)
+
+    @property
+    def P(self) -> torch.Tensor:
+        m = self.factors.shape[0]
+        return torch.eye(m, dtype=torch.float64)[self.p]
+
+    def issuccess(self) -> bool:
+        return self.info == 0
+
+    def solve(self, B, stream=None):
+        return ldiv(self, B, stream)
+
+
+_PIVOTS = {"rowmaximum": 1, "nopivot": 0}
+
+
+def _pivot_code(pivot) -> int:
+    key = str(pivot).replace("()", "").replace("_", "").lower()
+    if key not in _PIVOTS:
+        raise ValueError("pivot must be 'RowMaximum' or 'NoPivot'")
+    return _PIVOTS[key]
+
+
+def _chkfinite(A: DArray, stream=None):
+    """LAPACK.chkfinite(A) (linalg.jl:138-148): ArgumentError for Inf/NaN."""
+    if A.shape[0] == A.shape[1] and A.partitioning.blocksize[0] == A.partitioning.blocksize[1]:
+        ok = lib().dg_chkfinite_tiled(A.shape[0], A.partitioning.blocksize[0], A.tile_ptrs(),
+                                      _stream(stream))
+        if ok < 0:
+            check(ok)
+        ok = bool(ok)
+    else:
+        ok = all(bool(torch.isfinite(t).all()) for row in A.chunks for t in row)
+    if not ok:
+        raise ValueError("matrix contains Infs or NaNs")
+
+
+def lu_(A: DArray, pivot="RowMaximum", check_: bool = True, allowsingular: bool = False,
+        stream=None) -> LU:
+    """lu!(DA, RowMaximum()) / lu!(DA, NoPivot()) (src/array/lu.jl:306-410 /
+    5-54): the tiled factorization in place.  Non-square Blocks(mb, nb) are
+    re-blocked to Blocks(min, min) for the factorization and copied back
+    (maybe_copy_buffered, copy.jl:3-37).  check_: chkfinite first, then
+    SingularException(info) for an exactly zero pivot unless allowsingular."""
+    code = _pivot_code(pivot)
+    if A.ndim != 2:
+        raise ValueError("lu needs a 2-D DArray")
+    if check_:
+        _chkfinite(A, stream)
+    m, n = A.shape
+    mb, nbc = A.partitioning.blocksize
+    W = A
+    if mb != nbc:
+        b = min(mb, nbc)
+        W = DArray.from_array(A.collect(), Blocks(b, b), device=A.storage.device)
+    nb = W.partitioning.blocksize[0]
+    ipiv = torch.empty(max(min(m, n), 1), dtype=torch.int64, device=A.storage.device)
+    rc = lib().dg_lu_tiled(m, n, nb, W.tile_ptrs(), code, ipiv.data_ptr(), _stream(stream))
+    if rc < 0:
+        check(rc)
+    if W is not A:
+        A.copy_from(W.collect())
+    info = rc
+    if check_ and info > 0 and not allowsingular:
+        raise _lib.SingularException(info)
+    return LU(A if W is A else W, ipiv[:min(m, n)], info)
+
+
+def lu(A: DArray, pivot="RowMaximum", check_: bool = True, allowsingular: bool = False,
+       stream=None) -> LU:
+    """lu(DA, pivot): _lucopy then lu! (lu.jl:1-3, 306-309)."""
+    return lu_(A.copy(), pivot, check_, allowsingular, stream)
+
+
+def _ldiv_lu(F: LU, B: DArray, stream=None) -> DArray:
+    """ldiv!(F::LU, B) (linalg.jl:264-278), B blocked like the factors."""
+    A = F.factors
+    n = A.shape[0]
+    if A.shape[0] != A.shape[1]:
+        raise ValueError("ldiv! needs a square LU")
+    nb = A.partitioning.blocksize[0]
+    if B.shape[0] != n:
+        raise ValueError("arguments must have the same number of rows")
+    if B.partitioning.blocksize[0] != nb or (B.ndim == 2 and B.partitioning.blocksize[1] != nb):
+        raise ValueError("B must be blocked Blocks(nb, nb) (or Blocks(nb)) like the factors")
+    nrhs = 1 if B.ndim == 1 else B.shape[1]
+    rc = lib().dg_lu_solve_tiled(n, nb, A.tile_ptrs(), F.ipiv.data_ptr(), nrhs, B.tile_ptrs(),
+                                 _stream(stream))
+    check(rc)
+    return B
+
+
+def ldiv(F: LU, B, stream=None) -> DArray:
+    """ldiv(F::LU, B) / F \\ B (linalg.jl:221-262): B (a DArray, torch tensor
+    or numpy array, vector or matrix) staged into a DArray blocked like the
+    factors, solved in place there and returned."""
+    nb = F.factors.partitioning.blocksize[0]
+    src = B.collect() if isinstance(B, DArray) else B
+    t = torch.as_tensor(np.asarray(src)) if isinstance(src, np.ndarray) else src
+    part = Blocks(nb) if t.ndim == 1 else Blocks(nb, nb)
+    BB = DArray.from_array(t.to(torch.float64), part, device=F.factors.storage.device)
+    return _ldiv_lu(F, BB, stream)
 
 
 def _mul_blocks(*arrays):

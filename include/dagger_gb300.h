@@ -391,6 +391,52 @@ int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs, double *c
                              int max_iter, const int *bucket_w, int ctas_per_sm, int *info,
                              double *berr, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * LU factorization (src/array/lu.jl) and the solve with it (linalg.jl:264-308)
+ * ------------------------------------------------------------------------- */
+
+/* LAPACK.getrf!(A) -> (A, ipiv, info) on one column-major m x n matrix in
+ * device memory: the pivoted LU in place, L unit lower below the diagonal and
+ * U on and above it; ipiv (device, min(m, n) int64) the 1-based rows
+ * interchanged with each row, as LAPACK.  Replaces the panel task of
+ * lu!(A, RowMaximum()) (factor_panel_lapack!, src/array/lu.jl:263-304, whose
+ * GPU form is the per-column search_and_update_ipiv! / swaprows_panel! /
+ * update_panel_diag! / update_panel_offdiag! tasks, lu.jl:24-127).  Same
+ * pivots as LAPACK: the first row of largest magnitude; an exactly zero
+ * pivot sets info to its 1-based column and the factorization continues.
+ * Synchronises `stream`; *info_host = info, and the return value is info
+ * (>= 0) or a negative error.  m <= 768 x the device's SMs. */
+int dg_getrf(int m, int n, double *A, int lda, long long *ipiv, int *info_host, void *stream);
+
+/* lu!(A, RowMaximum()) (pivot = 1, lu.jl:306-410) or lu!(A, NoPivot())
+ * (pivot = 0, lu.jl:5-54) of the m x n DArray with Blocks(nb, nb) held as
+ * the mt x nt column-major tile grid `tiles` (tile (i, j) = tiles[i + j*mt],
+ * column-major, ld = its rows; ragged last row and column), in place, as one
+ * cached graph of the reference's task loop: per step the block column's
+ * panel factorization (dg_getrf's algorithm on the gathered panel, or the
+ * diagonal tile without pivoting), its row interchanges applied to every
+ * other block column (swaprows_trail!), TRSM('L','L','N','U') of the row
+ * panel (and, without pivoting, TRSM('R','U','N','N') of the column panel)
+ * and GEMM('N','N',-1) of the trailing tiles, with the FP64 engine chosen by
+ * dg_set_f64_engine (engine 2: emulated trailing updates).  ipiv (device,
+ * min(m, n) int64) receives the 1-based global pivots (1..min(m, n) without
+ * pivoting, as the reference's DVector).  Synchronises `stream`.  Returns 0,
+ * info > 0 (the first exactly zero pivot, 1-based, for
+ * LinearAlgebra._check_lu_success / SingularException), or a negative error.
+ * nb <= 1024, mt <= 256; library-owned workspace (one per device, shared with
+ * the other tiled calls: calls that overlap on the GPU must not share it). */
+int dg_lu_tiled(int m, int n, int nb, double *const *tiles, int pivot, long long *ipiv,
+                void *stream);
+
+/* ldiv!(F::LU, B) (linalg.jl:264-308) for the n x n factors of dg_lu_tiled
+ * (tiles, ipiv) and the n x nrhs right-hand sides held as the tile grid
+ * btiles (Blocks(nb, nb), tile (i, j) = btiles[i + j*mt]), overwritten with
+ * the solution: B's rows permuted by ipiv (_apply_ipiv_rows!, one
+ * permutation per block column of B), then the unit-lower forward and the
+ * upper backward block solves (Dagger.trsm!).  Synchronises `stream`. */
+int dg_lu_solve_tiled(int n, int nb, double *const *tiles, const long long *ipiv, int nrhs,
+                      double *const *btiles, void *stream);
+
 /* Measures the device's FP64 fused-multiply-add throughput (TFLOP/s) with
  * independent FMA chains on every SM; the benchmark's FP64 roofline.  No
  * counterpart in the reference (measurement utility). */

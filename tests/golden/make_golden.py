@@ -14,6 +14,10 @@ Recipes (paths within JuliaParallel/Dagger.jl):
   chol_ragged_U_130_32  a ragged tiling (130 = 4*32 + 2)
   solve_U_128_64_r5     test/array/linalg/solve.jl: A'A + I, DMatrix RHS
   solve_L_96_32_vec     vector right-hand side (trsv! path)
+  lu_rowmax_128_64      test/array/linalg/lu.jl: rand(128, 128), Blocks(64, 64), RowMaximum
+  lu_rowmax_ragged_200x150_64  a rectangular, ragged tiling
+  lu_nopiv_96_32        NoPivot on a diagonally dominant rand(96, 96) + 96 I
+  lu_solve_160_32_r5    lu(A) \\ B with 5 right-hand sides
 """
 import os
 import sys
@@ -23,6 +27,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
+from oracle import lu as olu  # noqa: E402
 from oracle import tiled as o  # noqa: E402
 
 
@@ -66,6 +71,29 @@ def main():
                np.asfortranarray(rng.random((128, 5))), 64, 'U')
     A = o.spd_uniform(96, 3)
     solve_case("solve_L_96_32_vec", A, rng.standard_normal(96), 32, 'L')
+
+    from scipy.linalg import lapack
+
+    def lu_case(name, A, nb, pivot):
+        F, ipiv, info = olu.lu(A, nb, pivot=pivot)
+        assert info == 0
+        d = dict(A=A, nb=np.int64(nb), pivot=np.array(pivot), tiled=F, ipiv=ipiv)
+        if pivot == 'rowmaximum' or np.all(lapack.dgetrf(A)[1] == np.arange(min(A.shape))):
+            d["lapack"] = lapack.dgetrf(A)[0]
+        cases[name] = d
+
+    lu_case("lu_rowmax_128_64", olu.rand_uniform(128, 128, 21), 64, 'rowmaximum')
+    lu_case("lu_rowmax_ragged_200x150_64", olu.rand_uniform(200, 150, 22), 64, 'rowmaximum')
+    A = olu.rand_uniform(96, 96, 23)
+    A[np.diag_indices(96)] += 96.0
+    lu_case("lu_nopiv_96_32", A, 32, 'nopivot')
+    A = olu.rand_uniform(160, 160, 24)
+    B = np.asfortranarray(np.random.default_rng(25).standard_normal((160, 5)))
+    F, ipiv, _ = olu.lu(A, 32)
+    X = olu.ldiv_lu(F, ipiv, B.copy(), 32)
+    lu, piv, _ = lapack.dgetrf(A)
+    cases["lu_solve_160_32_r5"] = dict(A=A, B=B, nb=np.int64(32), tiled=X,
+                                       lapack=lapack.dgetrs(lu, piv, B)[0])
 
     for name, arrs in cases.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)

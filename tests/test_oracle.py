@@ -15,7 +15,8 @@ def _rel(x, y):
     return np.abs(x - y).max() / np.abs(y).max()
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(HERE, "golden", "*.npz"))),
+@pytest.mark.parametrize("path", sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                                         if not os.path.basename(p).startswith("lu_")),
                          ids=lambda p: os.path.basename(p)[:-4])
 def test_golden_fixture(path):
     from oracle import tiled as o
