@@ -126,6 +126,11 @@ int lu_iota(long long *ipiv, int n, cudaStream_t s);
 int trinv_t_f64(char uplo, int n, const double *A, int lda, double *W, int ldw,
                 const int *abort_flag, cudaStream_t s);
 
+// W (n x n, ldw) = L^-1 of the unit lower triangle of A (lda; the diagonal
+// taken as 1), by column-parallel forward substitution on the unit vectors.
+int trinv_unit_lower_f64(int n, const double *A, int lda, double *W, int ldw,
+                         const int *abort_flag, cudaStream_t s);
+
 // Tile upload (upload.cu): the rows x cols block at host (row-major, row
 // stride ldh, page-locked host or device memory) into a column-major tile
 // (ld = rows).  device_readable: whether a kernel may read p.

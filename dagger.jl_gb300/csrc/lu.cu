@@ -43,6 +43,7 @@ constexpr int kLeafThreads = 256;
 constexpr int kLeafWarps = kLeafThreads / 32;
 constexpr int kLeafMaxRows = 768;      // rows one CTA keeps in shared memory
 constexpr int kLeafMaxGrid = 256;      // CTAs of a leaf launch at most
+constexpr int kLeafRowsTarget = 384;
 constexpr int kLeafSwapMax = 2 * kLeafW;
 constexpr int kListHash = 4096;        // >= 4 x the pivots of the widest panel
 constexpr int kMaxPanelPivots = 1024;
@@ -96,11 +97,25 @@ __device__ __forceinline__ void warp_best(double &bv, int &bi) {
   }
 }
 
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // One leaf: columns c0 .. c0+wl-1 of the panel, rows c0 .. c0+nrows-1.
-// Row r (counted from the leaf's diagonal) belongs to CTA r / R.
+// Row r (counted from the leaf's diagonal) belongs to CTA r / R.  Step j:
+// every CTA publishes its candidate row (and the diagonal row's owner that
+// row), arrives at the grid barrier and, while warp 0 waits, applies the
+// previous pivot's rank-1 update to columns j+1.. (deferred one step); then
+// the pivot is read from all candidates, rows j and p trade places, the
+// multipliers are scaled and only column j+1 is updated.  The critical path
+// of a column carries one column of FP64 work; the rest overlaps the wait.
+// A published row gets the deferred update on the fly (the same fma as the
+// deferred pass), so every CTA sees fully updated pivot rows.
 __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
   extern __shared__ double sm[];  // column c of this CTA's rows at sm + c*R
-  __shared__ double prow[kLeafW];
+  __shared__ double prow[kLeafW];   // the current column's pivot row
+  __shared__ double dprow[kLeafW];  // the pivot row of the deferred update
+  __shared__ double jrow_s[kLeafW]; // the displaced diagonal row (the pivot's owner)
   __shared__ double wv[kLeafWarps];
   __shared__ int wi[kLeafWarps];
   __shared__ int piv[kLeafW];
@@ -117,12 +132,19 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
       sm[c * R + r] = D[(size_t)(r0 + r) + (size_t)c * a.ld];
   __syncthreads();
   const int jmax = min(a.wl, a.nrows);
+  int dj = -1;  // the pivot whose update of columns dj+2.. is pending
   for (int j = 0; j < jmax; j++) {
     const int par = j & 1;
     double *sval = a.sval + par * G;
     int *sidx = a.sidx + par * G;
     double *srow = a.srow + (size_t)par * G * kLeafW;
     double *jrow = a.jrow + par * kLeafW;
+    // the value of row r (local), column c with the pending update applied
+    auto current = [&](int r, int c) {
+      double v = sm[c * R + r];
+      if (dj >= 0 && c >= dj + 2) v = fma(-sm[dj * R + r], dprow[c], v);
+      return v;
+    };
     // 1. this CTA's candidate: its first row of largest |a(r, j)|, r >= j
     if (!a.nopiv) {
       double bv = -1.0;
@@ -154,14 +176,20 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
       }
       __syncthreads();
       const int b = s_best;
-      if (b != INT_MAX && tid < a.wl) __stcg(&srow[(size_t)g * kLeafW + tid], sm[tid * R + (b - r0)]);
+      if (b != INT_MAX && tid < a.wl) __stcg(&srow[(size_t)g * kLeafW + tid], current(b - r0, tid));
     }
-    if (j >= r0 && j < r0 + rn && tid < a.wl) __stcg(&jrow[tid], sm[tid * R + (j - r0)]);
-    // 2. grid barrier (bounded)
+    if (j >= r0 && j < r0 + rn && tid < a.wl) __stcg(&jrow[tid], current(j - r0, tid));
+    // 2. arrive; the deferred update runs while warp 0 waits (bounded)
     __syncthreads();
+    if (tid == 0) red_release_add(a.counter, 1u);
+    if (dj >= 0 && warp > 0) {
+      for (int r = tid - 32; r < rn; r += kLeafThreads - 32) {
+        if (r0 + r <= dj) continue;
+        const double l = sm[dj * R + r];
+        for (int c = dj + 2; c < a.wl; c++) sm[c * R + r] = fma(-l, dprow[c], sm[c * R + r]);
+      }
+    }
     if (tid == 0) {
-      __threadfence();
-      atomicAdd(a.counter, 1u);
       const unsigned target = (unsigned)G * (unsigned)(j + 1);
       int stop = 0;
       if (ld_acquire_u32(a.counter) < target) {
@@ -178,46 +206,54 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
           }
         }
       }
-      __threadfence();
       s_stop = stop;
     }
     __syncthreads();
     if (s_stop) return;
-    // 3. the column's pivot, the same in every CTA
+    // 3. the column's pivot, the same in every CTA: all candidates loaded at once
     if (warp == 0) {
       double bv = -1.0;
       int bi = INT_MAX;
       if (!a.nopiv) {
-        for (int q = lane; q < G; q += 32) {
-          const int i = __ldcg(&sidx[q]);
-          const double v = __ldcg(&sval[q]);
-          if (i != INT_MAX && better(v, i, bv, bi)) {
-            bv = v;
-            bi = i;
-          }
+        double cv[kLeafMaxGrid / 32];
+        int ci[kLeafMaxGrid / 32];
+#pragma unroll
+        for (int t = 0; t < kLeafMaxGrid / 32; t++) {
+          const int q = lane + 32 * t;
+          ci[t] = q < G ? __ldcg(&sidx[q]) : INT_MAX;
+          cv[t] = q < G ? __ldcg(&sval[q]) : -1.0;
         }
+#pragma unroll
+        for (int t = 0; t < kLeafMaxGrid / 32; t++)
+          if (ci[t] != INT_MAX && better(cv[t], ci[t], bv, bi)) {
+            bv = cv[t];
+            bi = ci[t];
+          }
         warp_best(bv, bi);
       }
       if (lane == 0) s_best = (bi == INT_MAX) ? j : bi;
     }
     __syncthreads();
     const int p = s_best;
+    const int gp = p / R;
+    // the pivot row for everyone; the displaced row j for the pivot's owner
     if (tid < a.wl)
-      prow[tid] = (p == j) ? __ldcg(&jrow[tid]) : __ldcg(&srow[(size_t)(p / R) * kLeafW + tid]);
+      prow[tid] = (p == j) ? __ldcg(&jrow[tid]) : __ldcg(&srow[(size_t)gp * kLeafW + tid]);
+    else if (tid >= 32 && tid < 32 + a.wl && p != j && g == gp)
+      jrow_s[tid - 32] = __ldcg(&jrow[tid - 32]);
     if (tid == 0) piv[j] = p;
     __syncthreads();
     // 4. rows j and p trade places
     if (p != j && tid < a.wl) {
       if (j >= r0 && j < r0 + rn) sm[tid * R + (j - r0)] = prow[tid];
-      if (p >= r0 && p < r0 + rn) sm[tid * R + (p - r0)] = __ldcg(&jrow[tid]);
+      if (p >= r0 && p < r0 + rn) sm[tid * R + (p - r0)] = jrow_s[tid];
     }
     if (g == 0 && tid == 0) {
       a.lpiv[a.c0 + j] = a.c0 + p;
       if (prow[j] == 0.0) atomicMin(a.info, a.info_offset + a.c0 + j + 1);
     }
     __syncthreads();
-    // 5. multipliers below the diagonal, then the rank-1 update of the
-    //    leaf's remaining columns
+    // 5. multipliers below the diagonal; column j+1 now, the others deferred
     const double pv = prow[j];
     const bool scale = (pv != 0.0);
     const bool recip = a.nopiv || fabs(pv) >= DBL_MIN;
@@ -229,10 +265,21 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
         l = recip ? l * rinv : l / pv;
         sm[j * R + r] = l;
       }
-      for (int c = j + 1; c < a.wl; c++) sm[c * R + r] = fma(-l, prow[c], sm[c * R + r]);
+      if (j + 1 < a.wl) sm[(j + 1) * R + r] = fma(-l, prow[j + 1], sm[(j + 1) * R + r]);
     }
+    if (tid < a.wl) dprow[tid] = prow[tid];
+    dj = j;
     __syncthreads();
   }
+  // the last pivot's deferred update
+  if (dj >= 0) {
+    for (int r = tid; r < rn; r += kLeafThreads) {
+      if (r0 + r <= dj) continue;
+      const double l = sm[dj * R + r];
+      for (int c = dj + 2; c < a.wl; c++) sm[c * R + r] = fma(-l, dprow[c], sm[c * R + r]);
+    }
+  }
+  __syncthreads();
   for (int c = 0; c < a.wl; c++)
     for (int r = tid; r < rn; r += kLeafThreads)
       D[(size_t)(r0 + r) + (size_t)c * a.ld] = sm[c * R + r];
@@ -473,7 +520,10 @@ struct PanelCtx {
 
 int leaf_launch(const PanelCtx &c, int c0, int wl) {
   const int nrows = c.mrows - c0;
-  int G = (nrows + 63) / 64;
+  // about kLeafRowsTarget rows per CTA: enough rows to keep the per-column
+  // barrier cheap and leave most SMs to concurrent work, few enough that the
+  // deferred FP64 updates hide behind the barrier waits
+  int G = max((nrows + kLeafMaxRows - 1) / kLeafMaxRows, (nrows + kLeafRowsTarget - 1) / kLeafRowsTarget);
   G = min(G, min(dg_num_sms(), kLeafMaxGrid));
   if (G < 1) G = 1;
   const int R = (nrows + G - 1) / G;

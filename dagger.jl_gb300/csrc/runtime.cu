@@ -314,6 +314,10 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
       }
       break;
     }
+    case dg::OP_LU_LINV:
+      out.push_back({dg::footprint(t.a, t.n, t.n, t.lda, E), DG_IN});
+      out.push_back({dg::footprint(t.c, t.n, t.n, t.ldc, E), DG_OUT});
+      break;
     case dg::OP_LU_PERM:
       out.push_back({dg::footprint(t.a, t.k, 1, 1, 8), DG_IN});
       out.push_back({dg::footprint(t.c, t.n, 1, 1, 4), DG_OUT});
@@ -493,6 +497,8 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
       return lu_laswp_tiles((double *const *)t.a, t.k, t.ldb, t.m, t.n, (const int *)t.b, t.ldc, s);
     case OP_LU_PERM:
       return lu_perm((const long long *)t.a, t.k, t.n, (int *)t.c, s);
+    case OP_LU_LINV:
+      return trinv_unit_lower_f64(t.n, t.a, t.lda, t.c, t.ldc, info, s);
     case OP_LU_ROWS:
       return lu_rows_tiles((double *const *)t.a, t.k, t.ldb, t.m, t.n, (const int *)t.b, t.c, s);
   }
@@ -1626,6 +1632,9 @@ LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated) {
     off += L.ozp_bytes;
     L.ring = off;
     off += (size_t)kOzRingDepth * (mt + nt) * oz_slot_bytes((nb + 7) / 8 * 8, nb);
+    L.winv_bytes = r256((size_t)nb * nb * 8);
+    L.winv = off;
+    off += (size_t)kOzRingDepth * L.winv_bytes;
   }
   L.total = off;
   return L;
@@ -1640,8 +1649,8 @@ LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated) {
 // panel solved with TRSM('R', 'U', 'N', 'N').  With the emulated engine the
 // rows of L(i, k) and the columns of U(k, j) are cut into slices once per
 // step (ring slots (k mod depth, i) and (k mod depth, mt + j)) and every
-// trailing tile takes one emulated product; the row panel's TRSMs run their
-// recursion's updates emulated, with the slot of U(k, j) as scratch.
+// trailing tile takes one emulated product; each row panel tile is one
+// emulated product with the inverse of L(k, k).
 void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, bool pivot,
                      void *ws, long long *ipiv, bool emulated) {
   const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb, steps = mt < nt ? mt : nt;
@@ -1712,6 +1721,19 @@ void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, b
       }
     }
     if (k + 1 >= nt) continue;
+    // Emulated engine: the row panel's TRSMs become products with the inverse
+    // W = L(k, k)^-1, formed once per step by substitution; W's rows go to
+    // slot (k mod depth, k) with its unit diagonal kept apart (exact).
+    double *Wk = (double *)(w + L.winv + (size_t)(k % kOzRingDepth) * L.winv_bytes);
+    if (emulated) {
+      memset(&t, 0, sizeof t);
+      t.op = OP_LU_LINV; t.n = kk; t.a = T(k, k); t.lda = rows(k); t.c = Wk; t.ldc = kk;
+      add(0);
+      memset(&t, 0, sizeof t);
+      t.op = OP_OZ_SPLIT; t.a = Wk; t.lda = kk; t.m = kk; t.n = kk; t.trans = 'T'; t.diag = 'Z';
+      t.c = slot(k, k); t.ldc = ldk; t.k = nb;
+      add(0);
+    }
     if (emulated)
       for (int i = k + 1; i < mt; i++) {  // the rows of L(i, k): A-vectors of length kk
         memset(&t, 0, sizeof t);
@@ -1721,12 +1743,23 @@ void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, b
       }
     for (int j = k + 1; j < nt; j++) {
       const int lvl = j - k - 1;
-      memset(&t, 0, sizeof t);  // U(k, j) = L(k, k)^-1 A(k, j)
-      t.op = emulated ? OP_OZ_TRSM : DG_OP_TRSM; t.side = 'L'; t.uplo = 'L'; t.transa = 'N';
-      t.diag = 'U'; t.m = kk; t.n = cols(j); t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
-      t.c = T(k, j); t.ldc = rows(k);
-      if (emulated) { t.b = slot(k, mt + j); t.ldb = slot_units; }
-      add(lvl);
+      if (emulated) {  // U(k, j) = W A(k, j) = A(k, j) + offdiag(W) A(k, j)
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_SPLIT; t.trans = 'N'; t.a = T(k, j); t.lda = rows(k); t.m = kk;
+        t.n = cols(j); t.c = slot(k, mt + j); t.ldc = ldk; t.k = nb;
+        add(lvl);
+        memset(&t, 0, sizeof t);
+        t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = kk; t.n = cols(j); t.k = kk; t.alpha = 1.0;
+        t.beta = 0.0; t.a = slot(k, k); t.b = slot(k, mt + j); t.lda = ldk; t.ldb = nb;
+        t.c = T(k, j); t.ldc = rows(k); t.side = 'A';
+        add(lvl);
+      } else {  // U(k, j) = L(k, k)^-1 A(k, j)
+        memset(&t, 0, sizeof t);
+        t.op = DG_OP_TRSM; t.side = 'L'; t.uplo = 'L'; t.transa = 'N'; t.diag = 'U';
+        t.m = kk; t.n = cols(j); t.alpha = 1.0; t.a = T(k, k); t.lda = rows(k);
+        t.c = T(k, j); t.ldc = rows(k);
+        add(lvl);
+      }
       if (k + 1 >= mt) continue;
       if (emulated) {  // the columns of U(k, j): B-vectors of length kk
         memset(&t, 0, sizeof t);
@@ -1737,10 +1770,11 @@ void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, b
       for (int i = k + 1; i < mt; i++) {  // A(i, j) -= L(i, k) U(k, j)
         memset(&t, 0, sizeof t);
         if (emulated) {
+          // one output block per CTA: short CTAs hand their SMs back soon to
+          // the panel's leaves, which need many SMs at once
           t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = rows(i); t.n = cols(j); t.k = kk;
           t.alpha = -1.0; t.beta = 1.0; t.a = slot(k, i); t.b = slot(k, mt + j);
           t.lda = ldk; t.ldb = nb; t.c = T(i, j); t.ldc = rows(i);
-          if (lvl > 0) t.diag = 'P';
         } else {
           t.op = DG_OP_GEMM; t.transa = 'N'; t.transb = 'N'; t.m = rows(i); t.n = cols(j);
           t.k = kk; t.alpha = -1.0; t.beta = 1.0; t.a = T(i, k); t.lda = rows(i);

@@ -63,7 +63,9 @@ constexpr int OP_LU_PANEL = 109;
 constexpr int OP_LU_LASWP = 110;
 constexpr int OP_LU_PERM = 111;
 constexpr int OP_LU_ROWS = 112;
-constexpr int kOpLast = OP_LU_ROWS;
+//   OP_LU_LINV   c (n x n, ldc) = L^-1 of the unit lower triangle of a (lda)
+constexpr int OP_LU_LINV = 113;
+constexpr int kOpLast = OP_LU_LINV;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
 constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);
@@ -127,7 +129,7 @@ void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const
 // the slice slots of the trailing updates.
 struct LuLayout {
   size_t status = 0, info = 4, leaf = 256, lpiv = 0, lists = 0, panel = 0, panel_bytes = 0,
-         ozp = 0, ozp_bytes = 0, ring = 0, total = 0;
+         ozp = 0, ozp_bytes = 0, ring = 0, winv = 0, winv_bytes = 0, total = 0;
   int list_cap = 0;        // entries of one step's destination (and source) list
   size_t list_stride = 0;  // ints per step
 };

@@ -564,6 +564,20 @@ int trinv_t_f64(char uplo, int n, const double *A, int lda, double *W, int ldw,
   return trsm_cols<double>(tv, n, W, up ? 1 : ldw, up ? ldw : 1, n, abort_flag, nullptr, s, 1);
 }
 
+int trinv_unit_lower_f64(int n, const double *A, int lda, double *W, int ldw,
+                         const int *abort_flag, cudaStream_t s) {
+  if (n <= 0) return 0;
+  if (n > TC_MAX_LEN) return DG_ERR_UNSUPPORTED;
+  // L W = I, left side: column c of W is the solve with the unit vector e_c
+  TriView<double> tv;
+  tv.T_ = A;
+  tv.ld = lda;
+  tv.trans = false;
+  tv.lower = true;
+  tv.unit = true;
+  return trsm_cols<double>(tv, n, W, 1, ldw, n, abort_flag, nullptr, s, 1);
+}
+
 int trsm_f32(char side, char uplo, char transa, char diag, int m, int n, float alpha,
              const float *A, long long lda, float *B, long long ldb, const int *abort_flag,
              cudaStream_t s, const int *abort2) {
