@@ -42,7 +42,8 @@ constexpr int kLeafW = 32;             // columns of one leaf launch
 constexpr int kLeafThreads = 256;
 constexpr int kLeafWarps = kLeafThreads / 32;
 constexpr int kLeafMaxRows = 768;      // rows one CTA keeps in shared memory
-constexpr int kLeafMaxGrid = 256;      // CTAs of a leaf launch at most
+constexpr int kLeafMaxGrid = 96;       // CTAs of a leaf launch at most (their candidate rows
+                                       // sit in shared memory beside the strip)
 constexpr int kLeafRowsTarget = 384;
 constexpr int kLeafSwapMax = 2 * kLeafW;
 constexpr int kListHash = 4096;        // >= 4 x the pivots of the widest panel
@@ -112,7 +113,10 @@ __device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
 // A published row gets the deferred update on the fly (the same fma as the
 // deferred pass), so every CTA sees fully updated pivot rows.
 __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
-  extern __shared__ double sm[];  // column c of this CTA's rows at sm + c*R
+  extern __shared__ double sm[];  // column c of this CTA's rows at sm + c*R, then crow
+  double *crow = sm + (size_t)a.wl * a.R;  // [G][kLeafW] the candidate rows
+  __shared__ double cval[kLeafMaxGrid];
+  __shared__ int cidx[kLeafMaxGrid];
   __shared__ double prow[kLeafW];   // the current column's pivot row
   __shared__ double dprow[kLeafW];  // the pivot row of the deferred update
   __shared__ double jrow_s[kLeafW]; // the displaced diagonal row (the pivot's owner)
@@ -164,19 +168,18 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
         wi[warp] = bi;
       }
       __syncthreads();
+      bv = wv[0];
+      bi = wi[0];
+      for (int w = 1; w < kLeafWarps; w++)
+        if (better(wv[w], wi[w], bv, bi)) {
+          bv = wv[w];
+          bi = wi[w];
+        }
       if (tid == 0) {
-        for (int w = 1; w < kLeafWarps; w++)
-          if (better(wv[w], wi[w], bv, bi)) {
-            bv = wv[w];
-            bi = wi[w];
-          }
         __stcg(&sval[g], bv);
         __stcg(&sidx[g], bi);
-        s_best = bi;
       }
-      __syncthreads();
-      const int b = s_best;
-      if (b != INT_MAX && tid < a.wl) __stcg(&srow[(size_t)g * kLeafW + tid], current(b - r0, tid));
+      if (bi != INT_MAX && tid < a.wl) __stcg(&srow[(size_t)g * kLeafW + tid], current(bi - r0, tid));
     }
     if (j >= r0 && j < r0 + rn && tid < a.wl) __stcg(&jrow[tid], current(j - r0, tid));
     // 2. arrive; the deferred update runs while warp 0 waits (bounded)
@@ -210,24 +213,26 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
     }
     __syncthreads();
     if (s_stop) return;
-    // 3. the column's pivot, the same in every CTA: all candidates loaded at once
+    // 3. every candidate record and the diagonal row in one round trip, then
+    //    the column's pivot, the same in every CTA
+    if (!a.nopiv) {
+      for (int e = tid; e < G * kLeafW; e += kLeafThreads) crow[e] = __ldcg(&srow[e]);
+      for (int q = tid; q < G; q += kLeafThreads) {
+        cval[q] = __ldcg(&sval[q]);
+        cidx[q] = __ldcg(&sidx[q]);
+      }
+    }
+    if (tid >= kLeafThreads - kLeafW && tid - (kLeafThreads - kLeafW) < a.wl)
+      jrow_s[tid - (kLeafThreads - kLeafW)] = __ldcg(&jrow[tid - (kLeafThreads - kLeafW)]);
+    __syncthreads();
     if (warp == 0) {
       double bv = -1.0;
       int bi = INT_MAX;
       if (!a.nopiv) {
-        double cv[kLeafMaxGrid / 32];
-        int ci[kLeafMaxGrid / 32];
-#pragma unroll
-        for (int t = 0; t < kLeafMaxGrid / 32; t++) {
-          const int q = lane + 32 * t;
-          ci[t] = q < G ? __ldcg(&sidx[q]) : INT_MAX;
-          cv[t] = q < G ? __ldcg(&sval[q]) : -1.0;
-        }
-#pragma unroll
-        for (int t = 0; t < kLeafMaxGrid / 32; t++)
-          if (ci[t] != INT_MAX && better(cv[t], ci[t], bv, bi)) {
-            bv = cv[t];
-            bi = ci[t];
+        for (int q = lane; q < G; q += 32)
+          if (cidx[q] != INT_MAX && better(cval[q], cidx[q], bv, bi)) {
+            bv = cval[q];
+            bi = cidx[q];
           }
         warp_best(bv, bi);
       }
@@ -235,12 +240,7 @@ __global__ void __launch_bounds__(kLeafThreads, 1) lu_leaf_kernel(LeafArgs a) {
     }
     __syncthreads();
     const int p = s_best;
-    const int gp = p / R;
-    // the pivot row for everyone; the displaced row j for the pivot's owner
-    if (tid < a.wl)
-      prow[tid] = (p == j) ? __ldcg(&jrow[tid]) : __ldcg(&srow[(size_t)gp * kLeafW + tid]);
-    else if (tid >= 32 && tid < 32 + a.wl && p != j && g == gp)
-      jrow_s[tid - 32] = __ldcg(&jrow[tid - 32]);
+    if (tid < a.wl) prow[tid] = (p == j) ? jrow_s[tid] : crow[(p / R) * kLeafW + tid];
     if (tid == 0) piv[j] = p;
     __syncthreads();
     // 4. rows j and p trade places
@@ -476,7 +476,7 @@ std::once_flag g_attr_once;
 void set_attributes() {
   std::call_once(g_attr_once, [] {
     cudaFuncSetAttribute(lu_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kLeafW * kLeafMaxRows * 8);
+                         (kLeafW * kLeafMaxRows + kLeafMaxGrid * kLeafW) * 8);
     cudaFuncSetAttribute(lu_laswp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kLaswpWarps * 2 * kMaxPanelPivots * 8);
     cudaFuncSetAttribute(lu_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -548,7 +548,7 @@ int leaf_launch(const PanelCtx &c, int c0, int wl) {
   a.sidx = l.sidx;
   a.srow = l.srow;
   a.jrow = l.jrow;
-  lu_leaf_kernel<<<G, kLeafThreads, (size_t)wl * R * 8, c.s>>>(a);
+  lu_leaf_kernel<<<G, kLeafThreads, ((size_t)wl * R + (size_t)G * kLeafW) * 8, c.s>>>(a);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;

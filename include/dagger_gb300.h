@@ -405,7 +405,7 @@ int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs, double *c
  * pivots as LAPACK: the first row of largest magnitude; an exactly zero
  * pivot sets info to its 1-based column and the factorization continues.
  * Synchronises `stream`; *info_host = info, and the return value is info
- * (>= 0) or a negative error.  m <= 768 x the device's SMs. */
+ * (>= 0) or a negative error.  m <= 73728 (DG_ERR_UNSUPPORTED above). */
 int dg_getrf(int m, int n, double *A, int lda, long long *ipiv, int *info_host, void *stream);
 
 /* lu!(A, RowMaximum()) (pivot = 1, lu.jl:306-410) or lu!(A, NoPivot())
@@ -423,7 +423,7 @@ int dg_getrf(int m, int n, double *A, int lda, long long *ipiv, int *info_host, 
  * pivoting, as the reference's DVector).  Synchronises `stream`.  Returns 0,
  * info > 0 (the first exactly zero pivot, 1-based, for
  * LinearAlgebra._check_lu_success / SingularException), or a negative error.
- * nb <= 1024, mt <= 256; library-owned workspace (one per device, shared with
+ * nb <= 1024, mt <= 256, m <= 73728; library-owned workspace (one per device, shared with
  * the other tiled calls: calls that overlap on the GPU must not share it). */
 int dg_lu_tiled(int m, int n, int nb, double *const *tiles, int pivot, long long *ipiv,
                 void *stream);
