@@ -6,6 +6,7 @@ a profiler can capture exactly that kernel (ncu -k regex:<name> -c N).
     python -m dagger_gb300.profile_kernels trsm_f64   [--nb 1024]
     python -m dagger_gb300.profile_kernels batched    [--count 2000]
     python -m dagger_gb300.profile_kernels oz_gemm    [--m 8192] [--k 1024]
+    python -m dagger_gb300.profile_kernels lu_panel   [--m 32768] [--k 1024]
 
 gemm_f64   the FP64 trailing-update tile GEMM of the plain path,
            C(nb x nb) -= A' B with nb x nb tiles (2 nb^3 flops per launch)
@@ -16,6 +17,10 @@ batched    the persistent batched launch on `count` systems, n in [32, 1024]
 oz_gemm    the emulated FP64 GEMM (engine 2) on an m x m output with K = k:
            two split launches and one oz_gemm_kernel launch per call
            (2 m^2 k FP64 flops, 28 BF16 products of 2 m^2 k flops each)
+lu_panel   the pivoted panel factorization of the tiled LU (dg_getrf) on an
+           m x k column-major matrix (uniform [0, 1), seed 5) with the emulated
+           engine: 32-column leaf launches and the recursion's emulated
+           updates; the matrix is restored before every call
 Each prints the per-launch time measured with CUDA events.
 """
 from __future__ import annotations
@@ -42,7 +47,8 @@ def _time(fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched", "oz_gemm"])
+    ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched", "oz_gemm",
+                                       "lu_panel"])
     ap.add_argument("--nb", type=int, default=1024)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--k", type=int, default=1024)
@@ -53,6 +59,26 @@ def main(argv=None):
     L = _lib.lib()
     s = _stream(None)
     dev = torch.device("cuda")
+    if a.kernel == "lu_panel":
+        from . import linalg
+        old = linalg.set_f64_engine("emulated")
+        g = torch.Generator(device=dev)
+        g.manual_seed(5)
+        A0 = torch.rand(a.k, a.m, generator=g, device=dev, dtype=torch.float64).t()
+        A = torch.empty_strided((a.m, a.k), (1, a.m), dtype=torch.float64, device=dev)
+        total = 0.0
+        for _ in range(a.reps):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _, _, info = linalg.getrf_(A)
+            e1.record()
+            torch.cuda.synchronize()
+            total += e0.elapsed_time(e1)
+        linalg.set_f64_engine(old)
+        print(f"lu_panel m={a.m} k={a.k}: {total / a.reps:.2f} ms per panel (info {info})")
+        return
     if a.kernel == "gemm_f64":
         nb = a.nb
         A, B, C = (torch.randn(nb, nb, dtype=torch.float64, device=dev) for _ in range(3))

@@ -309,4 +309,43 @@ function mul_gb300!(C::DArray{Float64,2}, A::DArray{Float64,2}, B::DArray{Float6
     return C
 end
 
+"""
+    lu_gb300!(A::DArray{Float64,2}, pivot=RowMaximum(); check=true, allowsingular=false) -> LU
+
+lu!(A, RowMaximum()) / lu!(A, NoPivot()) (src/array/lu.jl:5-54, 306-410) as
+one library graph (dg_lu_tiled) on Blocks(nb, nb) chunks that are
+GB300Arrays.  ipiv stays on the device (GB300Array{Int64,1}); info > 0 is
+the first exactly zero pivot, checked as LinearAlgebra._check_lu_success.
+"""
+function lu_gb300!(A::DArray{Float64,2}, pivot::Union{RowMaximum,NoPivot}=RowMaximum();
+                   check::Bool=true, allowsingular::Bool=false)
+    m, n = size(A)
+    nb = A.partitioning.blocksize[1]
+    ipiv = GB300Array{Int64,1}(undef, (max(min(m, n), 1),))
+    info = ccall((:dg_lu_tiled, libdg), Cint,
+                 (Cint, Cint, Cint, Ptr{Ptr{Float64}}, Cint, Ptr{Int64}, Ptr{Cvoid}),
+                 m, n, nb, tile_pointers(A), pivot isa RowMaximum ? 1 : 0, pointer(ipiv), C_NULL)
+    dgcheck(info)
+    check && LinearAlgebra._check_lu_success(Int(info), allowsingular)
+    return LU(A, ipiv, convert(LinearAlgebra.BlasInt, info))
+end
+
+"""
+    ldiv_gb300!(F::LU{Float64,<:DArray}, B::DArray) -> B
+
+ldiv!(F::LU, B) (src/array/linalg.jl:264-308) as one library call
+(dg_lu_solve_tiled): B's rows permuted by ipiv, then the unit-lower and the
+upper block solves.  B is blocked like the factors.
+"""
+function ldiv_gb300!(F::LU{Float64,<:DArray}, B::DArray{Float64})
+    A = F.factors
+    n = size(A, 1)
+    nb = A.partitioning.blocksize[1]
+    nrhs = ndims(B) == 1 ? 1 : size(B, 2)
+    dgcheck(ccall((:dg_lu_solve_tiled, libdg), Cint,
+                  (Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Int64}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
+                  n, nb, tile_pointers(A), pointer(F.ipiv), nrhs, tile_pointers(B), C_NULL))
+    return B
+end
+
 end # module
