@@ -11,10 +11,12 @@
 // LAPACK getrf (factor_panel_lapack!, lu.jl:263-304) or, on GPUs, column by
 // column as four kinds of tasks per column (search_and_update_ipiv!,
 // swaprows_panel!, update_panel_diag!, update_panel_offdiag!, lu.jl:24-127);
-// here a leaf is ONE launch of up to one CTA per SM: every CTA keeps a
-// contiguous range of the strip's rows in shared memory, and the grid agrees
-// on each column's pivot through one grid barrier per column (a counter in
-// global memory; every wait is bounded and records DG_ERR_TIMEOUT).  The
+// here a leaf is ONE launch of up to 96 CTAs (about 384 rows each, so most
+// SMs stay free for the trailing updates): every CTA keeps a contiguous range
+// of the strip's rows in shared memory, and the grid agrees on each column's
+// pivot through one grid barrier per column (a counter in global memory;
+// every wait is bounded and records DG_ERR_TIMEOUT), with the rank-1 updates
+// of the later columns deferred into the barrier waits.  The
 // result is LAPACK's: the pivot of a column is the first row of largest
 // magnitude (idamax), multipliers are scaled by the reciprocal of the pivot
 // when it is at least the smallest normal number, and an exactly zero pivot
