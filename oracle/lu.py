@@ -186,6 +186,39 @@ def ldiv_lu(F: np.ndarray, ipiv: np.ndarray, B: np.ndarray, nb: int):
     return B
 
 
+def panel_row_list(ipiv_k: np.ndarray, row0: int):
+    """One panel's interchanges as the (destination, source) row list the CUDA
+    path applies to every other block column, rows counted from row0: the
+    interchanges replayed on the contents of the first len(ipiv_k) rows and
+    of the rows below them that the pivots reach.  Restated here so that the
+    tests pin it against the reference's pair-by-pair swaprows_trail!."""
+    npiv = len(ipiv_k)
+    top = list(range(npiv))
+    below = {}
+    for p, g in enumerate(ipiv_k):
+        r = int(g) - 1 - row0
+        if r == p:
+            continue
+        if r < npiv:
+            top[p], top[r] = top[r], top[p]
+        else:
+            below.setdefault(r, r)
+            top[p], below[r] = below[r], top[p]
+    out = [(p, top[p]) for p in range(npiv) if top[p] != p]
+    out += [(r, v) for r, v in below.items() if v != r]
+    return out
+
+
+def apply_row_list(L, X: np.ndarray):
+    """X[dst] = X[src] for every pair, all sources read before any write."""
+    if not L:
+        return X
+    dst = np.array([d for d, _ in L])
+    src = np.array([s for _, s in L])
+    X[dst, ...] = X[src, ...].copy()
+    return X
+
+
 def permutation(ipiv: np.ndarray, m: int) -> np.ndarray:
     """perm[t] = the row of A at row t of P A."""
     perm = np.arange(m)

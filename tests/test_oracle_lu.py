@@ -114,6 +114,32 @@ def test_apply_ipiv_rows_is_the_permutation():
     assert np.array_equal(got, B[o.permutation(ipiv, n), :])
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_row_list_equals_pairwise_swaps(seed):
+    """The CUDA path applies a panel's interchanges to the other block columns
+    as one (destination, source) row list; the reference swaps tile pair by
+    tile pair in pivot order (swaprows_trail!).  Both must move the same rows,
+    including pivots that hit the same row twice and pivots inside the panel."""
+    r = np.random.default_rng(seed)
+    nb, mt, k = 16, 5, 1
+    m = nb * mt
+    row0 = k * nb
+    ipk = np.empty(nb, dtype=np.int64)
+    for p in range(nb):                       # LAPACK form: ipiv[p] >= row0 + p + 1
+        lo = row0 + p
+        ipk[p] = (lo if r.random() < 0.2 else r.integers(lo, m)) + 1
+    if seed % 2:                              # a row chosen twice
+        ipk[nb - 1] = ipk[nb // 2] = max(ipk[nb // 2], row0 + nb)
+    X = np.asfortranarray(r.standard_normal((m, 3)))
+    ref = X.copy(order='F')
+    for i in range(k, mt):
+        o.swaprows_trail(ref[row0:row0 + nb, :], ref[i * nb:(i + 1) * nb, :], ipk, i, nb)
+    got = X[row0:, :].copy()
+    o.apply_row_list(o.panel_row_list(ipk, row0), got)
+    assert np.array_equal(got, ref[row0:, :])
+    assert len(o.panel_row_list(ipk, row0)) <= 2 * nb
+
+
 @pytest.mark.parametrize("name", ["lu_rowmax_128_64", "lu_rowmax_ragged_200x150_64",
                                   "lu_nopiv_96_32", "lu_solve_160_32_r5"])
 def test_golden_fixtures(name):
