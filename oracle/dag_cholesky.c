@@ -1,5 +1,6 @@
 /*
- * CPU restatement of Dagger.jl's datadeps tiled Cholesky and Cholesky solve.
+ * CPU restatement of Dagger.jl's datadeps tiled Cholesky and Cholesky solve,
+ * and of the pivoted tiled LU (lu!(A, RowMaximum())).
  *
  * TEST INFRASTRUCTURE ONLY: this is the oracle's threaded form, used as the
  * checker at sizes the Python restatement is too slow for and as the CPU
@@ -11,6 +12,11 @@
  *                                        and their In/InOut arguments
  *   src/array/trsm.jl:89-140               the left-side block solves ldiv! uses
  *   src/array/linalg.jl:386-403            ldiv! solve order per uplo
+ *   src/array/lu.jl:263-304, :351-407      lu!(A, RowMaximum()) with the LAPACK
+ *                                        panel (factor_panel_lapack!, InOut on
+ *                                        every tile of the block column),
+ *                                        swaprows_trail! per tile pair, TRSM,
+ *                                        GEMM
  *   src/datadeps/queue.jl:43-53,
  *   src/datadeps/aliasing.jl:740-776       the dependency rules: a writer waits
  *                                        for the last writer and the readers
@@ -37,11 +43,18 @@ typedef void (*dtrsm_fn)(char *, char *, char *, char *, int *, int *, double *,
 typedef void (*dsyrk_fn)(char *, char *, int *, int *, double *, double *, int *, double *,
                          double *, int *);
 typedef void (*dpotrf_fn)(char *, int *, double *, int *, int *);
+typedef void (*dgetrf_fn)(int *, int *, double *, int *, int *, int *);
 
 static dgemm_fn g_dgemm;
 static dtrsm_fn g_dtrsm;
 static dsyrk_fn g_dsyrk;
 static dpotrf_fn g_dpotrf;
+static dgetrf_fn g_dgetrf;
+
+int oracle_set_getrf(void *dgetrf) {
+  g_dgetrf = (dgetrf_fn)dgetrf;
+  return dgetrf ? 0 : -1;
+}
 
 int oracle_set_blas(void *dgemm, void *dtrsm, void *dsyrk, void *dpotrf) {
   g_dgemm = (dgemm_fn)dgemm;
@@ -51,7 +64,7 @@ int oracle_set_blas(void *dgemm, void *dtrsm, void *dsyrk, void *dpotrf) {
   return (dgemm && dtrsm && dsyrk && dpotrf) ? 0 : -1;
 }
 
-enum { T_POTRF, T_TRSM, T_SYRK, T_GEMM };
+enum { T_POTRF, T_TRSM, T_SYRK, T_GEMM, T_GETRF, T_SWAP };
 
 typedef struct {
   int kind;
@@ -59,6 +72,10 @@ typedef struct {
   double alpha, beta;
   int a, b, c;   /* tile ids: a, b read; c read-write (-1 = unused)    */
   int offset;    /* global row offset of a POTRF tile, for info       */
+  char diag;     /* TRSM diag ('U' unit; 0 = 'N')                    */
+  int span;      /* c .. c+span-1 are written (a panel); 0 or 1 = c  */
+  int w2p1;      /* one more written tile + 1 (0 = none)             */
+  int step;      /* LU: the block row k of a panel / interchange      */
 } task_t;
 
 typedef struct {
@@ -75,6 +92,9 @@ typedef struct {
   int heap_n;
   int done;
   int failed_info;
+  int stop_on_info;  /* Cholesky: a failed POTRF stops the region; LU continues */
+  /* LU: global 1-based pivots, the panels' local pivots, the block size */
+  int *lu_ipiv, *lu_tmp, lu_n, lu_nb;
   pthread_mutex_t mu;
   pthread_cond_t cv;
 } dag_t;
@@ -117,12 +137,13 @@ static int build_edges(dag_t *d, int ntiles) {
   d->npred = calloc(d->ntasks, sizeof(int));
   d->succ = calloc(d->ntasks, sizeof(int *));
   d->nsucc = calloc(d->ntasks, sizeof(int));
-  int preds[64];
+  enum { kMaxPreds = 1024 };
+  int preds[kMaxPreds];
 #define ADD_PRED(p)                                              \
   do {                                                           \
     int _p = (p), _dup = 0;                                      \
     for (int _i = 0; _i < np; _i++) if (preds[_i] == _p) _dup = 1; \
-    if (!_dup && np < 64) preds[np++] = _p;                      \
+    if (!_dup && np < kMaxPreds) preds[np++] = _p;               \
   } while (0)
   for (int t = 0; t < d->ntasks; t++) {
     task_t *k = &d->tasks[t];
@@ -130,15 +151,21 @@ static int build_edges(dag_t *d, int ntiles) {
     int rd[2] = {k->a, k->b};
     for (int r = 0; r < 2; r++)
       if (rd[r] >= 0 && last_writer[rd[r]] >= 0) ADD_PRED(last_writer[rd[r]]);
-    if (k->c >= 0) {
-      if (last_writer[k->c] >= 0) ADD_PRED(last_writer[k->c]);
+    /* written tiles: c (and c+1 .. c+span-1 for a panel), w2p1 - 1 */
+    int wr[2 + 256], nw = 0;
+    if (k->c >= 0)
+      for (int q = 0; q < (k->span > 1 ? k->span : 1) && nw < 256; q++) wr[nw++] = k->c + q;
+    if (k->w2p1 > 0) wr[nw++] = k->w2p1 - 1;
+    for (int q = 0; q < nw; q++) {
+      int w = wr[q];
+      if (last_writer[w] >= 0) ADD_PRED(last_writer[w]);
       /* readers since the last write; kept bounded by the tile DAG's shape */
-      for (int i = 0; i < nreaders[k->c]; i++) {
-        int p = readers[k->c][i];
+      for (int i = 0; i < nreaders[w]; i++) {
+        int p = readers[w][i];
         int dup = 0;
         for (int j = 0; j < np; j++) if (preds[j] == p) dup = 1;
         if (!dup) {
-          if (np >= 64) return -2;
+          if (np >= kMaxPreds) return -2;
           preds[np++] = p;
         }
       }
@@ -152,9 +179,9 @@ static int build_edges(dag_t *d, int ntiles) {
       }
       readers[tl][nreaders[tl]++] = t;
     }
-    if (k->c >= 0) {
-      last_writer[k->c] = t;
-      nreaders[k->c] = 0;
+    for (int q = 0; q < nw; q++) {
+      last_writer[wr[q]] = t;
+      nreaders[wr[q]] = 0;
     }
     for (int i = 0; i < np; i++) {
       int p = preds[i];
@@ -185,8 +212,40 @@ static void run_task(dag_t *d, int t) {
       if (d->failed_info == 0 || g < d->failed_info) d->failed_info = g;
       pthread_mutex_unlock(&d->mu);
     }
+  } else if (k->kind == T_GETRF) {
+    /* factor_panel_lapack!: getrf on the block column from the diagonal down
+     * (one column-major view of the whole matrix) */
+    int r0 = k->step * d->lu_nb;
+    int m = d->lu_n - r0, n = d->cols[k->c], lda = d->ld[k->c], info = 0;
+    int *lp = d->lu_tmp + r0;
+    g_dgetrf(&m, &n, d->ptr[k->c], &lda, lp, &info);
+    int np = m < n ? m : n;
+    for (int p = 0; p < np; p++) d->lu_ipiv[r0 + p] = r0 + lp[p];
+    if (info > 0) {
+      pthread_mutex_lock(&d->mu);
+      int g = r0 + info;
+      if (d->failed_info == 0 || g < d->failed_info) d->failed_info = g;
+      pthread_mutex_unlock(&d->mu);
+    }
+  } else if (k->kind == T_SWAP) {
+    /* swaprows_trail!(Ac[k, j], Ac[i, j], ipiv_k, i, nb): the pivots of step
+     * k whose row lies in block i, in order */
+    int nb = d->lu_nb, r0 = k->step * nb, i = k->offset;
+    double *A = d->ptr[k->c], *M = d->ptr[k->w2p1 - 1];
+    int ncols = d->cols[k->c], lda = d->ld[k->c], np = d->rows[k->c];
+    for (int p = 0; p < np; p++) {
+      int g = d->lu_ipiv[r0 + p] - 1;
+      if (g / nb != i) continue;
+      int r = g - i * nb;
+      if (A + p == M + r) continue;
+      for (int cc = 0; cc < ncols; cc++) {
+        double x = A[p + (size_t)cc * lda];
+        A[p + (size_t)cc * lda] = M[r + (size_t)cc * lda];
+        M[r + (size_t)cc * lda] = x;
+      }
+    }
   } else if (k->kind == T_TRSM) {
-    char side = k->side, uplo = k->uplo, ta = k->ta, diag = 'N';
+    char side = k->side, uplo = k->uplo, ta = k->ta, diag = k->diag ? k->diag : 'N';
     int m = d->rows[k->c], n = d->cols[k->c];
     int lda = d->ld[k->a], ldb = d->ld[k->c];
     double alpha = k->alpha;
@@ -215,7 +274,7 @@ static void *worker(void *arg) {
     while (d->heap_n == 0 && d->done < d->ntasks) pthread_cond_wait(&d->cv, &d->mu);
     if (d->done >= d->ntasks) break;
     int t = heap_pop(d);
-    int skip = d->failed_info != 0;  /* potrf_checked! stops the region */
+    int skip = d->stop_on_info && d->failed_info != 0;  /* potrf_checked! stops the region */
     pthread_mutex_unlock(&d->mu);
     if (!skip) run_task(d, t);
     pthread_mutex_lock(&d->mu);
@@ -275,6 +334,7 @@ int oracle_chol_tiled(char uplo, int n, int nb, double *A, int lda, int nthreads
   int ntiles = mt * mt;
   dag_t d;
   memset(&d, 0, sizeof d);
+  d.stop_on_info = 1;
   d.ptr = malloc(sizeof(double *) * ntiles);
   d.rows = malloc(sizeof(int) * ntiles);
   d.cols = malloc(sizeof(int) * ntiles);
@@ -367,4 +427,77 @@ int oracle_solve_tiled(char uplo, int n, int nb, double *F, int ldf, int nrhs, d
     if (!rc) rc = solve_pass('L', 'T', n, nb, F, ldf, nrhs, B, ldb, nthreads);
   }
   return rc;
+}
+
+/* lu!(A, RowMaximum()) (lu.jl:351-407 with factor_panel_lapack!) on an n x n
+ * column-major matrix with Blocks(nb, nb): per step k the panel task (getrf
+ * of the block column from the diagonal down, InOut on all its tiles and on
+ * the step's pivots), swaprows_trail! for every other block column j and
+ * every block i >= k (InOut on tiles (k, j) and (i, j), In on the pivots),
+ * TRSM('L','L','N','U') of tile (k, j) and GEMM('N','N',-1) of the trailing
+ * tiles.  ipiv: n global 1-based pivots.  Returns LAPACK's info (the first
+ * exactly zero pivot, 1-based; the factorization continues) or < 0. */
+int oracle_lu_tiled(int n, int nb, double *A, int lda, int *ipiv, int nthreads) {
+  if (n <= 0) return 0;
+  if (!g_dgetrf) return -11;
+  int mt = (n + nb - 1) / nb;
+  if (mt > 256) return -12;
+  int ntiles = mt * mt + mt;  /* the tiles, then one pivot chunk per step */
+  dag_t d;
+  memset(&d, 0, sizeof d);
+  d.stop_on_info = 0;
+  d.ptr = malloc(sizeof(double *) * ntiles);
+  d.rows = malloc(sizeof(int) * ntiles);
+  d.cols = malloc(sizeof(int) * ntiles);
+  d.ld = malloc(sizeof(int) * ntiles);
+  tile_geometry(&d, A, lda, n, n, nb, nb, 0);
+  for (int k = 0; k < mt; k++) {
+    d.ptr[mt * mt + k] = NULL;
+    d.rows[mt * mt + k] = d.cols[mt * mt + k] = d.ld[mt * mt + k] = 0;
+  }
+  d.lu_ipiv = ipiv;
+  d.lu_tmp = malloc(sizeof(int) * n);
+  d.lu_n = n;
+  d.lu_nb = nb;
+  long cap = (long)mt * mt * mt + 4L * mt * mt + 8;
+  d.tasks = malloc(sizeof(task_t) * cap);
+  int nt = 0;
+#define TILE(i, j) ((i) + (j) * mt)
+#define PIV(k) (mt * mt + (k))
+  for (int k = 0; k < mt; k++) {
+    task_t t;
+    memset(&t, 0, sizeof t);
+    t.kind = T_GETRF; t.a = -1; t.b = -1; t.c = TILE(k, k); t.span = mt - k;
+    t.w2p1 = PIV(k) + 1; t.step = k;
+    d.tasks[nt++] = t;
+    for (int j = 0; j < mt; j++) {
+      if (j == k) continue;
+      for (int i = k; i < mt; i++) {
+        memset(&t, 0, sizeof t);
+        t.kind = T_SWAP; t.a = PIV(k); t.b = -1; t.c = TILE(k, j);
+        t.w2p1 = (i == k) ? 0 : TILE(i, j) + 1; t.offset = i; t.step = k;
+        if (i == k) t.w2p1 = TILE(k, j) + 1;  /* swaps inside tile (k, j) */
+        d.tasks[nt++] = t;
+      }
+    }
+    for (int j = k + 1; j < mt; j++) {
+      memset(&t, 0, sizeof t);
+      t.kind = T_TRSM; t.side = 'L'; t.uplo = 'L'; t.ta = 'N'; t.diag = 'U'; t.alpha = 1.0;
+      t.a = TILE(k, k); t.b = -1; t.c = TILE(k, j);
+      d.tasks[nt++] = t;
+      for (int i = k + 1; i < mt; i++) {
+        memset(&t, 0, sizeof t);
+        t.kind = T_GEMM; t.ta = 'N'; t.tb = 'N'; t.alpha = -1.0; t.beta = 1.0;
+        t.a = TILE(i, k); t.b = TILE(k, j); t.c = TILE(i, j);
+        d.tasks[nt++] = t;
+      }
+    }
+  }
+#undef TILE
+#undef PIV
+  d.ntasks = nt;
+  int rc = run_dag(&d, ntiles, nthreads);
+  int info = d.failed_info;
+  free(d.ptr); free(d.rows); free(d.cols); free(d.ld); free(d.tasks); free(d.lu_tmp);
+  return rc ? rc : info;
 }

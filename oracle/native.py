@@ -1,4 +1,5 @@
-"""Loader for the oracle's threaded C restatement (oracle/dag_cholesky.c).
+"""Loader for the oracle's threaded C restatement (oracle/dag_cholesky.c):
+the tiled Cholesky and its solve, and the pivoted tiled LU.
 
 TEST INFRASTRUCTURE ONLY: used by tests/ as a checker at larger sizes and by
 bench.py's CPU-baseline leg.  The product library never loads it.
@@ -77,11 +78,15 @@ def lib():
         L.oracle_solve_tiled.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.oracle_set_getrf.argtypes = [ctypes.c_void_p]
+        L.oracle_lu_tiled.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_int]
         rc = L.oracle_set_blas(_capsule_ptr(cb.__pyx_capi__["dgemm"]),
                                _capsule_ptr(cb.__pyx_capi__["dtrsm"]),
                                _capsule_ptr(cb.__pyx_capi__["dsyrk"]),
                                _capsule_ptr(cl.__pyx_capi__["dpotrf"]))
         assert rc == 0
+        assert L.oracle_set_getrf(_capsule_ptr(cl.__pyx_capi__["dgetrf"])) == 0
         _lib = L
     return _lib
 
@@ -107,3 +112,16 @@ def ldiv_tiled(F: np.ndarray, uplo: str, B: np.ndarray, nb: int, nthreads: int =
     if rc != 0:
         raise RuntimeError(f"oracle_solve_tiled failed: {rc}")
     return B
+
+
+def lu_tiled(A: np.ndarray, nb: int, nthreads: int = 1, inplace=False):
+    """Threaded lu!(A, RowMaximum()) (square A): returns (F, ipiv, info), F
+    Fortran-ordered, ipiv the 1-based global pivots (int64)."""
+    F = A if inplace else np.array(A, dtype=np.float64, order='F', copy=True)
+    assert F.flags.f_contiguous and F.dtype == np.float64 and F.shape[0] == F.shape[1]
+    n = F.shape[0]
+    ipiv = np.zeros(max(n, 1), dtype=np.int32)
+    info = lib().oracle_lu_tiled(n, nb, F.ctypes.data, n, ipiv.ctypes.data, nthreads)
+    if info < 0:
+        raise RuntimeError(f"oracle_lu_tiled failed: {info}")
+    return F, ipiv[:n].astype(np.int64), int(info)

@@ -114,6 +114,21 @@ def test_apply_ipiv_rows_is_the_permutation():
     assert np.array_equal(got, B[o.permutation(ipiv, n), :])
 
 
+@pytest.mark.parametrize("n,nb", [(128, 64), (130, 32), (600, 128), (1024, 256)])
+def test_threaded_c_lu_matches_python_oracle(n, nb):
+    """oracle/dag_cholesky.c's threaded lu!(A, RowMaximum()) (the benchmark's
+    CPU baseline) against the Python restatement and LAPACK."""
+    from oracle import native
+    A = o.rand_uniform(n, n, n + nb)
+    F, ipiv, info = native.lu_tiled(A, nb, nthreads=4)
+    F0, p0, i0 = o.lu_rowmaximum(A, nb)
+    assert info == i0 == 0
+    assert np.array_equal(ipiv, p0)
+    assert np.linalg.norm(F - F0) <= 1e-14 * np.linalg.norm(F0)
+    Z = np.asfortranarray(np.ones((128, 128)))
+    assert native.lu_tiled(Z, 64, nthreads=4)[2] == 2
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_row_list_equals_pairwise_swaps(seed):
     """The CUDA path applies a panel's interchanges to the other block columns
