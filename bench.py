@@ -21,15 +21,18 @@ Reported:
                update, 2 nb^3 flops per launch) timed alone with CUDA events,
                against the FP64 FMA throughput measured in the same run
   cpu_baseline the oracle's threaded C restatement of the reference's
-               datadeps Cholesky (OpenBLAS tiles) on the host cores, on a
-               bounded sample (N = 16384, same tiling and RHS count)
+               datadeps Cholesky (OpenBLAS tiles) on the host cores: one
+               factor+solve of the same system (same N, tiling and RHS)
+  parity_vs_oracle  that CPU run's factor and solution against the GPU's
+               last timed step (max-norm relative; untimed)
   accuracy     normwise backward error of every RHS (inf-norms) and a
                probed ||A - U'U|| / ||A|| for the factor
   mul          G G' on the same tiling (syrk_dagger! + copytri!), the
                reference benchmark's input construction, TFLOP/s (n^3)
 
 `--impl reference` times only the CPU baseline (the reference's algorithm
-restated in C, run with all host threads) on the same metric.
+restated in C, run with all host threads) on the same metric and the same
+configuration (N = 32768 by default); its warm-up steps run at N = 8192.
 Multi-GPU: the path does not shard (one factorization per GPU), so N GPUs
 run N independent replicas; value is the sum over ranks.
 """
@@ -62,7 +65,10 @@ def parse():
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--cond", type=float, default=1e4)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-n", type=int, default=16384)
+    ap.add_argument("--cpu-n", type=int, default=0,
+                    help="order of the CPU runs (default: --n, the same configuration)")
+    ap.add_argument("--cpu-warmup-n", type=int, default=8192,
+                    help="order of the reference arm's untimed warm-up steps")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
@@ -74,8 +80,8 @@ def parse():
     ap.add_argument("--mixed-precision", default="auto")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serve-count", type=int, default=60)
-    ap.add_argument("--serve-rates", default="10,40")
+    ap.add_argument("--serve-count", type=int, default=500)
+    ap.add_argument("--serve-rates", default="25,50,100,200,400,800")
     ap.add_argument("--f64-engine", default="emulated", choices=["emulated", "dfma", "dmma"],
                     help="FP64 tile engine of the headline: 'emulated' runs the trailing "
                          "updates and the TRSM/POTRF recursion updates on the BF16 tensor cores "
@@ -201,7 +207,10 @@ class ClockSampler:
 # CPU baseline: the oracle's threaded C restatement (OpenBLAS tiles)
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(n, nb, r, A_host=None, B_host=None, reps=1):
+def cpu_baseline(n, nb, r, A_host=None, B_host=None, reps=1, keep=False):
+    """The oracle's threaded C restatement of the reference's Cholesky +
+    ldiv! on all host cores, timed; with keep=True also returns its factor
+    and solution (Fortran-ordered) for the parity comparison."""
     import numpy as np
     from oracle import native
     native.set_blas_threads(1)
@@ -211,6 +220,7 @@ def cpu_baseline(n, nb, r, A_host=None, B_host=None, reps=1):
         A_host = o.spd_uniform(n, 1)
         B_host = o.rhs_normal(n, r, 1)
     best = None
+    F = X = None
     for _ in range(reps):
         F = np.array(A_host, order='F', copy=True)
         X = np.array(B_host, order='F', copy=True)
@@ -220,26 +230,41 @@ def cpu_baseline(n, nb, r, A_host=None, B_host=None, reps=1):
         dt = time.perf_counter() - t0
         assert info == 0
         best = dt if best is None else min(best, dt)
-    return {"value": flops(n, r) / best / 1e12, "unit": "TFLOP/s", "cores": cores,
-            "kind": "port",
-            "sample": f"CPU restatement of the Dagger datadeps Cholesky + ldiv! (OpenBLAS "
-                      f"single-thread tiles, {cores} worker threads): N={n}, Blocks({nb},{nb}), "
-                      f"{r} RHS, A = Q diag(logspace(0,4)) Q'; {best:.2f} s per factor+solve"}
+    out = {"value": flops(n, r) / best / 1e12, "unit": "TFLOP/s", "cores": cores,
+           "kind": "port",
+           "sample": f"CPU restatement of the Dagger datadeps Cholesky + ldiv! (OpenBLAS "
+                     f"single-thread tiles, {cores} worker threads): N={n}, Blocks({nb},{nb}), "
+                     f"{r} RHS, A = Q diag(logspace(0,4)) Q'; {best:.2f} s per factor+solve"}
+    if keep:
+        return out, F, X
+    return out
 
 
 def run_reference(args):
-    """--impl reference: the CPU implementation of the path, all host threads."""
+    """--impl reference: the CPU implementation of the path, all host threads,
+    on the same configuration as our arm.  The untimed warm-up steps run the
+    same code at N = --cpu-warmup-n (thread pool, BLAS and page warm-up)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import numpy as np
-    n, nb, r = args.cpu_n, args.nb, args.nrhs
-    A, B = _cpu_sample_inputs(n, r, args.cond, args.seed)
+    n, nb, r = (args.cpu_n or args.n), args.nb, args.nrhs
     from oracle import native
     native.set_blas_threads(1)
     cores = os.cpu_count() or 1
+    wn = min(args.cpu_warmup_n, n)
+    if args.warmup:
+        Aw, Bw = _cpu_sample_inputs(wn, r, args.cond, args.seed)
+        for _ in range(args.warmup):
+            F = np.array(Aw, order='F', copy=True)
+            X = np.array(Bw, order='F', copy=True)
+            F, info = native.chol_tiled(F, nb, 'U', nthreads=cores, inplace=True)
+            native.ldiv_tiled(F, 'U', X, nb, nthreads=cores)
+            assert info == 0
+        del Aw, Bw, F, X
+    A, B = _cpu_sample_inputs(n, r, args.cond, args.seed)
     times = []
-    for i in range(args.warmup + args.steps):
+    for i in range(args.steps):
         F = np.array(A, order='F', copy=True)
         X = np.array(B, order='F', copy=True)
         t0 = time.perf_counter()
@@ -247,25 +272,33 @@ def run_reference(args):
         native.ldiv_tiled(F, 'U', X, nb, nthreads=cores)
         dt = time.perf_counter() - t0
         assert info == 0
-        if i >= args.warmup:
-            times.append(dt)
+        times.append(dt)
+        del F, X
     total = sum(times)
     value = flops(n, r) * len(times) / total / 1e12
     sample = (f"CPU restatement of the Dagger datadeps Cholesky + ldiv! (OpenBLAS single-thread "
-              f"tiles, {cores} worker threads), N={n}, Blocks({nb},{nb}), {r} RHS per step")
+              f"tiles, {cores} worker threads), N={n}, Blocks({nb},{nb}), {r} RHS per step "
+              f"(the full workload; warm-up steps at N={wn})")
     out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "impl": "reference",
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"tiled Cholesky + solve FP64, N={n} (CPU-bounded sample of "
-                                  f"N={args.n}), Blocks({nb},{nb}), {r} RHS, kappa={args.cond:g}",
-                      "n": n, "nb": nb, "nrhs": r},
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian QR; no dataset)",
+           "config": _config(args, n),
            "solves_per_s": r * len(times) / total,
            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                             "sample": sample},
            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def _config(args, n=None, world=1):
+    n = n or args.n
+    return {"workload": f"plain FP64 tiled Cholesky + solve, N={n}, Blocks({args.nb},{args.nb}), "
+                        f"{args.nrhs} RHS, A = Q diag(logspace(0,{math.log10(args.cond):g})) Q'",
+            "n": n, "nb": args.nb, "nrhs": args.nrhs, "cond": args.cond,
+            "l2": "inputs 8 N^2 bytes >> 129 MB L2 (no flush needed)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def _cpu_sample_inputs(n, r, cond, seed):
@@ -286,6 +319,45 @@ def _cpu_sample_inputs(n, r, cond, seed):
         pass
     from oracle import tiled as o
     return o.spd_spectrum(n, cond, seed), o.rhs_normal(n, r, seed)
+
+
+def _guarded(fn, *a):
+    """Runs one secondary measurement; an exception is reported in its entry
+    of the JSON line instead of ending the run (the headline stands)."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        import torch
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+
+
+def _fortran(t):
+    """A 2-D torch tensor as a Fortran-ordered numpy array on the host."""
+    import numpy as np
+    return np.asfortranarray(t.cpu().numpy())
+
+
+def parity_vs_oracle(W, DX, Fo, Xo, dev):
+    """The GPU's factor (upper triangle of the tiles W) and solution (DX)
+    against the oracle's F and X (Fortran-ordered numpy), max-norm relative,
+    compared on the device."""
+    import torch
+    G = torch.triu(W.collect())
+    Ft = torch.triu(torch.from_numpy(Fo.T).to(dev).T)
+    ef = float(((G - Ft).abs().max() / Ft.abs().max()).item())
+    del G, Ft
+    X = DX.collect()
+    Xt = torch.from_numpy(Xo.T).to(dev).T
+    ex = float(((X - Xt).abs().max() / Xt.abs().max()).item())
+    del X, Xt
+    torch.cuda.empty_cache()
+    return {"factor_rel_err": ef, "solve_rel_err": ex, "norm": "max-norm relative",
+            "against": "oracle/dag_cholesky.c (the cpu_baseline run, same A and B)",
+            "factor_tol": 1e-13, "solve_tol": 1e-12,
+            "solve_tol_reason": "kappa = 1e4: two FP64 solvers differ by ~3e-13 here "
+                                "(LAPACK dpotrs vs the oracle at N = 4096, 8192)"}
 
 
 # ---------------------------------------------------------------------------
@@ -368,6 +440,21 @@ def run_ours(args):
     V = torch.randn(n, 4, device=dev, dtype=torch.float64, generator=gen)
     fres = float(((A @ V - U.T @ (U @ V)).norm() / (A @ V).norm()).item())
     del U, R, X
+
+    # CPU baseline on the same system (all host cores), and the parity of the
+    # GPU's last timed step against it (both untimed for the GPU line)
+    cpu = parity = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cn = args.cpu_n or n
+        if cn == n:
+            An = A.cpu().numpy().T                      # A is exactly symmetric: a Fortran view
+            Bn = _fortran(B)
+        else:
+            An, Bn = _cpu_sample_inputs(cn, r, args.cond, args.seed)
+        cpu, Fo, Xo = cpu_baseline(cn, nb, r, An, Bn, keep=True)
+        if cn == n:
+            parity = parity_vs_oracle(W, DBw, Fo, Xo, dev)
+        del An, Bn, Fo, Xo
 
     # e2e through the public API from pinned host buffers
     e2e = None
@@ -464,44 +551,38 @@ def run_ours(args):
         roof = roof_dfma
 
     del Ta, Tb, Tc
+    del W, DBw
+    torch.cuda.empty_cache()
     mixed = None
     if not args.no_mixed:
-        del W, DBw
-        torch.cuda.empty_cache()
-        mixed = bench_mixed(args, d, DA, A, B, stream, world)
+        mixed = _guarded(bench_mixed, args, d, DA, A, B, stream, world)
+    del DA, DB0, A, B
+    torch.cuda.empty_cache()
     mul = None
     if not args.no_mul:
-        mul = bench_mul(args, d, dev, stream)
+        mul = _guarded(bench_mul, args, d, dev, stream)
     lu = None
     if not args.no_lu:
-        lu = bench_lu(args, d, dev, stream)
+        lu = _guarded(bench_lu, args, d, dev, stream)
     batched = None
     if not args.no_batched:
-        batched = bench_batched(args, d, dev, rank)
+        batched = _guarded(bench_batched, args, d, dev, rank)
     serving = None
     if not args.no_serving and rank == 0:
-        serving = bench_serving(args, dev)
+        serving = _guarded(bench_serving, args, dev)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        An, Bn = _cpu_sample_inputs(args.cpu_n, r, args.cond, args.seed)
-        cpu = cpu_baseline(args.cpu_n, nb, r, An, Bn)
 
     out = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded Gaussian QR; no dataset)",
-           "config": {"workload": f"plain FP64 tiled Cholesky + solve, N={n}, Blocks({nb},{nb}), "
-                                  f"{r} RHS, A = Q diag(logspace(0,{math.log10(args.cond):g})) Q'",
-                      "n": n, "nb": nb, "nrhs": r, "cond": args.cond,
-                      "l2": "inputs 8 N^2 bytes >> 129 MB L2 (no flush needed)",
-                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "config": _config(args, n, world),
            "f64_engine": args.f64_engine, "dfma_engine": dfma,
            "solves_per_s": r * args.steps * world / t,
            "accuracy": {"backward_error_max": float(berr.max().item()),
                         "factor_residual_probe": fres},
            "roofline": roof, "gpu_launches": int(launches),
-           "clocks": clk, "e2e": e2e, "cpu_baseline": cpu,
+           "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "parity_vs_oracle": parity,
            "mixed": mixed, "mul": mul, "lu": lu, "batched": batched, "serving": serving}
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -521,9 +602,14 @@ def _measured_bf16_peak():
 # multiplies the 28 slice pairs (s, t) with s + t <= 8.
 EMULATED_SLICES = 7
 EMULATED_PRODUCTS = 28
-# DRAM bytes (read + write) of one 1024^3 emulated tile launch, ncu capture:
-# the 29 MiB of slices mostly hit L2 and C's write-back stays in L2.
-OZ_TILE_DRAM_BYTES = 23160576 + 0
+# DRAM bytes (read + write) of one 1024^3 emulated tile launch, from the ncu
+# capture summarised in profiles/oz_gemm_tile_1024.md (dram__bytes_read.sum +
+# dram__bytes_write.sum); the 29 MiB of slices mostly hit L2 and C's
+# write-back stays in L2.  A constant from that capture, not measured here:
+# bench.py runs without a profiler.
+OZ_TILE_DRAM_BYTES = 23160576
+OZ_TILE_DRAM_SOURCE = ("ncu capture of one 1024^3 launch (profiles/oz_gemm_tile_1024.md), "
+                       "not measured in this run")
 
 
 def roofline_emulated(L, nb, dev, stream, s):
@@ -571,6 +657,7 @@ def roofline_emulated(L, nb, dev, stream, s):
             # dram__bytes_read.sum + dram__bytes_write.sum of one launch at
             # nb = 1024 from an ncu capture of the same launch (profiles/)
             "traffic": OZ_TILE_DRAM_BYTES if nb == 1024 else None,
+            "traffic_source": OZ_TILE_DRAM_SOURCE,
             "traffic_unit": "bytes per launch"}
 
 
@@ -783,13 +870,17 @@ def bench_batched(args, d, dev, rank):
 def bench_serving(args, dev):
     """Serving loop: Poisson arrivals at swept rates, n log-uniform on [64,
     16384], kappa log-uniform on [1e2, 1e6], 1-64 RHS, 30% of requests
-    reusing a resident factor, 150 GB HBM admission budget."""
+    reusing a resident factor, 150 GB HBM admission budget.  Every rate
+    serves the same --serve-count requests (same matrices and right-hand
+    sides, arrival times drawn per rate); p50 / p99 are order statistics of
+    all completed requests of a rate."""
     import torch
     from dagger_gb300.serving import MatrixFactory, Server, latency_stats, make_workload, run_workload
     fac = MatrixFactory(dev, args.seed)
     out = {"budget_gb": 150, "requests_per_rate": args.serve_count, "slots": 8, "rates": []}
     for rate in [float(x) for x in args.serve_rates.split(",") if x]:
-        work = make_workload(args.serve_count, rate, seed=args.seed + int(rate), factory=fac)
+        work = make_workload(args.serve_count, rate, seed=args.seed, factory=fac)
+        fac.drop_q()
         torch.cuda.synchronize()
         srv = Server(budget_bytes=150e9, slots=8)
         wall = run_workload(srv, work, realtime=True)
@@ -808,14 +899,25 @@ def bench_serving(args, dev):
             fl += 2.0 * r.n * r.n * r.nrhs
         factored = {r.matrix_id: r.n for r in reqs if r.error is None}
         fl += sum(n ** 3 / 3.0 for n in factored.values())
+        span = max(t for t, _ in work)
         out["rates"].append({"rate_per_s": rate, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-                             "mean_ms": st.get("mean_ms"), "completed": st["count"],
+                             "mean_ms": st.get("mean_ms"), "samples": st["count"],
+                             "completed": st["count"],
                              "rejected": sum(1 for r in reqs if r.error is not None),
+                             "offered_req_per_s": len(work) / span if span > 0 else None,
                              "throughput_req_per_s": st["count"] / wall,
                              "throughput_TFLOP_s": fl / wall / 1e12,
                              "backward_error_max": worst, "wall_s": wall})
         del work, reqs
         torch.cuda.empty_cache()
+    del fac
+    torch.cuda.empty_cache()
+    rates = out["rates"]
+    if rates and rates[0]["p99_ms"]:
+        base = rates[0]["p99_ms"]
+        knee = [x["rate_per_s"] for x in rates if x["p99_ms"] and x["p99_ms"] > 2 * base]
+        out["p99_doubles_at_rate"] = knee[0] if knee else None
+        out["saturated"] = any(x["throughput_req_per_s"] < 0.9 * x["rate_per_s"] for x in rates)
     return out
 
 

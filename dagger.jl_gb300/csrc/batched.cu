@@ -490,12 +490,15 @@ extern "C" int dg_batched_potrs(int count, const int *n, const int *nrhs, double
 // this variant takes them from one file-scope device array instead.
 //
 // The array lives in every GPU that loads the library until the process
-// exits.  In host code the symbol is only a host-side stand-in, so its device
-// address is looked up once per device (cudaGetSymbolAddress, with that device
-// current) by the first call on that device; make that first call before any
-// stream capture.  Every call shares the array and it keeps the previous
-// call's contents, so the ticket counters and error words are cleared on each
-// call; calls that overlap on the GPU (concurrent streams) race on it.
+// exits.  In host code the symbol is only a host-side stand-in, so every call
+// looks up its device address for the current device (cudaGetSymbolAddress,
+// which allocates nothing); no address is cached, so a context that was reset
+// and reloaded the module gets the new address.  The call is synchronous: it
+// stages its descriptors from host memory and waits for the launch, so it
+// cannot be made while its stream is being captured.  Every call shares the
+// array and it keeps the previous call's contents, so the ticket counters and
+// error words are cleared on each call; calls that overlap on the GPU
+// (concurrent streams or host threads) race on it.
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB
@@ -503,23 +506,17 @@ constexpr int kNoAllocMaxSystems = 4096;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-void *g_noalloc_addr[64] = {nullptr};
 thread_local dg::BatchSys t_sys[kNoAllocMaxSystems];
 thread_local int t_idx[kNoAllocMaxSystems];
 thread_local int t_info[2 * kNoAllocMaxSystems];
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// The array's device address on the current device, looked up on each call.
 int noalloc_scratch(void **out) {
-  int dev = 0;
-  DG_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return DG_ERR_UNSUPPORTED;
-  if (!g_noalloc_addr[dev]) {
-    void *p = nullptr;
-    DG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_addr[dev] = p;
-  }
-  *out = g_noalloc_addr[dev];
+  void *p = nullptr;
+  DG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  *out = p;
   return 0;
 }
 

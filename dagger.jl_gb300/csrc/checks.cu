@@ -82,9 +82,10 @@ __global__ void __launch_bounds__(256) herm_pair_kernel(const double *const *til
   }
 }
 
-__global__ void finite_kernel(const double *const *tiles, int n, int nb, int mt, int *flag) {
+__global__ void finite_kernel(const double *const *tiles, int m, int n, int mb, int nb, int mt,
+                              int *flag) {
   const int i = blockIdx.x, j = blockIdx.y;
-  const int ri = min(nb, n - i * nb), cj = min(nb, n - j * nb);
+  const int ri = min(mb, m - i * mb), cj = min(nb, n - j * nb);
   const double *X = tiles[i + (size_t)j * mt];
   int bad = 0;
   for (size_t e = threadIdx.x; e < (size_t)ri * cj; e += blockDim.x)
@@ -92,23 +93,24 @@ __global__ void finite_kernel(const double *const *tiles, int n, int nb, int mt,
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
-int run_check(bool herm, int n, int nb, double *const *tiles, cudaStream_t s) {
-  const int mt = (n + nb - 1) / nb;
-  DG_CHECK_ARG(mt <= 65535, 2);
+// herm: n x n with Blocks(nb, nb); otherwise m x n with Blocks(mb, nb).
+int run_check(bool herm, int m, int n, int mb, int nb, double *const *tiles, cudaStream_t s) {
+  const int mt = (m + mb - 1) / mb, nt = (n + nb - 1) / nb;
+  DG_CHECK_ARG(mt <= 65535 && nt <= 65535, 2);
   int *flag = nullptr;
   int rc = dg::device_state().scratch_int(&flag);
   if (rc) return rc;
   // the tile pointer grid is staged through a small device buffer
   const double **dptrs = nullptr;
-  size_t bytes = sizeof(double *) * (size_t)mt * mt;
+  size_t bytes = sizeof(double *) * (size_t)mt * nt;
   DG_CUDA_TRY(cudaMallocAsync((void **)&dptrs, bytes, s));
   DG_CUDA_TRY(cudaMemcpyAsync(dptrs, tiles, bytes, cudaMemcpyHostToDevice, s));
   DG_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
-  dim3 grid(mt, mt);
+  dim3 grid(mt, nt);
   if (herm)
     herm_pair_kernel<<<grid, 256, 0, s>>>(dptrs, n, nb, mt, flag);
   else
-    finite_kernel<<<grid, 256, 0, s>>>(dptrs, n, nb, mt, flag);
+    finite_kernel<<<grid, 256, 0, s>>>(dptrs, m, n, mb, nb, mt, flag);
   DG_CUDA_TRY(cudaGetLastError());
   dg::count_launches(1);
   int h = 0;
@@ -125,7 +127,7 @@ extern "C" int dg_ishermitian_tiled(int n, int nb, double *const *tiles, void *s
   DG_CHECK_ARG(nb > 0, 2);
   if (n == 0) return 1;
   DG_CHECK_ARG(tiles != nullptr, 3);
-  return run_check(true, n, nb, tiles, (cudaStream_t)stream);
+  return run_check(true, n, n, nb, nb, tiles, (cudaStream_t)stream);
 }
 
 extern "C" int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream) {
@@ -133,5 +135,16 @@ extern "C" int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *str
   DG_CHECK_ARG(nb > 0, 2);
   if (n == 0) return 1;
   DG_CHECK_ARG(tiles != nullptr, 3);
-  return run_check(false, n, nb, tiles, (cudaStream_t)stream);
+  return run_check(false, n, n, nb, nb, tiles, (cudaStream_t)stream);
+}
+
+extern "C" int dg_chkfinite_tiled_mn(int m, int n, int mb, int nb, double *const *tiles,
+                                     void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(mb > 0, 3);
+  DG_CHECK_ARG(nb > 0, 4);
+  if (m == 0 || n == 0) return 1;
+  DG_CHECK_ARG(tiles != nullptr, 5);
+  return run_check(false, m, n, mb, nb, tiles, (cudaStream_t)stream);
 }

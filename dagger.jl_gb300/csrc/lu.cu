@@ -15,7 +15,8 @@
 // SMs stay free for the trailing updates): every CTA keeps a contiguous range
 // of the strip's rows in shared memory, and the grid agrees on each column's
 // pivot through one grid barrier per column (a counter in global memory;
-// every wait is bounded and records DG_ERR_TIMEOUT), with the rank-1 updates
+// every wait is bounded and records DG_ERR_TIMEOUT; the launch is
+// cooperative, so all CTAs are co-resident), with the rank-1 updates
 // of the later columns deferred into the barrier waits.  The
 // result is LAPACK's: the pivot of a column is the first row of largest
 // magnitude (idamax), multipliers are scaled by the reciprocal of the pivot
@@ -550,8 +551,23 @@ int leaf_launch(const PanelCtx &c, int c0, int wl) {
   a.sidx = l.sidx;
   a.srow = l.srow;
   a.jrow = l.jrow;
-  lu_leaf_kernel<<<G, kLeafThreads, ((size_t)wl * R + (size_t)G * kLeafW) * 8, c.s>>>(a);
-  DG_CUDA_TRY(cudaGetLastError());
+  // A cooperative launch: the G CTAs are scheduled together, so the
+  // per-column grid barrier never waits for a CTA that other kernels of the
+  // region (the look-ahead trailing updates on other streams) keep from
+  // starting.  The attribute is kept when the launch is captured into the
+  // region's graph.
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.gridDim = dim3(G);
+  cfg.blockDim = dim3(kLeafThreads);
+  cfg.dynamicSmemBytes = ((size_t)wl * R + (size_t)G * kLeafW) * 8;
+  cfg.stream = c.s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  DG_CUDA_TRY(cudaLaunchKernelEx(&cfg, lu_leaf_kernel, a));
   count_launches(1);
   return 0;
 }

@@ -290,6 +290,15 @@ static void task_accesses(const dg_task &t, std::vector<dg_region::Access> &out)
       out.push_back({dg::footprint(ws + L.leaf, (int)(L.lpiv - L.leaf), 1, 1, 1), DG_OUT});
       if (L.ozp_bytes)
         out.push_back({dg::footprint(ws + L.ozp, (int)(L.ozp_bytes / 256), 1, 1, 256), DG_OUT});
+      // this step's slice of the leaves' pivot rows (panel rows per column)
+      const int npanel = t.m < t.n ? t.m : t.n;
+      if (npanel > 0)
+        out.push_back({dg::footprint(ws + L.lpiv + (size_t)t.info_offset * 4, npanel, 1, 1, 4),
+                       DG_OUT});
+      // The info word (an atomicMin of the first zero pivot's column) and the
+      // status word (a sticky error code) take no edge: every step only
+      // lowers or sets them and nothing inside the region reads them for
+      // ordering; the host reads both after the region.
       if (piv) {
         const int npiv = t.m < t.n ? t.m : t.n;
         out.push_back({dg::footprint(ws + L.lists + (size_t)step * L.list_stride * 4,

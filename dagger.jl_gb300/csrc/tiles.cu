@@ -73,3 +73,70 @@ int tile_mirror_upper(double *A, long long lda, int n, cudaStream_t s) {
 }
 
 }  // namespace dg
+
+// ---------------------------------------------------------------------------
+// Re-blocking copy: copyto!(buffer, A) between two tilings of one m x n matrix
+// (copy_buffered / darray_copyto!, src/array/copy.jl:11-37 of Dagger.jl).
+// Source and destination are tile grids (column-major grid, tile (i, j) =
+// tiles[i + j*mt], each tile column-major with leading dimension equal to its
+// row count).  One CTA copies a 32 x 32 block of the matrix: each warp walks
+// columns, lane l reads row r0 + l of the source tile and writes the same row
+// of the destination tile, so reads and writes are coalesced runs within one
+// tile column (a block that straddles a tile edge splits the run).  8 bytes
+// read and 8 written per element: an HBM-bound copy.
+// ---------------------------------------------------------------------------
+namespace dg {
+namespace {
+
+__global__ void __launch_bounds__(256) reblock_kernel(int m, int n, int smb, int snb, int smt,
+                                                      const double *const *__restrict__ src,
+                                                      int dmb, int dnb, int dmt,
+                                                      double *const *__restrict__ dst) {
+  const int r = blockIdx.x * 32 + threadIdx.x;
+  if (r >= m) return;
+  const int si = r / smb, sr = r - si * smb, di = r / dmb, dr = r - di * dmb;
+  const int sld = min(smb, m - si * smb), dld = min(dmb, m - di * dmb);
+  for (int q = threadIdx.y; q < 32; q += 8) {
+    const int c = blockIdx.y * 32 + q;
+    if (c >= n) break;
+    const int sj = c / snb, sc = c - sj * snb, dj = c / dnb, dc = c - dj * dnb;
+    const double v = src[si + (size_t)sj * smt][sr + (size_t)sc * sld];
+    dst[di + (size_t)dj * dmt][dr + (size_t)dc * dld] = v;
+  }
+}
+
+}  // namespace
+}  // namespace dg
+
+extern "C" int dg_copy_reblock(int m, int n, int src_mb, int src_nb, double *const *src_tiles,
+                               int dst_mb, int dst_nb, double *const *dst_tiles, void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(src_mb > 0, 3);
+  DG_CHECK_ARG(src_nb > 0, 4);
+  DG_CHECK_ARG(dst_mb > 0, 6);
+  DG_CHECK_ARG(dst_nb > 0, 7);
+  if (m == 0 || n == 0) return 0;
+  DG_CHECK_ARG(src_tiles != nullptr, 5);
+  DG_CHECK_ARG(dst_tiles != nullptr, 8);
+  const int smt = (m + src_mb - 1) / src_mb, snt = (n + src_nb - 1) / src_nb;
+  const int dmt = (m + dst_mb - 1) / dst_mb, dnt = (n + dst_nb - 1) / dst_nb;
+  const dim3 grid((m + 31) / 32, (n + 31) / 32), blk(32, 8);
+  DG_CHECK_ARG(grid.y <= 65535, 2);
+  cudaStream_t s = (cudaStream_t)stream;
+  // both pointer grids staged through one stream-ordered device buffer
+  const size_t ns = (size_t)smt * snt, nd = (size_t)dmt * dnt;
+  double **dptrs = nullptr;
+  DG_CUDA_TRY(cudaMallocAsync((void **)&dptrs, sizeof(double *) * (ns + nd), s));
+  DG_CUDA_TRY(cudaMemcpyAsync(dptrs, src_tiles, sizeof(double *) * ns, cudaMemcpyHostToDevice, s));
+  DG_CUDA_TRY(
+      cudaMemcpyAsync(dptrs + ns, dst_tiles, sizeof(double *) * nd, cudaMemcpyHostToDevice, s));
+  dg::reblock_kernel<<<grid, blk, 0, s>>>(m, n, src_mb, src_nb, smt, dptrs, dst_mb, dst_nb, dmt,
+                                          dptrs + ns);
+  DG_CUDA_TRY(cudaGetLastError());
+  dg::count_launches(1);
+  // stream-ordered: the host pointer grids were staged by the pageable copies
+  // before they returned, so the caller may free them at once
+  DG_CUDA_TRY(cudaFreeAsync(dptrs, s));
+  return 0;
+}

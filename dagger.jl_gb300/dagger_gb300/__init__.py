@@ -10,7 +10,8 @@ tile calls).
 from ._lib import DaggerGB300Error, PosDefException, SingularException, lib
 from .darray import Blocks, DArray, distribute
 from .datadeps import In, InOut, Out, copyto_, spawn, spawn_datadeps
-from .linalg import (Cholesky, cholesky, cholesky_, cholesky_distribute, gemm_, gemm_dagger_,
+from .linalg import (Cholesky, chkfinite, cholesky, cholesky_, cholesky_distribute, copy_reblock,
+                     gemm_, gemm_dagger_,
                      matmul, mul_, syrk_dagger_, gemm_f64_emulated_tn, gemv_,
                      get_f64_engine, getrf_, ishermitian, issymmetric, LU, ldiv, ldiv_, lu, lu_,
                      potrf_, set_f64_engine, syrk_, trsm_, trsv_)
@@ -22,4 +23,5 @@ __all__ = [
     "ishermitian", "issymmetric", "potrf_", "trsm_", "syrk_", "gemm_", "trsv_", "gemv_",
     "gemm_f64_emulated_tn", "set_f64_engine", "get_f64_engine", "spawn_datadeps", "spawn", "In", "Out", "InOut", "copyto_", "PosDefException",
     "DaggerGB300Error", "lib", "LU", "lu", "lu_", "ldiv", "getrf_", "SingularException",
+    "chkfinite", "copy_reblock",
 ]

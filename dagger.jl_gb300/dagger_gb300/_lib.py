@@ -113,6 +113,9 @@ SIGNATURES = {
     "dg_get_f64_engine": (c_int, []),
     "dg_ishermitian_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
     "dg_chkfinite_tiled": (c_int, [c_int, c_int, c_void_p, c_void_p]),
+    "dg_chkfinite_tiled_mn": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
+    "dg_copy_reblock": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p,
+                                c_void_p]),
     "dg_probe_fp64_fma_tflops": (c_int, [c_int, ctypes.POINTER(c_double), c_void_p]),
     "dg_mixed_factor": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_void_p, c_int,
                                 c_void_p]),

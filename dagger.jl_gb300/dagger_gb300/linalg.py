@@ -173,13 +173,15 @@ class Cholesky:
     With the emulated FP64 engine the factorization also keeps the
     transposed inverses of its diagonal tiles (winv, formed for the panel
     products anyway), which ldiv_ applies as emulated products; a Cholesky
-    built from factors alone solves by substitution."""
+    built from factors alone solves by substitution.  winv_nb is the block
+    size the inverses were formed at (the factorization's square blocks)."""
 
-    def __init__(self, factors: DArray, uplo: str, info: int, winv=None):
+    def __init__(self, factors: DArray, uplo: str, info: int, winv=None, winv_nb=None):
         self.factors = factors
         self.uplo = uplo
         self.info = info
         self.winv = winv
+        self.winv_nb = winv_nb
 
     @property
     def U(self) -> torch.Tensor:
@@ -195,37 +197,70 @@ class Cholesky:
         return self.info == 0
 
 
+def _dims2(A: DArray):
+    return (A.shape[0], A.shape[1]) if A.ndim == 2 else (A.shape[0], 1)
+
+
+def _blocks2(part: Blocks):
+    return part.blocksize if len(part.blocksize) == 2 else (part.blocksize[0], 1)
+
+
+def copy_reblock(src: DArray, dst: DArray, stream=None) -> DArray:
+    """copyto!(dst, src) between two tilings of one matrix, on the device
+    (darray_copyto! of copy_buffered, src/array/copy.jl:11-37)."""
+    if src.shape != dst.shape:
+        raise ValueError(f"copyto!: shapes {src.shape} and {dst.shape} differ")
+    m, n = _dims2(src)
+    smb, snb = _blocks2(src.partitioning)
+    dmb, dnb = _blocks2(dst.partitioning)
+    check(lib().dg_copy_reblock(m, n, smb, snb, src.tile_ptrs(), dmb, dnb, dst.tile_ptrs(),
+                                _stream(stream)))
+    return dst
+
+
+def _buffered(A: DArray, part: Blocks, stream=None) -> DArray:
+    """The argument as the region needs it: A itself when its partitioning is
+    already `part`, else a copy re-blocked to `part` (maybe_copy_buffered,
+    copy.jl:3-10; allocate_copy_buffer, copy.jl:34-36)."""
+    if A.partitioning == part:
+        return A
+    buf = DArray(A.shape, part, device=A.storage.device, dtype=A.dtype)
+    return copy_reblock(A, buf, stream)
+
+
 def _square_blocks(A: DArray):
     if A.ndim != 2 or A.shape[0] != A.shape[1]:
         raise ValueError(f"matrix is not square: dimensions are {A.shape}")  # checksquare
-    mb, nb = A.partitioning.blocksize
-    if mb != nb:
-        # maybe_copy_buffered(A => Blocks(min_bs, min_bs)) (copy.jl:3-10)
-        raise ValueError("non-square Blocks are re-blocked by the caller: use Blocks(nb, nb)")
-    return nb
+    return min(A.partitioning.blocksize)
 
 
 def cholesky_(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Cholesky:
-    """cholesky!(DA): in-place tiled factorization (_chol!, cholesky.jl:19-108)."""
+    """cholesky!(DA): in-place tiled factorization (_chol!, cholesky.jl:19-108).
+    A DArray blocked Blocks(mb, nb) with mb != nb is factored in a copy
+    re-blocked to Blocks(min, min) and copied back (maybe_copy_buffered,
+    cholesky.jl:34)."""
     if uplo not in ('U', 'L'):
         raise ValueError("uplo must be 'U' or 'L'")
     nb = _square_blocks(A)
+    W = _buffered(A, Blocks(nb, nb), stream)
     n = A.shape[0]
     winv = None
     if n > 0 and nb <= 1024 and lib().dg_get_f64_engine() == F64_ENGINES["emulated"]:
         mt = (n + nb - 1) // nb
         winv = torch.empty(mt * nb * nb, dtype=torch.float64, device=A.storage.device)
-        rc = lib().dg_cholesky_tiled_winv(ch(uplo), n, nb, A.tile_ptrs(), winv.data_ptr(),
+        rc = lib().dg_cholesky_tiled_winv(ch(uplo), n, nb, W.tile_ptrs(), winv.data_ptr(),
                                           _stream(stream))
     else:
-        rc = lib().dg_cholesky_tiled(ch(uplo), n, nb, A.tile_ptrs(), _stream(stream))
+        rc = lib().dg_cholesky_tiled(ch(uplo), n, nb, W.tile_ptrs(), _stream(stream))
     if rc < 0:
         check(rc)
+    if W is not A:
+        copy_reblock(W, A, stream)
     if rc > 0:
         winv = None
         if check_:
             raise PosDefException(rc)
-    return Cholesky(A, uplo, rc, winv)
+    return Cholesky(A, uplo, rc, winv, winv_nb=nb)
 
 
 def cholesky_distribute(A, part: Blocks, uplo: str = 'U', check_: bool = True, stream=None,
@@ -271,7 +306,7 @@ def cholesky_distribute(A, part: Blocks, uplo: str = 'U', check_: bool = True, s
         winv = None
         if check_:
             raise PosDefException(rc)
-    return Cholesky(D, uplo, rc, winv)
+    return Cholesky(D, uplo, rc, winv, winv_nb=nb)
 
 
 def cholesky(A: DArray, uplo: str = 'U', check_: bool = True, stream=None) -> Cholesky:
@@ -283,26 +318,32 @@ def ldiv_(C, B: DArray, stream=None) -> DArray:
     """ldiv!(C, B): B <- A^-1 B with A = U'U or LL' (linalg.jl:352-405), or
     with A = P' L U for an LU (linalg.jl:264-278).
 
-    B is an N-vector or an N x r matrix; its row blocking must equal the
-    factor's block size (ldiv! re-blocks B to Blocks(min_bsa, min_bsa),
+    B is an N-vector or an N x r matrix.  As in the reference, the factor
+    and B are solved at Blocks(min_bsa, min_bsa) (Blocks(min_bsa) for a
+    vector), min_bsa the factor's smaller block size; an argument blocked
+    otherwise is copied to that blocking and back (maybe_copy_buffered,
     linalg.jl:362-364)."""
     if isinstance(C, LU):
         return _ldiv_lu(C, B, stream)
     F = C.factors
-    nb = F.partitioning.blocksize[0]
     if B.shape[0] != F.shape[0]:
         raise ValueError("dimension mismatch")
-    if B.partitioning.blocksize[0] != nb or (B.ndim == 2 and B.partitioning.blocksize[1] != nb):
-        raise ValueError("B must be blocked Blocks(nb, nb) (or Blocks(nb)) like the factor")
+    nb = min(F.partitioning.blocksize)
+    partB = Blocks(nb) if B.ndim == 1 else Blocks(nb, nb)
+    Fb = _buffered(F, Blocks(nb, nb), stream)
+    Bb = _buffered(B, partB, stream)
     nrhs = 1 if B.ndim == 1 else B.shape[1]
-    if C.winv is not None and lib().dg_get_f64_engine() == F64_ENGINES["emulated"]:
-        rc = lib().dg_cholesky_solve_tiled_winv(ch(C.uplo), F.shape[0], nb, F.tile_ptrs(),
-                                                C.winv.data_ptr(), nrhs, B.tile_ptrs(),
+    if (C.winv is not None and C.winv_nb == nb
+            and lib().dg_get_f64_engine() == F64_ENGINES["emulated"]):
+        rc = lib().dg_cholesky_solve_tiled_winv(ch(C.uplo), F.shape[0], nb, Fb.tile_ptrs(),
+                                                C.winv.data_ptr(), nrhs, Bb.tile_ptrs(),
                                                 _stream(stream))
     else:
-        rc = lib().dg_cholesky_solve_tiled(ch(C.uplo), F.shape[0], nb, F.tile_ptrs(), nrhs,
-                                           B.tile_ptrs(), _stream(stream))
+        rc = lib().dg_cholesky_solve_tiled(ch(C.uplo), F.shape[0], nb, Fb.tile_ptrs(), nrhs,
+                                           Bb.tile_ptrs(), _stream(stream))
     check(rc)
+    if Bb is not B:
+        copy_reblock(Bb, B, stream)
     return B
 
 
@@ -361,18 +402,21 @@ def _pivot_code(pivot) -> int:
     return _PIVOTS[key]
 
 
-def _chkfinite(A: DArray, stream=None):
-    """LAPACK.chkfinite(A) (linalg.jl:138-148): ArgumentError for Inf/NaN."""
-    if A.shape[0] == A.shape[1] and A.partitioning.blocksize[0] == A.partitioning.blocksize[1]:
-        ok = lib().dg_chkfinite_tiled(A.shape[0], A.partitioning.blocksize[0], A.tile_ptrs(),
-                                      _stream(stream))
-        if ok < 0:
-            check(ok)
-        ok = bool(ok)
-    else:
-        ok = all(bool(torch.isfinite(t).all()) for row in A.chunks for t in row)
+def chkfinite(A: DArray, stream=None) -> bool:
+    """LAPACK.chkfinite(::DArray) (linalg.jl:126-148): True when every
+    element is finite; ValueError (Julia's ArgumentError "matrix has Inf or
+    NaN") otherwise.  One device pass over the tiles."""
+    m, n = _dims2(A)
+    mb, nb = _blocks2(A.partitioning)
+    ok = lib().dg_chkfinite_tiled_mn(m, n, mb, nb, A.tile_ptrs(), _stream(stream))
+    if ok < 0:
+        check(ok)
     if not ok:
-        raise ValueError("matrix contains Infs or NaNs")
+        raise ValueError("matrix has Inf or NaN")
+    return True
+
+
+_chkfinite = chkfinite
 
 
 def lu_(A: DArray, pivot="RowMaximum", check_: bool = True, allowsingular: bool = False,
@@ -388,18 +432,15 @@ def lu_(A: DArray, pivot="RowMaximum", check_: bool = True, allowsingular: bool 
     if check_:
         _chkfinite(A, stream)
     m, n = A.shape
-    mb, nbc = A.partitioning.blocksize
-    W = A
-    if mb != nbc:
-        b = min(mb, nbc)
-        W = DArray.from_array(A.collect(), Blocks(b, b), device=A.storage.device)
-    nb = W.partitioning.blocksize[0]
+    b = min(A.partitioning.blocksize)
+    W = _buffered(A, Blocks(b, b), stream)
+    nb = b
     ipiv = torch.empty(max(min(m, n), 1), dtype=torch.int64, device=A.storage.device)
     rc = lib().dg_lu_tiled(m, n, nb, W.tile_ptrs(), code, ipiv.data_ptr(), _stream(stream))
     if rc < 0:
         check(rc)
     if W is not A:
-        A.copy_from(W.collect())
+        copy_reblock(W, A, stream)
     info = rc
     if check_ and info > 0 and not allowsingular:
         raise _lib.SingularException(info)
@@ -413,20 +454,26 @@ def lu(A: DArray, pivot="RowMaximum", check_: bool = True, allowsingular: bool =
 
 
 def _ldiv_lu(F: LU, B: DArray, stream=None) -> DArray:
-    """ldiv!(F::LU, B) (linalg.jl:264-278), B blocked like the factors."""
+    """ldiv!(F::LU, B) (linalg.jl:247-251): the row interchanges, then the
+    unit-lower and upper block solves.  The factors and B are solved at
+    Blocks(nb, nb) (Blocks(nb) for a vector), nb the factors' smaller block
+    size; an argument blocked otherwise is copied there and back
+    (maybe_copy_buffered, linalg.jl:262-276)."""
     A = F.factors
     n = A.shape[0]
     if A.shape[0] != A.shape[1]:
         raise ValueError("ldiv! needs a square LU")
-    nb = A.partitioning.blocksize[0]
     if B.shape[0] != n:
         raise ValueError("arguments must have the same number of rows")
-    if B.partitioning.blocksize[0] != nb or (B.ndim == 2 and B.partitioning.blocksize[1] != nb):
-        raise ValueError("B must be blocked Blocks(nb, nb) (or Blocks(nb)) like the factors")
+    nb = min(A.partitioning.blocksize)
+    Ab = _buffered(A, Blocks(nb, nb), stream)
+    Bb = _buffered(B, Blocks(nb) if B.ndim == 1 else Blocks(nb, nb), stream)
     nrhs = 1 if B.ndim == 1 else B.shape[1]
-    rc = lib().dg_lu_solve_tiled(n, nb, A.tile_ptrs(), F.ipiv.data_ptr(), nrhs, B.tile_ptrs(),
+    rc = lib().dg_lu_solve_tiled(n, nb, Ab.tile_ptrs(), F.ipiv.data_ptr(), nrhs, Bb.tile_ptrs(),
                                  _stream(stream))
     check(rc)
+    if Bb is not B:
+        copy_reblock(Bb, B, stream)
     return B
 
 
@@ -443,16 +490,24 @@ def ldiv(F: LU, B, stream=None) -> DArray:
 
 
 def _mul_blocks(*arrays):
-    nb = None
+    """The one square block size the tile products run at: the operands'
+    own when they all share Blocks(nb, nb), else the smallest block size of
+    any operand (the reference's _repartition_matmatmul falls back to the
+    smallest blocking, mul.jl:44-94)."""
     for X in arrays:
         if X.ndim != 2 or len(X.partitioning.blocksize) != 2:
             raise ValueError("mul needs 2-D DArrays")
-        b0, b1 = X.partitioning.blocksize
-        if b0 != b1 or (nb is not None and b0 != nb):
-            raise ValueError("mul needs every operand blocked Blocks(nb, nb) with the same nb "
-                             "(maybe_copy_buffered re-blocks in the reference)")
-        nb = b0
-    return nb
+    return min(min(X.partitioning.blocksize) for X in arrays)
+
+
+def _buffered_all(nb, arrays, stream):
+    seen = {}
+    out = []
+    for X in arrays:  # an operand passed twice (A === B) is copied once
+        if id(X) not in seen:
+            seen[id(X)] = _buffered(X, Blocks(nb, nb), stream)
+        out.append(seen[id(X)])
+    return out
 
 
 def _trans(t: str) -> bytes:
@@ -470,9 +525,12 @@ def gemm_dagger_(C: DArray, transA: str, transB: str, A: DArray, B: DArray, alph
     k2, n = (B.shape if transB == 'N' else B.shape[::-1])
     if k != k2 or C.shape != (m, n):
         raise ValueError(f"DimensionMismatch: op(A) {m}x{k}, op(B) {k2}x{n}, C {C.shape}")
+    Ab, Bb, Cb = _buffered_all(nb, (A, B, C), stream)
     check(lib().dg_gemm_tiled(_trans(transA), _trans(transB), m, n, k, nb, float(alpha),
-                              A.tile_ptrs(), B.tile_ptrs(), float(beta), C.tile_ptrs(),
+                              Ab.tile_ptrs(), Bb.tile_ptrs(), float(beta), Cb.tile_ptrs(),
                               _stream(stream)))
+    if Cb is not C:
+        copy_reblock(Cb, C, stream)
     return C
 
 
@@ -484,8 +542,11 @@ def syrk_dagger_(C: DArray, trans: str, A: DArray, alpha=1.0, beta=0.0, stream=N
     n, k = (A.shape if trans == 'N' else A.shape[::-1])
     if C.shape != (n, n):
         raise ValueError(f"DimensionMismatch: op(A) {n}x{k}, C {C.shape}")
-    check(lib().dg_syrk_tiled(_trans(trans), n, k, nb, float(alpha), A.tile_ptrs(), float(beta),
-                              C.tile_ptrs(), _stream(stream)))
+    Ab, Cb = _buffered_all(nb, (A, C), stream)
+    check(lib().dg_syrk_tiled(_trans(trans), n, k, nb, float(alpha), Ab.tile_ptrs(), float(beta),
+                              Cb.tile_ptrs(), _stream(stream)))
+    if Cb is not C:
+        copy_reblock(Cb, C, stream)
     return C
 
 
@@ -507,18 +568,16 @@ def matmul(A: DArray, B: DArray, transA: str = 'N', transB: str = 'N', stream=No
     return mul_(C, A, B, 1.0, 0.0, transA, transB, stream)
 
 
-def _herm_pairs(A: DArray):
-    nb = _square_blocks(A)
-    return nb
-
-
 def ishermitian(A: DArray, stream=None) -> bool:
     """ishermitian(::DArray) (linalg.jl:90-124): diagonal tiles exactly
-    symmetric; off-diagonal pairs within sqrt(eps) in Frobenius norm."""
+    symmetric; off-diagonal pairs within sqrt(eps) in Frobenius norm.  A
+    DArray with Blocks(mb, nb), mb != nb, is checked on a copy re-blocked to
+    Blocks(min, min), as the reference does."""
     if A.ndim != 2 or A.shape[0] != A.shape[1]:
         return False
     nb = _square_blocks(A)
-    rc = lib().dg_ishermitian_tiled(A.shape[0], nb, A.tile_ptrs(), _stream(stream))
+    W = _buffered(A, Blocks(nb, nb), stream)
+    rc = lib().dg_ishermitian_tiled(A.shape[0], nb, W.tile_ptrs(), _stream(stream))
     if rc < 0:
         check(rc)
     return rc == 1

@@ -287,12 +287,15 @@ def latency_stats(reqs):
 class MatrixFactory:
     """Seeded SPD matrices A = Q diag(l) Q' (Q from the QR of a Gaussian, one
     per distinct order, computed in FP32 and cached; l log-spaced on
-    [1, kappa]), built on the device and widened to FP64."""
+    [1, kappa]), built on the device and widened to FP64.  Matrices are
+    cached by (n, kappa), so request streams drawn with the same seed at
+    different arrival rates share their matrices."""
 
     def __init__(self, device, seed=0):
         self.device = torch.device(device)
         self.seed = seed
         self.q = {}
+        self.mats = {}
 
     def Q(self, n):
         if n not in self.q:
@@ -303,6 +306,9 @@ class MatrixFactory:
         return self.q[n]
 
     def matrix(self, n, kappa):
+        key = (n, kappa)
+        if key in self.mats:
+            return self.mats[key]
         Q = self.Q(n)
         lam = torch.logspace(0.0, math.log10(kappa), n, device=self.device, dtype=torch.float32)
         prev = torch.backends.cuda.matmul.allow_tf32
@@ -310,7 +316,12 @@ class MatrixFactory:
         A = ((Q * lam) @ Q.T).double()
         torch.backends.cuda.matmul.allow_tf32 = prev
         A = 0.5 * (A + A.T)
+        self.mats[key] = A
         return A
+
+    def drop_q(self):
+        """Frees the cached orthogonal factors (the matrices stay)."""
+        self.q.clear()
 
 
 def make_workload(count, rate, seed=0, nlo=64, nhi=16384, klo=1e2, khi=1e6, rmax=64,
@@ -318,16 +329,19 @@ def make_workload(count, rate, seed=0, nlo=64, nhi=16384, klo=1e2, khi=1e6, rmax
     """Poisson arrivals at `rate` per second: n log-uniform on [nlo, nhi]
     (rounded to a multiple of round_to), kappa log-uniform on [klo, khi],
     1..rmax right-hand sides, a fraction `reuse` of requests reusing an
-    earlier matrix (a resident factor) with new right-hand sides.  Returns
-    a list of (arrival offset in s, Request)."""
+    earlier matrix (a resident factor) with new right-hand sides.  The
+    requests' contents depend on `seed` only and the arrival times on
+    (seed, rate), so streams at different rates carry the same requests.
+    Returns a list of (arrival offset in s, Request)."""
     import random
     rnd = random.Random(seed)
+    arr = random.Random(f"arrivals:{seed}:{rate}")
     fac = factory or MatrixFactory(device, seed)
     t = 0.0
     out = []
     mats = []   # (matrix_id, A, kappa)
     for i in range(count):
-        t += rnd.expovariate(rate) if rate > 0 else 0.0
+        t += arr.expovariate(rate) if rate > 0 else 0.0
         if mats and rnd.random() < reuse:
             mid, A, kap = mats[rnd.randrange(len(mats))]
         else:

@@ -240,6 +240,19 @@ int dg_ishermitian_tiled(int n, int nb, double *const *tiles, void *stream);
 /* LAPACK.chkfinite(::DArray) (src/array/linalg.jl:138-148): 1 when every
  * element is finite, 0 otherwise.  Synchronises `stream`. */
 int dg_chkfinite_tiled(int n, int nb, double *const *tiles, void *stream);
+/* The same over an m x n tile grid with Blocks(mb, nb) (lu!'s chkfinite of a
+ * rectangular DArray, src/array/lu.jl:306-309 -> linalg.jl:138-148). */
+int dg_chkfinite_tiled_mn(int m, int n, int mb, int nb, double *const *tiles, void *stream);
+
+/* copyto!(buffer, A) between two tilings of one m x n matrix: the copy of
+ * maybe_copy_buffered / copy_buffered (src/array/copy.jl:3-37), which
+ * _chol! (cholesky.jl:34), ldiv! (linalg.jl:362-404) and mul!
+ * (mul.jl:11-41) use to move an argument to the Blocks they need and back.
+ * src_tiles / dst_tiles: host arrays of device tile pointers for Blocks(src_mb,
+ * src_nb) and Blocks(dst_mb, dst_nb); a vector is n = 1 with nb = 1.
+ * Stream-ordered (the pointer grids are staged before the call returns). */
+int dg_copy_reblock(int m, int n, int src_mb, int src_nb, double *const *src_tiles, int dst_mb,
+                    int dst_nb, double *const *dst_tiles, void *stream);
 
 /* Selects the FP64 tile engine: 0 = DFMA register tiles, 1 = DMMA
  * (mma.sync.m8n8k4.f64), 2 = DFMA for POTRF/TRSM plus, inside
@@ -380,12 +393,14 @@ int dg_batched_potrs(int count, const int *n, const int *nrhs, double *const *A,
  * that loads the library until exit) and calls no allocator.  Limits: at most
  * 4096 systems, and in mode 1 the FP32 workspaces (4 n^2 bytes per system,
  * 256-byte aligned) plus the descriptors must fit the 64 MiB; a larger batch
- * returns DG_ERR_NOMEM without launching.  The first call on a device looks up
- * the array's device address (set-up, once per device): make that first call
- * before any stream capture.  Every call uses the same array, so calls that
- * overlap on the GPU (on different streams) race; serialise them.  The call
- * synchronises `stream`.  Arguments and results as dg_batched_potrs, without
- * the timing output. */
+ * returns DG_ERR_NOMEM without launching.  Each call looks up the array's
+ * device address on the current device (cudaGetSymbolAddress, no
+ * allocation).  The call is synchronous: it stages descriptors from host
+ * memory and synchronises `stream` before it returns, so it cannot be called
+ * while `stream` is being captured into a graph.  Every call uses the same
+ * array, so calls that overlap on the GPU (on different streams or host
+ * threads) race; serialise them.  Arguments and results as dg_batched_potrs,
+ * without the timing output. */
 int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs, double *const *A,
                              const double *const *B, double *const *X, int mode, double tol,
                              int max_iter, const int *bucket_w, int ctas_per_sm, int *info,

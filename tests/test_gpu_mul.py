@@ -91,10 +91,9 @@ def test_gemm_argument_errors():
     import dagger_gb300 as d
     P = d.Blocks(64, 64)
     A = d.DArray.zeros(P, (128, 64))
-    B = d.DArray.zeros(d.Blocks(32, 32), (64, 64))
     C = d.DArray.zeros(P, (128, 64))
     with pytest.raises(ValueError):
-        d.gemm_dagger_(C, 'N', 'N', A, B)      # mixed block sizes
+        d.gemm_dagger_(C, 'N', 'N', A, d.DArray.zeros(P, (32, 64)))  # 128x64 times 32x64
     with pytest.raises(ValueError):
         d.gemm_dagger_(C, 'T', 'N', A, d.DArray.zeros(P, (64, 64)))  # 64x128 times 64x64
     assert d.lib().dg_gemm_tiled(b'X', b'N', 1, 1, 1, 1, 1.0, None, None, 0.0, None, None) == -1
