@@ -153,6 +153,17 @@ int potrf_f64(char uplo, int n, double *A, int lda, int *info_out, int info_offs
 int potrf_f32(char uplo, int n, float *A, long long lda, int *info_out, int info_offset,
               cudaStream_t s, const int *abort_flag = nullptr, const int *abort2 = nullptr);
 
+// FP32 factor U (A = U'U, upper, in place) of one n x n block (n <= 1024) and
+// V = U^-1 (upper, zero below), one cooperative launch (mixed_diag.cu).
+// mode 0 factors and inverts (info: atomicCAS of info_off + column + 1 on a
+// failed pivot); mode 1 only inverts an already factored block, and runs only
+// when *run_if != 0.  scratch: diag_chol_inv_scratch_bytes(), not shared by
+// launches that may overlap.
+size_t diag_chol_inv_scratch_bytes();
+int diag_chol_inv_f32(float *D, long long ld, int n, float *V, long long ldv, void *scratch,
+                      int *info, int info_off, int *status, const int *run_if, int mode,
+                      cudaStream_t s);
+
 // W (n x n, ldw) = I.
 int eye_f64(int n, double *W, int ldw, const int *abort_flag, cudaStream_t s);
 int scale_f64(int m, int n, double alpha, double *B, int ldb, const int *abort_flag,

@@ -292,6 +292,12 @@ int launch(const GemmArgs &g, cudaStream_t s) {
       gemm_dmma<<<grid, 128, 0, s>>>(g);
     else
       gemm_fma<double, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(g);
+  } else if (g.n <= 64 && !g.tnb && (long long)g.m >= 128LL * dg_num_sms()) {
+    // tall and narrow (the refinement's triangular solves with up to 64
+    // right-hand sides): 128 x 64 tiles, 8 x 4 registers per thread
+    dim3 grid((g.m + 127) / 128, (g.n + 63) / 64);
+    if (grid.y > 65535) return DG_ERR_UNSUPPORTED;
+    gemm_fma<float, 128, 64, 16, 8, 4><<<grid, 256, 0, s>>>(g);
   } else if (g.n <= 64 || (long long)g.m * g.n < 128LL * 128 * 2 * dg_num_sms()) {
     // narrow or small outputs (the triangular solves' few right-hand sides):
     // 32 x 64 tiles give enough CTAs to fill the GPU

@@ -46,13 +46,18 @@ struct dg_mixed {
   double *s = nullptr;           // diagonal scaling
   double **tiles_dev = nullptr;  // caller's FP64 tiles (device array of pointers)
   void *P_hi = nullptr, *P_lo = nullptr;  // 16-bit panel operands (T x nb, K-major)
+  void *P_mid = nullptr;                  // the middle slices (bf16x6 only)
   float *diag_backup = nullptr;  // diagonal block before its FP32 POTRF
   double *d64 = nullptr;         // FP64 scratch of the retry
   float *panel_max = nullptr;    // per-step |panel| maximum (FP16 scaling)
   float *alpha_dev = nullptr;    // per-step -1/scale^2 of the trailing update
   float *Vinv = nullptr;         // inverses of the diagonal blocks (mt x nb x nb)
   float *Lp = nullptr;           // block columns of the factor, transposed (backward solves)
-  int *words = nullptr;          // [0] status, [1] retries, [2] first bad diagonal, [3..] info_k
+  void *diag_scratch = nullptr;  // the diagonal-block kernel's barrier words and scratch
+  void *S3v = nullptr;           // 3 BF16 slices of Vinv_k (nb x nb each)
+  void *S3r = nullptr;           // 3 BF16 slices of panel k's rest (nb x (n - nb) each)
+  int *words = nullptr;          // [0] status, [1] retries, [2] first bad diagonal,
+                                 // [3..3+mt) info_k, [3+mt..3+2mt) retried_k
   double normA = 0.0;            // ||A||_inf
   size_t bytes = 0;
   int info = 0, retries = 0;
@@ -86,19 +91,26 @@ __global__ void diag_scale_kernel(const double *const *tiles, int n, int nb, int
   }
 }
 
-// Row sums of |A| over the tile grid (for ||A||_inf).
+// Row sums of |A| over the tile grid (for ||A||_inf): CTA (x, y) sums the
+// rows x*256.. over tile column y (each thread one row, reading down the
+// tile's columns: consecutive threads read consecutive addresses) and adds its
+// partial sums into out (zeroed before the launch).
 __global__ void row_abs_sum_kernel(const double *const *tiles, int n, int nb, int mt, double *out) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int t = i / nb, p = i - t * nb;
-    const int rows = min(nb, n - t * nb);
-    double acc = 0.0;
-    for (int tj = 0; tj < mt; tj++) {
-      const double *a = tile_ptr(tiles, mt, t, tj) + p;
-      const int cols = min(nb, n - tj * nb);
-      for (int c = 0; c < cols; c++) acc += fabs(a[(size_t)c * rows]);
-    }
-    out[i] = acc;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, tj = blockIdx.y;
+  if (i >= n) return;
+  const int t = i / nb, p = i - t * nb;
+  const int rows = min(nb, n - t * nb), cols = min(nb, n - tj * nb);
+  const double *a = tile_ptr(tiles, mt, t, tj) + p;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int c = 0;
+  for (; c + 4 <= cols; c += 4) {
+    s0 += fabs(a[(size_t)c * rows]);
+    s1 += fabs(a[(size_t)(c + 1) * rows]);
+    s2 += fabs(a[(size_t)(c + 2) * rows]);
+    s3 += fabs(a[(size_t)(c + 3) * rows]);
   }
+  for (; c < cols; c++) s0 += fabs(a[(size_t)c * rows]);
+  atomicAdd(out + i, (s0 + s1) + (s2 + s3));
 }
 
 __host__ __device__ inline long long panel_base(long long r, long long n, long long nb) {
@@ -162,7 +174,8 @@ __global__ void pack_kernel(const double *const *tiles, int n, int nb, int mt, c
 // factored right-looking in FP64 (lower form, L = U'), narrowed back.
 __global__ void __launch_bounds__(1024) retry_potrf_kernel(int nbk, int ld, const float *backup,
                                                            double *L, float *diag, int *info_k,
-                                                           int *status, int *retries, int offset) {
+                                                           int *status, int *retries, int offset,
+                                                           int *retried_k) {
   if (*(volatile int *)info_k == 0 || *(volatile int *)status != 0) return;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < nbk * nbk; e += nt) {
@@ -204,6 +217,7 @@ __global__ void __launch_bounds__(1024) retry_potrf_kernel(int nbk, int ld, cons
   __syncthreads();
   if (tid == 0) {
     *info_k = 0;
+    *retried_k = 1;
     atomicAdd(retries, 1);
   }
 }
@@ -244,6 +258,26 @@ __global__ void convert_kernel(const float *src, long long n, int terms, void *h
       ((__nv_bfloat16 *)hi_)[i] = h;
       if (terms == 3) ((__nv_bfloat16 *)lo_)[i] = __float2bfloat16_rn(x - __bfloat162float(h));
     }
+  }
+}
+
+// x -> three BF16 slices (x = hi + mid + lo up to the rounding of lo): the
+// operands of the FP32-accurate tensor-core product (tc_gemm terms 6).
+// `rows` of every `ld` elements are converted (n elements in all).
+__global__ void split3_kernel(const float *src, long long n, __nv_bfloat16 *hi, __nv_bfloat16 *mid,
+                              __nv_bfloat16 *lo, const int *a1, const int *a2, int rows = 0,
+                              long long ld = 0) {
+  if (aborted(a1, a2)) return;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = rows ? (e % rows) + (e / rows) * ld : e;
+    const float x = src[i];
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+    hi[i] = h;
+    mid[i] = m;
+    lo[i] = __float2bfloat16_rn(r1 - __bfloat162float(m));
   }
 }
 
@@ -295,40 +329,68 @@ int grid_for(long long n) {
 // ---------------------------------------------------------------------------
 // factorization
 // ---------------------------------------------------------------------------
-namespace {
-__global__ void identity_kernel(float *V, int nbk, int ld) {
-  const long long total = (long long)ld * nbk;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(e % ld), j = (int)(e / ld);
-    V[e] = (i == j && i < nbk) ? 1.f : 0.f;
-  }
-}
-}  // namespace
 
-int mixed_invert_diagonal_block(dg_mixed *f, int k, cudaStream_t s);
-
-// Step k's panel: FP32 POTRF of the diagonal block (FP64 retry on a failed
-// pivot), the inverse of the block (kept for the solves), the FP32 TRSM of the
-// rest of the panel, and its conversion to 16-bit operands in P buffer k % 2.
+// Step k's panel: the FP32 factor of the diagonal block and its inverse in
+// one cooperative launch (mixed_diag.cu; an FP64 retry on a failed pivot,
+// then the inverse of the retried factor), the solve of the rest of the
+// panel as the product Vinv_k' A(k, k+1:) on the tensor cores with
+// FP32-accurate operands (3 BF16 slices, 6 products), and its conversion to
+// the 16-bit operands of the trailing update in P buffer k % 2.
 static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
-  const int n = f->n, nb = f->nb;
+  const int n = f->n, nb = f->nb, mt = f->mt;
   int *status = f->words, *retries = f->words + 1, *ik = f->words + 3 + k;
+  int *retried = f->words + 3 + mt + k;
   float *Pk = f->W + panel_base(k, n, nb);
+  float *Vk = f->Vinv + (size_t)k * nb * nb;
   const int nbk = std::min(nb, n - k * nb);
   const long long T = (long long)n - (long long)(k + 1) * nb;
   DG_CUDA_TRY(cudaMemcpyAsync(f->diag_backup, Pk, sizeof(float) * (size_t)nb * nbk,
                               cudaMemcpyDeviceToDevice, s));
-  DG_TRY(potrf_f32('U', nbk, Pk, nb, ik, k * nb, s, status));
+  DG_TRY(diag_chol_inv_f32(Pk, nb, nbk, Vk, nb, f->diag_scratch, ik, k * nb, status, nullptr, 0,
+                           s));
   retry_potrf_kernel<<<1, 1024, 0, s>>>(nbk, nb, f->diag_backup, f->d64, Pk, ik, status, retries,
-                                        k * nb);
+                                        k * nb, retried);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
-  DG_TRY(mixed_invert_diagonal_block(f, k, s));
+  DG_TRY(diag_chol_inv_f32(Pk, nb, nbk, Vk, nb, f->diag_scratch, ik, k * nb, status, retried, 1,
+                           s));
   if (T <= 0) return 0;
   float *Rk = Pk + (size_t)nb * nb;  // the rest of panel k: nb x T
-  DG_TRY(trsm_f32('L', 'U', 'T', 'N', nbk, (int)T, 1.f, Pk, nb, Rk, nb, ik, s, status));
+  {
+    // Rk = Vk' Rk: both operands cut into three BF16 slices
+    const size_t vn = (size_t)nb * nb, rn = (size_t)nb * T;
+    __nv_bfloat16 *v3 = (__nv_bfloat16 *)f->S3v, *r3 = (__nv_bfloat16 *)f->S3r;
+    const size_t rcap = (size_t)nb * std::max(0, n - nb);
+    split3_kernel<<<grid_for((long long)vn), 256, 0, s>>>(Vk, (long long)vn, v3, v3 + vn,
+                                                          v3 + 2 * vn, ik, status);
+    split3_kernel<<<grid_for((long long)rn), 256, 0, s>>>(Rk, (long long)rn, r3, r3 + rcap,
+                                                          r3 + 2 * rcap, ik, status);
+    count_launches(2);
+    DG_CUDA_TRY(cudaGetLastError());
+    TcGemmArgs g;
+    memset(&g, 0, sizeof g);
+    g.m = nbk; g.n = (int)T; g.k = nbk; g.terms = 6;
+    g.a_hi = v3; g.a_mid = v3 + vn; g.a_lo = v3 + 2 * vn;
+    g.lda = nb; g.a_rows = nbk; g.a_row0 = 0;
+    g.b_hi = r3; g.b_mid = r3 + rcap; g.b_lo = r3 + 2 * rcap;
+    g.ldb = nb; g.b_rows = (int)T; g.b_row0 = 0;
+    g.alpha = 1.f; g.beta = 0.f;
+    g.c = Rk; g.ldc = nb; g.layout = 0; g.upper = 0;
+    g.bn = 128; g.status = status;
+    DG_TRY(tc_gemm_bf16(g, s));
+  }
   if (f->precision == DG_PREC_FP32) return 0;
+  const size_t half0 = (size_t)std::max(0LL, (long long)n - nb) * nb;
+  if (f->precision == DG_PREC_BF16X6) {
+    __nv_bfloat16 *h = (__nv_bfloat16 *)f->P_hi + (size_t)(k & 1) * half0;
+    __nv_bfloat16 *m = (__nv_bfloat16 *)f->P_mid + (size_t)(k & 1) * half0;
+    __nv_bfloat16 *l = (__nv_bfloat16 *)f->P_lo + (size_t)(k & 1) * half0;
+    const long long elems = (long long)nb * T;
+    split3_kernel<<<grid_for(elems), 256, 0, s>>>(Rk, elems, h, m, l, ik, status);
+    count_launches(1);
+    DG_CUDA_TRY(cudaGetLastError());
+    return 0;
+  }
   const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
   const int terms = (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
   const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;  // elements per P buffer
@@ -359,7 +421,8 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   const long long T = (long long)n - (long long)(k + 1) * nb;
   if (T <= 0) return 0;
   const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
-  const int terms = (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
+  const int terms = f->precision == DG_PREC_BF16X6 ? 6
+                  : (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
   const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;
   TcGemmArgs g;
   memset(&g, 0, sizeof g);
@@ -378,6 +441,11 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   g.b_hi = g.a_hi; g.b_lo = g.a_lo;
   g.lda = nb; g.ldb = nb; g.a_rows = (int)T; g.b_rows = (int)T;
   g.alpha = -1.f; g.alpha_dev = f->alpha_dev + k; g.beta = 1.f;
+  if (terms == 6) {
+    g.a_mid = (char *)f->P_mid + (size_t)(k & 1) * half * 2;
+    g.b_mid = g.a_mid;
+    g.alpha_dev = nullptr;  // unscaled BF16 slices: alpha = -1
+  }
   g.c = f->W; g.layout = 1; g.upper = 1;
   g.nb = nb; g.ntot = n;
   g.bn = 128; g.status = f->words;
@@ -404,7 +472,7 @@ static int trailing_f32(dg_mixed *f, int k, cudaStream_t s) {
 int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
   const int n = f->n, nb = f->nb, mt = f->mt;
   int *bad = f->words + 2;
-  DG_CUDA_TRY(cudaMemsetAsync(f->words, 0, sizeof(int) * (3 + mt), s));
+  DG_CUDA_TRY(cudaMemsetAsync(f->words, 0, sizeof(int) * (3 + 2 * mt), s));
   DG_CUDA_TRY(cudaMemsetAsync(bad, 0x7f, sizeof(int), s));
   diag_scale_kernel<<<grid_for(n), 256, 0, s>>>(f->tiles_dev, n, nb, mt, f->s, bad);
   pack_kernel<<<dim3(std::max(1, std::min(1024, (int)((long long)nb * n / 256 + 1))), mt), 256, 0,
@@ -439,20 +507,6 @@ int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
   return 0;
 }
 
-
-// Vinv_k = U~_kk^-1 for diagonal block k (FP32, upper triangular, zero
-// below): the triangular solves of refinement then become GEMMs, whose
-// parallelism does not depend on the number of right-hand sides.
-int mixed_invert_diagonal_block(dg_mixed *f, int k, cudaStream_t s) {
-  const int n = f->n, nb = f->nb;
-  const float *Pk = f->W + panel_base(k, n, nb);
-  const int nbk = std::min(nb, n - k * nb);
-  float *V = f->Vinv + (size_t)k * nb * nb;
-  identity_kernel<<<grid_for((long long)nb * nbk), 256, 0, s>>>(V, nbk, nb);
-  count_launches(1);
-  DG_CUDA_TRY(cudaGetLastError());
-  return trsm_f32('L', 'U', 'N', 'N', nbk, nbk, 1.f, Pk, nb, V, nb, f->words + 3 + k, s, f->words);
-}
 
 // Solves U~' U~ Z = Z (FP32, n x r, column-major ldz) on the packed panels,
 // with Z2 (same shape) as the second buffer: forward Z2_k = Vinv_k' Z_k and
@@ -523,7 +577,7 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   DG_CHECK_ARG(tiles != nullptr, 4);
   DG_CHECK_ARG(precision == DG_PREC_BF16 || precision == DG_PREC_BF16X3 ||
                    precision == DG_PREC_FP16 || precision == DG_PREC_FP16X3 ||
-                   precision == DG_PREC_FP32,
+                   precision == DG_PREC_FP32 || precision == DG_PREC_BF16X6,
                5);
   DG_CHECK_ARG(shift >= 0.0, 6);
   cudaStream_t s = (cudaStream_t)stream;
@@ -545,13 +599,18 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
       {(void **)&f->tiles_dev, sizeof(double *) * (size_t)mt * mt},
       {(void **)&f->P_hi, 2 * 2 * (size_t)std::max(1LL, tmax) * nb},
       {(void **)&f->P_lo, 2 * 2 * (size_t)std::max(1LL, tmax) * nb},
+      {(void **)&f->P_mid, precision == DG_PREC_BF16X6 ? 2 * 2 * (size_t)std::max(1LL, tmax) * nb
+                                                        : (size_t)256},
       {(void **)&f->diag_backup, sizeof(float) * (size_t)nb * nb},
       {(void **)&f->d64, sizeof(double) * (size_t)nb * nb},
       {(void **)&f->panel_max, sizeof(float) * (size_t)mt},
       {(void **)&f->alpha_dev, sizeof(float) * (size_t)mt},
-      {(void **)&f->words, sizeof(int) * (size_t)(3 + mt)},
+      {(void **)&f->words, sizeof(int) * (size_t)(3 + 2 * mt)},
       {(void **)&f->Vinv, sizeof(float) * (size_t)mt * nb * nb},
       {(void **)&f->Lp, sizeof(float) * (size_t)dg::lp_base(mt, nb)},
+      {(void **)&f->diag_scratch, dg::diag_chol_inv_scratch_bytes()},
+      {(void **)&f->S3v, 3 * 2 * (size_t)nb * nb},
+      {(void **)&f->S3r, 3 * 2 * (size_t)std::max(1LL, tmax) * nb},
   };
   f->stream = s;
   for (auto &a : allocs) {
@@ -570,7 +629,8 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   if (cudaMallocAsync((void **)&rows, sizeof(double) * (n + 1), s) != cudaSuccess)
     return fail(DG_ERR_NOMEM);
   dmax = rows + n;
-  dg::row_abs_sum_kernel<<<grid_for(n), 256, 0, s>>>(f->tiles_dev, n, nb, mt, rows);
+  if (cudaMemsetAsync(rows, 0, sizeof(double) * n, s) != cudaSuccess) return fail(DG_ERR_CUDA);
+  dg::row_abs_sum_kernel<<<dim3((n + 255) / 256, mt), 256, 0, s>>>(f->tiles_dev, n, nb, mt, rows);
   dg::colmax_kernel<<<1, 1024, 0, s>>>(rows, n, n, dmax);
   dg::count_launches(2);
   cudaMemcpyAsync(&f->normA, dmax, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -611,8 +671,9 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
 
 extern "C" void dg_mixed_destroy(dg_mixed *f) {
   if (!f) return;
-  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
-                f->panel_max, f->alpha_dev, f->words, f->Vinv, f->Lp};
+  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->P_mid, f->diag_backup, f->d64,
+                f->panel_max, f->alpha_dev, f->words, f->Vinv, f->Lp, f->diag_scratch,
+                f->S3v, f->S3r};
   for (void *p : ps)
     if (p) cudaFreeAsync(p, f->stream);  // stream-ordered: no device-wide synchronisation
   if (f->ev_next) cudaEventDestroy(f->ev_next);
@@ -980,4 +1041,35 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
     return DG_ERR_NOCONVERGE;
   }
   return 0;
+}
+
+extern "C" int dg_gemm_f32_tc_tn(int m, int n, int k, float alpha, const float *A, int lda,
+                                 const float *B, int ldb, float beta, float *C, int ldc,
+                                 void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(k > 0 && k % 8 == 0, 3);
+  DG_CHECK_ARG(lda >= k && lda % 8 == 0, 6);
+  DG_CHECK_ARG(ldb >= k && ldb % 8 == 0, 8);
+  DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 11);
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t an = (size_t)lda * m, bn = (size_t)ldb * n;
+  __nv_bfloat16 *buf = nullptr;
+  DG_CUDA_TRY(cudaMallocAsync((void **)&buf, sizeof(__nv_bfloat16) * 3 * (an + bn), s));
+  __nv_bfloat16 *a3 = buf, *b3 = buf + 3 * an;
+  dg::split3_kernel<<<grid_for((long long)k * m), 256, 0, s>>>(
+      A, (long long)k * m, a3, a3 + an, a3 + 2 * an, nullptr, nullptr, k, lda);
+  dg::split3_kernel<<<grid_for((long long)k * n), 256, 0, s>>>(
+      B, (long long)k * n, b3, b3 + bn, b3 + 2 * bn, nullptr, nullptr, k, ldb);
+  dg::count_launches(2);
+  dg::TcGemmArgs g;
+  memset(&g, 0, sizeof g);
+  g.m = m; g.n = n; g.k = k; g.terms = 6;
+  g.a_hi = a3; g.a_mid = a3 + an; g.a_lo = a3 + 2 * an; g.lda = lda; g.a_rows = m;
+  g.b_hi = b3; g.b_mid = b3 + bn; g.b_lo = b3 + 2 * bn; g.ldb = ldb; g.b_rows = n;
+  g.alpha = alpha; g.beta = beta; g.c = C; g.ldc = ldc; g.layout = 0; g.upper = 0; g.bn = 128;
+  int rc = dg::tc_gemm_bf16(g, s);
+  cudaFreeAsync(buf, s);
+  return rc;
 }

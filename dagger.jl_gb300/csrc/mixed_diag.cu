@@ -1,0 +1,523 @@
+// Diagonal block of the mixed-precision factor: the FP32 Cholesky factor
+// U (A = U'U) of one n x n block (n <= 1024) and its inverse V = U^-1, in one
+// cooperative launch.
+//
+// The mixed factorization's critical path is, per block step, the
+// factorization of the diagonal block and the solve of its row panel.  Done
+// as a recursion of small launches (64 x 64 leaves, recursive TRSMs and
+// GEMMs) that chain took several milliseconds per step; here it is one
+// launch of G CTAs working on the L2-resident block with a grid barrier per
+// 32-column step:
+//
+//   step j (blocks of 32 rows/columns, bj = j * 32):
+//     CTA 0        finishes the diagonal tile (j+1, j+1): its last update
+//                  -= U(j, j+1)' U(j, j+1), then one warp factors it and
+//                  inverts the 32 x 32 factor (register-resident, shuffles)
+//     CTAs 1..G-1  update the other tiles (r, c), j+1 <= r <= c, by
+//                  -= U(j, r)' U(j, c), forming the row-panel blocks
+//                  U(j, r) = I_j' A(j, r) on the fly from the inverse I_j of
+//                  the diagonal factor (so no barrier separates the panel
+//                  solve from the update)
+//     grid barrier
+//   then every off-diagonal block of U is formed, U(j, c) = I_j' A(j, c),
+//   and V = U^-1 by recursive doubling over the 32-block inverses:
+//     V12 = -V11 U12 V22, levels of 32, 64, ..., 512 (two barriers each).
+//
+// Blocks past n are read as the identity and never written, so a ragged last
+// block needs no special case.  Every barrier wait is bounded (DG_ERR_TIMEOUT
+// in the status word, then every CTA returns).  A pivot that is not positive
+// (or NaN) records the LAPACK-style info (atomicCAS of offset + column + 1)
+// and stops the launch; the caller's FP64 retry then refactors the block and
+// a second launch in "inverse only" mode forms V from the retried factor.
+#include <math.h>
+
+#include <algorithm>
+
+#include "dg_common.cuh"
+#include "runtime.h"
+#include "tc_ptx.cuh"
+
+namespace dg {
+namespace {
+
+constexpr int DB = 32;            // sub-block order
+constexpr int DT = 256;           // threads per CTA
+constexpr int DP = DB + 1;        // padded shared-memory column
+constexpr int kDiagMaxN = 1024;
+constexpr int kDiagMaxGrid = 64;
+constexpr unsigned FULL = 0xffffffffu;
+
+struct DiagArgs {
+  float *D;            // the block, column-major, ld
+  long long ld;
+  int n;
+  float *V;            // inverse, column-major, ldv (upper; zero below)
+  long long ldv;
+  float *I;            // [nblk][32 x 32] inverses of the diagonal 32-blocks
+  float *T;            // doubling scratch (512 x 512)
+  unsigned *bar;       // barrier counter (zero at launch)
+  int *fail;           // set when a pivot fails (zero at launch)
+  int *info;           // first failed column, 1-based plus info_off
+  int info_off;
+  int *status;         // sticky error word; non-zero on entry = skip
+  const int *run_if;   // mode 1: run only when *run_if != 0
+  int mode;            // 0 = factor + inverse, 1 = inverse of a factored block
+};
+
+__device__ __forceinline__ unsigned ld_acq(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_rel(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier number `epoch` (1, 2, ...); false when the launch must stop
+// (a timeout here or elsewhere, or a failed pivot).
+__device__ bool grid_sync(const DiagArgs &a, unsigned epoch, int *s_stop) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    red_rel(a.bar, 1u);
+    const unsigned target = gridDim.x * epoch;
+    int stop = 0;
+    if (ld_acq(a.bar) < target) {
+      const uint64_t t0 = ptx::globaltimer();
+      while (ld_acq(a.bar) < target) {
+        if (*(volatile int *)a.status) {
+          stop = 1;
+          break;
+        }
+        if (ptx::globaltimer() - t0 > ptx::kWaitNs) {
+          atomicCAS(a.status, 0, DG_ERR_TIMEOUT);
+          stop = 1;
+          break;
+        }
+      }
+    }
+    if (*(volatile int *)a.fail || *(volatile int *)a.status) stop = 1;
+    *s_stop = stop;
+  }
+  __syncthreads();
+  return *s_stop == 0;
+}
+
+// Element (r, c) of an n x n matrix with the identity outside it.
+__device__ __forceinline__ float rd_pad(const float *M, long long ld, int n, int r, int c) {
+  if (r < n && c < n) return __ldcg(M + r + (size_t)c * ld);
+  return r == c ? 1.f : 0.f;
+}
+
+// 32 x 32 tile at (r0, c0) of M into shared t[c * DP + r] (identity padded).
+__device__ __forceinline__ void load_tile(float *t, const float *M, long long ld, int n, int r0,
+                                          int c0) {
+  const int r = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int c = (threadIdx.x >> 5) + 8 * q;
+    t[c * DP + r] = rd_pad(M, ld, n, r0 + r, c0 + c);
+  }
+}
+
+__device__ __forceinline__ void store_tile(const float *t, float *M, long long ld, int n, int r0,
+                                           int c0, bool upper_only) {
+  const int r = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int c = (threadIdx.x >> 5) + 8 * q;
+    if (r0 + r < n && c0 + c < n && (!upper_only || r <= c))
+      __stcg(M + (r0 + r) + (size_t)(c0 + c) * ld, t[c * DP + r]);
+  }
+}
+
+// acc[q] (+)= sum_p X(p, r) Y(p, c): X' Y for this thread's four outputs
+// (r = tid & 31, c = (tid >> 5) + 8 q).
+__device__ __forceinline__ void mma_tn(float (&acc)[4], const float *x, const float *y) {
+  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
+#pragma unroll 8
+  for (int p = 0; p < DB; p++) {
+    const float xv = x[r * DP + p];
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[q] = fmaf(xv, y[(cw + 8 * q) * DP + p], acc[q]);
+  }
+}
+
+// acc[q] (+)= sum_p X(r, p) Y(p, c): X Y.
+__device__ __forceinline__ void mma_nn(float (&acc)[4], const float *x, const float *y) {
+  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
+#pragma unroll 8
+  for (int p = 0; p < DB; p++) {
+    const float xv = x[p * DP + r];
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[q] = fmaf(xv, y[(cw + 8 * q) * DP + p], acc[q]);
+  }
+}
+
+__device__ __forceinline__ void put(float *t, const float (&acc)[4]) {
+  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; q++) t[(cw + 8 * q) * DP + r] = acc[q];
+}
+
+// One warp: b[r] in lane c holds B(r, c), r <= c, of a symmetric 32 x 32
+// block.  On return b[r] = U(r, c) with B = U'U and iv[r] = (U^-1)(r, c)
+// (zero for r > c).  Returns the first column whose pivot is not positive,
+// or -1.
+__device__ int warp_chol32(float (&b)[32], int lane) {
+  int fail = -1;
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    const float d = __shfl_sync(FULL, b[j], j);
+    // d is the same in every lane, so these branches are uniform (and the
+    // loop has no break, so it unrolls and b stays in registers)
+    if (fail < 0 && !(d > 0.f)) fail = j;
+    if (fail >= 0) continue;
+    const float u = sqrtf(d);
+    const float ru = 1.0f / u;
+    if (lane == j) b[j] = u;
+    else if (lane > j) b[j] *= ru;
+#pragma unroll
+    for (int r = j + 1; r < 32; r++) {
+      const float ujr = __shfl_sync(FULL, b[j], r);
+      if (lane >= r) b[r] = fmaf(-ujr, b[j], b[r]);
+    }
+  }
+  return fail;
+}
+
+__device__ void warp_inv32(const float (&b)[32], float (&iv)[32], int lane) {
+  float rd = 0.f;
+#pragma unroll
+  for (int j = 0; j < 32; j++)
+    if (lane == j) rd = 1.0f / b[j];
+#pragma unroll
+  for (int r = 31; r >= 0; r--) {
+    float acc = 0.f;
+#pragma unroll
+    for (int t = r + 1; t < 32; t++) acc = fmaf(__shfl_sync(FULL, b[r], t), iv[t], acc);
+    const float rdr = __shfl_sync(FULL, rd, r);
+    iv[r] = lane > r ? -acc * rdr : (lane == r ? rdr : 0.f);
+  }
+}
+
+// Warp 0 of the calling CTA factors (or, mode 1, only inverts) the tile in
+// shared t; the factor goes back to t, its inverse to ti.  Returns the failed
+// column or -1 (valid in every thread).
+__device__ int tile_factor(float *t, float *ti, bool factor, int *s_fail) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (warp == 0) {
+    float b[32], iv[32];
+#pragma unroll
+    for (int r = 0; r < 32; r++) b[r] = r <= lane ? t[lane * DP + r] : 0.f;
+    int f = -1;
+    if (factor) f = warp_chol32(b, lane);
+    if (f < 0) {
+      warp_inv32(b, iv, lane);
+#pragma unroll
+      for (int r = 0; r < 32; r++) {
+        t[lane * DP + r] = r <= lane ? b[r] : 0.f;
+        ti[lane * DP + r] = iv[r];
+      }
+    }
+    if (lane == 0) *s_fail = f;
+  }
+  __syncthreads();
+  return *s_fail;
+}
+
+__global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
+  __shared__ float sI[DB * DP], sA[DB * DP], sB[DB * DP], sC[DB * DP], sUr[DB * DP],
+      sUc[DB * DP];
+  __shared__ int s_stop, s_fail;
+  // (every CTA takes the same decision: the status word can change during
+  // the launch, but a CTA that returns here leaves the others' barrier
+  // waits to see it and stop)
+  if (*(volatile int *)a.status) return;
+  if (a.mode == 1 && (!a.run_if || *(volatile const int *)a.run_if == 0)) return;
+  const int n = a.n, nblk = (n + DB - 1) / DB;
+  const int G = gridDim.x, g = blockIdx.x;
+  unsigned epoch = 0;
+  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
+
+  if (a.mode == 0) {
+    // ---- block 0 ----
+    if (g == 0) {
+      load_tile(sC, a.D, a.ld, n, 0, 0);
+      const int f = tile_factor(sC, sI, true, &s_fail);
+      if (f >= 0) {
+        if (threadIdx.x == 0) {
+          atomicCAS(a.info, 0, a.info_off + f + 1);
+          atomicExch(a.fail, 1);
+        }
+      } else {
+        store_tile(sC, a.D, a.ld, n, 0, 0, true);
+        store_tile(sI, a.I, DB, DB, 0, 0, false);
+      }
+    }
+    if (!grid_sync(a, ++epoch, &s_stop)) return;
+    // ---- steps ----
+    for (int j = 0; j + 1 < nblk; j++) {
+      const int bj = j * DB;
+      if (g == 0) {
+        // sI holds I_j (formed by this CTA in the previous step)
+        load_tile(sA, a.D, a.ld, n, bj, bj + DB);            // A(j, j+1)
+        load_tile(sC, a.D, a.ld, n, bj + DB, bj + DB);       // tile (j+1, j+1)
+        __syncthreads();
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tn(acc, sI, sA);                                 // U(j, j+1)
+        __syncthreads();
+        put(sUr, acc);
+        __syncthreads();
+        float up[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tn(up, sUr, sUr);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int c = cw + 8 * q;
+          sC[c * DP + r] -= up[q];
+        }
+        const int f = tile_factor(sC, sB, true, &s_fail);
+        if (f >= 0) {
+          if (threadIdx.x == 0) {
+            atomicCAS(a.info, 0, a.info_off + bj + DB + f + 1);
+            atomicExch(a.fail, 1);
+          }
+        } else {
+          store_tile(sC, a.D, a.ld, n, bj + DB, bj + DB, true);
+          store_tile(sB, a.I + (size_t)(j + 1) * DB * DB, DB, DB, 0, 0, false);
+          // sI <- I_(j+1) for the next step
+          for (int e = threadIdx.x; e < DB * DP; e += DT) sI[e] = sB[e];
+        }
+      } else {
+        // the other tiles (r, c), j+1 <= rr <= cc < nblk, (rr, cc) != (j+1, j+1)
+        const int m = nblk - 1 - j;
+        const int ntiles = m * (m + 1) / 2 - 1;
+        if (ntiles > 0) {
+          load_tile(sI, a.I + (size_t)j * DB * DB, DB, DB, 0, 0);
+          for (int t = g - 1; t < ntiles; t += G - 1) {
+            // tile t + 1 of the upper triangle of the m x m tile grid, row-major
+            int idx = t + 1, rr = 0;
+            while (idx >= m - rr) {
+              idx -= m - rr;
+              rr++;
+            }
+            const int cc = rr + idx;
+            const int R0 = (j + 1 + rr) * DB, C0 = (j + 1 + cc) * DB;
+            __syncthreads();
+            load_tile(sA, a.D, a.ld, n, bj, R0);  // A(j, rr)
+            load_tile(sB, a.D, a.ld, n, bj, C0);  // A(j, cc)
+            load_tile(sC, a.D, a.ld, n, R0, C0);  // A(rr, cc)
+            __syncthreads();
+            float ur[4] = {0.f, 0.f, 0.f, 0.f}, uc[4] = {0.f, 0.f, 0.f, 0.f};
+            mma_tn(ur, sI, sA);
+            mma_tn(uc, sI, sB);
+            put(sUr, ur);
+            put(sUc, uc);
+            __syncthreads();
+            float up[4] = {0.f, 0.f, 0.f, 0.f};
+            mma_tn(up, sUr, sUc);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const int c = cw + 8 * q;
+              sC[c * DP + r] -= up[q];
+            }
+            __syncthreads();
+            store_tile(sC, a.D, a.ld, n, R0, C0, rr == cc);
+          }
+        }
+      }
+      if (!grid_sync(a, ++epoch, &s_stop)) return;
+    }
+    // ---- the off-diagonal blocks of U: U(j, c) = I_j' A(j, c) ----
+    {
+      const int nb2 = nblk * (nblk - 1) / 2;
+      int loaded = -1;
+      for (int t = g; t < nb2; t += G) {
+        int idx = t, jj = 0;
+        while (idx >= nblk - 1 - jj) {
+          idx -= nblk - 1 - jj;
+          jj++;
+        }
+        const int cc = jj + 1 + idx;
+        __syncthreads();
+        if (loaded != jj) {
+          load_tile(sI, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0);
+          loaded = jj;
+        }
+        load_tile(sA, a.D, a.ld, n, jj * DB, cc * DB);
+        __syncthreads();
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tn(acc, sI, sA);
+        put(sC, acc);
+        __syncthreads();
+        store_tile(sC, a.D, a.ld, n, jj * DB, cc * DB, false);
+      }
+    }
+  } else {
+    // ---- mode 1: inverses of the diagonal 32-blocks of a factored block ----
+    for (int jj = g; jj < nblk; jj += G) {
+      __syncthreads();
+      load_tile(sC, a.D, a.ld, n, jj * DB, jj * DB);
+      tile_factor(sC, sB, false, &s_fail);
+      store_tile(sB, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0, false);
+    }
+  }
+  // ---- V: I_j on the diagonal, zero below ----
+  for (int t = g; t < nblk * nblk; t += G) {
+    const int rb = t % nblk, cb = t / nblk;
+    if (rb < cb) continue;
+    __syncthreads();
+    if (rb == cb) {
+      load_tile(sC, a.I + (size_t)rb * DB * DB, DB, DB, 0, 0);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) sC[(cw + 8 * q) * DP + r] = 0.f;
+    }
+    __syncthreads();
+    store_tile(sC, a.V, a.ldv, n, rb * DB, cb * DB, false);
+  }
+  if (!grid_sync(a, ++epoch, &s_stop)) return;
+  // ---- recursive doubling: V12 = -V11 U12 V22 ----
+  int npad = DB;
+  while (npad < n) npad *= 2;
+  for (int s = DB; s < npad; s *= 2) {
+    const int nodes = npad / (2 * s), sb = s / DB;
+    const int per = sb * sb;
+    // phase 1: T_q = V11 U12 (V11 upper: k-blocks kb >= rb)
+    for (int t = g; t < nodes * per; t += G) {
+      const int q = t / per, rb = (t % per) % sb, cb = (t % per) / sb;
+      const int b0 = q * 2 * s;
+      if (b0 + s >= n) continue;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int kb = rb; kb < sb; kb++) {
+        __syncthreads();
+        load_tile(sA, a.V, a.ldv, n, b0 + rb * DB, b0 + kb * DB);
+        load_tile(sB, a.D, a.ld, n, b0 + kb * DB, b0 + s + cb * DB);
+        __syncthreads();
+        mma_nn(acc, sA, sB);
+      }
+      float *Tq = a.T + (size_t)q * s * s;
+#pragma unroll
+      for (int qq = 0; qq < 4; qq++) {
+        const int c = cw + 8 * qq;
+        __stcg(Tq + (rb * DB + r) + (size_t)(cb * DB + c) * s, acc[qq]);
+      }
+    }
+    if (!grid_sync(a, ++epoch, &s_stop)) return;
+    // phase 2: V12 = -T_q V22 (V22 upper: k-blocks kb <= cb)
+    for (int t = g; t < nodes * per; t += G) {
+      const int q = t / per, rb = (t % per) % sb, cb = (t % per) / sb;
+      const int b0 = q * 2 * s;
+      if (b0 + s >= n) continue;
+      const float *Tq = a.T + (size_t)q * s * s;
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int kb = 0; kb <= cb; kb++) {
+        __syncthreads();
+#pragma unroll
+        for (int qq = 0; qq < 4; qq++) {
+          const int c = cw + 8 * qq;
+          sA[c * DP + r] = __ldcg(Tq + (rb * DB + r) + (size_t)(kb * DB + c) * s);
+        }
+        load_tile(sB, a.V, a.ldv, n, b0 + s + kb * DB, b0 + s + cb * DB);
+        __syncthreads();
+        mma_nn(acc, sA, sB);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int qq = 0; qq < 4; qq++) acc[qq] = -acc[qq];
+      put(sC, acc);
+      __syncthreads();
+      store_tile(sC, a.V, a.ldv, n, b0 + rb * DB, b0 + s + cb * DB, false);
+    }
+    if (s * 2 < npad && !grid_sync(a, ++epoch, &s_stop)) return;
+  }
+}
+
+}  // namespace
+
+size_t diag_chol_inv_scratch_bytes() {
+  // barrier word + fail word | 32 inverses of 32 x 32 | doubling scratch 512 x 512
+  return 256 + sizeof(float) * (size_t)(kDiagMaxN / DB) * DB * DB +
+         sizeof(float) * (size_t)(kDiagMaxN / 2) * (kDiagMaxN / 2);
+}
+
+int diag_chol_inv_f32(float *D, long long ld, int n, float *V, long long ldv, void *scratch,
+                      int *info, int info_off, int *status, const int *run_if, int mode,
+                      cudaStream_t s) {
+  if (n <= 0) return 0;
+  if (n > kDiagMaxN || ld < n || ldv < n) return DG_ERR_UNSUPPORTED;
+  char *sc = (char *)scratch;
+  DiagArgs a;
+  a.D = D;
+  a.ld = ld;
+  a.n = n;
+  a.V = V;
+  a.ldv = ldv;
+  a.bar = (unsigned *)sc;
+  a.fail = (int *)(sc + 4);
+  a.I = (float *)(sc + 256);
+  a.T = a.I + (size_t)(kDiagMaxN / DB) * DB * DB;
+  a.info = info;
+  a.info_off = info_off;
+  a.status = status;
+  a.run_if = run_if;
+  a.mode = mode;
+  const int nblk = (n + DB - 1) / DB;
+  int G = std::min(kDiagMaxGrid, std::max(2, nblk * (nblk + 1) / 2 + 1));
+  G = std::min(G, dg_num_sms());
+  DG_CUDA_TRY(cudaMemsetAsync(sc, 0, 8, s));
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.gridDim = dim3(G);
+  cfg.blockDim = dim3(DT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  DG_CUDA_TRY(cudaLaunchKernelEx(&cfg, diag_chol_inv_kernel, a));
+  count_launches(1);
+  return 0;
+}
+
+}  // namespace dg
+
+// Building block of the mixed form (no counterpart in the reference): the
+// FP32 factor U (A = U'U, upper) of one n x n block in place and V = U^-1,
+// both column-major; *info_host = the 1-based column of the first pivot that
+// is not positive (0 when none).  Synchronises `stream`.
+extern "C" int dg_potrf_inv_f32(int n, float *A, int lda, float *V, int ldv, int *info_host,
+                                void *stream) {
+  DG_CHECK_ARG(n >= 0 && n <= 1024, 1);
+  DG_CHECK_ARG(A != nullptr || n == 0, 2);
+  DG_CHECK_ARG(lda >= (n > 1 ? n : 1), 3);
+  DG_CHECK_ARG(V != nullptr || n == 0, 4);
+  DG_CHECK_ARG(ldv >= (n > 1 ? n : 1), 5);
+  DG_CHECK_ARG(info_host != nullptr, 6);
+  *info_host = 0;
+  if (n == 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  char *buf = nullptr;
+  const size_t sb = dg::diag_chol_inv_scratch_bytes();
+  DG_CUDA_TRY(cudaMallocAsync((void **)&buf, sb + 256, s));
+  int *words = (int *)(buf + sb);  // [0] info, [1] status
+  DG_CUDA_TRY(cudaMemsetAsync(words, 0, 8, s));
+  int rc = dg::diag_chol_inv_f32(A, lda, n, V, ldv, buf, words, 0, words + 1, nullptr, 0, s);
+  int h[2] = {0, 0};
+  if (!rc) {
+    DG_CUDA_TRY(cudaMemcpyAsync(h, words, 8, cudaMemcpyDeviceToHost, s));
+  }
+  DG_CUDA_TRY(cudaFreeAsync(buf, s));
+  DG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (rc) return rc;
+  if (h[1]) {
+    dg_set_last_error(__FILE__, __LINE__, "a bounded grid barrier wait timed out");
+    return h[1];
+  }
+  *info_host = h[0];
+  return h[0];
+}

@@ -10,6 +10,12 @@
 // hi*hi + hi*lo + lo*hi accumulate into the same FP32 TMEM accumulator,
 // carrying about 16 significant bits per operand instead of 8.
 //
+// With `terms` = 6 each operand is given as three BF16 slices (x = hi + mid
+// + lo, each slice the rounding of what the previous ones leave) and the six
+// products whose slice orders sum to at most 4 (hh, hm, mh, hl, mm, lh)
+// accumulate together: about 24 significant bits, an FP32-accurate product
+// on the BF16 tensor cores (the panel solve of the mixed factor).
+//
 // One CTA computes a 128 x BN tile of C with 4 warps:
 //   warp 0, one thread   TMA producer: per K-block of 64, loads the A and B
 //                        slabs (128B-swizzled, 1024-byte aligned stages) and
@@ -48,8 +54,9 @@ template <int BN, int TERMS>
 struct Smem {
   static constexpr int A_BYTES = BM * BK * 2;
   static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int STAGE_BYTES = TERMS == 1 ? (A_BYTES + B_BYTES) : 2 * (A_BYTES + B_BYTES);
-  static constexpr int STAGES = TERMS == 1 ? (BN == 128 ? 4 : 4) : (BN == 128 ? 3 : 2);
+  static constexpr int SLICES = TERMS == 1 ? 1 : (TERMS == 3 ? 2 : 3);
+  static constexpr int STAGE_BYTES = SLICES * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = TERMS == 1 ? 4 : (TERMS == 3 ? (BN == 128 ? 3 : 2) : 2);
   static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 };
 
@@ -110,9 +117,13 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
       const int kx = kb * BK;
       tma_load_2d(st, &p.a_hi, &full[s], kx, p.a_row0 + i0);
       tma_load_2d(st + S::A_BYTES, &p.b_hi, &full[s], kx, p.b_row0 + j0);
-      if (TERMS == 3) {
+      if (TERMS >= 3) {
         tma_load_2d(st + S::A_BYTES + S::B_BYTES, &p.a_lo, &full[s], kx, p.a_row0 + i0);
         tma_load_2d(st + 2 * S::A_BYTES + S::B_BYTES, &p.b_lo, &full[s], kx, p.b_row0 + j0);
+      }
+      if (TERMS == 6) {
+        tma_load_2d(st + 2 * S::A_BYTES + 2 * S::B_BYTES, &p.a_mid, &full[s], kx, p.a_row0 + i0);
+        tma_load_2d(st + 3 * S::A_BYTES + 2 * S::B_BYTES, &p.b_mid, &full[s], kx, p.b_row0 + j0);
       }
       issued++;
     }
@@ -138,11 +149,22 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
         const uint64_t a = sw128_desc(st + koff);
         const uint64_t b = sw128_desc(st + S::A_BYTES + koff);
         mma_bf16(tmem, a, b, idesc, (kb | kk) ? 1u : 0u);
-        if (TERMS == 3) {
+        if (TERMS >= 3) {
           const uint64_t alo = sw128_desc(st + S::A_BYTES + S::B_BYTES + koff);
           const uint64_t blo = sw128_desc(st + 2 * S::A_BYTES + S::B_BYTES + koff);
-          mma_bf16(tmem, a, blo, idesc, 1u);
-          mma_bf16(tmem, alo, b, idesc, 1u);
+          if (TERMS == 3) {
+            mma_bf16(tmem, a, blo, idesc, 1u);
+            mma_bf16(tmem, alo, b, idesc, 1u);
+          } else {
+            // slice orders: hi 1, mid 2, lo 3; the products with order sum <= 4
+            const uint64_t amid = sw128_desc(st + 2 * S::A_BYTES + 2 * S::B_BYTES + koff);
+            const uint64_t bmid = sw128_desc(st + 3 * S::A_BYTES + 2 * S::B_BYTES + koff);
+            mma_bf16(tmem, a, bmid, idesc, 1u);
+            mma_bf16(tmem, amid, b, idesc, 1u);
+            mma_bf16(tmem, a, blo, idesc, 1u);
+            mma_bf16(tmem, amid, bmid, idesc, 1u);
+            mma_bf16(tmem, alo, b, idesc, 1u);
+          }
         }
       }
       mma_commit(&empty[s]);
@@ -266,11 +288,12 @@ int launch(const TcParams &p, cudaStream_t s) {
 
 int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
   if (g.m <= 0 || g.n <= 0) return 0;
-  if (g.terms != 1 && g.terms != 3) return DG_ERR_UNSUPPORTED;
+  if (g.terms != 1 && g.terms != 3 && g.terms != 6) return DG_ERR_UNSUPPORTED;
   if (g.k <= 0 || g.k % 8 != 0 || g.lda % 8 != 0 || g.ldb % 8 != 0) return DG_ERR_UNSUPPORTED;
   if (((uintptr_t)g.a_hi | (uintptr_t)g.b_hi) & 15) return DG_ERR_UNSUPPORTED;
-  if (g.terms == 3 && (((uintptr_t)g.a_lo | (uintptr_t)g.b_lo) & 15)) return DG_ERR_UNSUPPORTED;
-  const int bn = g.bn == 256 ? 256 : 128;
+  if (g.terms >= 3 && (((uintptr_t)g.a_lo | (uintptr_t)g.b_lo) & 15)) return DG_ERR_UNSUPPORTED;
+  if (g.terms == 6 && (((uintptr_t)g.a_mid | (uintptr_t)g.b_mid) & 15)) return DG_ERR_UNSUPPORTED;
+  const int bn = (g.bn == 256 && g.terms != 6) ? 256 : 128;
   TcParams p;
   memset(&p, 0, sizeof p);
   const bool h = g.fp16 != 0;
@@ -279,8 +302,13 @@ int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
     dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
     return DG_ERR_CUDA;
   }
-  if (g.terms == 3 && (!encode_map(&p.a_lo, g.a_lo, g.k, g.a_rows, g.lda, BM, h) ||
+  if (g.terms >= 3 && (!encode_map(&p.a_lo, g.a_lo, g.k, g.a_rows, g.lda, BM, h) ||
                        !encode_map(&p.b_lo, g.b_lo, g.k, g.b_rows, g.ldb, bn, h))) {
+    dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
+    return DG_ERR_CUDA;
+  }
+  if (g.terms == 6 && (!encode_map(&p.a_mid, g.a_mid, g.k, g.a_rows, g.lda, BM, h) ||
+                       !encode_map(&p.b_mid, g.b_mid, g.k, g.b_rows, g.ldb, bn, h))) {
     dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
     return DG_ERR_CUDA;
   }
@@ -295,6 +323,7 @@ int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
   p.alpha_dev = g.alpha_dev;
   if (g.terms == 1)
     return bn == 256 ? launch<256, 1>(p, s) : launch<128, 1>(p, s);
+  if (g.terms == 6) return launch<128, 6>(p, s);
   return bn == 256 ? launch<256, 3>(p, s) : launch<128, 3>(p, s);
 }
 

@@ -9,7 +9,7 @@ namespace dg {
 // Kernel parameters (passed as one __grid_constant__ struct so the tensor
 // maps stay in parameter space, as TMA requires).
 struct TcParams {
-  CUtensorMap a_hi, b_hi, a_lo, b_lo;
+  CUtensorMap a_hi, b_hi, a_lo, b_lo, a_mid, b_mid;
   int m, n, k;
   int a_row0, b_row0;  // first panel row of the A / B operand
   float alpha, beta;
@@ -26,8 +26,9 @@ struct TcParams {
 };
 
 struct TcGemmArgs {
-  int m, n, k, terms;                 // terms: 1 (bf16) or 3 (bf16 hi/lo split)
+  int m, n, k, terms;                 // terms: 1 (bf16), 3 (hi/lo split) or 6 (hi/mid/lo)
   const void *a_hi, *a_lo;            // K-major BF16 panels
+  const void *a_mid, *b_mid;          // terms 6: the middle slices
   int lda, a_rows, a_row0;
   const void *b_hi, *b_lo;
   int ldb, b_rows, b_row0;

@@ -281,6 +281,8 @@ int dg_get_f64_engine(void);
 #define DG_PREC_FP16 11   /* FP16 operands, per-panel power-of-two scaling   */
 #define DG_PREC_FP16X3 13 /* FP16 hi/lo split with per-panel scaling        */
 #define DG_PREC_FP32 32   /* FP32 CUDA-core trailing updates                */
+#define DG_PREC_BF16X6 6  /* BF16 hi/mid/lo split, six products: FP32-accurate
+                             tensor-core trailing updates                    */
 
 typedef struct dg_mixed dg_mixed;
 
@@ -337,6 +339,24 @@ void dg_mixed_destroy(dg_mixed *f);
 int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const void *a_hi, const void *a_lo,
                   int lda, const void *b_hi, const void *b_lo, int ldb, float alpha, float beta,
                   float *C, int ldc, int bn, int *status, void *stream);
+
+/* FP32-accurate GEMM on the BF16 tensor cores (the mixed factor's panel
+ * solve and its bf16x6 updates; no counterpart in the reference): C = alpha
+ * A'B + beta C with A k x m, B k x n and C m x n column-major FP32 on the
+ * device; each operand is cut into three BF16 slices and the six slice
+ * products whose orders sum to at most 4 accumulate in FP32 (about 24
+ * significant bits).  k, lda, ldb multiples of 8.  Allocates stream-ordered
+ * scratch for the slices. */
+int dg_gemm_f32_tc_tn(int m, int n, int k, float alpha, const float *A, int lda, const float *B,
+                      int ldb, float beta, float *C, int ldc, void *stream);
+
+/* The diagonal-block kernel of the mixed factor (no counterpart in the
+ * reference): the FP32 Cholesky factor U (A = U'U, upper, in place) of one
+ * n x n block, n <= 1024, and V = U^-1 (upper, zero below), both column-major
+ * on the device, in one cooperative launch.  Returns (and stores in
+ * *info_host) the 1-based column of the first pivot that is not positive, or
+ * 0.  Synchronises `stream`. */
+int dg_potrf_inv_f32(int n, float *A, int lda, float *V, int ldv, int *info_host, void *stream);
 
 /* FP64 GEMM emulated on the BF16 tensor cores: C = alpha A'B + beta C with
  * A k x m, B k x n and C m x n column-major FP64 on the device, k <= 131072.

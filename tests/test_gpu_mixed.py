@@ -64,9 +64,9 @@ def _spd(n, cond, seed):
     return o.spd_spectrum(n, cond, seed)
 
 
-@pytest.mark.parametrize("precision", ["bf16", "bf16x3", "fp16", "fp16x3", "fp32"])
+@pytest.mark.parametrize("precision", ["bf16", "bf16x3", "bf16x6", "fp16", "fp16x3", "fp32"])
 @pytest.mark.parametrize("n,nb,cond,nrhs", [(512, 128, None, 3), (1000, 128, 1e2, 1),
-                                            (1536, 256, 1e4, 5)])
+                                            (1536, 256, 1e4, 5), (2100, 1024, 1e4, 4)])
 def test_mixed_solve(precision, n, nb, cond, nrhs):
     import torch
     import dagger_gb300 as d
