@@ -363,6 +363,7 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
       tile_factor(sC, sB, false, &s_fail);
       store_tile(sB, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0, false);
     }
+    if (!grid_sync(a, ++epoch, &s_stop)) return;  // every I_j before V is assembled
   }
   // ---- V: I_j on the diagonal, zero below ----
   for (int t = g; t < nblk * nblk; t += G) {
