@@ -103,7 +103,7 @@ int run_check(bool herm, int m, int n, int mb, int nb, double *const *tiles, cud
   // the tile pointer grid is staged through a small device buffer
   const double **dptrs = nullptr;
   size_t bytes = sizeof(double *) * (size_t)mt * nt;
-  DG_CUDA_TRY(cudaMallocAsync((void **)&dptrs, bytes, s));
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&dptrs, bytes, s));
   DG_CUDA_TRY(cudaMemcpyAsync(dptrs, tiles, bytes, cudaMemcpyHostToDevice, s));
   DG_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
   dim3 grid(mt, nt);

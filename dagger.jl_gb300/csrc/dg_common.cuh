@@ -38,6 +38,16 @@ void dg_set_last_error(const char *file, int line, const char *msg);
 // Number of SMs of the current device (cached per device).
 int dg_num_sms();
 
+namespace dg {
+// Stream-ordered device allocation from the library's own memory pool on the
+// current device.  The pool keeps freed memory mapped for reuse (no release
+// threshold), so calls that allocate the same workspaces again (a factor per
+// request, a solve per factor) do not map and unmap gigabytes each time;
+// dg_finalize trims it.  Free with cudaFreeAsync.
+cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t s);
+void pool_trim_all();
+}  // namespace dg
+
 // Kernels of one factorization skip their work when either of two device
 // "abort" words is non-zero on entry (a failed pivot or a failed step).
 __device__ __forceinline__ bool aborted(const int *a, const int *b) {

@@ -45,17 +45,30 @@ struct dg_mixed {
   float *W = nullptr;            // packed upper panels of the scaled factor
   double *s = nullptr;           // diagonal scaling
   double **tiles_dev = nullptr;  // caller's FP64 tiles (device array of pointers)
-  void *P_hi = nullptr, *P_lo = nullptr;  // 16-bit panel operands (T x nb, K-major)
-  void *P_mid = nullptr;                  // the middle slices (bf16x6 only)
-  float *diag_backup = nullptr;  // diagonal block before its FP32 POTRF
+  void *P_hi = nullptr, *P_lo = nullptr;  // FP16 (scaled) panel operands (T x nb, K-major)
+  float *diag_backup = nullptr;  // diagonal block before its FP32 factorization
   double *d64 = nullptr;         // FP64 scratch of the retry
   float *panel_max = nullptr;    // per-step |panel| maximum (FP16 scaling)
   float *alpha_dev = nullptr;    // per-step -1/scale^2 of the trailing update
   float *Vinv = nullptr;         // inverses of the diagonal blocks (mt x nb x nb)
-  float *Lp = nullptr;           // block columns of the factor, transposed (backward solves)
   void *diag_scratch = nullptr;  // the diagonal-block kernel's barrier words and scratch
-  void *S3v = nullptr;           // 3 BF16 slices of Vinv_k (nb x nb each)
-  void *S3r = nullptr;           // 3 BF16 slices of panel k's rest (nb x (n - nb) each)
+  void *S3r = nullptr;           // 3 BF16 slices of panel k's rest before its solve
+  // FP32-accurate BF16 slices (hi | mid | lo) of the finished factor: the
+  // operands of the trailing updates (hi, mid = the hi/lo split of bf16x3)
+  // and of the refinement's triangular solves on the tensor cores
+  __nv_bfloat16 *R3 = nullptr;   // every panel's rest, at the offsets of W
+  long long r3_stride = 0;       // elements per slice of R3
+  __nv_bfloat16 *V3 = nullptr;   // every Vinv_k (k nb^2 offsets)
+  __nv_bfloat16 *VT3 = nullptr;  // every Vinv_k'
+  __nv_bfloat16 *L3 = nullptr;   // block columns of U transposed (lp_base offsets)
+  long long v3_stride = 0, l3_stride = 0;
+  // slices of A's rows for the emulated FP64 residual, cut on `aux2` while
+  // the factorization runs (ev_oz marks their completion)
+  void *ozA = nullptr;
+  unsigned long long *ozAs = nullptr;
+  long long oz_ldk = 0;
+  cudaStream_t aux2 = nullptr;
+  cudaEvent_t ev_oz = nullptr;
   int *words = nullptr;          // [0] status, [1] retries, [2] first bad diagonal,
                                  // [3..3+mt) info_k, [3+mt..3+2mt) retried_k
   double normA = 0.0;            // ||A||_inf
@@ -64,7 +77,7 @@ struct dg_mixed {
   float factor_ms = 0.f;
   cudaStream_t stream = nullptr;  // allocations are stream-ordered on this stream
   double shift = 0.0;             // added to the unit diagonal of S A S before factoring
-  cudaStream_t aux = nullptr;     // lookahead stream (the next panel's POTRF/TRSM)
+  cudaStream_t aux = nullptr;     // lookahead stream (the next panel's step)
   cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
 };
 
@@ -123,25 +136,38 @@ __host__ __device__ inline long long lp_base(long long k, long long nb) {
   return nb * nb * (k * (k + 1) / 2);
 }
 
-// Lp_k(:, j nb + i) = U(j nb + i, k nb + :) for the block (j, k), j <= k, in
-// 32 x 32 tiles through shared memory; blockIdx.z enumerates the blocks.
-__global__ void transpose_blocks_kernel(const float *W, float *Lp, int n, int nb,
-                                        const int2 *blocks) {
+// One block of a transposing three-slice split: dst(c, r) = slices of
+// src(r, c) for a rows x cols block (src column-major lds, dst column-major
+// ldd); every slice array is `stride` elements after the previous one.
+struct TJob {
+  long long src, dst;
+  int rows, cols;
+};
+
+// 32 x 32 tiles through shared memory; blockIdx.z enumerates the jobs.
+__global__ void tsplit3_kernel(const float *src, long long lds, __nv_bfloat16 *dst,
+                               long long ldd, long long stride, const TJob *jobs) {
   __shared__ float t[32][33];
-  const int2 b = blocks[blockIdx.z];
-  const int j = b.x, k = b.y;
-  const float *P = W + panel_base(j, n, nb) + (long long)(k - j) * nb * nb;  // U(j, k), ld nb
-  float *L = Lp + lp_base(k, nb) + (long long)j * nb * nb;                   // its transpose
+  const TJob jb = jobs[blockIdx.z];
   const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-  const int cols = min(nb, n - k * nb);  // columns of block column k
+  if (r0 >= jb.rows || c0 >= jb.cols) return;
+  const float *S = src + jb.src;
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
     const int c = c0 + y, r = r0 + threadIdx.x;
-    t[y][threadIdx.x] = (c < cols) ? P[r + (long long)c * nb] : 0.f;
+    t[y][threadIdx.x] = (c < jb.cols && r < jb.rows) ? S[r + (long long)c * lds] : 0.f;
   }
   __syncthreads();
   for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-    const int r = r0 + y, c = c0 + threadIdx.x;
-    L[c + (long long)r * nb] = t[threadIdx.x][y];
+    const int r = r0 + y, c = c0 + threadIdx.x;  // dst(c, r)
+    if (r >= jb.rows || c >= jb.cols) continue;
+    const float x = t[threadIdx.x][y];
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+    __nv_bfloat16 *D = dst + jb.dst + c + (long long)r * ldd;
+    D[0] = h;
+    D[stride] = m;
+    D[2 * stride] = __float2bfloat16_rn(r1 - __bfloat162float(m));
   }
 }
 
@@ -263,21 +289,24 @@ __global__ void convert_kernel(const float *src, long long n, int terms, void *h
 
 // x -> three BF16 slices (x = hi + mid + lo up to the rounding of lo): the
 // operands of the FP32-accurate tensor-core product (tc_gemm terms 6).
-// `rows` of every `ld` elements are converted (n elements in all).
+// With rows > 0, `rows` of every `ld` source elements are converted (n in
+// all) to the same positions with leading dimension ldd (default ld).
 __global__ void split3_kernel(const float *src, long long n, __nv_bfloat16 *hi, __nv_bfloat16 *mid,
                               __nv_bfloat16 *lo, const int *a1, const int *a2, int rows = 0,
-                              long long ld = 0) {
+                              long long ld = 0, long long ldd = 0) {
   if (aborted(a1, a2)) return;
+  if (ldd == 0) ldd = ld;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x) {
     const long long i = rows ? (e % rows) + (e / rows) * ld : e;
+    const long long o = rows ? (e % rows) + (e / rows) * ldd : e;
     const float x = src[i];
     const __nv_bfloat16 h = __float2bfloat16_rn(x);
     const float r1 = x - __bfloat162float(h);
     const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-    hi[i] = h;
-    mid[i] = m;
-    lo[i] = __float2bfloat16_rn(r1 - __bfloat162float(m));
+    hi[o] = h;
+    mid[o] = m;
+    lo[o] = __float2bfloat16_rn(r1 - __bfloat162float(m));
   }
 }
 
@@ -332,10 +361,12 @@ int grid_for(long long n) {
 
 // Step k's panel: the FP32 factor of the diagonal block and its inverse in
 // one cooperative launch (mixed_diag.cu; an FP64 retry on a failed pivot,
-// then the inverse of the retried factor), the solve of the rest of the
+// then the inverse of the retried factor), the inverse cut into three BF16
+// slices (kept for the refinement's solves), the solve of the rest of the
 // panel as the product Vinv_k' A(k, k+1:) on the tensor cores with
-// FP32-accurate operands (3 BF16 slices, 6 products), and its conversion to
-// the 16-bit operands of the trailing update in P buffer k % 2.
+// FP32-accurate operands (3 BF16 slices, 6 products), and the result cut
+// into the three slices the trailing updates and the solves read (FP16
+// forms: also the scaled conversion into P buffer k % 2).
 static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
   const int n = f->n, nb = f->nb, mt = f->mt;
   int *status = f->words, *retries = f->words + 1, *ik = f->words + 3 + k;
@@ -354,23 +385,26 @@ static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
   count_launches(1);
   DG_TRY(diag_chol_inv_f32(Pk, nb, nbk, Vk, nb, f->diag_scratch, ik, k * nb, status, retried, 1,
                            s));
+  const size_t vn = (size_t)nb * nb;
+  __nv_bfloat16 *v3 = f->V3 + (size_t)k * vn;
+  split3_kernel<<<grid_for((long long)vn), 256, 0, s>>>(Vk, (long long)vn, v3, v3 + f->v3_stride,
+                                                        v3 + 2 * f->v3_stride, ik, status);
+  count_launches(1);
   if (T <= 0) return 0;
   float *Rk = Pk + (size_t)nb * nb;  // the rest of panel k: nb x T
+  const size_t rn = (size_t)nb * T;
   {
     // Rk = Vk' Rk: both operands cut into three BF16 slices
-    const size_t vn = (size_t)nb * nb, rn = (size_t)nb * T;
-    __nv_bfloat16 *v3 = (__nv_bfloat16 *)f->S3v, *r3 = (__nv_bfloat16 *)f->S3r;
+    __nv_bfloat16 *r3 = (__nv_bfloat16 *)f->S3r;
     const size_t rcap = (size_t)nb * std::max(0, n - nb);
-    split3_kernel<<<grid_for((long long)vn), 256, 0, s>>>(Vk, (long long)vn, v3, v3 + vn,
-                                                          v3 + 2 * vn, ik, status);
     split3_kernel<<<grid_for((long long)rn), 256, 0, s>>>(Rk, (long long)rn, r3, r3 + rcap,
                                                           r3 + 2 * rcap, ik, status);
-    count_launches(2);
+    count_launches(1);
     DG_CUDA_TRY(cudaGetLastError());
     TcGemmArgs g;
     memset(&g, 0, sizeof g);
     g.m = nbk; g.n = (int)T; g.k = nbk; g.terms = 6;
-    g.a_hi = v3; g.a_mid = v3 + vn; g.a_lo = v3 + 2 * vn;
+    g.a_hi = v3; g.a_mid = v3 + f->v3_stride; g.a_lo = v3 + 2 * f->v3_stride;
     g.lda = nb; g.a_rows = nbk; g.a_row0 = 0;
     g.b_hi = r3; g.b_mid = r3 + rcap; g.b_lo = r3 + 2 * rcap;
     g.ldb = nb; g.b_rows = (int)T; g.b_row0 = 0;
@@ -379,36 +413,26 @@ static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
     g.bn = 128; g.status = status;
     DG_TRY(tc_gemm_bf16(g, s));
   }
-  if (f->precision == DG_PREC_FP32) return 0;
-  const size_t half0 = (size_t)std::max(0LL, (long long)n - nb) * nb;
-  if (f->precision == DG_PREC_BF16X6) {
-    __nv_bfloat16 *h = (__nv_bfloat16 *)f->P_hi + (size_t)(k & 1) * half0;
-    __nv_bfloat16 *m = (__nv_bfloat16 *)f->P_mid + (size_t)(k & 1) * half0;
-    __nv_bfloat16 *l = (__nv_bfloat16 *)f->P_lo + (size_t)(k & 1) * half0;
-    const long long elems = (long long)nb * T;
-    split3_kernel<<<grid_for(elems), 256, 0, s>>>(Rk, elems, h, m, l, ik, status);
+  {
+    __nv_bfloat16 *o3 = f->R3 + (Rk - f->W);
+    split3_kernel<<<grid_for((long long)rn), 256, 0, s>>>(Rk, (long long)rn, o3, o3 + f->r3_stride,
+                                                          o3 + 2 * f->r3_stride, ik, status);
     count_launches(1);
-    DG_CUDA_TRY(cudaGetLastError());
-    return 0;
   }
   const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
-  const int terms = (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
-  const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;  // elements per P buffer
-  void *hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
-  void *lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
-  float *pmax = f->panel_max + k;
-  float *alpha = f->alpha_dev + k;
-  const long long elems = (long long)nb * T;
   if (fp16) {
+    const int terms = f->precision == DG_PREC_FP16X3 ? 3 : 1;
+    const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;  // elements per P buffer
+    void *hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
+    void *lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
+    float *pmax = f->panel_max + k;
+    float *alpha = f->alpha_dev + k;
+    const long long elems = (long long)nb * T;
     DG_CUDA_TRY(cudaMemsetAsync(pmax, 0, sizeof(float), s));
     absmax_kernel<<<grid_for(elems), 256, 0, s>>>(Rk, elems, pmax, ik, status);
     convert_kernel<true><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, hi, lo, pmax, alpha, ik,
                                                          status);
     count_launches(2);
-  } else {
-    convert_kernel<false><<<grid_for(elems), 256, 0, s>>>(Rk, elems, terms, hi, lo, nullptr, alpha,
-                                                          ik, status);
-    count_launches(1);
   }
   DG_CUDA_TRY(cudaGetLastError());
   return 0;
@@ -416,6 +440,8 @@ static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
 
 // Step k's trailing update on the tensor cores, in two parts: `next` = the
 // block row of panel k+1 (so the next panel can start), else the rest.
+// BF16 forms read the factor's slices of panel k (hi; hi + mid as the hi/lo
+// pair of bf16x3; all three for bf16x6), FP16 forms the scaled P buffer.
 static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   const int n = f->n, nb = f->nb;
   const long long T = (long long)n - (long long)(k + 1) * nb;
@@ -423,7 +449,6 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
   const int terms = f->precision == DG_PREC_BF16X6 ? 6
                   : (f->precision == DG_PREC_BF16X3 || f->precision == DG_PREC_FP16X3) ? 3 : 1;
-  const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;
   TcGemmArgs g;
   memset(&g, 0, sizeof g);
   const int nb1 = (int)std::min<long long>(nb, T);
@@ -436,16 +461,20 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
     g.off = (long long)(k + 2) * nb;
   }
   g.k = nb; g.terms = terms; g.fp16 = fp16;
-  g.a_hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
-  g.a_lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
-  g.b_hi = g.a_hi; g.b_lo = g.a_lo;
-  g.lda = nb; g.ldb = nb; g.a_rows = (int)T; g.b_rows = (int)T;
-  g.alpha = -1.f; g.alpha_dev = f->alpha_dev + k; g.beta = 1.f;
-  if (terms == 6) {
-    g.a_mid = (char *)f->P_mid + (size_t)(k & 1) * half * 2;
-    g.b_mid = g.a_mid;
-    g.alpha_dev = nullptr;  // unscaled BF16 slices: alpha = -1
+  if (fp16) {
+    const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;
+    g.a_hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
+    g.a_lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
+    g.alpha_dev = f->alpha_dev + k;
+  } else {
+    const __nv_bfloat16 *r3 = f->R3 + (panel_base(k, n, nb) + (long long)nb * nb);
+    g.a_hi = r3;
+    g.a_mid = r3 + f->r3_stride;
+    g.a_lo = terms == 3 ? r3 + f->r3_stride : r3 + 2 * f->r3_stride;  // bf16x3: lo = mid slice
   }
+  g.b_hi = g.a_hi; g.b_lo = g.a_lo; g.b_mid = g.a_mid;
+  g.lda = nb; g.ldb = nb; g.a_rows = (int)T; g.b_rows = (int)T;
+  g.alpha = -1.f; g.beta = 1.f;
   g.c = f->W; g.layout = 1; g.upper = 1;
   g.nb = nb; g.ntot = n;
   g.bn = 128; g.status = f->words;
@@ -508,52 +537,100 @@ int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
 }
 
 
-// Solves U~' U~ Z = Z (FP32, n x r, column-major ldz) on the packed panels,
-// with Z2 (same shape) as the second buffer: forward Z2_k = Vinv_k' Z_k and
-// Z_(k+1:) -= U~_(k,k+1:)' Z2_k; backward Z2_k -= U~_(k,k+1:) Z_(k+1:) and
-// Z_k = Vinv_k Z2_k.  The result is in Z.
-int mixed_tri_solve(const dg_mixed *f, float *Z, float *Z2, long long ldz, int r, cudaStream_t s) {
+// One FP32-accurate product on the tensor cores for the triangular solves:
+// C (m x r, ldc) = alpha A' Zb + beta C with A given by its three slices
+// (K-major, lda, stride apart) and Zb the k x r FP32 block at Zsrc (ldz), cut
+// into slices in zs (3 k x r, ld nb) first.
+static int tc6(const dg_mixed *f, int m, int r, int k, const __nv_bfloat16 *a3, long long astride,
+               int lda, const float *Zsrc, long long ldz, __nv_bfloat16 *zs, float alpha,
+               float beta, float *C, long long ldc, cudaStream_t s) {
+  const int nb = f->nb;
+  const size_t zn = (size_t)nb * r;
+  const long long e = (long long)k * r;
+  split3_kernel<<<grid_for(e), 256, 0, s>>>(Zsrc, e, zs, zs + zn, zs + 2 * zn, nullptr, nullptr,
+                                            k, ldz, nb);
+  count_launches(1);
+  TcGemmArgs g;
+  memset(&g, 0, sizeof g);
+  g.m = m; g.n = r; g.k = k; g.terms = 6;
+  g.a_hi = a3; g.a_mid = a3 + astride; g.a_lo = a3 + 2 * astride;
+  g.lda = lda; g.a_rows = m; g.a_row0 = 0;
+  g.b_hi = zs; g.b_mid = zs + zn; g.b_lo = zs + 2 * zn;
+  g.ldb = nb; g.b_rows = r; g.b_row0 = 0;
+  g.alpha = alpha; g.beta = beta;
+  g.c = C; g.ldc = ldc; g.layout = 0; g.upper = 0;
+  g.bn = 128; g.status = nullptr;
+  return tc_gemm_bf16(g, s);
+}
+
+// Solves U~' U~ Z = Z (FP32, n x r, column-major ldz) with the factor's
+// slices on the tensor cores (FP32-accurate products), Z2 (same shape) the
+// second buffer: forward Z2_k = Vinv_k' Z_k and Z_(k+1:) -= U~_(k,k+1:)' Z2_k;
+// backward, right-looking, Z_k = Vinv_k Z2_k and Z2_(0:k) -= U~_(0:k, k) Z_k
+// as one tall product with the transposed block column.  zs: 3 nb r BF16
+// (the right-hand block's slices).  The result is in Z.
+static int tri_solve_passes(const dg_mixed *f, float *Z, float *Z2, long long ldz, int r,
+                            __nv_bfloat16 *zs, cudaStream_t s) {
   const int n = f->n, nb = f->nb, mt = f->mt;
   for (int k = 0; k < mt; k++) {
-    const float *Pk = f->W + panel_base(k, n, nb);
-    const float *V = f->Vinv + (size_t)k * nb * nb;
     const int nbk = std::min(nb, n - k * nb);
     const long long T = (long long)n - (long long)(k + 1) * nb;
-    DG_TRY(gemm_f32('T', 'N', nbk, r, nbk, 1.f, V, nb, Z + (size_t)k * nb, ldz, 0.f,
-                    Z2 + (size_t)k * nb, ldz, TRI_NONE, nullptr, s));
+    DG_TRY(tc6(f, nbk, r, nbk, f->V3 + (size_t)k * nb * nb, f->v3_stride, nb,
+               Z + (size_t)k * nb, ldz, zs, 1.f, 0.f, Z2 + (size_t)k * nb, ldz, s));
     if (T > 0)
-      DG_TRY(gemm_f32('T', 'N', (int)T, r, nbk, -1.f, Pk + (size_t)nb * nb, nb, Z2 + (size_t)k * nb,
-                      ldz, 1.f, Z + (size_t)(k + 1) * nb, ldz, TRI_NONE, nullptr, s));
+      DG_TRY(tc6(f, (int)T, r, nbk, f->R3 + (panel_base(k, n, nb) + (long long)nb * nb),
+                 f->r3_stride, nb, Z2 + (size_t)k * nb, ldz, zs, -1.f, 1.f,
+                 Z + (size_t)(k + 1) * nb, ldz, s));
   }
-  // backward, right-looking: Z_k = Vinv_k Z2_k, then every block above it
-  // takes its share, Z2_(0:k) -= U~_(0:k, k) Z_k, as one tall GEMM on the
-  // transposed block column
   for (int k = mt - 1; k >= 0; k--) {
-    const float *V = f->Vinv + (size_t)k * nb * nb;
     const int nbk = std::min(nb, n - k * nb);
-    DG_TRY(gemm_f32('N', 'N', nbk, r, nbk, 1.f, V, nb, Z2 + (size_t)k * nb, ldz, 0.f,
-                    Z + (size_t)k * nb, ldz, TRI_NONE, nullptr, s));
+    DG_TRY(tc6(f, nbk, r, nbk, f->VT3 + (size_t)k * nb * nb, f->v3_stride, nb,
+               Z2 + (size_t)k * nb, ldz, zs, 1.f, 0.f, Z + (size_t)k * nb, ldz, s));
     if (k > 0)
-      DG_TRY(gemm_f32('T', 'N', k * nb, r, nbk, -1.f, f->Lp + lp_base(k, nb), nb,
-                      Z + (size_t)k * nb, ldz, 1.f, Z2, ldz, TRI_NONE, nullptr, s));
+      DG_TRY(tc6(f, k * nb, r, nbk, f->L3 + lp_base(k, nb), f->l3_stride, nb,
+                 Z + (size_t)k * nb, ldz, zs, -1.f, 1.f, Z2, ldz, s));
   }
   return 0;
 }
 
-// Fills Lp from the finished panels (one launch over every block j <= k).
+int mixed_tri_solve(const dg_mixed *f, float *Z, float *Z2, long long ldz, int r, cudaStream_t s) {
+  __nv_bfloat16 *zs = nullptr;
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&zs, sizeof(__nv_bfloat16) * 3 * (size_t)f->nb * r, s));
+  const int rc = tri_solve_passes(f, Z, Z2, ldz, r, zs, s);
+  cudaFreeAsync(zs, s);
+  return rc;
+}
+
+// After the factorization: the slices of every Vinv_k' (VT3) and of the
+// factor's block columns transposed (L3, the blocks (j, k), j < k), in one
+// transposing split launch over a job table.
 int mixed_transpose_columns(dg_mixed *f, cudaStream_t s) {
-  const int mt = f->mt, nb = f->nb;
-  std::vector<int2> hb;
-  for (int k = 0; k < mt; k++)
-    for (int j = 0; j <= k; j++) hb.push_back(make_int2(j, k));
-  int2 *db = nullptr;
-  DG_CUDA_TRY(cudaMallocAsync((void **)&db, sizeof(int2) * hb.size(), s));
-  DG_CUDA_TRY(cudaMemcpyAsync(db, hb.data(), sizeof(int2) * hb.size(), cudaMemcpyHostToDevice, s));
-  dim3 grid((nb + 31) / 32, (nb + 31) / 32, (unsigned)hb.size());
-  transpose_blocks_kernel<<<grid, dim3(32, 8), 0, s>>>(f->W, f->Lp, f->n, nb, db);
+  const int mt = f->mt, nb = f->nb, n = f->n;
+  std::vector<TJob> jv, jl;
+  for (int k = 0; k < mt; k++) {
+    const int nbk = std::min(nb, n - k * nb);
+    jv.push_back({(long long)k * nb * nb, (long long)k * nb * nb, nbk, nbk});
+    for (int j = 0; j < k; j++)  // U(j, k): nb x nbk at W (ld nb) -> Lp_k block j (nbk x nb)
+      jl.push_back({panel_base(j, n, nb) + (long long)(k - j) * nb * nb,
+                    lp_base(k, nb) + (long long)j * nb * nb, nb, nbk});
+  }
+  TJob *dj = nullptr;
+  const size_t nj = jv.size() + jl.size();
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&dj, sizeof(TJob) * nj, s));
+  DG_CUDA_TRY(cudaMemcpyAsync(dj, jv.data(), sizeof(TJob) * jv.size(), cudaMemcpyHostToDevice, s));
+  if (!jl.empty())
+    DG_CUDA_TRY(cudaMemcpyAsync(dj + jv.size(), jl.data(), sizeof(TJob) * jl.size(),
+                                cudaMemcpyHostToDevice, s));
+  const dim3 blk(32, 8), g1((nb + 31) / 32, (nb + 31) / 32, (unsigned)jv.size());
+  tsplit3_kernel<<<g1, blk, 0, s>>>(f->Vinv, nb, f->VT3, nb, f->v3_stride, dj);
   count_launches(1);
+  if (!jl.empty()) {
+    const dim3 g2((nb + 31) / 32, (nb + 31) / 32, (unsigned)jl.size());
+    tsplit3_kernel<<<g2, blk, 0, s>>>(f->W, nb, f->L3, nb, f->l3_stride, dj + jv.size());
+    count_launches(1);
+  }
   DG_CUDA_TRY(cudaGetLastError());
-  cudaFreeAsync(db, s);  // (a copy from pageable memory is staged before the call returns)
+  cudaFreeAsync(dj, s);  // (copies from pageable memory are staged before the calls return)
   return 0;
 }
 
@@ -592,29 +669,33 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
     dg_mixed_destroy(f);
     return rc;
   };
+  const bool fp16 = (precision == DG_PREC_FP16 || precision == DG_PREC_FP16X3);
+  f->r3_stride = wsize;
+  f->v3_stride = (long long)mt * nb * nb;
+  f->l3_stride = std::max(1LL, dg::lp_base(mt, nb));
   struct Alloc { void **p; size_t bytes; };
   Alloc allocs[] = {
       {(void **)&f->W, sizeof(float) * (size_t)wsize},
       {(void **)&f->s, sizeof(double) * (size_t)n},
       {(void **)&f->tiles_dev, sizeof(double *) * (size_t)mt * mt},
-      {(void **)&f->P_hi, 2 * 2 * (size_t)std::max(1LL, tmax) * nb},
-      {(void **)&f->P_lo, 2 * 2 * (size_t)std::max(1LL, tmax) * nb},
-      {(void **)&f->P_mid, precision == DG_PREC_BF16X6 ? 2 * 2 * (size_t)std::max(1LL, tmax) * nb
-                                                        : (size_t)256},
+      {(void **)&f->P_hi, fp16 ? 2 * 2 * (size_t)std::max(1LL, tmax) * nb : (size_t)256},
+      {(void **)&f->P_lo, fp16 ? 2 * 2 * (size_t)std::max(1LL, tmax) * nb : (size_t)256},
       {(void **)&f->diag_backup, sizeof(float) * (size_t)nb * nb},
       {(void **)&f->d64, sizeof(double) * (size_t)nb * nb},
       {(void **)&f->panel_max, sizeof(float) * (size_t)mt},
       {(void **)&f->alpha_dev, sizeof(float) * (size_t)mt},
       {(void **)&f->words, sizeof(int) * (size_t)(3 + 2 * mt)},
       {(void **)&f->Vinv, sizeof(float) * (size_t)mt * nb * nb},
-      {(void **)&f->Lp, sizeof(float) * (size_t)dg::lp_base(mt, nb)},
       {(void **)&f->diag_scratch, dg::diag_chol_inv_scratch_bytes()},
-      {(void **)&f->S3v, 3 * 2 * (size_t)nb * nb},
       {(void **)&f->S3r, 3 * 2 * (size_t)std::max(1LL, tmax) * nb},
+      {(void **)&f->R3, 3 * 2 * (size_t)f->r3_stride},
+      {(void **)&f->V3, 3 * 2 * (size_t)f->v3_stride},
+      {(void **)&f->VT3, 3 * 2 * (size_t)f->v3_stride},
+      {(void **)&f->L3, 3 * 2 * (size_t)f->l3_stride},
   };
   f->stream = s;
   for (auto &a : allocs) {
-    if (cudaMallocAsync(a.p, a.bytes, s) != cudaSuccess) {
+    if (dg::pool_malloc_async(a.p, a.bytes, s) != cudaSuccess) {
       cudaGetLastError();
       dg_set_last_error(__FILE__, __LINE__, "device allocation for the mixed factor failed");
       return fail(DG_ERR_NOMEM);
@@ -624,9 +705,39 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   if (cudaMemcpyAsync(f->tiles_dev, tiles, sizeof(double *) * (size_t)mt * mt,
                       cudaMemcpyHostToDevice, s) != cudaSuccess)
     return fail(DG_ERR_CUDA);
+  // With the emulated FP64 engine the refinement's residual is an emulated
+  // product with A's rows cut into BF16 slices; they depend on A alone, so
+  // they are cut here, on a low-priority stream beside the factorization.
+  if (dg::get_f64_engine() == 2 && n <= 131072) {
+    const long long ldk = ((long long)n + 7) / 8 * 8;
+    const size_t ba = 16 * (size_t)ldk * n;
+    if (dg::pool_malloc_async(&f->ozA, ba + 8 * (size_t)n, s) == cudaSuccess) {
+      f->oz_ldk = ldk;
+      f->ozAs = (unsigned long long *)((char *)f->ozA + ba);
+      f->bytes += ba + 8 * (size_t)n;
+      int least = 0, greatest = 0;
+      cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      if (cudaStreamCreateWithPriority(&f->aux2, cudaStreamNonBlocking, least) != cudaSuccess ||
+          cudaEventCreateWithFlags(&f->ev_oz, cudaEventDisableTiming) != cudaSuccess)
+        return fail(DG_ERR_CUDA);
+      cudaEvent_t ready;
+      if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess)
+        return fail(DG_ERR_CUDA);
+      cudaEventRecord(ready, s);  // the tile pointers and the slice buffer are in place
+      cudaStreamWaitEvent(f->aux2, ready, 0);
+      cudaEventDestroy(ready);
+      const int rc = dg::oz_split_tile_rows((const double *const *)f->tiles_dev, n, nb, f->ozA,
+                                            ldk, f->ozAs, nullptr, f->aux2);
+      if (rc) return fail(rc);
+      cudaEventRecord(f->ev_oz, f->aux2);
+    } else {
+      cudaGetLastError();  // no room: the solve cuts its own slices or uses the FP64 pipe
+      f->ozA = nullptr;
+    }
+  }
   // ||A||_inf
   double *rows = nullptr, *dmax = nullptr;
-  if (cudaMallocAsync((void **)&rows, sizeof(double) * (n + 1), s) != cudaSuccess)
+  if (dg::pool_malloc_async((void **)&rows, sizeof(double) * (n + 1), s) != cudaSuccess)
     return fail(DG_ERR_NOMEM);
   dmax = rows + n;
   if (cudaMemsetAsync(rows, 0, sizeof(double) * n, s) != cudaSuccess) return fail(DG_ERR_CUDA);
@@ -671,14 +782,18 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
 
 extern "C" void dg_mixed_destroy(dg_mixed *f) {
   if (!f) return;
-  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->P_mid, f->diag_backup, f->d64,
-                f->panel_max, f->alpha_dev, f->words, f->Vinv, f->Lp, f->diag_scratch,
-                f->S3v, f->S3r};
+  // the slices of A are cut on aux2: the frees below wait for them
+  if (f->ev_oz && f->stream) cudaStreamWaitEvent(f->stream, f->ev_oz, 0);
+  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
+                f->panel_max, f->alpha_dev, f->words, f->Vinv, f->diag_scratch, f->S3r,
+                f->R3, f->V3, f->VT3, f->L3, f->ozA};
   for (void *p : ps)
     if (p) cudaFreeAsync(p, f->stream);  // stream-ordered: no device-wide synchronisation
   if (f->ev_next) cudaEventDestroy(f->ev_next);
   if (f->ev_panel) cudaEventDestroy(f->ev_panel);
+  if (f->ev_oz) cudaEventDestroy(f->ev_oz);
   if (f->aux) cudaStreamDestroy(f->aux);
+  if (f->aux2) cudaStreamDestroy(f->aux2);
   delete f;
 }
 
@@ -814,11 +929,11 @@ int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int 
   const size_t col = (size_t)n;
   double *V = nullptr, *W = nullptr, *D = nullptr, *sc = nullptr;
   float *Z32 = nullptr;
-  if (cudaMallocAsync((void **)&V, sizeof(double) * col * r * (m + 1), s) != cudaSuccess ||
-      cudaMallocAsync((void **)&W, sizeof(double) * col * r * 2, s) != cudaSuccess ||
-      cudaMallocAsync((void **)&D, sizeof(double) * col * r, s) != cudaSuccess ||
-      cudaMallocAsync((void **)&sc, sizeof(double) * r * (m + 4), s) != cudaSuccess ||
-      cudaMallocAsync((void **)&Z32, sizeof(float) * col * r * 2, s) != cudaSuccess) {
+  if (dg::pool_malloc_async((void **)&V, sizeof(double) * col * r * (m + 1), s) != cudaSuccess ||
+      dg::pool_malloc_async((void **)&W, sizeof(double) * col * r * 2, s) != cudaSuccess ||
+      dg::pool_malloc_async((void **)&D, sizeof(double) * col * r, s) != cudaSuccess ||
+      dg::pool_malloc_async((void **)&sc, sizeof(double) * r * (m + 4), s) != cudaSuccess ||
+      dg::pool_malloc_async((void **)&Z32, sizeof(float) * col * r * 2, s) != cudaSuccess) {
     cudaGetLastError();
     return DG_ERR_NOMEM;
   }
@@ -950,9 +1065,9 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
   if (opts) o = *opts;
   double *R = nullptr, *cm = nullptr;
   float *Z = nullptr;
-  if (cudaMallocAsync((void **)&R, sizeof(double) * (size_t)n * r, s) != cudaSuccess ||
-      cudaMallocAsync((void **)&cm, sizeof(double) * 3 * r, s) != cudaSuccess ||
-      cudaMallocAsync((void **)&Z, sizeof(float) * (size_t)n * r * 2, s) != cudaSuccess) {
+  if (dg::pool_malloc_async((void **)&R, sizeof(double) * (size_t)n * r, s) != cudaSuccess ||
+      dg::pool_malloc_async((void **)&cm, sizeof(double) * 3 * r, s) != cudaSuccess ||
+      dg::pool_malloc_async((void **)&Z, sizeof(float) * (size_t)n * r * 2, s) != cudaSuccess) {
     cudaGetLastError();
     return DG_ERR_NOMEM;
   }
@@ -961,23 +1076,35 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   OzResidual oz;
+  bool own_a = false;
   if (dg::get_f64_engine() == 2 && n <= 131072) {
     oz.ldk = ((long long)n + 7) / 8 * 8;
     const size_t ba = 16 * (size_t)oz.ldk * n, bx = 16 * (size_t)oz.ldk * r;
-    if (cudaMallocAsync(&oz.a, ba + 8 * (size_t)n, s) != cudaSuccess ||
-        cudaMallocAsync(&oz.x, bx + 8 * (size_t)r, s) != cudaSuccess) {
-      cudaGetLastError();  // no room for the slices: the FP64 residual
-      if (oz.a) cudaFreeAsync(oz.a, s);
-      oz.a = oz.x = nullptr;
-    } else {
+    if (f->ozA) {
+      // A's slices were cut beside the factorization
+      oz.a = f->ozA;
+      oz.as = f->ozAs;
+      DG_CUDA_TRY(cudaStreamWaitEvent(s, f->ev_oz, 0));
+    } else if (dg::pool_malloc_async(&oz.a, ba + 8 * (size_t)n, s) == cudaSuccess) {
+      own_a = true;
       oz.as = (unsigned long long *)((char *)oz.a + ba);
-      oz.xs = (unsigned long long *)((char *)oz.x + bx);
       if (dg::oz_split_tile_rows((const double *const *)f->tiles_dev, n, f->nb, oz.a, oz.ldk,
                                  oz.as, nullptr, s)) {
         cudaFreeAsync(oz.a, s);
-        cudaFreeAsync(oz.x, s);
-        oz.a = oz.x = nullptr;
+        oz.a = nullptr;
+        own_a = false;
       }
+    } else {
+      cudaGetLastError();
+      oz.a = nullptr;
+    }
+    if (oz.a && dg::pool_malloc_async(&oz.x, bx + 8 * (size_t)r, s) == cudaSuccess) {
+      oz.xs = (unsigned long long *)((char *)oz.x + bx);
+    } else {
+      cudaGetLastError();  // no room for the slices: the FP64 residual
+      if (own_a) cudaFreeAsync(oz.a, s);
+      oz.a = oz.x = nullptr;
+      own_a = false;
     }
   }
   DG_CUDA_TRY(cudaMemset2DAsync(X, sizeof(double) * ldx, 0, sizeof(double) * n, r, s));
@@ -1023,7 +1150,7 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
   cudaFreeAsync(R, s);
   cudaFreeAsync(cm, s);
   cudaFreeAsync(Z, s);
-  if (oz.a) cudaFreeAsync(oz.a, s);
+  if (own_a) cudaFreeAsync(oz.a, s);
   if (oz.x) cudaFreeAsync(oz.x, s);
   if (rep) {
     rep->iterations = outer;
@@ -1056,7 +1183,7 @@ extern "C" int dg_gemm_f32_tc_tn(int m, int n, int k, float alpha, const float *
   cudaStream_t s = (cudaStream_t)stream;
   const size_t an = (size_t)lda * m, bn = (size_t)ldb * n;
   __nv_bfloat16 *buf = nullptr;
-  DG_CUDA_TRY(cudaMallocAsync((void **)&buf, sizeof(__nv_bfloat16) * 3 * (an + bn), s));
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&buf, sizeof(__nv_bfloat16) * 3 * (an + bn), s));
   __nv_bfloat16 *a3 = buf, *b3 = buf + 3 * an;
   dg::split3_kernel<<<grid_for((long long)k * m), 256, 0, s>>>(
       A, (long long)k * m, a3, a3 + an, a3 + 2 * an, nullptr, nullptr, k, lda);

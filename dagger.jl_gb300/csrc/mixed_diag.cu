@@ -504,7 +504,7 @@ extern "C" int dg_potrf_inv_f32(int n, float *A, int lda, float *V, int ldv, int
   cudaStream_t s = (cudaStream_t)stream;
   char *buf = nullptr;
   const size_t sb = dg::diag_chol_inv_scratch_bytes();
-  DG_CUDA_TRY(cudaMallocAsync((void **)&buf, sb + 256, s));
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&buf, sb + 256, s));
   int *words = (int *)(buf + sb);  // [0] info, [1] status
   DG_CUDA_TRY(cudaMemsetAsync(words, 0, 8, s));
   int rc = dg::diag_chol_inv_f32(A, lda, n, V, ldv, buf, words, 0, words + 1, nullptr, 0, s);

@@ -814,7 +814,7 @@ extern "C" int dg_gemm_f64_emulated_tn(int m, int n, int k, double alpha, const 
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = dg::oz_scratch_bytes(m, n, k, false);
   void *buf = nullptr;
-  DG_CUDA_TRY(cudaMallocAsync(&buf, bytes, s));
+  DG_CUDA_TRY(dg::pool_malloc_async(&buf, bytes, s));
   int rc = dg::oz_gemm_general('T', 'N', m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, buf,
                                bytes, nullptr, nullptr, s);
   cudaFreeAsync(buf, s);

@@ -884,8 +884,49 @@ static bool is_one_of(char c, const char *set) { return c && strchr(set, c) != n
 extern "C" const char *dg_version(void) { return "libdaggergb300 0.1 (sm_103a)"; }
 extern "C" const char *dg_last_error(void) { return t_last_error.c_str(); }
 
+namespace dg {
+namespace {
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+}  // namespace
+
+cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, s);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (!g_pools[dev]) {
+      cudaMemPoolProps props;
+      memset(&props, 0, sizeof props);
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      e = cudaMemPoolCreate(&g_pools[dev], &props);
+      if (e != cudaSuccess) {
+        g_pools[dev] = nullptr;
+        return e;
+      }
+      unsigned long long keep = ~0ull;
+      cudaMemPoolSetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool = g_pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+void pool_trim_all() {
+  std::lock_guard<std::mutex> g(g_pool_mu);
+  for (int d = 0; d < 64; d++)
+    if (g_pools[d]) cudaMemPoolTrimTo(g_pools[d], 0);
+}
+}  // namespace dg
+
 extern "C" int dg_finalize(void) {
   dg::clear_graphs();
+  dg::pool_trim_all();
   return 0;
 }
 

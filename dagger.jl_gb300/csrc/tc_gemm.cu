@@ -289,7 +289,10 @@ int launch(const TcParams &p, cudaStream_t s) {
 int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
   if (g.m <= 0 || g.n <= 0) return 0;
   if (g.terms != 1 && g.terms != 3 && g.terms != 6) return DG_ERR_UNSUPPORTED;
-  if (g.k <= 0 || g.k % 8 != 0 || g.lda % 8 != 0 || g.ldb % 8 != 0) return DG_ERR_UNSUPPORTED;
+  // K itself may be ragged: the tensor maps' K extent is g.k and the last
+  // block's columns past it are filled with zeros by TMA (only the row
+  // strides need 16-byte multiples)
+  if (g.k <= 0 || g.lda % 8 != 0 || g.ldb % 8 != 0) return DG_ERR_UNSUPPORTED;
   if (((uintptr_t)g.a_hi | (uintptr_t)g.b_hi) & 15) return DG_ERR_UNSUPPORTED;
   if (g.terms >= 3 && (((uintptr_t)g.a_lo | (uintptr_t)g.b_lo) & 15)) return DG_ERR_UNSUPPORTED;
   if (g.terms == 6 && (((uintptr_t)g.a_mid | (uintptr_t)g.b_mid) & 15)) return DG_ERR_UNSUPPORTED;

