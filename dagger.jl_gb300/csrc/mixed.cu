@@ -517,21 +517,29 @@ int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
     }
     return 0;
   }
-  // one-step lookahead: the next panel is factored on the auxiliary stream
-  // while the rest of the trailing matrix is updated on `s`
-  if (!f->aux) DG_CUDA_TRY(cudaStreamCreateWithFlags(&f->aux, cudaStreamNonBlocking));
+  // One-step lookahead.  The critical chain runs on the auxiliary stream at
+  // the device's greatest priority: the update of block row k+1 by panel k
+  // (`next`, which waits for the previous step's bulk update of the rows
+  // below it), then panel k+1.  The bulk update of the rows below (`rest`)
+  // runs on `s` beside it and waits only for panel k.  Block rows written by
+  // two launches are always ordered: row k+1 by rest(k-1) before next(k).
+  if (!f->aux) {
+    int least = 0, greatest = 0;
+    DG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    DG_CUDA_TRY(cudaStreamCreateWithPriority(&f->aux, cudaStreamNonBlocking, greatest));
+  }
   if (!f->ev_next) DG_CUDA_TRY(cudaEventCreateWithFlags(&f->ev_next, cudaEventDisableTiming));
   if (!f->ev_panel) DG_CUDA_TRY(cudaEventCreateWithFlags(&f->ev_panel, cudaEventDisableTiming));
-  DG_CUDA_TRY(cudaEventRecord(f->ev_panel, s));
+  DG_CUDA_TRY(cudaEventRecord(f->ev_panel, s));  // panel 0
   DG_CUDA_TRY(cudaStreamWaitEvent(f->aux, f->ev_panel, 0));
   for (int k = 0; k + 1 < f->mt; k++) {
-    DG_TRY(trailing_tc(f, k, /*next=*/true, s));
-    DG_CUDA_TRY(cudaEventRecord(f->ev_next, s));
-    DG_CUDA_TRY(cudaStreamWaitEvent(f->aux, f->ev_next, 0));
+    if (k > 0) DG_CUDA_TRY(cudaStreamWaitEvent(f->aux, f->ev_next, 0));  // rest(k-1)
+    DG_TRY(trailing_tc(f, k, /*next=*/true, f->aux));
     DG_TRY(panel_step(f, k + 1, f->aux));
     DG_CUDA_TRY(cudaEventRecord(f->ev_panel, f->aux));
     DG_TRY(trailing_tc(f, k, /*next=*/false, s));
-    DG_CUDA_TRY(cudaStreamWaitEvent(s, f->ev_panel, 0));
+    DG_CUDA_TRY(cudaEventRecord(f->ev_next, s));
+    DG_CUDA_TRY(cudaStreamWaitEvent(s, f->ev_panel, 0));  // panel k+1 before rest(k+1)
   }
   return 0;
 }
@@ -744,8 +752,6 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   dg::row_abs_sum_kernel<<<dim3((n + 255) / 256, mt), 256, 0, s>>>(f->tiles_dev, n, nb, mt, rows);
   dg::colmax_kernel<<<1, 1024, 0, s>>>(rows, n, n, dmax);
   dg::count_launches(2);
-  cudaMemcpyAsync(&f->normA, dmax, sizeof(double), cudaMemcpyDeviceToHost, s);
-  cudaFreeAsync(rows, s);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -756,15 +762,20 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   if (rc) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaFreeAsync(rows, s);
     return fail(rc);
   }
+  // the host reads ||A||_inf and the status words once, after the factorization
   int words[3];
   if (cudaMemcpyAsync(words, f->words, sizeof(words), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&f->normA, dmax, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaFreeAsync(rows, s);
     return fail(DG_ERR_CUDA);
   }
+  cudaFreeAsync(rows, s);
   cudaEventElapsedTime(&f->factor_ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -17,7 +17,9 @@
 //                  -= U(j, r)' U(j, c), forming the row-panel blocks
 //                  U(j, r) = I_j' A(j, r) on the fly from the inverse I_j of
 //                  the diagonal factor (so no barrier separates the panel
-//                  solve from the update)
+//                  solve from the update); each CTA works on four tiles at
+//                  once, one per group of 64 threads with 4 x 4 outputs per
+//                  thread (half a shared-memory load per FMA)
 //     grid barrier
 //   then every off-diagonal block of U is formed, U(j, c) = I_j' A(j, c),
 //   and V = U^-1 by recursive doubling over the 32-block inverses:
@@ -42,10 +44,15 @@ namespace {
 
 constexpr int DB = 32;            // sub-block order
 constexpr int DT = 256;           // threads per CTA
+constexpr int GT = 64;            // threads per group (one 32 x 32 tile product)
+constexpr int NG = DT / GT;       // groups per CTA
 constexpr int DP = DB + 1;        // padded shared-memory column
+constexpr int TS = DB * DP;       // floats per shared tile
 constexpr int kDiagMaxN = 1024;
-constexpr int kDiagMaxGrid = 64;
+constexpr int kDiagMaxGrid = 128;
 constexpr unsigned FULL = 0xffffffffu;
+// shared memory: the CTA's I_j, then five tiles per group
+constexpr int kDiagSmem = (1 + NG * 5) * TS * (int)sizeof(float);
 
 struct DiagArgs {
   float *D;            // the block, column-major, ld
@@ -110,61 +117,90 @@ __device__ __forceinline__ float rd_pad(const float *M, long long ld, int n, int
   return r == c ? 1.f : 0.f;
 }
 
-// 32 x 32 tile at (r0, c0) of M into shared t[c * DP + r] (identity padded).
+__device__ __forceinline__ void gsync(int grp) {
+  asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(GT) : "memory");
+}
+
+// 32 x 32 tile at (r0, c0) of M into shared t[c * DP + r] (identity padded),
+// by the 64 threads of a group (l = thread within the group).
 __device__ __forceinline__ void load_tile(float *t, const float *M, long long ld, int n, int r0,
-                                          int c0) {
-  const int r = threadIdx.x & 31;
+                                          int c0, int l) {
+  const int r = l & 31;
 #pragma unroll
-  for (int q = 0; q < 4; q++) {
-    const int c = (threadIdx.x >> 5) + 8 * q;
+  for (int q = 0; q < 16; q++) {
+    const int c = (l >> 5) + 2 * q;
     t[c * DP + r] = rd_pad(M, ld, n, r0 + r, c0 + c);
   }
 }
 
 __device__ __forceinline__ void store_tile(const float *t, float *M, long long ld, int n, int r0,
-                                           int c0, bool upper_only) {
-  const int r = threadIdx.x & 31;
+                                           int c0, bool upper_only, int l) {
+  const int r = l & 31;
 #pragma unroll
-  for (int q = 0; q < 4; q++) {
-    const int c = (threadIdx.x >> 5) + 8 * q;
+  for (int q = 0; q < 16; q++) {
+    const int c = (l >> 5) + 2 * q;
     if (r0 + r < n && c0 + c < n && (!upper_only || r <= c))
       __stcg(M + (r0 + r) + (size_t)(c0 + c) * ld, t[c * DP + r]);
   }
 }
 
-// acc[q] (+)= sum_p X(p, r) Y(p, c): X' Y for this thread's four outputs
-// (r = tid & 31, c = (tid >> 5) + 8 q).
-__device__ __forceinline__ void mma_tn(float (&acc)[4], const float *x, const float *y) {
-  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
-#pragma unroll 8
+// acc[i][j] (+)= sum_p X(p, r0 + i) Y(p, c0 + j): X' Y on this thread's 4 x 4
+// outputs, r0 = (l & 7) * 4, c0 = (l >> 3) * 4.
+__device__ __forceinline__ void mma_tn(float (&acc)[4][4], const float *x, const float *y, int l) {
+  const int r0 = (l & 7) * 4, c0 = (l >> 3) * 4;
+#pragma unroll 4
   for (int p = 0; p < DB; p++) {
-    const float xv = x[r * DP + p];
+    float xv[4], yv[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) acc[q] = fmaf(xv, y[(cw + 8 * q) * DP + p], acc[q]);
+    for (int i = 0; i < 4; i++) xv[i] = x[(r0 + i) * DP + p];
+#pragma unroll
+    for (int j = 0; j < 4; j++) yv[j] = y[(c0 + j) * DP + p];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = fmaf(xv[i], yv[j], acc[i][j]);
   }
 }
 
-// acc[q] (+)= sum_p X(r, p) Y(p, c): X Y.
-__device__ __forceinline__ void mma_nn(float (&acc)[4], const float *x, const float *y) {
-  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
-#pragma unroll 8
+// acc[i][j] (+)= sum_p X(r0 + i, p) Y(p, c0 + j): X Y.
+__device__ __forceinline__ void mma_nn(float (&acc)[4][4], const float *x, const float *y, int l) {
+  const int r0 = (l & 7) * 4, c0 = (l >> 3) * 4;
+#pragma unroll 4
   for (int p = 0; p < DB; p++) {
-    const float xv = x[p * DP + r];
+    float xv[4], yv[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) acc[q] = fmaf(xv, y[(cw + 8 * q) * DP + p], acc[q]);
+    for (int i = 0; i < 4; i++) xv[i] = x[p * DP + r0 + i];
+#pragma unroll
+    for (int j = 0; j < 4; j++) yv[j] = y[(c0 + j) * DP + p];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = fmaf(xv[i], yv[j], acc[i][j]);
   }
 }
 
-__device__ __forceinline__ void put(float *t, const float (&acc)[4]) {
-  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
+__device__ __forceinline__ void zero(float (&acc)[4][4]) {
 #pragma unroll
-  for (int q = 0; q < 4; q++) t[(cw + 8 * q) * DP + r] = acc[q];
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
+}
+
+// t = acc (sign 0) or t += sign * acc on this thread's outputs.
+__device__ __forceinline__ void put(float *t, const float (&acc)[4][4], int l, float sign = 0.f) {
+  const int r0 = (l & 7) * 4, c0 = (l >> 3) * 4;
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      float *e = t + (c0 + j) * DP + r0 + i;
+      *e = sign == 0.f ? acc[i][j] : fmaf(sign, acc[i][j], *e);
+    }
 }
 
 // One warp: b[r] in lane c holds B(r, c), r <= c, of a symmetric 32 x 32
-// block.  On return b[r] = U(r, c) with B = U'U and iv[r] = (U^-1)(r, c)
-// (zero for r > c).  Returns the first column whose pivot is not positive,
-// or -1.
+// block.  On return b[r] = U(r, c) with B = U'U.  Returns the first column
+// whose pivot is not positive, or -1.
 __device__ int warp_chol32(float (&b)[32], int lane) {
   int fail = -1;
 #pragma unroll
@@ -187,6 +223,7 @@ __device__ int warp_chol32(float (&b)[32], int lane) {
   return fail;
 }
 
+// iv[r] in lane c = (U^-1)(r, c) for the upper factor held as b (zero r > c).
 __device__ void warp_inv32(const float (&b)[32], float (&iv)[32], int lane) {
   float rd = 0.f;
 #pragma unroll
@@ -202,13 +239,13 @@ __device__ void warp_inv32(const float (&b)[32], float (&iv)[32], int lane) {
   }
 }
 
-// Warp 0 of the calling CTA factors (or, mode 1, only inverts) the tile in
-// shared t; the factor goes back to t, its inverse to ti.  Returns the failed
-// column or -1 (valid in every thread).
-__device__ int tile_factor(float *t, float *ti, bool factor, int *s_fail) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();
-  if (warp == 0) {
+// The first warp of group `grp` factors (or only inverts) the tile in shared
+// t; the factor goes back to t, its inverse to ti.  Returns the failed column
+// or -1 (valid in every thread of the group).
+__device__ int tile_factor(float *t, float *ti, bool factor, int *s_fail, int grp, int l) {
+  gsync(grp);
+  if (l < 32) {
+    const int lane = l;
     float b[32], iv[32];
 #pragma unroll
     for (int r = 0; r < 32; r++) b[r] = r <= lane ? t[lane * DP + r] : 0.f;
@@ -222,16 +259,25 @@ __device__ int tile_factor(float *t, float *ti, bool factor, int *s_fail) {
         ti[lane * DP + r] = iv[r];
       }
     }
-    if (lane == 0) *s_fail = f;
+    if (lane == 0) s_fail[grp] = f;
   }
-  __syncthreads();
-  return *s_fail;
+  gsync(grp);
+  return s_fail[grp];
+}
+
+// Tile `idx` (0-based, row-major) of the upper triangle of an m x m tile grid.
+__device__ __forceinline__ void upper_tile(int idx, int m, int &rr, int &cc) {
+  rr = 0;
+  while (idx >= m - rr) {
+    idx -= m - rr;
+    rr++;
+  }
+  cc = rr + idx;
 }
 
 __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
-  __shared__ float sI[DB * DP], sA[DB * DP], sB[DB * DP], sC[DB * DP], sUr[DB * DP],
-      sUc[DB * DP];
-  __shared__ int s_stop, s_fail;
+  extern __shared__ float smem[];
+  __shared__ int s_stop, s_fail[NG];
   // (every CTA takes the same decision: the status word can change during
   // the launch, but a CTA that returns here leaves the others' barrier
   // waits to see it and stop)
@@ -239,22 +285,27 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
   if (a.mode == 1 && (!a.run_if || *(volatile const int *)a.run_if == 0)) return;
   const int n = a.n, nblk = (n + DB - 1) / DB;
   const int G = gridDim.x, g = blockIdx.x;
+  const int grp = threadIdx.x / GT, l = threadIdx.x % GT;
+  float *sI = smem;
+  float *g0 = smem + TS * (1 + 5 * grp);  // this group's five tiles
+  float *tA = g0, *tB = g0 + TS, *tC = g0 + 2 * TS, *tU = g0 + 3 * TS, *tV = g0 + 4 * TS;
   unsigned epoch = 0;
-  const int r = threadIdx.x & 31, cw = threadIdx.x >> 5;
+  const int ngroups = G * NG;             // every group of the grid
+  const int gid = g * NG + grp;
 
   if (a.mode == 0) {
-    // ---- block 0 ----
-    if (g == 0) {
-      load_tile(sC, a.D, a.ld, n, 0, 0);
-      const int f = tile_factor(sC, sI, true, &s_fail);
+    // ---- block 0 (group 0 of CTA 0) ----
+    if (g == 0 && grp == 0) {
+      load_tile(tC, a.D, a.ld, n, 0, 0, l);
+      const int f = tile_factor(tC, sI, true, s_fail, 0, l);
       if (f >= 0) {
-        if (threadIdx.x == 0) {
+        if (l == 0) {
           atomicCAS(a.info, 0, a.info_off + f + 1);
           atomicExch(a.fail, 1);
         }
       } else {
-        store_tile(sC, a.D, a.ld, n, 0, 0, true);
-        store_tile(sI, a.I, DB, DB, 0, 0, false);
+        store_tile(tC, a.D, a.ld, n, 0, 0, true, l);
+        store_tile(sI, a.I, DB, DB, 0, 0, false, l);
       }
     }
     if (!grid_sync(a, ++epoch, &s_stop)) return;
@@ -262,69 +313,66 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
     for (int j = 0; j + 1 < nblk; j++) {
       const int bj = j * DB;
       if (g == 0) {
-        // sI holds I_j (formed by this CTA in the previous step)
-        load_tile(sA, a.D, a.ld, n, bj, bj + DB);            // A(j, j+1)
-        load_tile(sC, a.D, a.ld, n, bj + DB, bj + DB);       // tile (j+1, j+1)
-        __syncthreads();
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        mma_tn(acc, sI, sA);                                 // U(j, j+1)
-        __syncthreads();
-        put(sUr, acc);
-        __syncthreads();
-        float up[4] = {0.f, 0.f, 0.f, 0.f};
-        mma_tn(up, sUr, sUr);
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const int c = cw + 8 * q;
-          sC[c * DP + r] -= up[q];
-        }
-        const int f = tile_factor(sC, sB, true, &s_fail);
-        if (f >= 0) {
-          if (threadIdx.x == 0) {
-            atomicCAS(a.info, 0, a.info_off + bj + DB + f + 1);
-            atomicExch(a.fail, 1);
+        // group 0: the critical chain (sI holds I_j from the previous step)
+        if (grp == 0) {
+          load_tile(tA, a.D, a.ld, n, bj, bj + DB, l);            // A(j, j+1)
+          load_tile(tC, a.D, a.ld, n, bj + DB, bj + DB, l);       // tile (j+1, j+1)
+          gsync(0);
+          float acc[4][4];
+          zero(acc);
+          mma_tn(acc, sI, tA, l);                                 // U(j, j+1)
+          put(tU, acc, l);
+          gsync(0);
+          zero(acc);
+          mma_tn(acc, tU, tU, l);
+          put(tC, acc, l, -1.f);
+          const int f = tile_factor(tC, tV, true, s_fail, 0, l);
+          if (f >= 0) {
+            if (l == 0) {
+              atomicCAS(a.info, 0, a.info_off + bj + DB + f + 1);
+              atomicExch(a.fail, 1);
+            }
+          } else {
+            store_tile(tC, a.D, a.ld, n, bj + DB, bj + DB, true, l);
+            store_tile(tV, a.I + (size_t)(j + 1) * DB * DB, DB, DB, 0, 0, false, l);
+            for (int e = l; e < TS; e += GT) sI[e] = tV[e];      // I_(j+1) for the next step
           }
-        } else {
-          store_tile(sC, a.D, a.ld, n, bj + DB, bj + DB, true);
-          store_tile(sB, a.I + (size_t)(j + 1) * DB * DB, DB, DB, 0, 0, false);
-          // sI <- I_(j+1) for the next step
-          for (int e = threadIdx.x; e < DB * DP; e += DT) sI[e] = sB[e];
         }
       } else {
-        // the other tiles (r, c), j+1 <= rr <= cc < nblk, (rr, cc) != (j+1, j+1)
+        // the other tiles (rr, cc), j+1 <= rr <= cc < nblk, (rr, cc) != (j+1, j+1),
+        // one per group of CTAs 1 .. G-1
         const int m = nblk - 1 - j;
         const int ntiles = m * (m + 1) / 2 - 1;
         if (ntiles > 0) {
-          load_tile(sI, a.I + (size_t)j * DB * DB, DB, DB, 0, 0);
-          for (int t = g - 1; t < ntiles; t += G - 1) {
-            // tile t + 1 of the upper triangle of the m x m tile grid, row-major
-            int idx = t + 1, rr = 0;
-            while (idx >= m - rr) {
-              idx -= m - rr;
-              rr++;
-            }
-            const int cc = rr + idx;
+          __syncthreads();
+          for (int e = threadIdx.x; e < TS; e += DT) {
+            const int c = e / DP, r = e - c * DP;
+            if (r < DB) sI[e] = __ldcg(a.I + (size_t)j * DB * DB + r + c * DB);
+          }
+          __syncthreads();
+          const int wgid = gid - NG, nw = ngroups - NG;  // worker groups
+          for (int t = wgid; t < ntiles; t += nw) {
+            int rr, cc;
+            upper_tile(t + 1, m, rr, cc);
             const int R0 = (j + 1 + rr) * DB, C0 = (j + 1 + cc) * DB;
-            __syncthreads();
-            load_tile(sA, a.D, a.ld, n, bj, R0);  // A(j, rr)
-            load_tile(sB, a.D, a.ld, n, bj, C0);  // A(j, cc)
-            load_tile(sC, a.D, a.ld, n, R0, C0);  // A(rr, cc)
-            __syncthreads();
-            float ur[4] = {0.f, 0.f, 0.f, 0.f}, uc[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_tn(ur, sI, sA);
-            mma_tn(uc, sI, sB);
-            put(sUr, ur);
-            put(sUc, uc);
-            __syncthreads();
-            float up[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_tn(up, sUr, sUc);
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-              const int c = cw + 8 * q;
-              sC[c * DP + r] -= up[q];
-            }
-            __syncthreads();
-            store_tile(sC, a.D, a.ld, n, R0, C0, rr == cc);
+            gsync(grp);
+            load_tile(tA, a.D, a.ld, n, bj, R0, l);  // A(j, rr)
+            load_tile(tB, a.D, a.ld, n, bj, C0, l);  // A(j, cc)
+            load_tile(tC, a.D, a.ld, n, R0, C0, l);  // A(rr, cc)
+            gsync(grp);
+            float acc[4][4];
+            zero(acc);
+            mma_tn(acc, sI, tA, l);
+            put(tU, acc, l);
+            zero(acc);
+            mma_tn(acc, sI, tB, l);
+            put(tV, acc, l);
+            gsync(grp);
+            zero(acc);
+            mma_tn(acc, tU, tV, l);
+            put(tC, acc, l, -1.f);
+            gsync(grp);
+            store_tile(tC, a.D, a.ld, n, R0, C0, rr == cc, l);
           }
         }
       }
@@ -333,106 +381,107 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
     // ---- the off-diagonal blocks of U: U(j, c) = I_j' A(j, c) ----
     {
       const int nb2 = nblk * (nblk - 1) / 2;
-      int loaded = -1;
-      for (int t = g; t < nb2; t += G) {
-        int idx = t, jj = 0;
-        while (idx >= nblk - 1 - jj) {
-          idx -= nblk - 1 - jj;
-          jj++;
-        }
-        const int cc = jj + 1 + idx;
-        __syncthreads();
-        if (loaded != jj) {
-          load_tile(sI, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0);
-          loaded = jj;
-        }
-        load_tile(sA, a.D, a.ld, n, jj * DB, cc * DB);
-        __syncthreads();
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        mma_tn(acc, sI, sA);
-        put(sC, acc);
-        __syncthreads();
-        store_tile(sC, a.D, a.ld, n, jj * DB, cc * DB, false);
+      for (int t = gid; t < nb2; t += ngroups) {
+        int jj, idx;
+        upper_tile(t, nblk - 1, jj, idx);  // row jj of the strict upper grid
+        const int cc = idx + 1;
+        gsync(grp);
+        load_tile(tV, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0, l);
+        load_tile(tA, a.D, a.ld, n, jj * DB, cc * DB, l);
+        gsync(grp);
+        float acc[4][4];
+        zero(acc);
+        mma_tn(acc, tV, tA, l);
+        put(tC, acc, l);
+        gsync(grp);
+        store_tile(tC, a.D, a.ld, n, jj * DB, cc * DB, false, l);
       }
     }
   } else {
     // ---- mode 1: inverses of the diagonal 32-blocks of a factored block ----
-    for (int jj = g; jj < nblk; jj += G) {
-      __syncthreads();
-      load_tile(sC, a.D, a.ld, n, jj * DB, jj * DB);
-      tile_factor(sC, sB, false, &s_fail);
-      store_tile(sB, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0, false);
+    for (int jj = gid; jj < nblk; jj += ngroups) {
+      gsync(grp);
+      load_tile(tC, a.D, a.ld, n, jj * DB, jj * DB, l);
+      tile_factor(tC, tV, false, s_fail, grp, l);
+      store_tile(tV, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0, false, l);
     }
     if (!grid_sync(a, ++epoch, &s_stop)) return;  // every I_j before V is assembled
   }
   // ---- V: I_j on the diagonal, zero below ----
-  for (int t = g; t < nblk * nblk; t += G) {
+  for (int t = gid; t < nblk * nblk; t += ngroups) {
     const int rb = t % nblk, cb = t / nblk;
     if (rb < cb) continue;
-    __syncthreads();
+    gsync(grp);
     if (rb == cb) {
-      load_tile(sC, a.I + (size_t)rb * DB * DB, DB, DB, 0, 0);
+      load_tile(tC, a.I + (size_t)rb * DB * DB, DB, DB, 0, 0, l);
     } else {
-#pragma unroll
-      for (int q = 0; q < 4; q++) sC[(cw + 8 * q) * DP + r] = 0.f;
+      for (int e = l; e < TS; e += GT) tC[e] = 0.f;
     }
-    __syncthreads();
-    store_tile(sC, a.V, a.ldv, n, rb * DB, cb * DB, false);
+    gsync(grp);
+    store_tile(tC, a.V, a.ldv, n, rb * DB, cb * DB, false, l);
   }
   if (!grid_sync(a, ++epoch, &s_stop)) return;
   // ---- recursive doubling: V12 = -V11 U12 V22 ----
   int npad = DB;
   while (npad < n) npad *= 2;
-  for (int s = DB; s < npad; s *= 2) {
-    const int nodes = npad / (2 * s), sb = s / DB;
+  for (int sz = DB; sz < npad; sz *= 2) {
+    const int nodes = npad / (2 * sz), sb = sz / DB;
     const int per = sb * sb;
     // phase 1: T_q = V11 U12 (V11 upper: k-blocks kb >= rb)
-    for (int t = g; t < nodes * per; t += G) {
+    for (int t = gid; t < nodes * per; t += ngroups) {
       const int q = t / per, rb = (t % per) % sb, cb = (t % per) / sb;
-      const int b0 = q * 2 * s;
-      if (b0 + s >= n) continue;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      const int b0 = q * 2 * sz;
+      if (b0 + sz >= n) continue;
+      float acc[4][4];
+      zero(acc);
       for (int kb = rb; kb < sb; kb++) {
-        __syncthreads();
-        load_tile(sA, a.V, a.ldv, n, b0 + rb * DB, b0 + kb * DB);
-        load_tile(sB, a.D, a.ld, n, b0 + kb * DB, b0 + s + cb * DB);
-        __syncthreads();
-        mma_nn(acc, sA, sB);
+        gsync(grp);
+        load_tile(tA, a.V, a.ldv, n, b0 + rb * DB, b0 + kb * DB, l);
+        load_tile(tB, a.D, a.ld, n, b0 + kb * DB, b0 + sz + cb * DB, l);
+        gsync(grp);
+        mma_nn(acc, tA, tB, l);
       }
-      float *Tq = a.T + (size_t)q * s * s;
+      float *Tq = a.T + (size_t)q * sz * sz;
+      const int r0 = (l & 7) * 4, c0 = (l >> 3) * 4;
 #pragma unroll
-      for (int qq = 0; qq < 4; qq++) {
-        const int c = cw + 8 * qq;
-        __stcg(Tq + (rb * DB + r) + (size_t)(cb * DB + c) * s, acc[qq]);
-      }
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int jx = 0; jx < 4; jx++)
+          __stcg(Tq + (rb * DB + r0 + i) + (size_t)(cb * DB + c0 + jx) * sz, acc[i][jx]);
     }
     if (!grid_sync(a, ++epoch, &s_stop)) return;
     // phase 2: V12 = -T_q V22 (V22 upper: k-blocks kb <= cb)
-    for (int t = g; t < nodes * per; t += G) {
+    for (int t = gid; t < nodes * per; t += ngroups) {
       const int q = t / per, rb = (t % per) % sb, cb = (t % per) / sb;
-      const int b0 = q * 2 * s;
-      if (b0 + s >= n) continue;
-      const float *Tq = a.T + (size_t)q * s * s;
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      const int b0 = q * 2 * sz;
+      if (b0 + sz >= n) continue;
+      const float *Tq = a.T + (size_t)q * sz * sz;
+      float acc[4][4];
+      zero(acc);
       for (int kb = 0; kb <= cb; kb++) {
-        __syncthreads();
+        gsync(grp);
+        {
+          const int r = l & 31;
 #pragma unroll
-        for (int qq = 0; qq < 4; qq++) {
-          const int c = cw + 8 * qq;
-          sA[c * DP + r] = __ldcg(Tq + (rb * DB + r) + (size_t)(kb * DB + c) * s);
+          for (int qq = 0; qq < 16; qq++) {
+            const int c = (l >> 5) + 2 * qq;
+            tA[c * DP + r] = __ldcg(Tq + (rb * DB + r) + (size_t)(kb * DB + c) * sz);
+          }
         }
-        load_tile(sB, a.V, a.ldv, n, b0 + s + kb * DB, b0 + s + cb * DB);
-        __syncthreads();
-        mma_nn(acc, sA, sB);
+        load_tile(tB, a.V, a.ldv, n, b0 + sz + kb * DB, b0 + sz + cb * DB, l);
+        gsync(grp);
+        mma_nn(acc, tA, tB, l);
       }
-      __syncthreads();
+      gsync(grp);
 #pragma unroll
-      for (int qq = 0; qq < 4; qq++) acc[qq] = -acc[qq];
-      put(sC, acc);
-      __syncthreads();
-      store_tile(sC, a.V, a.ldv, n, b0 + rb * DB, b0 + s + cb * DB, false);
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int jx = 0; jx < 4; jx++) acc[i][jx] = -acc[i][jx];
+      put(tC, acc, l);
+      gsync(grp);
+      store_tile(tC, a.V, a.ldv, n, b0 + rb * DB, b0 + sz + cb * DB, false, l);
     }
-    if (s * 2 < npad && !grid_sync(a, ++epoch, &s_stop)) return;
+    if (sz * 2 < npad && !grid_sync(a, ++epoch, &s_stop)) return;
   }
 }
 
@@ -466,14 +515,23 @@ int diag_chol_inv_f32(float *D, long long ld, int n, float *V, long long ldv, vo
   a.run_if = run_if;
   a.mode = mode;
   const int nblk = (n + DB - 1) / DB;
-  int G = std::min(kDiagMaxGrid, std::max(2, nblk * (nblk + 1) / 2 + 1));
+  // CTA 0 runs the chain; enough worker groups for the first step's tiles
+  int G = std::min(kDiagMaxGrid, std::max(2, 1 + (nblk * (nblk + 1) / 2 + NG - 1) / NG));
   G = std::min(G, dg_num_sms());
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  DG_CUDA_TRY(cudaGetDevice(&dev));
+  if (!attr_set[dev & 63]) {
+    DG_CUDA_TRY(cudaFuncSetAttribute(diag_chol_inv_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kDiagSmem));
+    attr_set[dev & 63] = true;
+  }
   DG_CUDA_TRY(cudaMemsetAsync(sc, 0, 8, s));
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof cfg);
   cfg.gridDim = dim3(G);
   cfg.blockDim = dim3(DT);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = kDiagSmem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
