@@ -478,6 +478,9 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   g.c = f->W; g.layout = 1; g.upper = 1;
   g.nb = nb; g.ntot = n;
   g.bn = 128; g.status = f->words;
+  // CTAs of the bulk update finish every few tiles, so the critical chain's
+  // launches on the high-priority stream get SMs without waiting for it
+  g.tiles_per_cta = 8;
   return tc_gemm_bf16(g, s);
 }
 

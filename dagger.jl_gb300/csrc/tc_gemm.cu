@@ -38,6 +38,8 @@
 // returns; nothing traps.
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "dg_common.cuh"
 #include "runtime.h"
 #include "tc_gemm.h"
@@ -230,6 +232,221 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_kernel(const __grid_constant__
                  : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Persistent form: one CTA per SM walks the output tiles (column by column of
+// tiles, so the CTAs running together share a B tile in L2) with two TMEM
+// accumulators, so the epilogue of one tile (TMEM -> registers -> the C
+// read-modify-write) overlaps the products of the next.
+//   warp 0, one thread   TMA producer over every tile's K blocks
+//   warp 1, one thread   MMA issuer: waits for an empty accumulator, issues
+//                        the tile's products into it, commits "accumulator
+//                        full"
+//   warps 2-5            epilogue: wait "full", read their TMEM lane quarter,
+//                        update C, arrive on "accumulator empty"
+// Every wait is bounded as in the one-tile kernel; a wait that gives up stops
+// all three roles, drains what was issued, and records DG_ERR_TIMEOUT.
+// ---------------------------------------------------------------------------
+template <int BN, int TERMS>
+struct SmemP {
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int SLICES = TERMS == 1 ? 1 : 2;
+  static constexpr int STAGE_BYTES = SLICES * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = (196608 / STAGE_BYTES) < 8 ? (196608 / STAGE_BYTES) : 8;
+  static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 + 256;
+};
+
+template <int BN, int TERMS>
+__global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_constant__ TcParams p) {
+  using S = SmemP<BN, TERMS>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *full = (uint64_t *)(smem + S::STAGES * S::STAGE_BYTES);
+  uint64_t *empty = full + S::STAGES;
+  uint64_t *accf = empty + S::STAGES;  // [2] accumulator full
+  uint64_t *acce = accf + 2;           // [2] accumulator empty
+  uint64_t *drain = acce + 2;
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+  int *abort_flag = (int *)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (p.status && *(volatile int *)p.status) return;
+  const int mtiles = (p.m + BM - 1) / BM, ntiles = (p.n + BN - 1) / BN;
+  const int total = mtiles * ntiles;
+  const int nk = (p.k + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S::STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(2 * BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer ----------------
+    uint32_t it = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < total && !stop; t += gridDim.x) {
+      const int i0 = (t % mtiles) * BM, j0 = (t / mtiles) * BN;
+      if (p.upper && i0 > j0 + BN - 1) continue;
+      for (int kb = 0; kb < nk; kb++, it++) {
+        const int s = it % S::STAGES;
+        if (it >= (uint32_t)S::STAGES && !mbar_wait(&empty[s], ((it / S::STAGES) - 1) & 1)) {
+          atomicExch(abort_flag, 1);
+          stop = true;
+          break;
+        }
+        if (*(volatile int *)abort_flag) {
+          stop = true;
+          break;
+        }
+        uint8_t *st = smem + s * S::STAGE_BYTES;
+        mbar_expect_tx(&full[s], S::STAGE_BYTES);
+        const int kx = kb * BK;
+        tma_load_2d(st, &p.a_hi, &full[s], kx, p.a_row0 + i0);
+        tma_load_2d(st + S::A_BYTES, &p.b_hi, &full[s], kx, p.b_row0 + j0);
+        if (TERMS == 3) {
+          tma_load_2d(st + S::A_BYTES + S::B_BYTES, &p.a_lo, &full[s], kx, p.a_row0 + i0);
+          tma_load_2d(st + 2 * S::A_BYTES + S::B_BYTES, &p.b_lo, &full[s], kx, p.b_row0 + j0);
+        }
+      }
+    }
+    // every load issued must land before the CTA may exit
+    for (uint32_t q = (it > (uint32_t)S::STAGES ? it - S::STAGES : 0); q < it; q++)
+      if (!mbar_wait(&full[q % S::STAGES], (q / S::STAGES) & 1)) atomicExch(abort_flag, 1);
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t sbase = smem_u32(smem);
+    uint32_t it = 0, lt = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < total && !stop; t += gridDim.x) {
+      const int i0 = (t % mtiles) * BM, j0 = (t / mtiles) * BN;
+      if (p.upper && i0 > j0 + BN - 1) continue;
+      const uint32_t buf = lt & 1;
+      if (!mbar_wait(&acce[buf], ((lt >> 1) & 1) ^ 1)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d = tmem + buf * BN;
+      for (int kb = 0; kb < nk; kb++, it++) {
+        const int s = it % S::STAGES;
+        if (*(volatile int *)abort_flag || !mbar_wait(&full[s], (it / S::STAGES) & 1)) {
+          atomicExch(abort_flag, 1);
+          stop = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = sbase + s * S::STAGE_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; kk++) {
+          const uint32_t koff = kk * 32;
+          const uint64_t a = sw128_desc(st + koff);
+          const uint64_t b = sw128_desc(st + S::A_BYTES + koff);
+          mma_bf16(d, a, b, p.idesc, (kb | kk) ? 1u : 0u);
+          if (TERMS == 3) {
+            const uint64_t alo = sw128_desc(st + S::A_BYTES + S::B_BYTES + koff);
+            const uint64_t blo = sw128_desc(st + 2 * S::A_BYTES + S::B_BYTES + koff);
+            mma_bf16(d, a, blo, p.idesc, 1u);
+            mma_bf16(d, alo, b, p.idesc, 1u);
+          }
+        }
+        mma_commit(&empty[s]);
+      }
+      if (stop) break;
+      mma_commit(&accf[buf]);
+      lt++;
+    }
+    // all products issued by this thread are complete before TMEM is freed
+    mma_commit(drain);
+    if (!mbar_wait(drain, 0)) atomicExch(abort_flag, 1);
+  } else if (warp >= 2) {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3;  // the TMEM lane quarter this warp may read
+    const float alpha = p.alpha_dev ? *p.alpha_dev : p.alpha;
+    const bool upper = p.layout == 1 || p.upper;
+    const bool read_c = p.layout == 1 || p.beta != 0.f;
+    const float beta = p.layout == 1 ? 1.f : p.beta;
+    uint32_t lt = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+      const int i0 = (t % mtiles) * BM, j0 = (t / mtiles) * BN;
+      if (p.upper && i0 > j0 + BN - 1) continue;
+      const uint32_t buf = lt & 1;
+      if (*(volatile int *)abort_flag || !mbar_wait(&accf[buf], (lt >> 1) & 1)) {
+        atomicExch(abort_flag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int row = i0 + q * 32 + lane;
+      long long r_panel = 0, base = 0;
+      if (p.layout == 1) {
+        const long long gi = p.off + row;
+        r_panel = gi / p.nb;
+        base = (long long)p.nb * (r_panel * p.ntot - p.nb * r_panel * (r_panel - 1) / 2) +
+               (gi - r_panel * p.nb);
+      }
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * BN + c0, v);
+        if (row >= p.m || j0 + c0 >= p.n) continue;
+        float *cp0;
+        long long cstride;
+        if (p.layout == 0) {
+          cp0 = p.c + (size_t)row + (size_t)(j0 + c0) * p.ldc;
+          cstride = p.ldc;
+        } else {
+          cp0 = p.c + base + (p.off + j0 + c0 - r_panel * p.nb) * p.nb;
+          cstride = p.nb;
+        }
+        float old[32];
+#pragma unroll
+        for (int c = 0; c < 32; c++) {
+          const int col = j0 + c0 + c;
+          const bool in = col < p.n && !(upper && row > col);
+          old[c] = (in && read_c) ? cp0[(size_t)c * cstride] : 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < 32; c++) {
+          const int col = j0 + c0 + c;
+          if (col >= p.n || (upper && row > col)) continue;
+          cp0[(size_t)c * cstride] = read_c ? fmaf(alpha, v[c], beta * old[c]) : alpha * v[c];
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[buf]);
+      lt++;
+    }
+  }
+  __syncthreads();
+  if (*(volatile int *)abort_flag && threadIdx.x == 0 && p.status)
+    atomicCAS(p.status, 0, DG_ERR_TIMEOUT);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN)
+                 : "memory");
+}
+
 // cuTensorMapEncodeTiled is a driver API call; it is resolved through the
 // runtime's entry-point query so the library does not link libcuda (it then
 // loads on machines without a driver, e.g. for ABI checks).
@@ -284,6 +501,34 @@ int launch(const TcParams &p, cudaStream_t s) {
   return 0;
 }
 
+template <int BN, int TERMS>
+int launch_persist(const TcParams &p, int tiles_per_cta, cudaStream_t s) {
+  using S = SmemP<BN, TERMS>;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr_set[dev & 63]) {
+    DG_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_persist_kernel<BN, TERMS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
+    attr_set[dev & 63] = true;
+  }
+  const long long mt = (p.m + BM - 1) / BM, nt = (p.n + BN - 1) / BN;
+  long long tiles = mt * nt;
+  if (p.upper) {  // tiles not wholly below the diagonal
+    tiles = 0;
+    for (long long bj = 0; bj < nt; bj++)
+      tiles += std::min(mt, (bj * BN + BN - 1) / BM + 1);
+  }
+  if (tiles <= 0) return 0;
+  long long grid = dg_num_sms();
+  if (tiles_per_cta > 0) grid = std::max(grid, (tiles + tiles_per_cta - 1) / tiles_per_cta);
+  grid = std::min<long long>(std::min<long long>(grid, tiles), 1 << 30);
+  tc_gemm_persist_kernel<BN, TERMS><<<(unsigned)grid, 192, S::TOTAL, s>>>(p);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return 0;
+}
+
 }  // namespace
 
 int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
@@ -324,10 +569,11 @@ int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
   p.status = g.status;
   p.idesc = idesc_f16kind(BM, bn, h);
   p.alpha_dev = g.alpha_dev;
-  if (g.terms == 1)
-    return bn == 256 ? launch<256, 1>(p, s) : launch<128, 1>(p, s);
   if (g.terms == 6) return launch<128, 6>(p, s);
-  return bn == 256 ? launch<256, 3>(p, s) : launch<128, 3>(p, s);
+  const int tpc = g.tiles_per_cta;
+  if (g.terms == 1)
+    return bn == 256 ? launch_persist<256, 1>(p, tpc, s) : launch_persist<128, 1>(p, tpc, s);
+  return bn == 256 ? launch_persist<256, 3>(p, tpc, s) : launch_persist<128, 3>(p, tpc, s);
 }
 
 }  // namespace dg

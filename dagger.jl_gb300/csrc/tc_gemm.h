@@ -43,6 +43,9 @@ struct TcGemmArgs {
   int *status;
   int fp16;                           // operands are FP16 instead of BF16
   const float *alpha_dev;             // optional device-resident alpha
+  int tiles_per_cta;                  // 0: one wave (a CTA per SM walks all tiles); else about
+                                      // that many tiles per CTA, so that CTAs finish and
+                                      // launches of other streams can take their SMs
 };
 
 int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s);
