@@ -11,8 +11,9 @@
 //
 //   step j (blocks of 32 rows/columns, bj = j * 32):
 //     CTA 0        finishes the diagonal tile (j+1, j+1): its last update
-//                  -= U(j, j+1)' U(j, j+1), then one warp factors it and
-//                  inverts the 32 x 32 factor (register-resident, shuffles)
+//                  -= U(j, j+1)' U(j, j+1), then all its threads factor it and
+//                  invert the 32 x 32 factor in shared memory (one barrier
+//                  per column)
 //     CTAs 1..G-1  update the other tiles (r, c), j+1 <= r <= c, by
 //                  -= U(j, r)' U(j, c), forming the row-panel blocks
 //                  U(j, r) = I_j' A(j, r) on the fly from the inverse I_j of
@@ -50,7 +51,6 @@ constexpr int DP = DB + 1;        // padded shared-memory column
 constexpr int TS = DB * DP;       // floats per shared tile
 constexpr int kDiagMaxN = 1024;
 constexpr int kDiagMaxGrid = 128;
-constexpr unsigned FULL = 0xffffffffu;
 // shared memory: the CTA's I_j, then five tiles per group
 constexpr int kDiagSmem = (1 + NG * 5) * TS * (int)sizeof(float);
 
@@ -198,71 +198,82 @@ __device__ __forceinline__ void put(float *t, const float (&acc)[4][4], int l, f
     }
 }
 
-// One warp: b[r] in lane c holds B(r, c), r <= c, of a symmetric 32 x 32
-// block.  On return b[r] = U(r, c) with B = U'U.  Returns the first column
-// whose pivot is not positive, or -1.
-__device__ int warp_chol32(float (&b)[32], int lane) {
-  int fail = -1;
-#pragma unroll
-  for (int j = 0; j < 32; j++) {
-    const float d = __shfl_sync(FULL, b[j], j);
-    // d is the same in every lane, so these branches are uniform (and the
-    // loop has no break, so it unrolls and b stays in registers)
-    if (fail < 0 && !(d > 0.f)) fail = j;
-    if (fail >= 0) continue;
-    const float u = sqrtf(d);
-    const float ru = 1.0f / u;
-    if (lane == j) b[j] = u;
-    else if (lane > j) b[j] *= ru;
-#pragma unroll
-    for (int r = j + 1; r < 32; r++) {
-      const float ujr = __shfl_sync(FULL, b[j], r);
-      if (lane >= r) b[r] = fmaf(-ujr, b[j], b[r]);
-    }
-  }
-  return fail;
+// Barrier over the NT threads of the calling set: the whole CTA (NT = DT)
+// or one group (NT = GT, named barrier grp + 1).
+template <int NT>
+__device__ __forceinline__ void tsync(int grp) {
+  if (NT == DT) __syncthreads();
+  else gsync(grp);
 }
 
-// iv[r] in lane c = (U^-1)(r, c) for the upper factor held as b (zero r > c).
-__device__ void warp_inv32(const float (&b)[32], float (&iv)[32], int lane) {
-  float rd = 0.f;
+// Cholesky factor and inverse of the 32 x 32 tile T (shared, T[c * DP + r] =
+// element (r, c), upper triangle read), by NT threads (tid in 0..NT-1).
+// Right-looking with one barrier per column: step j reads pivot T(j, j) and
+// row j unscaled and updates T(r, c) -= T(j, r) T(j, c) / T(j, j) for
+// j < r <= c; row j's scaling to U(j, :) waits until step j + 1, which no
+// longer reads it.  The inverse X = U^-1 (into W) is a back substitution of
+// the same shape: step j (from the bottom) takes row j of the working rows,
+// unscaled, W(r, c) -= U(r, j) W(j, c) / U(j, j) for r < j <= c, and scales row
+// j at step j - 1.  piv: 32 floats of shared scratch.  factor = false only
+// inverts (T already holds U).  Returns the first failed column or -1 (valid
+// in every calling thread); on failure T is left partly factored and W unset.
+template <int NT>
+__device__ int tile_chol_inv(float *T, float *W, float *piv, bool factor, int tid, int grp) {
+  constexpr int PER = DB * DB / NT;
+  tsync<NT>(grp);
+  if (factor) {
+    for (int j = 0; j < DB; j++) {
+      const float d = T[j * DP + j];
+      if (!(d > 0.f)) return j;  // the same value in every thread: a uniform exit
+      const float rcp = 1.0f / d;
+      if (tid == 0) piv[j] = d;
 #pragma unroll
-  for (int j = 0; j < 32; j++)
-    if (lane == j) rd = 1.0f / b[j];
-#pragma unroll
-  for (int r = 31; r >= 0; r--) {
-    float acc = 0.f;
-#pragma unroll
-    for (int t = r + 1; t < 32; t++) acc = fmaf(__shfl_sync(FULL, b[r], t), iv[t], acc);
-    const float rdr = __shfl_sync(FULL, rd, r);
-    iv[r] = lane > r ? -acc * rdr : (lane == r ? rdr : 0.f);
-  }
-}
-
-// The first warp of group `grp` factors (or only inverts) the tile in shared
-// t; the factor goes back to t, its inverse to ti.  Returns the failed column
-// or -1 (valid in every thread of the group).
-__device__ int tile_factor(float *t, float *ti, bool factor, int *s_fail, int grp, int l) {
-  gsync(grp);
-  if (l < 32) {
-    const int lane = l;
-    float b[32], iv[32];
-#pragma unroll
-    for (int r = 0; r < 32; r++) b[r] = r <= lane ? t[lane * DP + r] : 0.f;
-    int f = -1;
-    if (factor) f = warp_chol32(b, lane);
-    if (f < 0) {
-      warp_inv32(b, iv, lane);
-#pragma unroll
-      for (int r = 0; r < 32; r++) {
-        t[lane * DP + r] = r <= lane ? b[r] : 0.f;
-        ti[lane * DP + r] = iv[r];
+      for (int q = 0; q < PER; q++) {
+        const int e = tid + NT * q, r = e & 31, c = e >> 5;
+        if (r > j && r <= c) T[c * DP + r] = fmaf(-T[r * DP + j] * rcp, T[c * DP + j], T[c * DP + r]);
+        if (j > 0 && r == j - 1 && c >= r) {
+          const float u = sqrtf(piv[r]);
+          T[c * DP + r] = c == r ? u : T[c * DP + r] / u;
+        }
       }
+      tsync<NT>(grp);
     }
-    if (lane == 0) s_fail[grp] = f;
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int e = tid + NT * q, r = e & 31, c = e >> 5;
+      if (r == DB - 1 && c >= r) T[c * DP + r] = sqrtf(piv[r]);
+    }
   }
-  gsync(grp);
-  return s_fail[grp];
+  // W = I, then the back substitution
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int e = tid + NT * q, r = e & 31, c = e >> 5;
+    W[c * DP + r] = r == c ? 1.f : 0.f;
+  }
+  tsync<NT>(grp);
+  for (int j = DB - 1; j >= 0; j--) {
+    const float rcp = 1.0f / T[j * DP + j];
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int e = tid + NT * q, r = e & 31, c = e >> 5;
+      if (r < j && c >= j) W[c * DP + r] = fmaf(-T[j * DP + r] * rcp, W[c * DP + j], W[c * DP + r]);
+      if (j < DB - 1 && r == j + 1 && c >= r) W[c * DP + r] = W[c * DP + r] / T[r * DP + r];
+    }
+    tsync<NT>(grp);
+  }
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int e = tid + NT * q, r = e & 31, c = e >> 5;
+    if (r == 0 && c >= r) W[c * DP + r] = W[c * DP + r] / T[0];
+  }
+  // the strict lower part of T: zero (the factor is upper triangular)
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int e = tid + NT * q, r = e & 31, c = e >> 5;
+    if (r > c) T[c * DP + r] = 0.f;
+  }
+  tsync<NT>(grp);
+  return -1;
 }
 
 // Tile `idx` (0-based, row-major) of the upper triangle of an m x m tile grid.
@@ -277,7 +288,8 @@ __device__ __forceinline__ void upper_tile(int idx, int m, int &rr, int &cc) {
 
 __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
   extern __shared__ float smem[];
-  __shared__ int s_stop, s_fail[NG];
+  __shared__ int s_stop;
+  __shared__ float s_piv[NG][DB];
   // (every CTA takes the same decision: the status word can change during
   // the launch, but a CTA that returns here leaves the others' barrier
   // waits to see it and stop)
@@ -294,17 +306,20 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
   const int gid = g * NG + grp;
 
   if (a.mode == 0) {
-    // ---- block 0 (group 0 of CTA 0) ----
-    if (g == 0 && grp == 0) {
-      load_tile(tC, a.D, a.ld, n, 0, 0, l);
-      const int f = tile_factor(tC, sI, true, s_fail, 0, l);
+    // group 0's tiles, used by the whole of CTA 0 for the critical chain
+    float *cA = smem + TS, *cC = smem + 3 * TS, *cU = smem + 4 * TS, *cV = smem + 5 * TS;
+    // ---- block 0 (CTA 0) ----
+    if (g == 0) {
+      if (grp == 0) load_tile(cC, a.D, a.ld, n, 0, 0, l);
+      const int f = tile_chol_inv<DT>(cC, sI, s_piv[0], true, threadIdx.x, 0);
       if (f >= 0) {
-        if (l == 0) {
+        if (threadIdx.x == 0) {
           atomicCAS(a.info, 0, a.info_off + f + 1);
           atomicExch(a.fail, 1);
         }
-      } else {
-        store_tile(tC, a.D, a.ld, n, 0, 0, true, l);
+      } else if (grp == 0) {
+        store_tile(cC, a.D, a.ld, n, 0, 0, true, l);
+      } else if (grp == 1) {
         store_tile(sI, a.I, DB, DB, 0, 0, false, l);
       }
     }
@@ -313,30 +328,30 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
     for (int j = 0; j + 1 < nblk; j++) {
       const int bj = j * DB;
       if (g == 0) {
-        // group 0: the critical chain (sI holds I_j from the previous step)
+        // CTA 0: the critical chain (sI holds I_j from the previous step)
+        if (grp == 0) load_tile(cA, a.D, a.ld, n, bj, bj + DB, l);       // A(j, j+1)
+        if (grp == 1) load_tile(cC, a.D, a.ld, n, bj + DB, bj + DB, l);  // tile (j+1, j+1)
+        __syncthreads();
         if (grp == 0) {
-          load_tile(tA, a.D, a.ld, n, bj, bj + DB, l);            // A(j, j+1)
-          load_tile(tC, a.D, a.ld, n, bj + DB, bj + DB, l);       // tile (j+1, j+1)
-          gsync(0);
           float acc[4][4];
           zero(acc);
-          mma_tn(acc, sI, tA, l);                                 // U(j, j+1)
-          put(tU, acc, l);
+          mma_tn(acc, sI, cA, l);                                 // U(j, j+1)
+          put(cU, acc, l);
           gsync(0);
           zero(acc);
-          mma_tn(acc, tU, tU, l);
-          put(tC, acc, l, -1.f);
-          const int f = tile_factor(tC, tV, true, s_fail, 0, l);
-          if (f >= 0) {
-            if (l == 0) {
-              atomicCAS(a.info, 0, a.info_off + bj + DB + f + 1);
-              atomicExch(a.fail, 1);
-            }
-          } else {
-            store_tile(tC, a.D, a.ld, n, bj + DB, bj + DB, true, l);
-            store_tile(tV, a.I + (size_t)(j + 1) * DB * DB, DB, DB, 0, 0, false, l);
-            for (int e = l; e < TS; e += GT) sI[e] = tV[e];      // I_(j+1) for the next step
+          mma_tn(acc, cU, cU, l);
+          put(cC, acc, l, -1.f);
+        }
+        const int f = tile_chol_inv<DT>(cC, cV, s_piv[0], true, threadIdx.x, 0);
+        if (f >= 0) {
+          if (threadIdx.x == 0) {
+            atomicCAS(a.info, 0, a.info_off + bj + DB + f + 1);
+            atomicExch(a.fail, 1);
           }
+        } else {
+          if (grp == 0) store_tile(cC, a.D, a.ld, n, bj + DB, bj + DB, true, l);
+          if (grp == 1) store_tile(cV, a.I + (size_t)(j + 1) * DB * DB, DB, DB, 0, 0, false, l);
+          for (int e = threadIdx.x; e < TS; e += DT) sI[e] = cV[e];  // I_(j+1) for the next step
         }
       } else {
         // the other tiles (rr, cc), j+1 <= rr <= cc < nblk, (rr, cc) != (j+1, j+1),
@@ -402,7 +417,7 @@ __global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
     for (int jj = gid; jj < nblk; jj += ngroups) {
       gsync(grp);
       load_tile(tC, a.D, a.ld, n, jj * DB, jj * DB, l);
-      tile_factor(tC, tV, false, s_fail, grp, l);
+      tile_chol_inv<GT>(tC, tV, s_piv[grp], false, l, grp);
       store_tile(tV, a.I + (size_t)jj * DB * DB, DB, DB, 0, 0, false, l);
     }
     if (!grid_sync(a, ++epoch, &s_stop)) return;  // every I_j before V is assembled
