@@ -208,13 +208,15 @@ __device__ __forceinline__ void tsync(int grp) {
 
 // Cholesky factor and inverse of the 32 x 32 tile T (shared, T[c * DP + r] =
 // element (r, c), upper triangle read), by NT threads (tid in 0..NT-1).
-// Right-looking with one barrier per column: step j reads pivot T(j, j) and
-// row j unscaled and updates T(r, c) -= T(j, r) T(j, c) / T(j, j) for
-// j < r <= c; row j's scaling to U(j, :) waits until step j + 1, which no
+// Right-looking with one barrier per column: step j reads pivot d = T(j, j)
+// and row j unscaled, s = rsqrt(d) (the hardware approximation: about 2^-22
+// relative, far below what the mixed form's operands carry), and updates
+// T(r, c) -= (s T(j, r)) (s T(j, c)) for j < r <= c; row j's scaling by s
+// (U(j, :), the diagonal d s = sqrt(d)) waits until step j + 1, which no
 // longer reads it.  The inverse X = U^-1 (into W) is a back substitution of
-// the same shape: step j (from the bottom) takes row j of the working rows,
-// unscaled, W(r, c) -= U(r, j) W(j, c) / U(j, j) for r < j <= c, and scales row
-// j at step j - 1.  piv: 32 floats of shared scratch.  factor = false only
+// the same shape with 1 / U(j, j) = s kept per column: step j (from the
+// bottom) subtracts U(r, j) s W(j, c) from W(r, c) for r < j <= c and scales
+// row j at step j - 1.  piv: 32 floats of shared scratch.  factor = false only
 // inverts (T already holds U).  Returns the first failed column or -1 (valid
 // in every calling thread); on failure T is left partly factored and W unset.
 template <int NT>
@@ -225,24 +227,26 @@ __device__ int tile_chol_inv(float *T, float *W, float *piv, bool factor, int ti
     for (int j = 0; j < DB; j++) {
       const float d = T[j * DP + j];
       if (!(d > 0.f)) return j;  // the same value in every thread: a uniform exit
-      const float rcp = 1.0f / d;
-      if (tid == 0) piv[j] = d;
+      const float sj = rsqrtf(d);
+      if (tid == 0) piv[j] = sj;
+      const float pm = j > 0 ? piv[j - 1] : 0.f;
 #pragma unroll
       for (int q = 0; q < PER; q++) {
         const int e = tid + NT * q, r = e & 31, c = e >> 5;
-        if (r > j && r <= c) T[c * DP + r] = fmaf(-T[r * DP + j] * rcp, T[c * DP + j], T[c * DP + r]);
-        if (j > 0 && r == j - 1 && c >= r) {
-          const float u = sqrtf(piv[r]);
-          T[c * DP + r] = c == r ? u : T[c * DP + r] / u;
-        }
+        if (r > j && r <= c)
+          T[c * DP + r] = fmaf(-(T[r * DP + j] * sj), T[c * DP + j] * sj, T[c * DP + r]);
+        if (r == j - 1 && c >= r) T[c * DP + r] *= pm;
       }
       tsync<NT>(grp);
     }
+    const float pl = piv[DB - 1];
 #pragma unroll
     for (int q = 0; q < PER; q++) {
       const int e = tid + NT * q, r = e & 31, c = e >> 5;
-      if (r == DB - 1 && c >= r) T[c * DP + r] = sqrtf(piv[r]);
+      if (r == DB - 1 && c >= r) T[c * DP + r] *= pl;
     }
+  } else if (tid < DB) {
+    piv[tid] = 1.0f / T[tid * DP + tid];
   }
   // W = I, then the back substitution
 #pragma unroll
@@ -252,25 +256,21 @@ __device__ int tile_chol_inv(float *T, float *W, float *piv, bool factor, int ti
   }
   tsync<NT>(grp);
   for (int j = DB - 1; j >= 0; j--) {
-    const float rcp = 1.0f / T[j * DP + j];
+    const float sj = piv[j], sn = j < DB - 1 ? piv[j + 1] : 0.f;
 #pragma unroll
     for (int q = 0; q < PER; q++) {
       const int e = tid + NT * q, r = e & 31, c = e >> 5;
-      if (r < j && c >= j) W[c * DP + r] = fmaf(-T[j * DP + r] * rcp, W[c * DP + j], W[c * DP + r]);
-      if (j < DB - 1 && r == j + 1 && c >= r) W[c * DP + r] = W[c * DP + r] / T[r * DP + r];
+      if (r < j && c >= j) W[c * DP + r] = fmaf(-(T[j * DP + r] * sj), W[c * DP + j], W[c * DP + r]);
+      if (r == j + 1 && c >= r) W[c * DP + r] *= sn;
     }
     tsync<NT>(grp);
   }
+  const float p0 = piv[0];
 #pragma unroll
   for (int q = 0; q < PER; q++) {
     const int e = tid + NT * q, r = e & 31, c = e >> 5;
-    if (r == 0 && c >= r) W[c * DP + r] = W[c * DP + r] / T[0];
-  }
-  // the strict lower part of T: zero (the factor is upper triangular)
-#pragma unroll
-  for (int q = 0; q < PER; q++) {
-    const int e = tid + NT * q, r = e & 31, c = e >> 5;
-    if (r > c) T[c * DP + r] = 0.f;
+    if (r == 0) W[c * DP + r] *= p0;
+    if (r > c) T[c * DP + r] = 0.f;  // the factor is upper triangular
   }
   tsync<NT>(grp);
   return -1;
