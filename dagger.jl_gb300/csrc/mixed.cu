@@ -477,7 +477,7 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   g.alpha = -1.f; g.beta = 1.f;
   g.c = f->W; g.layout = 1; g.upper = 1;
   g.nb = nb; g.ntot = n;
-  g.bn = 128; g.status = f->words;
+  g.bn = 256; g.status = f->words;
   // CTAs of the bulk update finish every few tiles, so the critical chain's
   // launches on the high-priority stream get SMs without waiting for it
   g.tiles_per_cta = 8;
@@ -501,7 +501,8 @@ static int trailing_f32(dg_mixed *f, int k, cudaStream_t s) {
   return 0;
 }
 
-int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
+// The status words, the diagonal scaling and the packed FP32 copy S A S.
+int mixed_prepare(dg_mixed *f, cudaStream_t s) {
   const int n = f->n, nb = f->nb, mt = f->mt;
   int *bad = f->words + 2;
   DG_CUDA_TRY(cudaMemsetAsync(f->words, 0, sizeof(int) * (3 + 2 * mt), s));
@@ -511,6 +512,11 @@ int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
                 s>>>(f->tiles_dev, n, nb, mt, f->s, f->W, f->shift);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(2);
+  return 0;
+}
+
+// The blocked factorization of the packed copy (after mixed_prepare).
+int mixed_factor_run(dg_mixed *f, cudaStream_t s) {
   const bool tensor = f->precision != DG_PREC_FP32;
   DG_TRY(panel_step(f, 0, s));
   if (!tensor) {
@@ -716,52 +722,69 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   if (cudaMemcpyAsync(f->tiles_dev, tiles, sizeof(double *) * (size_t)mt * mt,
                       cudaMemcpyHostToDevice, s) != cudaSuccess)
     return fail(DG_ERR_CUDA);
-  // With the emulated FP64 engine the refinement's residual is an emulated
-  // product with A's rows cut into BF16 slices; they depend on A alone, so
-  // they are cut here, on a low-priority stream beside the factorization.
-  if (dg::get_f64_engine() == 2 && n <= 131072) {
-    const long long ldk = ((long long)n + 7) / 8 * 8;
-    const size_t ba = 16 * (size_t)ldk * n;
-    if (dg::pool_malloc_async(&f->ozA, ba + 8 * (size_t)n, s) == cudaSuccess) {
-      f->oz_ldk = ldk;
-      f->ozAs = (unsigned long long *)((char *)f->ozA + ba);
-      f->bytes += ba + 8 * (size_t)n;
-      int least = 0, greatest = 0;
-      cudaDeviceGetStreamPriorityRange(&least, &greatest);
-      if (cudaStreamCreateWithPriority(&f->aux2, cudaStreamNonBlocking, least) != cudaSuccess ||
-          cudaEventCreateWithFlags(&f->ev_oz, cudaEventDisableTiming) != cudaSuccess)
-        return fail(DG_ERR_CUDA);
-      cudaEvent_t ready;
-      if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess)
-        return fail(DG_ERR_CUDA);
-      cudaEventRecord(ready, s);  // the tile pointers and the slice buffer are in place
-      cudaStreamWaitEvent(f->aux2, ready, 0);
-      cudaEventDestroy(ready);
-      const int rc = dg::oz_split_tile_rows((const double *const *)f->tiles_dev, n, nb, f->ozA,
-                                            ldk, f->ozAs, nullptr, f->aux2);
-      if (rc) return fail(rc);
-      cudaEventRecord(f->ev_oz, f->aux2);
-    } else {
-      cudaGetLastError();  // no room: the solve cuts its own slices or uses the FP64 pipe
-      f->ozA = nullptr;
-    }
-  }
-  // ||A||_inf
-  double *rows = nullptr, *dmax = nullptr;
-  if (dg::pool_malloc_async((void **)&rows, sizeof(double) * (n + 1), s) != cudaSuccess)
-    return fail(DG_ERR_NOMEM);
-  dmax = rows + n;
-  if (cudaMemsetAsync(rows, 0, sizeof(double) * n, s) != cudaSuccess) return fail(DG_ERR_CUDA);
-  dg::row_abs_sum_kernel<<<dim3((n + 255) / 256, mt), 256, 0, s>>>(f->tiles_dev, n, nb, mt, rows);
-  dg::colmax_kernel<<<1, 1024, 0, s>>>(rows, n, n, dmax);
-  dg::count_launches(2);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  int rc = dg::mixed_factor_run(f, s);
+  // the scaled FP32 copy first, on s: the factorization starts from it
+  int rc = dg::mixed_prepare(f, s);
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return fail(rc);
+  }
+  // ||A||_inf (for the backward errors of the solve) and, with the emulated
+  // FP64 engine, A's rows cut into the BF16 slices of the refinement's
+  // emulated residual: both depend on A alone, so they run on a
+  // low-priority stream beside the factorization, after the copy above
+  // (which also reads A); ev_oz marks their completion.
+  double *rows = nullptr, *dmax = nullptr;
+  if (dg::pool_malloc_async((void **)&rows, sizeof(double) * (n + 1), s) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return fail(DG_ERR_NOMEM);
+  }
+  dmax = rows + n;
+  const bool oz = dg::get_f64_engine() == 2 && n <= 131072;
+  const long long ldk = ((long long)n + 7) / 8 * 8;
+  const size_t ba = 16 * (size_t)ldk * n;
+  if (oz && dg::pool_malloc_async(&f->ozA, ba + 8 * (size_t)n, s) != cudaSuccess) {
+    cudaGetLastError();  // no room: the solve cuts its own slices or uses the FP64 pipe
+    f->ozA = nullptr;
+  }
+  {
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    cudaEvent_t ready;
+    if (cudaStreamCreateWithPriority(&f->aux2, cudaStreamNonBlocking, least) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f->ev_oz, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cudaFreeAsync(rows, s);
+      return fail(DG_ERR_CUDA);
+    }
+    cudaEventRecord(ready, s);  // tile pointers, buffers and the copy of A are in place
+    cudaStreamWaitEvent(f->aux2, ready, 0);
+    cudaEventDestroy(ready);
+    cudaMemsetAsync(rows, 0, sizeof(double) * n, f->aux2);
+    dg::row_abs_sum_kernel<<<dim3((n + 255) / 256, mt), 256, 0, f->aux2>>>(f->tiles_dev, n, nb, mt,
+                                                                          rows);
+    dg::colmax_kernel<<<1, 1024, 0, f->aux2>>>(rows, n, n, dmax);
+    dg::count_launches(2);
+    if (f->ozA) {
+      f->oz_ldk = ldk;
+      f->ozAs = (unsigned long long *)((char *)f->ozA + ba);
+      f->bytes += ba + 8 * (size_t)n;
+      rc = dg::oz_split_tile_rows((const double *const *)f->tiles_dev, n, nb, f->ozA, ldk,
+                                  f->ozAs, nullptr, f->aux2);
+    }
+    cudaEventRecord(f->ev_oz, f->aux2);
+  }
+  if (!rc) rc = dg::mixed_factor_run(f, s);
   if (!rc) rc = dg::mixed_transpose_columns(f, s);
   cudaEventRecord(e1, s);
+  cudaStreamWaitEvent(s, f->ev_oz, 0);  // ||A||_inf is read below
   if (rc) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -50,7 +50,7 @@ constexpr int NG = DT / GT;       // groups per CTA
 constexpr int DP = DB + 1;        // padded shared-memory column
 constexpr int TS = DB * DP;       // floats per shared tile
 constexpr int kDiagMaxN = 1024;
-constexpr int kDiagMaxGrid = 128;
+constexpr int kDiagMaxGrid = 64;   // the chain shares the GPU with the bulk update
 // shared memory: the CTA's I_j, then five tiles per group
 constexpr int kDiagSmem = (1 + NG * 5) * TS * (int)sizeof(float);
 
