@@ -933,6 +933,38 @@ __global__ void dots_kernel(const double *U, long long ldu, const double *V, lon
   }
 }
 
+// out[i r + j] = V_i(:, j) . W(:, j) for the kk basis blocks V_i (stride vs):
+// CTA (j, i).  The classical Gram-Schmidt projections of one GMRES step.
+__global__ void multi_dots_kernel(const double *V, long long vs, const double *W, int n, int r,
+                                  double *out) {
+  const int j = blockIdx.x, i = blockIdx.y;
+  const double *v = V + vs * i + (size_t)j * n, *w = W + (size_t)j * n;
+  double acc = 0.0;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) acc = fma(v[e], w[e], acc);
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) out[(size_t)i * r + j] = acc;
+  }
+}
+
+// W(:, j) -= sum_i h[i r + j] V_i(:, j), i < kk.
+__global__ void multi_axpy_kernel(const double *V, long long vs, int kk, double *W, int n, int r,
+                                  const double *h) {
+  const long long total = (long long)n * r;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e / n);
+    double acc = W[e];
+    for (int i = 0; i < kk; i++) acc = fma(-h[(size_t)i * r + j], V[vs * i + e], acc);
+    W[e] = acc;
+  }
+}
+
 // V(:, j) = a[j] * U(:, j) + b[j] * V(:, j)   (coefficients from device memory)
 __global__ void axpby_kernel(const double *U, long long ldu, double *V, long long ldv, int n, int r,
                              const double *a, const double *b, int neg_a) {
@@ -960,8 +992,22 @@ int precond(const dg_mixed *f, const double *Y, double *Zo, float *Z32, int r, c
 
 // Restarted GMRES(m) on A d = r0 (FP64), left preconditioned by the factor,
 // each column an independent Krylov space.  x += d.  Returns iterations.
+// Y = A V (FP64, n x r, ld n): the emulated product from A's slices when
+// they exist, else the FP64 tile GEMM.
+int matvec(const dg_mixed *f, const double *V, double *Y, int r, cudaStream_t s,
+           const OzResidual *oz) {
+  const int n = f->n;
+  if (oz && oz->a) {
+    DG_TRY(dg::oz_split(V, n, 1, n, r, oz->x, oz->ldk, oz->ldk * r, oz->xs, nullptr, s));
+    return dg::oz_gemm(n, r, n, 1.0, oz->a, oz->ldk, oz->ldk * n, oz->as, oz->x, oz->ldk,
+                       oz->ldk * r, oz->xs, 0.0, Y, n, 0, nullptr, s);
+  }
+  return dg::gemm_tiles_f64(n, f->nb, r, 1.0, (const double *const *)f->tiles_dev, V, n, 0.0, Y, n,
+                            nullptr, s);
+}
+
 int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int r, int m,
-             int max_iters, double inner_tol, cudaStream_t s, int *iters_out) {
+             int max_iters, double inner_tol, cudaStream_t s, int *iters_out, const OzResidual *oz) {
   const int n = f->n;
   const size_t col = (size_t)n;
   double *V = nullptr, *W = nullptr, *D = nullptr, *sc = nullptr;
@@ -975,6 +1021,18 @@ int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int 
     return DG_ERR_NOMEM;
   }
   double *T = W + col * r;  // second scratch block
+  double *hb = nullptr;      // the Gram-Schmidt coefficients, 2 (m + 1) r
+  if (dg::pool_malloc_async((void **)&hb, sizeof(double) * 2 * (size_t)(m + 1) * r, s) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    cudaFreeAsync(V, s);
+    cudaFreeAsync(W, s);
+    cudaFreeAsync(D, s);
+    cudaFreeAsync(sc, s);
+    cudaFreeAsync(Z32, s);
+    return DG_ERR_NOMEM;
+  }
+  std::vector<double> hh;
   auto Vk = [&](int k) { return V + col * r * k; };
   std::vector<double> H((size_t)(m + 1) * m * r), g((size_t)(m + 1) * r), hcol(r), cs(m * r), sn(m * r);
   int total_it = 0;
@@ -1000,24 +1058,30 @@ int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int 
     int kdone = 0;
     for (int k = 0; k < m && total_it < max_iters; k++, total_it++) {
       // w = M^-1 A v_k
-      rc = dg::gemm_tiles_f64(n, f->nb, r, 1.0, (const double *const *)f->tiles_dev, Vk(k), n, 0.0,
-                              T, n, nullptr, s);
+      rc = matvec(f, Vk(k), T, r, s, oz);
       if (rc) break;
       rc = precond(f, T, W, Z32, r, s);
       if (rc) break;
-      // modified Gram-Schmidt
-      for (int i = 0; i <= k; i++) {
-        dots_kernel<<<r, 256, 0, s>>>(W, n, Vk(i), n, n, sc + 3 * r);
-        cudaMemcpyAsync(hcol.data(), sc + 3 * r, sizeof(double) * r, cudaMemcpyDeviceToHost, s);
-        axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(Vk(i), n, W, n, n, r, sc + 3 * r, nullptr, 1);
-        dg::count_launches(2);
-        cudaStreamSynchronize(s);
-        for (int j = 0; j < r; j++) H[((size_t)i * m + k) * r + j] = hcol[j];
-      }
+      // classical Gram-Schmidt twice (CGS2): the projections on all of
+      // v_0..v_k in one launch, the update in one more, repeated once; the
+      // host reads both sets of coefficients and the norm in one copy
+      const int kk = k + 1;
+      const long long vs = (long long)col * r;
+      multi_dots_kernel<<<dim3(r, kk), 256, 0, s>>>(V, vs, W, n, r, hb);
+      multi_axpy_kernel<<<grid_for(col * r), 256, 0, s>>>(V, vs, kk, W, n, r, hb);
+      multi_dots_kernel<<<dim3(r, kk), 256, 0, s>>>(V, vs, W, n, r, hb + (size_t)kk * r);
+      multi_axpy_kernel<<<grid_for(col * r), 256, 0, s>>>(V, vs, kk, W, n, r, hb + (size_t)kk * r);
       dots_kernel<<<r, 256, 0, s>>>(W, n, W, n, n, sc);
-      cudaMemcpyAsync(hcol.data(), sc, sizeof(double) * r, cudaMemcpyDeviceToHost, s);
+      dg::count_launches(5);
+      hh.resize((size_t)2 * kk * r + r);
+      cudaMemcpyAsync(hh.data(), hb, sizeof(double) * 2 * kk * r, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(hh.data() + 2 * kk * r, sc, sizeof(double) * r, cudaMemcpyDeviceToHost, s);
       cudaStreamSynchronize(s);
-      for (int j = 0; j < r; j++) H[((size_t)(k + 1) * m + k) * r + j] = std::sqrt(hcol[j]);
+      for (int i = 0; i <= k; i++)
+        for (int j = 0; j < r; j++)
+          H[((size_t)i * m + k) * r + j] = hh[(size_t)i * r + j] + hh[(size_t)(kk + i) * r + j];
+      for (int j = 0; j < r; j++)
+        H[((size_t)(k + 1) * m + k) * r + j] = std::sqrt(hh[(size_t)2 * kk * r + j]);
       inv_kernel<<<(r + 127) / 128, 128, 0, s>>>(sc, sc + r, r);
       cudaMemsetAsync(Vk(k + 1), 0, sizeof(double) * col * r, s);
       axpby_kernel<<<grid_for(col * r), 256, 0, s>>>(W, n, Vk(k + 1), n, n, r, sc + r, nullptr, 0);
@@ -1077,6 +1141,7 @@ int gmres_ir(const dg_mixed *f, const double *R0, double *X, long long ldx, int 
   cudaFreeAsync(D, s);
   cudaFreeAsync(sc, s);
   cudaFreeAsync(Z32, s);
+  cudaFreeAsync(hb, s);
   *iters_out = total_it;
   return rc;
 }
@@ -1155,7 +1220,7 @@ extern "C" int dg_mixed_solve(const dg_mixed *f, int nrhs, const double *B, int 
       rc = correction(f, R, n, X, ldx, Z, r, s);
     } else {
       int gi = 0;
-      rc = gmres_ir(f, R, X, ldx, r, o.restart, o.restart, o.gmres_inner_tol, s, &gi);
+      rc = gmres_ir(f, R, X, ldx, r, o.restart, o.restart, o.gmres_inner_tol, s, &gi, &oz);
       gm_iters += gi;
     }
     if (rc) break;
