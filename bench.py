@@ -78,6 +78,10 @@ def parse():
                     help="skip the tiled LU line (lu(A, RowMaximum()) and lu(A) \\ b)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--mixed-precision", default="auto")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the mixed form's sweep over N, kappa and right-hand sides")
+    ap.add_argument("--sweep-n", default="32768,65536")
+    ap.add_argument("--sweep-cond", default="1e2,1e4,1e6,1e8")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-count", type=int, default=500)
@@ -558,6 +562,9 @@ def run_ours(args):
         mixed = _guarded(bench_mixed, args, d, DA, A, B, stream, world)
     del DA, DB0, A, B
     torch.cuda.empty_cache()
+    sweep = None
+    if not args.no_sweep and rank == 0:
+        sweep = _guarded(bench_mixed_sweep, args, d, dev)
     mul = None
     if not args.no_mul:
         mul = _guarded(bench_mul, args, d, dev, stream)
@@ -583,11 +590,19 @@ def run_ours(args):
                         "factor_residual_probe": fres},
            "roofline": roof, "gpu_launches": int(launches),
            "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "parity_vs_oracle": parity,
-           "mixed": mixed, "mul": mul, "lu": lu, "batched": batched, "serving": serving}
+           "mixed": mixed, "mixed_sweep": sweep, "mul": mul, "lu": lu, "batched": batched, "serving": serving}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def _measured_bf16_sustained():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops_sustained"])
+    except (OSError, KeyError, ValueError):
+        return 1700.0
 
 
 def _measured_bf16_peak():
@@ -662,10 +677,106 @@ def roofline_emulated(L, nb, dev, stream, s):
 
 
 def choose_precision(cond):
-    """Operand precision of the mixed form by conditioning: BF16 hi/lo split up
-    to 1e6, FP32 updates beyond (the factor must stay usable as a
-    preconditioner for GMRES-IR)."""
-    return "bf16x3" if cond <= 1e6 else "fp32"
+    """Operand precision of the mixed form by conditioning (measured at N =
+    32768, 64 RHS): the BF16 hi/lo split up to 1e4 (3 refinement steps), the
+    three-slice FP32-accurate BF16 updates at 1e6 (7 steps against 9); from
+    1e8 on, a factor whose preconditioner is applied at FP32 accuracy no
+    longer lets refinement reach 1e-12, and the FP64 form (the emulated
+    engine) is used instead."""
+    if cond <= 1e4:
+        return "bf16x3"
+    if cond <= 1e6:
+        return "bf16x6"
+    return "fp64"
+
+
+def bench_mixed_sweep(args, d, dev):
+    """The mixed form over N in {32768, 65536} x kappa in {1e2, 1e4, 1e6,
+    1e8} x {1, 64} right-hand sides, A = Q diag(logspace(0, log10 kappa)) Q'
+    (one Q per N, FP32 QR of a seeded Gaussian), tile 1024.  Each point: one
+    factor + refined solve after a warm-up of the same call, TFLOP/s counted
+    as N^3/3 + 2 N^2 r, the refinement's iteration counts, the normwise
+    backward error (FP64, on the device), and the factor's BF16 tensor work
+    (terms x N^3/3 of the trailing updates and 6 x 2 nb N^2 / 2 of the panel
+    solves) per second as a fraction of the sustained BF16 peak."""
+    import torch
+    nb = args.nb
+    peak = _measured_bf16_sustained()
+    out = {"points": [], "nb": nb, "bf16_peak_sustained": peak}
+    terms = {"bf16": 1, "bf16x3": 3, "bf16x6": 6}
+    for n in [int(x) for x in args.sweep_n.split(",") if x]:
+        g = torch.Generator(device=dev)
+        g.manual_seed(args.seed)
+        G = torch.randn(n, n, generator=g, device=dev, dtype=torch.float32)
+        Q, _ = torch.linalg.qr(G)
+        del G
+        torch.cuda.empty_cache()
+        Bs = {r: make_rhs_gpu(n, r, args.seed + r, dev) for r in (1, 64)}
+        for cond in [float(x) for x in args.sweep_cond.split(",") if x]:
+            lam = torch.logspace(0.0, math.log10(cond), n, device=dev, dtype=torch.float32)
+            prev = torch.backends.cuda.matmul.allow_tf32
+            torch.backends.cuda.matmul.allow_tf32 = False
+            A = ((Q * lam) @ Q.T).double()
+            torch.backends.cuda.matmul.allow_tf32 = prev
+            A += A.T.clone()
+            A *= 0.5
+            DA = d.DArray.from_array(A, d.Blocks(nb, nb))
+            nA = A.abs().sum(dim=1).max()
+            prec = choose_precision(cond)
+            for r in (64, 1):
+                B = Bs[r]
+                X = torch.empty((r, n), dtype=torch.float64, device=dev).t()
+                Bc = B.t().contiguous().t()
+                st = torch.cuda.current_stream()
+                rep = None
+
+                def once():
+                    nonlocal rep
+                    if prec == "fp64":
+                        old = d.set_f64_engine("emulated")
+                        C = d.cholesky(DA, 'U', stream=st)
+                        DB = d.DArray.from_array(B, d.Blocks(nb, nb))
+                        d.ldiv_(C, DB, stream=st)
+                        X.copy_(DB.collect())
+                        d.set_f64_engine(old)
+                        rep = ({"iterations": 0, "gmres_iterations": 0, "solve_ms": None},
+                               {"factor_ms": None, "shift": 0.0})
+                        del C, DB
+                    else:
+                        F = d.cholesky_mixed(DA, prec, stream=st)
+                        _, rr = F.solve(Bc, tol=1e-12, out=X, raise_on_failure=False)
+                        rep = (rr, F.stats())
+                        F.close()
+                once()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                once()
+                e1.record(st)
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1) / 1e3
+                R = B - A @ X
+                be = float((R.abs().amax(dim=0) / (nA * X.abs().amax(dim=0) +
+                                                    B.abs().amax(dim=0))).max())
+                rr, fs = rep
+                pt = {"n": n, "cond": cond, "nrhs": r, "precision": prec, "ms": 1e3 * t,
+                      "TFLOP_s": flops(n, r) / t / 1e12, "solves_per_s": r / t,
+                      "factor_ms": fs.get("factor_ms"), "refine_ms": rr.get("solve_ms"),
+                      "ir_iterations": rr.get("iterations"),
+                      "gmres_iterations": rr.get("gmres_iterations"),
+                      "shift": fs.get("shift"), "backward_error": be}
+                if prec in terms and fs.get("factor_ms"):
+                    tc = terms[prec] * n ** 3 / 3.0 + 6.0 * nb * n * n
+                    pt["factor_bf16_TFLOP_s"] = tc / (fs["factor_ms"] / 1e3) / 1e12
+                    pt["factor_bf16_frac_sustained"] = pt["factor_bf16_TFLOP_s"] / peak
+                out["points"].append(pt)
+                del R, X, Bc
+            del A, DA
+            torch.cuda.empty_cache()
+        del Q, Bs
+        torch.cuda.empty_cache()
+    return out
 
 
 def bench_mul(args, d, dev, stream):
