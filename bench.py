@@ -562,9 +562,13 @@ def run_ours(args):
         mixed = _guarded(bench_mixed, args, d, DA, A, B, stream, world)
     del DA, DB0, A, B
     torch.cuda.empty_cache()
+    L.dg_release_memory()
+    torch.cuda.empty_cache()
     sweep = None
     if not args.no_sweep and rank == 0:
         sweep = _guarded(bench_mixed_sweep, args, d, dev)
+        L.dg_release_memory()
+        torch.cuda.empty_cache()
     mul = None
     if not args.no_mul:
         mul = _guarded(bench_mul, args, d, dev, stream)
@@ -693,7 +697,8 @@ def choose_precision(cond):
 def bench_mixed_sweep(args, d, dev):
     """The mixed form over N in {32768, 65536} x kappa in {1e2, 1e4, 1e6,
     1e8} x {1, 64} right-hand sides, A = Q diag(logspace(0, log10 kappa)) Q'
-    (one Q per N, FP32 QR of a seeded Gaussian), tile 1024.  Each point: one
+    (one Q per N, the FP32 QR of a seeded Gaussian; the product in FP64),
+    tile 1024.  Each point: one
     factor + refined solve after a warm-up of the same call, TFLOP/s counted
     as N^3/3 + 2 N^2 r, the refinement's iteration counts, the normwise
     backward error (FP64, on the device), and the factor's BF16 tensor work
@@ -713,15 +718,29 @@ def bench_mixed_sweep(args, d, dev):
         torch.cuda.empty_cache()
         Bs = {r: make_rhs_gpu(n, r, args.seed + r, dev) for r in (1, 64)}
         for cond in [float(x) for x in args.sweep_cond.split(",") if x]:
-            lam = torch.logspace(0.0, math.log10(cond), n, device=dev, dtype=torch.float32)
-            prev = torch.backends.cuda.matmul.allow_tf32
-            torch.backends.cuda.matmul.allow_tf32 = False
-            A = ((Q * lam) @ Q.T).double()
-            torch.backends.cuda.matmul.allow_tf32 = prev
-            A += A.T.clone()
-            A *= 0.5
-            DA = d.DArray.from_array(A, d.Blocks(nb, nb))
+            if choose_precision(cond) == "fp64" and n > 32768:
+                # the FP64 form's copy of A does not fit beside the rest at this N
+                out.setdefault("skipped", []).append(
+                    {"n": n, "cond": cond, "reason": "FP64-form copy of A does not fit in HBM "
+                                                      "beside the sweep's other buffers"})
+                continue
+            torch.cuda.empty_cache()
+            # A = S S' with S = Q diag(sqrt(l)) in FP64, formed by syrk_dagger!
+            # on the emulated FP64 engine: exactly symmetric and positive
+            # definite to FP64 accuracy at every kappa (an FP32 product is not,
+            # beyond about 1e5)
+            lam = torch.logspace(0.0, math.log10(cond), n, device=dev, dtype=torch.float64)
+            DS = d.DArray.from_array(Q.double() * lam.sqrt(), d.Blocks(nb, nb))
+            DA = d.DArray((n, n), d.Blocks(nb, nb), device=dev)
+            old_engine = d.set_f64_engine("emulated")
+            d.syrk_dagger_(DA, 'N', DS, 1.0, 0.0)
+            d.set_f64_engine(old_engine)
+            del DS, lam
+            torch.cuda.empty_cache()
+            A = DA.collect()
             nA = A.abs().sum(dim=1).max()
+            del A
+            torch.cuda.empty_cache()
             prec = choose_precision(cond)
             for r in (64, 1):
                 B = Bs[r]
@@ -756,7 +775,10 @@ def bench_mixed_sweep(args, d, dev):
                 e1.record(st)
                 torch.cuda.synchronize()
                 t = e0.elapsed_time(e1) / 1e3
+                torch.cuda.empty_cache()
+                A = DA.collect()
                 R = B - A @ X
+                del A
                 be = float((R.abs().amax(dim=0) / (nA * X.abs().amax(dim=0) +
                                                     B.abs().amax(dim=0))).max())
                 rr, fs = rep
@@ -772,7 +794,7 @@ def bench_mixed_sweep(args, d, dev):
                     pt["factor_bf16_frac_sustained"] = pt["factor_bf16_TFLOP_s"] / peak
                 out["points"].append(pt)
                 del R, X, Bc
-            del A, DA
+            del DA
             torch.cuda.empty_cache()
         del Q, Bs
         torch.cuda.empty_cache()

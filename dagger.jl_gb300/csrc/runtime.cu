@@ -914,7 +914,20 @@ cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t s) {
     }
     pool = g_pools[dev];
   }
-  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+  e = cudaMallocFromPoolAsync(p, bytes, pool, s);
+  if (e == cudaErrorMemoryAllocation) {
+    // Freed blocks the pool keeps may be what is missing: once the stream has
+    // passed its pending frees, give them back to the device and try once more.
+    cudaGetLastError();
+    if (cudaStreamSynchronize(s) == cudaSuccess) {
+      cudaMemPoolTrimTo(pool, 0);
+      e = cudaMallocFromPoolAsync(p, bytes, pool, s);
+    }
+  }
+  // a failed allocation leaves no error behind for the next CUDA call of the
+  // process (another library would otherwise report it as its own)
+  if (e != cudaSuccess) cudaGetLastError();
+  return e;
 }
 
 void pool_trim_all() {
@@ -923,6 +936,11 @@ void pool_trim_all() {
     if (g_pools[d]) cudaMemPoolTrimTo(g_pools[d], 0);
 }
 }  // namespace dg
+
+extern "C" int dg_release_memory(void) {
+  dg::pool_trim_all();
+  return 0;
+}
 
 extern "C" int dg_finalize(void) {
   dg::clear_graphs();

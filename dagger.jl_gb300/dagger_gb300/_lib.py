@@ -67,6 +67,7 @@ SIGNATURES = {
     "dg_version": (ctypes.c_char_p, []),
     "dg_last_error": (ctypes.c_char_p, []),
     "dg_finalize": (c_int, []),
+    "dg_release_memory": (c_int, []),
     "dg_kernel_launches": (ctypes.c_longlong, []),
     "dg_set_device": (c_int, [c_int]),
     "dg_device_alloc": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),

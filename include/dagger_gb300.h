@@ -54,6 +54,10 @@ long long dg_kernel_launches(void);
 /* Frees library-owned workspaces and cached graphs of the current device.
  * Caller memory is never freed by the library. */
 int dg_finalize(void);
+/* Returns the device memory that the library's stream-ordered pool keeps
+ * for reuse (freed workspaces of earlier calls) to the device.  Blocks still
+ * in use are not touched; later calls allocate again as needed. */
+int dg_release_memory(void);
 
 /* Device memory and streams for hosts that do not link a CUDA binding (the
  * reference reaches the GPU through CUDA.jl; a backend on this library
