@@ -331,10 +331,15 @@ def _guarded(fn, *a):
     try:
         return fn(*a)
     except Exception as e:  # noqa: BLE001
+        import traceback
         import torch
-        torch.cuda.synchronize()
-        torch.cuda.empty_cache()
-        return {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+        where = traceback.format_exc().strip().splitlines()[-4:-1]
+        try:
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
+        except Exception:  # noqa: BLE001
+            pass
+        return {"error": f"{type(e).__name__}: {str(e)[:300]}", "where": where}
 
 
 def _fortran(t):
@@ -438,6 +443,7 @@ def run_ours(args):
     R = B - A @ X
     nA = A.abs().sum(dim=1).max()
     berr = (R.abs().amax(dim=0) / (nA * X.abs().amax(dim=0) + B.abs().amax(dim=0)))
+    berr_max = float(berr.max().item())
     U = torch.triu(W.collect())
     gen = torch.Generator(device=dev)
     gen.manual_seed(7)
@@ -590,7 +596,7 @@ def run_ours(args):
            "config": _config(args, n, world),
            "f64_engine": args.f64_engine, "dfma_engine": dfma,
            "solves_per_s": r * args.steps * world / t,
-           "accuracy": {"backward_error_max": float(berr.max().item()),
+           "accuracy": {"backward_error_max": berr_max,
                         "factor_residual_probe": fres},
            "roofline": roof, "gpu_launches": int(launches),
            "clocks": clk, "e2e": e2e, "cpu_baseline": cpu, "parity_vs_oracle": parity,
@@ -724,6 +730,7 @@ def bench_mixed_sweep(args, d, dev):
                     {"n": n, "cond": cond, "reason": "FP64-form copy of A does not fit in HBM "
                                                       "beside the sweep's other buffers"})
                 continue
+            d.lib().dg_release_memory()
             torch.cuda.empty_cache()
             # A = S S' with S = Q diag(sqrt(l)) in FP64, formed by syrk_dagger!
             # on the emulated FP64 engine: exactly symmetric and positive

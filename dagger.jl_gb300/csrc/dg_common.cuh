@@ -10,12 +10,17 @@
 
 #include "../../include/dagger_gb300.h"
 
+// A failed runtime call is recorded (dg_last_error) and, when the error does
+// not persist in the context (an allocation or an argument refused), cleared
+// from the runtime's per-thread error state, so that the next CUDA call of the
+// process, in this library or another, does not report it as its own.
 #define DG_CUDA_TRY(expr)                                                       \
   do {                                                                          \
     cudaError_t _e = (expr);                                                    \
     if (_e != cudaSuccess) {                                                    \
       dg_set_last_error(__FILE__, __LINE__, cudaGetErrorString(_e));            \
-      return DG_ERR_CUDA;                                                       \
+      cudaGetLastError();                                                       \
+      return _e == cudaErrorMemoryAllocation ? DG_ERR_NOMEM : DG_ERR_CUDA;      \
     }                                                                           \
   } while (0)
 
