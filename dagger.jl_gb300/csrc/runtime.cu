@@ -743,7 +743,21 @@ static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t o
     // kernel nodes keep the priority of the stream they were captured from
     e = cudaGraphInstantiateWithFlags(&entry.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
-    DG_CUDA_TRY(e);
+    if (e != cudaSuccess) {
+      // A region too large for an executable graph (its nodes' memory) runs
+      // on the same streams and events without one: the same tasks, order
+      // and results, with the host issuing every launch.
+      cudaGetLastError();
+      cudaFree(entry.info);
+      int *info = nullptr;
+      rc = device_state().scratch_int(&info);
+      if (rc) return rc;
+      std::vector<cudaEvent_t> ev2;
+      rc = issue(*r, pl, info, origin, serial, ev2);
+      for (auto x : ev2) cudaEventDestroy(x);
+      if (rc) return rc;
+      return sync ? read_info(info, origin) : 0;
+    }
     std::lock_guard<std::mutex> g(g_graph_mu);
     if (g_graphs.size() >= kMaxGraphs) {
       auto victim = g_graphs.begin();
