@@ -7,6 +7,11 @@ a profiler can capture exactly that kernel (ncu -k regex:<name> -c N).
     python -m dagger_gb300.profile_kernels batched    [--count 2000]
     python -m dagger_gb300.profile_kernels oz_gemm    [--m 8192] [--k 1024]
     python -m dagger_gb300.profile_kernels lu_panel   [--m 32768] [--k 1024]
+    python -m dagger_gb300.profile_kernels potrf_f64  [--nb 1024]
+    python -m dagger_gb300.profile_kernels herm       [--m 8192] [--nb 1024]
+    python -m dagger_gb300.profile_kernels diag       [--nb 1024]
+    python -m dagger_gb300.profile_kernels tc6        [--m 8192] [--k 1024]
+    python -m dagger_gb300.profile_kernels reblock    [--m 8192]
 
 gemm_f64   the FP64 trailing-update tile GEMM of the plain path,
            C(nb x nb) -= A' B with nb x nb tiles (2 nb^3 flops per launch)
@@ -21,6 +26,16 @@ lu_panel   the pivoted panel factorization of the tiled LU (dg_getrf) on an
            m x k column-major matrix (uniform [0, 1), seed 5) with the emulated
            engine: 32-column leaf launches and the recursion's emulated
            updates; the matrix is restored before every call
+potrf_f64  the FP64 factorization of one nb x nb diagonal tile (dg_potrf: 64 x 64
+           potrf_base_kernel leaves, trsm_cols_kernel / trsm_base_kernel and
+           the recursion's FP64 GEMMs)
+herm       ishermitian on an m x m tile grid (herm_pair_kernel, one pass over A)
+diag       the mixed form's FP32 factor + inverse of one nb x nb block
+           (diag_chol_inv_kernel, one cooperative launch)
+tc6        the FP32-accurate tensor-core product C(m x 64) = A'B, K = k, of the
+           mixed form's solves (split3_kernel, tc_gemm_kernel<128, 6>)
+reblock    copyto! between Blocks(1024, 1024) and Blocks(1000, 1000) of an m x m
+           matrix (reblock_kernel; 16 bytes per element)
 Each prints the per-launch time measured with CUDA events.
 """
 from __future__ import annotations
@@ -48,7 +63,7 @@ def _time(fn, reps):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched", "oz_gemm",
-                                       "lu_panel"])
+                                       "lu_panel", "potrf_f64", "herm", "diag", "tc6", "reblock"])
     ap.add_argument("--nb", type=int, default=1024)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--k", type=int, default=1024)
@@ -115,6 +130,57 @@ def main(argv=None):
         ms = _time(lambda: L.dg_trsm(b'L', b'U', b'T', b'N', nb, nb, 1.0, T.data_ptr(), nb,
                                      B.data_ptr(), nb, s), a.reps)
         print(f"trsm_f64 {nb}^2 x {nb}: {ms * 1e3:.1f} us/call, {nb ** 3 / ms / 1e9:.3f} TFLOP/s")
+    elif a.kernel == "potrf_f64":
+        nb = a.nb
+        r = torch.rand(nb, nb, dtype=torch.float64, device=dev)
+        S = r @ r.T / nb
+        S.diagonal().add_(1.0)
+        T = S.clone()
+        import ctypes
+        info = ctypes.c_int(0)
+
+        def call():
+            T.copy_(S)
+            L.dg_potrf(b'U', nb, T.data_ptr(), nb, ctypes.byref(info), s)
+        ms = _time(call, a.reps)
+        print(f"potrf_f64 {nb}: {ms * 1e3:.1f} us/call (info {info.value})")
+    elif a.kernel == "herm":
+        from .darray import Blocks, DArray
+        r = torch.rand(a.m, a.m, dtype=torch.float64, device=dev)
+        D = DArray.from_array(r + r.T, Blocks(a.nb, a.nb))
+        ms = _time(lambda: L.dg_ishermitian_tiled(a.m, a.nb, D.tile_ptrs(), s), a.reps)
+        print(f"herm {a.m}: {ms * 1e3:.1f} us/call, {8.0 * a.m * a.m / ms / 1e6:.0f} GB/s")
+    elif a.kernel == "diag":
+        nb = a.nb
+        r = torch.rand(nb, nb, device=dev)
+        S = r @ r.T / nb
+        S.diagonal().add_(1.0)
+        M, V = S.clone(), torch.empty_like(S)
+        import ctypes
+        info = ctypes.c_int(0)
+
+        def call():
+            M.copy_(S)
+            L.dg_potrf_inv_f32(nb, M.data_ptr(), nb, V.data_ptr(), nb, ctypes.byref(info), s)
+        ms = _time(call, a.reps)
+        print(f"diag {nb}: {ms * 1e3:.1f} us/call (info {info.value})")
+    elif a.kernel == "tc6":
+        m, k, r = a.m, a.k, 64
+        A = torch.randn(m, k, device=dev)
+        B = torch.randn(r, k, device=dev)
+        C = torch.zeros(r, m, device=dev)
+        ms = _time(lambda: L.dg_gemm_f32_tc_tn(m, r, k, -1.0, A.data_ptr(), k, B.data_ptr(), k,
+                                               1.0, C.data_ptr(), m, s), a.reps)
+        print(f"tc6 m={m} n={r} k={k}: {ms * 1e3:.1f} us/call, "
+              f"{6 * 2.0 * m * r * k / ms / 1e9:.1f} BF16 TFLOP/s")
+    elif a.kernel == "reblock":
+        from .darray import Blocks, DArray
+        from .linalg import copy_reblock
+        X = torch.randn(a.m, a.m, dtype=torch.float64, device=dev)
+        S1 = DArray.from_array(X, Blocks(1024, 1024))
+        S2 = DArray((a.m, a.m), Blocks(1000, 1000), device=dev)
+        ms = _time(lambda: copy_reblock(S1, S2), a.reps)
+        print(f"reblock {a.m}: {ms * 1e3:.1f} us/call, {16.0 * a.m * a.m / ms / 1e6:.0f} GB/s")
     else:
         from .autotune import sample_batch
         from .batched import PackedBatch, batched_solve_packed, flops
