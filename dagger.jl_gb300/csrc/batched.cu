@@ -26,6 +26,8 @@
 // A pivot that is not positive records info for that system and the CTA
 // moves on; no wait in this kernel depends on another CTA.
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <vector>
 
 #include "dg_common.cuh"
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(NT) batched_kernel(BatchParams p) {
 // The kernel's dynamic shared memory (solution, residual and correction
 // vectors) exceeds the 48 KiB default; the limit is raised once per device.
 static int set_batched_smem() {
-  static bool done[64] = {false};
+  static std::atomic<bool> done[64];  // zero-initialised: false
   int dev = 0;
   DG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev >= 0 && dev < 64 && done[dev]) return 0;
@@ -497,8 +499,9 @@ extern "C" int dg_batched_potrs(int count, const int *n, const int *nrhs, double
 // stages its descriptors from host memory and waits for the launch, so it
 // cannot be made while its stream is being captured.  Every call shares the
 // array and it keeps the previous call's contents, so the ticket counters and
-// error words are cleared on each call; calls that overlap on the GPU
-// (concurrent streams or host threads) race on it.
+// error words are cleared on each call, and calls take turns on a lock that
+// each holds until its launch has finished (host threads on different
+// streams would otherwise overlap on the array).
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB
@@ -511,6 +514,8 @@ thread_local int t_idx[kNoAllocMaxSystems];
 thread_local int t_info[2 * kNoAllocMaxSystems];
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+std::mutex g_noalloc_mu;  // one call at a time owns the array
 
 // The array's device address on the current device, looked up on each call.
 int noalloc_scratch(void **out) {
@@ -549,6 +554,7 @@ extern "C" int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs
                       "batch exceeds the 64 MiB scratch of dg_batched_potrs_noalloc");
     return DG_ERR_NOMEM;
   }
+  std::lock_guard<std::mutex> turn(g_noalloc_mu);
   void *base = nullptr;
   DG_TRY(noalloc_scratch(&base));
   unsigned char *sc = (unsigned char *)base;

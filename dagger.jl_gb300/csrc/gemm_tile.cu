@@ -19,6 +19,8 @@
 //
 // SYRK uses the same kernels with a triangle mask: CTA tiles wholly outside
 // the requested triangle exit at once and stores are limited to the triangle.
+#include <atomic>
+
 #include "dg_common.cuh"
 
 namespace dg {
@@ -44,7 +46,7 @@ struct GemmArgs {
   const void *const *tptr;
 };
 
-int g_engine = 0;
+std::atomic<int> g_engine{0};  // process-wide setting, read by every call
 
 template <typename T>
 __device__ __forceinline__ T load_a(const GemmArgs &g, int gi, int gp) {

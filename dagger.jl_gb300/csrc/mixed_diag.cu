@@ -35,6 +35,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "dg_common.cuh"
 #include "runtime.h"
@@ -533,7 +534,7 @@ int diag_chol_inv_f32(float *D, long long ld, int n, float *V, long long ldv, vo
   // CTA 0 runs the chain; enough worker groups for the first step's tiles
   int G = std::min(kDiagMaxGrid, std::max(2, 1 + (nblk * (nblk + 1) / 2 + NG - 1) / NG));
   G = std::min(G, dg_num_sms());
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];  // zero-initialised: false
   int dev = 0;
   DG_CUDA_TRY(cudaGetDevice(&dev));
   if (!attr_set[dev & 63]) {

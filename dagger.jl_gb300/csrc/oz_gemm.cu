@@ -55,6 +55,8 @@
 #include <cuda_bf16.h>
 #include <limits.h>
 
+#include <atomic>
+
 #include "dg_common.cuh"
 #include "runtime.h"
 #include "tc_ptx.cuh"
@@ -725,7 +727,7 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   p.dmode = dscale ? dmode : 0;
   p.guard = 11;
   for (long long kk = 1024; kk < k; kk *= 2) p.guard--;
-  static bool attr[64] = {false};
+  static std::atomic<bool> attr[64];  // zero-initialised: false
   int dev = 0;
   cudaGetDevice(&dev);
   if (!attr[dev & 63]) {
@@ -744,11 +746,8 @@ int oz_gemm(int m, int n, int k, double alpha, const void *a_slices, long long l
   p.blocks = (int)blocks;
   int per = blocks_per_cta;
   if (per <= 0) {  // one wave: ceil(blocks / SMs) blocks per CTA
-    static int sms[64] = {0};
-    if (!sms[dev & 63]) {
-      DG_CUDA_TRY(cudaDeviceGetAttribute(&sms[dev & 63], cudaDevAttrMultiProcessorCount, dev));
-    }
-    per = (int)((blocks + sms[dev & 63] - 1) / sms[dev & 63]);
+    const int sms = dg_num_sms();
+    per = (int)((blocks + sms - 1) / sms);
   }
   const long long ctas = (blocks + per - 1) / per;
   oz_gemm_kernel<<<(unsigned)ctas, OZ_THREADS, OZ_SMEM, s>>>(p);

@@ -42,16 +42,17 @@ void dg_set_last_error(const char *file, int line, const char *msg) {
 }
 
 int dg_num_sms() {
-  static int cache[64] = {0};
+  static std::atomic<int> cache[64];  // zero-initialised: not looked up yet
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
-  if (!cache[dev]) {
-    int v = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (!v) {
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    cache[dev] = v > 0 ? v : 1;
+    v = v > 0 ? v : 1;
+    cache[dev].store(v, std::memory_order_relaxed);
   }
-  return cache[dev];
+  return v;
 }
 
 namespace dg {
@@ -104,27 +105,66 @@ int DeviceState::scratch_int(int **p) {
   return 0;
 }
 
-// Grow-only workspace for the slice slots; growing it invalidates the cached
-// graphs that captured the old address.
-int DeviceState::oz_workspace(size_t bytes, void **p) {
+Workspace *DeviceState::workspace_of(cudaStream_t s) {
   std::lock_guard<std::mutex> g(mu);
-  if (oz_ring_bytes < bytes) {
-    if (oz_ring) {
-      cudaDeviceSynchronize();
-      cudaFree(oz_ring);
-      oz_ring = nullptr;
-      oz_ring_bytes = 0;
-      clear_graphs();
+  auto &w = workspaces[s];
+  if (!w) w.reset(new Workspace());
+  return w.get();
+}
+
+void DeviceState::release_idle_workspaces() {
+  std::lock_guard<std::mutex> g(mu);
+  for (auto &kv : workspaces) {
+    Workspace *w = kv.second.get();
+    if (!w->p || !w->use.try_lock()) continue;  // in use: keep it
+    if (!w->recorded || cudaEventSynchronize(w->done) == cudaSuccess) {
+      cudaFree(w->p);
+      w->p = nullptr;
+      w->bytes = 0;
     }
-    if (cudaMalloc(&oz_ring, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      dg_set_last_error(__FILE__, __LINE__, "cudaMalloc of the emulated-FP64 slice slots failed");
-      return DG_ERR_NOMEM;
-    }
-    oz_ring_bytes = bytes;
+    cudaGetLastError();
+    w->use.unlock();
   }
-  *p = oz_ring;
+}
+
+int WsLease::acquire(size_t bytes, cudaStream_t s, void **p) {
+  *p = nullptr;
+  Workspace *w = device_state().workspace_of(s);
+  w->use.lock();
+  auto fail = [&](const char *what) {
+    cudaGetLastError();
+    dg_set_last_error(__FILE__, __LINE__, what);
+    w->use.unlock();
+    return DG_ERR_NOMEM;
+  };
+  if (!w->done && cudaEventCreateWithFlags(&w->done, cudaEventDisableTiming) != cudaSuccess)
+    return fail("cannot create the workspace event");
+  // the work the previous lease of this stream handle queued comes first
+  if (w->recorded && cudaStreamWaitEvent(s, w->done, 0) != cudaSuccess)
+    return fail("cannot order the stream after the workspace's last use");
+  if (w->bytes < bytes) {
+    if (w->p) {
+      cudaFreeAsync(w->p, s);
+      w->p = nullptr;
+      w->bytes = 0;
+    }
+    if (pool_malloc_async(&w->p, bytes, s) != cudaSuccess) {
+      w->p = nullptr;
+      return fail("allocation of the emulated-FP64 / LU workspace failed");
+    }
+    w->bytes = bytes;
+  }
+  w_ = w;
+  s_ = s;
+  *p = w->p;
   return 0;
+}
+
+WsLease::~WsLease() {
+  if (!w_) return;
+  w_->recorded = cudaEventRecord(w_->done, s_) == cudaSuccess;
+  if (!w_->recorded) cudaGetLastError();
+  w_->use.unlock();
 }
 
 // A slot: the 8 BF16 slices of up to `cap` vectors of padded length ldk,
@@ -585,10 +625,25 @@ void mark_transfer(dg_region *r) {
   hash_bytes(r->hash, &kTransferLevel, sizeof kTransferLevel);
 }
 
-struct GraphEntry {
+// An executable graph and its info word, shared by the cache and every
+// launch being issued: an eviction or a clear on one thread never destroys a
+// graph that another thread is about to launch (the last holder destroys it;
+// a graph still running on the device finishes first).
+struct GraphObj {
   cudaGraphExec_t exec = nullptr;
   int *info = nullptr;
   long long nodes = 0;  // kernel launches captured in the graph
+  GraphObj() = default;
+  GraphObj(const GraphObj &) = delete;
+  GraphObj &operator=(const GraphObj &) = delete;
+  ~GraphObj() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (info) cudaFree(info);
+  }
+};
+
+struct GraphEntry {
+  std::shared_ptr<GraphObj> g;
   uint64_t last_used = 0;
 };
 
@@ -712,43 +767,42 @@ static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t o
   int dev = 0;
   cudaGetDevice(&dev);
   uint64_t key = r->hash ^ ((uint64_t)serial << 63) ^ ((uint64_t)stream_pool_size << 40);
-  GraphEntry entry;
-  bool found = false;
+  std::shared_ptr<GraphObj> entry;
   {
     std::lock_guard<std::mutex> g(g_graph_mu);
     auto it = g_graphs.find({dev, key});
     if (it != g_graphs.end()) {
       it->second.last_used = ++g_graph_clock;
-      entry = it->second;
-      found = true;
+      entry = it->second.g;
     }
   }
-  if (!found) {
-    DG_CUDA_TRY(cudaMalloc((void **)&entry.info, 256));
-    DG_CUDA_TRY(cudaMemset(entry.info, 0, 256));
+  if (!entry) {
+    entry = std::make_shared<GraphObj>();
+    DG_CUDA_TRY(cudaMalloc((void **)&entry->info, 256));
+    DG_CUDA_TRY(cudaMemset(entry->info, 0, 256));
     cudaGraph_t graph;
     DG_CUDA_TRY(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal));
     const long long before = launches();
-    int rc = issue(*r, pl, entry.info, origin, serial, events);
-    entry.nodes = launches() - before;
-    count_launches(-entry.nodes);  // captured, not executed
+    int rc = issue(*r, pl, entry->info, origin, serial, events);
+    entry->nodes = launches() - before;
+    count_launches(-entry->nodes);  // captured, not executed
     cudaError_t e = cudaStreamEndCapture(origin, &graph);
     cleanup();
     if (rc) {
       if (e == cudaSuccess) cudaGraphDestroy(graph);
-      cudaFree(entry.info);
       return rc;
     }
     DG_CUDA_TRY(e);
     // kernel nodes keep the priority of the stream they were captured from
-    e = cudaGraphInstantiateWithFlags(&entry.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+    e = cudaGraphInstantiateWithFlags(&entry->exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       // A region too large for an executable graph (its nodes' memory) runs
       // on the same streams and events without one: the same tasks, order
       // and results, with the host issuing every launch.
       cudaGetLastError();
-      cudaFree(entry.info);
+      entry->exec = nullptr;
+      entry.reset();
       int *info = nullptr;
       rc = device_state().scratch_int(&info);
       if (rc) return rc;
@@ -758,36 +812,40 @@ static int region_run_on(dg_region *r, int use_graph, int serial, cudaStream_t o
       if (rc) return rc;
       return sync ? read_info(info, origin) : 0;
     }
-    std::lock_guard<std::mutex> g(g_graph_mu);
-    if (g_graphs.size() >= kMaxGraphs) {
-      auto victim = g_graphs.begin();
-      for (auto it = g_graphs.begin(); it != g_graphs.end(); ++it)
-        if (it->second.last_used < victim->second.last_used) victim = it;
-      cudaGraphExecDestroy(victim->second.exec);
-      cudaFree(victim->second.info);
-      g_graphs.erase(victim);
+    std::shared_ptr<GraphObj> evicted;  // destroyed after the lock is released
+    {
+      std::lock_guard<std::mutex> g(g_graph_mu);
+      if (g_graphs.size() >= kMaxGraphs) {
+        auto victim = g_graphs.begin();
+        for (auto it = g_graphs.begin(); it != g_graphs.end(); ++it)
+          if (it->second.last_used < victim->second.last_used) victim = it;
+        evicted = std::move(victim->second.g);
+        g_graphs.erase(victim);
+      }
+      GraphEntry ge;
+      ge.g = entry;
+      ge.last_used = ++g_graph_clock;
+      g_graphs[{dev, key}] = ge;
     }
-    entry.last_used = ++g_graph_clock;
-    g_graphs[{dev, key}] = entry;
   }
-  DG_CUDA_TRY(cudaGraphLaunch(entry.exec, origin));
-  count_launches(entry.nodes);
-  return sync ? read_info(entry.info, origin) : 0;
+  DG_CUDA_TRY(cudaGraphLaunch(entry->exec, origin));
+  count_launches(entry->nodes);
+  return sync ? read_info(entry->info, origin) : 0;
 }
 
 // Launches the cached graph of `key` on origin (a legacy stream bridged to
 // the private capture stream as region_run does); false when it is not cached
-// (never built, evicted, or cleared when the workspace grew).
+// (never built, evicted or cleared).
 static bool launch_cached(uint64_t key, cudaStream_t origin, bool sync, int *rc) {
   int dev = 0;
   cudaGetDevice(&dev);
-  GraphEntry entry;
+  std::shared_ptr<GraphObj> entry;
   {
     std::lock_guard<std::mutex> g(g_graph_mu);
     auto it = g_graphs.find({dev, key});
     if (it == g_graphs.end()) return false;
     it->second.last_used = ++g_graph_clock;
-    entry = it->second;
+    entry = it->second.g;
   }
   const bool legacy = origin == nullptr || origin == cudaStreamLegacy || origin == cudaStreamPerThread;
   cudaStream_t s = origin;
@@ -804,12 +862,12 @@ static bool launch_cached(uint64_t key, cudaStream_t origin, bool sync, int *rc)
     cudaStreamWaitEvent(s, in, 0);
   }
   *rc = 0;
-  if (cudaGraphLaunch(entry.exec, s) != cudaSuccess) {
+  if (cudaGraphLaunch(entry->exec, s) != cudaSuccess) {
     cudaGetLastError();
     dg_set_last_error(__FILE__, __LINE__, "cudaGraphLaunch failed");
     *rc = DG_ERR_CUDA;
   } else {
-    count_launches(entry.nodes);
+    count_launches(entry->nodes);
   }
   if (legacy) {
     cudaEventRecord(out, s);
@@ -817,7 +875,7 @@ static bool launch_cached(uint64_t key, cudaStream_t origin, bool sync, int *rc)
     cudaEventDestroy(in);
     cudaEventDestroy(out);
   }
-  if (*rc == 0 && sync) *rc = read_info(entry.info, s);
+  if (*rc == 0 && sync) *rc = read_info(entry->info, s);
   return true;
 }
 
@@ -869,13 +927,13 @@ uint64_t call_hash(int fn, const void *args, size_t bytes, const void *const *pt
 }
 
 void clear_graphs() {
+  std::vector<std::shared_ptr<GraphObj>> dropped;  // destroyed after the lock is released
   std::lock_guard<std::mutex> g(g_graph_mu);
   int dev = 0;
   cudaGetDevice(&dev);
   for (auto it = g_graphs.begin(); it != g_graphs.end();) {
     if (it->first.first == dev) {
-      cudaGraphExecDestroy(it->second.exec);
-      cudaFree(it->second.info);
+      dropped.push_back(std::move(it->second.g));
       it = g_graphs.erase(it);
     } else {
       ++it;
@@ -952,12 +1010,14 @@ void pool_trim_all() {
 }  // namespace dg
 
 extern "C" int dg_release_memory(void) {
+  dg::device_state().release_idle_workspaces();
   dg::pool_trim_all();
   return 0;
 }
 
 extern "C" int dg_finalize(void) {
   dg::clear_graphs();
+  dg::device_state().release_idle_workspaces();
   dg::pool_trim_all();
   return 0;
 }
@@ -1963,9 +2023,10 @@ extern "C" int dg_gemm_tiled(char transa, char transb, int m, int n, int k, int 
   DG_CHECK_ARG(atiles != nullptr, 8);
   DG_CHECK_ARG(btiles != nullptr, 9);
   const char ta = is_one_of(transa, "Nn") ? 'N' : 'T', tb = is_one_of(transb, "Nn") ? 'N' : 'T';
+  dg::WsLease lease;
   void *ring = nullptr;
   if (dg::get_f64_engine() == 2 && nb <= 1024)
-    DG_TRY(dg::device_state().oz_workspace(dg::mul_ring_bytes_for(m, n, nb), &ring));
+    DG_TRY(lease.acquire(dg::mul_ring_bytes_for(m, n, nb), (cudaStream_t)stream, &ring));
   const size_t mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb, kt = (k + nb - 1) / nb;
   struct { int64_t m, n, k, nb; double alpha, beta; const void *ring; char ta, tb; } a;
   memset(&a, 0, sizeof a);
@@ -2004,9 +2065,10 @@ extern "C" int dg_syrk_tiled(char trans, int n, int k, int nb, double alpha,
         (cudaStream_t)stream, true);
   }
   DG_CHECK_ARG(atiles != nullptr, 6);
+  dg::WsLease lease;
   void *ring = nullptr;
   if (dg::get_f64_engine() == 2 && nb <= 1024)
-    DG_TRY(dg::device_state().oz_workspace(dg::mul_ring_bytes_for(n, 0, nb), &ring));
+    DG_TRY(lease.acquire(dg::mul_ring_bytes_for(n, 0, nb), (cudaStream_t)stream, &ring));
   struct { int64_t n, k, nb; double alpha, beta; const void *ring; char tr; } a;
   memset(&a, 0, sizeof a);
   a.n = n; a.k = k; a.nb = nb; a.alpha = alpha; a.beta = beta; a.ring = ring; a.tr = tr;
@@ -2026,9 +2088,10 @@ extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles,
   DG_CHECK_ARG(nb > 0, 3);
   DG_CHECK_ARG(tiles != nullptr || n == 0, 4);
   if (n == 0) return 0;
+  dg::WsLease lease;
   void *ring = nullptr;
   if (dg::get_f64_engine() == 2 && nb <= 1024)
-    DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+    DG_TRY(lease.acquire(dg::oz_ring_bytes_for(n, nb), (cudaStream_t)stream, &ring));
   return dg::region_run_cached(
       call_key(1, uplo, n, nb, 0, 0, ring, nullptr, nullptr, tiles, nullptr),
       [&](dg_region *r) { dg::build_cholesky_region(r, uplo, n, nb, tiles, ring); },
@@ -2044,8 +2107,9 @@ extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *t
   DG_CHECK_ARG(winv != nullptr || n == 0, 5);
   if (dg::get_f64_engine() != 2 || nb > 1024) return DG_ERR_UNSUPPORTED;
   if (n == 0) return 0;
+  dg::WsLease lease;
   void *ring = nullptr;
-  DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+  DG_TRY(lease.acquire(dg::oz_ring_bytes_for(n, nb), (cudaStream_t)stream, &ring));
   return dg::region_run_cached(
       call_key(2, uplo, n, nb, 0, 0, ring, winv, nullptr, tiles, nullptr),
       [&](dg_region *r) { dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, winv); },
@@ -2067,8 +2131,9 @@ extern "C" int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *ho
   DG_CHECK_ARG(tiles != nullptr, 6);
   const bool emulated = dg::get_f64_engine() == 2 && nb <= 1024;
   if (winv && !emulated) return DG_ERR_UNSUPPORTED;
+  dg::WsLease lease;
   void *ring = nullptr;
-  if (emulated) DG_TRY(dg::device_state().oz_workspace(dg::oz_ring_bytes_for(n, nb), &ring));
+  if (emulated) DG_TRY(lease.acquire(dg::oz_ring_bytes_for(n, nb), (cudaStream_t)stream, &ring));
   return dg::region_run_cached(
       call_key(3, uplo, n, nb, 0, ldh, ring, winv, host, tiles, nullptr),
       [&](dg_region *r) {
@@ -2091,8 +2156,10 @@ extern "C" int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *co
   DG_CHECK_ARG(winv != nullptr, 5);
   DG_CHECK_ARG(btiles != nullptr, 7);
   const bool up = (uplo == 'U' || uplo == 'u');
+  dg::WsLease lease;
   void *ring = nullptr;
-  DG_TRY(dg::device_state().oz_workspace(dg::oz_solve_ring_bytes_for(n, nb, nrhs, true), &ring));
+  DG_TRY(lease.acquire(dg::oz_solve_ring_bytes_for(n, nb, nrhs, true), (cudaStream_t)stream,
+                       &ring));
   const int mt = (n + nb - 1) / nb;
   return dg::region_run_cached(
       call_key(4, uplo, n, nb, nrhs, 0, ring, winv, nullptr, tiles, btiles),
@@ -2115,9 +2182,10 @@ extern "C" int dg_cholesky_solve_tiled(char uplo, int n, int nb, double *const *
   DG_CHECK_ARG(tiles != nullptr, 4);
   DG_CHECK_ARG(btiles != nullptr, 6);
   const bool up = (uplo == 'U' || uplo == 'u');
+  dg::WsLease lease;
   void *ring = nullptr;
   if (dg::get_f64_engine() == 2 && nb <= 1024)
-    DG_TRY(dg::device_state().oz_workspace(dg::oz_solve_ring_bytes_for(n, nb, nrhs), &ring));
+    DG_TRY(lease.acquire(dg::oz_solve_ring_bytes_for(n, nb, nrhs), (cudaStream_t)stream, &ring));
   const int mt = (n + nb - 1) / nb;
   return dg::region_run_cached(
       call_key(5, uplo, n, nb, nrhs, 0, ring, nullptr, nullptr, tiles, btiles),
@@ -2184,8 +2252,9 @@ extern "C" int dg_getrf(int m, int n, double *A, int lda, long long *ipiv, int *
   const int h = n / 2 + 32;
   const size_t ozp = emulated ? r256(dg::oz_scratch_bytes(m, h, h, false)) : 0;
   dg::lu_prepare();
+  dg::WsLease lease;
   void *ws = nullptr;
-  DG_TRY(dg::device_state().oz_workspace(256 + leaf + lpiv + ozp, &ws));
+  DG_TRY(lease.acquire(256 + leaf + lpiv + ozp, (cudaStream_t)stream, &ws));
   char *w = (char *)ws;
   cudaStream_t s = (cudaStream_t)stream;
   DG_TRY(lu_words_reset(ws, s));
@@ -2211,8 +2280,9 @@ extern "C" int dg_lu_tiled(int m, int n, int nb, double *const *tiles, int pivot
   const bool emulated = dg::get_f64_engine() == 2;
   const dg::LuLayout L = dg::lu_layout(m, n, nb, pivot != 0, emulated);
   dg::lu_prepare();
+  dg::WsLease lease;
   void *ws = nullptr;
-  DG_TRY(dg::device_state().oz_workspace(L.total, &ws));
+  DG_TRY(lease.acquire(L.total, (cudaStream_t)stream, &ws));
   cudaStream_t s = (cudaStream_t)stream;
   DG_TRY(lu_words_reset(ws, s));
   const int rc = dg::region_run_cached(
@@ -2237,8 +2307,9 @@ extern "C" int dg_lu_solve_tiled(int n, int nb, double *const *tiles, const long
   if (mt > dg::kMaxTileRows) return DG_ERR_UNSUPPORTED;
   const bool emulated = dg::get_f64_engine() == 2 && nb <= 1024;
   dg::lu_prepare();
+  dg::WsLease lease;
   void *ws = nullptr;
-  DG_TRY(dg::device_state().oz_workspace(dg::lu_solve_bytes(n, nb, nrhs, emulated), &ws));
+  DG_TRY(lease.acquire(dg::lu_solve_bytes(n, nb, nrhs, emulated), (cudaStream_t)stream, &ws));
   return dg::region_run_cached(
       lu_key(31, n, n, nb, nrhs, 1, emulated, ws, ipiv, tiles, (size_t)mt * mt, btiles,
              (size_t)mt * bnt),

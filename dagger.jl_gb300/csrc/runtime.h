@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
+#include <memory>
 #include <mutex>
 #include <functional>
 #include <vector>
@@ -71,6 +73,18 @@ constexpr int kOzBlocksPerCta = 6;
 size_t oz_slot_bytes(long long ldk, long long cap);
 size_t oz_ring_bytes_for(int n, int nb);
 
+// The emulated FP64 engine's and the LU's workspace (slice slots, leaf
+// scratch, pivot words) of one stream.  Calls issued on different streams
+// use different workspaces and run concurrently; calls on the same stream
+// handle take turns through a lease (below).
+struct Workspace {
+  std::mutex use;               // held by the lease from acquisition to release
+  void *p = nullptr;            // stream-ordered allocation of the library pool
+  size_t bytes = 0;
+  cudaEvent_t done = nullptr;   // recorded on the stream when a lease ends
+  bool recorded = false;
+};
+
 // Library-owned per-device state.
 struct DeviceState {
   static constexpr int kInfoWords = 4096;
@@ -78,10 +92,34 @@ struct DeviceState {
   int *info_words = nullptr;  // ring of device ints for synchronous calls
   unsigned next_info = 0;
   int scratch_int(int **p);
-  void *oz_ring = nullptr;     // slice slots of the emulated FP64 engine
-  size_t oz_ring_bytes = 0;
-  int oz_workspace(size_t bytes, void **p);
+  std::map<cudaStream_t, std::unique_ptr<Workspace>> workspaces;  // by stream handle
+  Workspace *workspace_of(cudaStream_t s);
+  // Frees the workspaces no lease holds, once the work queued with them is
+  // done (dg_release_memory).
+  void release_idle_workspaces();
   ~DeviceState();
+};
+
+// Exclusive use of the calling stream's workspace, grown to `bytes`, from
+// acquire() until the lease goes out of scope.  acquire() blocks while
+// another host thread holds a lease on the same stream handle, then makes the
+// stream wait for the work the previous lease queued; growth frees the old
+// block and allocates the new one in stream order (no device-wide
+// synchronisation, so calls on other streams keep running).  The release
+// records the workspace's event on the stream after everything the call
+// queued.  Graph and call caches key on the workspace address, so a graph
+// built for one stream's workspace is never launched with another's.
+class WsLease {
+ public:
+  WsLease() = default;
+  WsLease(const WsLease &) = delete;
+  WsLease &operator=(const WsLease &) = delete;
+  ~WsLease();
+  int acquire(size_t bytes, cudaStream_t s, void **p);
+
+ private:
+  Workspace *w_ = nullptr;
+  cudaStream_t s_ = nullptr;
 };
 
 DeviceState &device_state();

@@ -56,27 +56,36 @@ Base.unsafe_convert(::Type{Ptr{T}}, x::GB300Array{T}) where T = x.ptr
 Base.strides(x::GB300Array{T,2}) where T = (1, x.dims[1])
 Base.stride(x::GB300Array{T,2}, i::Int) where T = i == 1 ? 1 : x.dims[1]
 
+# One library stream per device, created on first use (Dagger's tasks may
+# ask for it from several threads at once, hence the lock).  A caller that
+# runs whole-region calls from concurrent tasks passes each task its own
+# stream (`new_stream`): the library gives every stream its own workspace,
+# so such calls run side by side.
 const STREAMS = Dict{Int,Ptr{Cvoid}}()
-function stream(device::Int)
-    get!(STREAMS, device) do
-        s = Ref{Ptr{Cvoid}}(C_NULL)
-        dgcheck(ccall((:dg_stream_create, libdg), Cint, (Ptr{Ptr{Cvoid}},), s))
-        s[]
+const STREAMS_LOCK = ReentrantLock()
+function new_stream()
+    s = Ref{Ptr{Cvoid}}(C_NULL)
+    dgcheck(ccall((:dg_stream_create, libdg), Cint, (Ptr{Ptr{Cvoid}},), s))
+    return s[]
+end
+function device_stream(device::Int)
+    lock(STREAMS_LOCK) do
+        get!(new_stream, STREAMS, device)
     end
 end
-synchronize(device::Int) = dgcheck(ccall((:dg_stream_synchronize, libdg), Cint, (Ptr{Cvoid},), stream(device)))
+synchronize(device::Int) = dgcheck(ccall((:dg_stream_synchronize, libdg), Cint, (Ptr{Cvoid},), device_stream(device)))
 
 function GB300Array(x::Array{T,N}; device::Int=0) where {T,N}
     y = GB300Array{T,N}(undef, size(x); device)
     dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
-                  y.ptr, pointer(x), sizeof(x), 0, stream(device)))
+                  y.ptr, pointer(x), sizeof(x), 0, device_stream(device)))
     synchronize(device)
     return y
 end
 function Base.Array(x::GB300Array{T,N}) where {T,N}
     y = Array{T,N}(undef, x.dims)
     dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
-                  pointer(y), x.ptr, sizeof(y), 1, stream(x.device)))
+                  pointer(y), x.ptr, sizeof(y), 1, device_stream(x.device)))
     synchronize(x.device)
     return y
 end
@@ -111,12 +120,12 @@ Dagger.unsafe_free!(x::GB300Array) = (finalize(x); nothing)
 # moves between host and device (ext/CUDAExt.jl:131-154)
 function Dagger.move!(::GB300MemorySpace, ::Dagger.CPURAMMemorySpace, to::GB300Array{T}, from::Array{T}) where T
     dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
-                  to.ptr, pointer(from), sizeof(from), 0, stream(to.device)))
+                  to.ptr, pointer(from), sizeof(from), 0, device_stream(to.device)))
     return
 end
 function Dagger.move!(::Dagger.CPURAMMemorySpace, ::GB300MemorySpace, to::Array{T}, from::GB300Array{T}) where T
     dgcheck(ccall((:dg_copy, libdg), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint, Ptr{Cvoid}),
-                  pointer(to), from.ptr, sizeof(to), 1, stream(from.device)))
+                  pointer(to), from.ptr, sizeof(to), 1, device_stream(from.device)))
     synchronize(from.device)
     return
 end
@@ -138,38 +147,38 @@ ld(A::GB300Array{T,2}) where T = max(1, size(A, 1))
 function gb300_potrf!(uplo::AbstractChar, A::GB300Array{Float64,2})
     info = Ref{Cint}(0)
     rc = ccall((:dg_potrf, libdg), Cint, (Cchar, Cint, Ptr{Float64}, Cint, Ptr{Cint}, Ptr{Cvoid}),
-               uplo, size(A, 1), A, ld(A), info, stream(A.device))
+               uplo, size(A, 1), A, ld(A), info, device_stream(A.device))
     dgcheck(rc)
     return A, Int(info[])
 end
 function gb300_trsm!(side, uplo, transa, diag, alpha::Float64, A::GB300Array{Float64,2}, B::GB300Array{Float64,2})
     dgcheck(ccall((:dg_trsm, libdg), Cint,
                   (Cchar, Cchar, Cchar, Cchar, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Ptr{Cvoid}),
-                  side, uplo, transa, diag, size(B, 1), size(B, 2), alpha, A, ld(A), B, ld(B), stream(B.device)))
+                  side, uplo, transa, diag, size(B, 1), size(B, 2), alpha, A, ld(A), B, ld(B), device_stream(B.device)))
     return B
 end
 function gb300_syrk!(uplo, trans, alpha::Float64, A::GB300Array{Float64,2}, beta::Float64, C::GB300Array{Float64,2})
     k = trans == 'N' ? size(A, 2) : size(A, 1)
     dgcheck(ccall((:dg_syrk, libdg), Cint,
                   (Cchar, Cchar, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Cvoid}),
-                  uplo, trans, size(C, 1), k, alpha, A, ld(A), beta, C, ld(C), stream(C.device)))
+                  uplo, trans, size(C, 1), k, alpha, A, ld(A), beta, C, ld(C), device_stream(C.device)))
     return C
 end
 function gb300_gemm!(ta, tb, alpha::Float64, A::GB300Array{Float64,2}, B::GB300Array{Float64,2}, beta::Float64, C::GB300Array{Float64,2})
     k = ta == 'N' ? size(A, 2) : size(A, 1)
     dgcheck(ccall((:dg_gemm, libdg), Cint,
                   (Cchar, Cchar, Cint, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Float64}, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Cvoid}),
-                  ta, tb, size(C, 1), size(C, 2), k, alpha, A, ld(A), B, ld(B), beta, C, ld(C), stream(C.device)))
+                  ta, tb, size(C, 1), size(C, 2), k, alpha, A, ld(A), B, ld(B), beta, C, ld(C), device_stream(C.device)))
     return C
 end
 function gb300_trsv!(uplo, trans, diag, A::GB300Array{Float64,2}, x::GB300Array{Float64,1})
     dgcheck(ccall((:dg_trsv, libdg), Cint, (Cchar, Cchar, Cchar, Cint, Ptr{Float64}, Cint, Ptr{Float64}, Ptr{Cvoid}),
-                  uplo, trans, diag, size(A, 1), A, ld(A), x, stream(x.device)))
+                  uplo, trans, diag, size(A, 1), A, ld(A), x, device_stream(x.device)))
     return x
 end
 function gb300_gemv!(trans, alpha::Float64, A::GB300Array{Float64,2}, x::GB300Array{Float64,1}, beta::Float64, y::GB300Array{Float64,1})
     dgcheck(ccall((:dg_gemv, libdg), Cint, (Cchar, Cint, Cint, Cdouble, Ptr{Float64}, Cint, Ptr{Float64}, Cdouble, Ptr{Float64}, Ptr{Cvoid}),
-                  trans, size(A, 1), size(A, 2), alpha, A, ld(A), x, beta, y, stream(y.device)))
+                  trans, size(A, 1), size(A, 2), alpha, A, ld(A), x, beta, y, device_stream(y.device)))
     return y
 end
 
@@ -184,6 +193,9 @@ Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.gemv!)) = gb300_gemv!
 # whole-region calls: one ccall per cholesky! / ldiv!
 # ---------------------------------------------------------------------------
 tile_pointers(A::DArray) = [pointer(fetch(c)::GB300Array{Float64,2}) for c in A.chunks]
+# the device holding a DArray's chunks, whose stream a whole-region call uses
+# unless the caller passes one
+device_of(A::DArray) = (fetch(first(A.chunks))::GB300Array).device
 
 """
     cholesky_gb300!(A::DArray{Float64,2}, uplo='U') -> Cholesky
@@ -193,12 +205,13 @@ library as one captured multi-stream CUDA graph.  All chunks must be
 GB300Arrays with Blocks(nb, nb) partitioning.  Throws PosDefException(info)
 like `potrf_checked!`.
 """
-function cholesky_gb300!(A::DArray{Float64,2}, uplo::Char='U')
+function cholesky_gb300!(A::DArray{Float64,2}, uplo::Char='U';
+                         stream::Ptr{Cvoid}=device_stream(device_of(A)))
     n = size(A, 1)
     nb = A.partitioning.blocksize[1]
     ptrs = tile_pointers(A)
     info = ccall((:dg_cholesky_tiled, libdg), Cint, (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
-                 uplo, n, nb, ptrs, C_NULL)
+                 uplo, n, nb, ptrs, stream)
     dgcheck(info)
     info > 0 && throw(PosDefException(Int(info)))
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0))
@@ -209,14 +222,15 @@ end
 
 ldiv! (src/array/linalg.jl:352-405) as one library call.
 """
-function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, B::DArray{Float64})
+function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, B::DArray{Float64};
+                     stream::Ptr{Cvoid}=device_stream(device_of(C.factors)))
     F = C.factors
     n = size(F, 1)
     nb = F.partitioning.blocksize[1]
     nrhs = ndims(B) == 1 ? 1 : size(B, 2)
     dgcheck(ccall((:dg_cholesky_solve_tiled, libdg), Cint,
                   (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
-                  C.uplo, n, nb, tile_pointers(F), nrhs, tile_pointers(B), C_NULL))
+                  C.uplo, n, nb, tile_pointers(F), nrhs, tile_pointers(B), stream))
     return B
 end
 
@@ -228,14 +242,15 @@ transposed inverses of the diagonal factor tiles the factorization forms for
 its panel products (winv: mt * nb * nb doubles on the device), so that
 ldiv_gb300!(C, winv, B) solves each diagonal block as one product.
 """
-function cholesky_gb300_winv!(A::DArray{Float64,2}, uplo::Char='U')
+function cholesky_gb300_winv!(A::DArray{Float64,2}, uplo::Char='U';
+                              stream::Ptr{Cvoid}=device_stream(device_of(A)))
     n = size(A, 1)
     nb = A.partitioning.blocksize[1]
     mt = cld(n, nb)
-    winv = GB300Array{Float64,1}(undef, (mt * nb * nb,))
+    winv = GB300Array{Float64,1}(undef, (mt * nb * nb,); device=device_of(A))
     info = ccall((:dg_cholesky_tiled_winv, libdg), Cint,
                  (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Cvoid}),
-                 uplo, n, nb, tile_pointers(A), pointer(winv), C_NULL)
+                 uplo, n, nb, tile_pointers(A), pointer(winv), stream)
     dgcheck(info)
     info > 0 && throw(PosDefException(Int(info)))
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0)), winv
@@ -251,7 +266,8 @@ dg_cholesky_tiled_host reads page-locked memory only, so H is copied into a
 buffer from dg_host_alloc for the call.  A receives the tiles and then the
 factor.
 """
-function cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo::Char='U')
+function cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo::Char='U';
+                              stream::Ptr{Cvoid}=device_stream(device_of(A)))
     n = size(A, 1)
     nb = A.partitioning.blocksize[1]
     buf = Ref{Ptr{Cvoid}}(C_NULL)
@@ -260,7 +276,7 @@ function cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo::Ch
         unsafe_copyto!(Ptr{Float64}(buf[]), pointer(H), length(H))
         ccall((:dg_cholesky_tiled_host, libdg), Cint,
               (Cchar, Cint, Cint, Ptr{Float64}, Clonglong, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Cvoid}),
-              uplo, n, nb, Ptr{Float64}(buf[]), stride(H, 2), tile_pointers(A), C_NULL, C_NULL)
+              uplo, n, nb, Ptr{Float64}(buf[]), stride(H, 2), tile_pointers(A), C_NULL, stream)
     finally
         ccall((:dg_host_free, libdg), Cint, (Ptr{Cvoid},), buf[])
     end
@@ -269,14 +285,15 @@ function cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo::Ch
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0))
 end
 
-function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, winv::GB300Array{Float64,1}, B::DArray{Float64})
+function ldiv_gb300!(C::Cholesky{Float64,<:DArray}, winv::GB300Array{Float64,1}, B::DArray{Float64};
+                     stream::Ptr{Cvoid}=device_stream(winv.device))
     F = C.factors
     n = size(F, 1)
     nb = F.partitioning.blocksize[1]
     nrhs = ndims(B) == 1 ? 1 : size(B, 2)
     dgcheck(ccall((:dg_cholesky_solve_tiled_winv, libdg), Cint,
                   (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Float64}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
-                  C.uplo, n, nb, tile_pointers(F), pointer(winv), nrhs, tile_pointers(B), C_NULL))
+                  C.uplo, n, nb, tile_pointers(F), pointer(winv), nrhs, tile_pointers(B), stream))
     return B
 end
 
@@ -289,7 +306,8 @@ exactly one transposed is syrk_dagger! + copytri!, anything else
 gemm_dagger!; each is one library graph (dg_syrk_tiled / dg_gemm_tiled).
 """
 function mul_gb300!(C::DArray{Float64,2}, A::DArray{Float64,2}, B::DArray{Float64,2},
-                    alpha::Real=1.0, beta::Real=0.0, tA::Char='N', tB::Char='N')
+                    alpha::Real=1.0, beta::Real=0.0, tA::Char='N', tB::Char='N';
+                    stream::Ptr{Cvoid}=device_stream(device_of(C)))
     nb = C.partitioning.blocksize[1]
     m, n = size(C)
     k = tA == 'N' ? size(A, 2) : size(A, 1)
@@ -298,13 +316,13 @@ function mul_gb300!(C::DArray{Float64,2}, A::DArray{Float64,2}, B::DArray{Float6
                       (Cchar, Cint, Cint, Cint, Cdouble, Ptr{Ptr{Float64}}, Cdouble,
                        Ptr{Ptr{Float64}}, Ptr{Cvoid}),
                       tA == 'N' ? 'N' : 'T', n, k, nb, alpha, tile_pointers(A), beta,
-                      tile_pointers(C), C_NULL))
+                      tile_pointers(C), stream))
     else
         dgcheck(ccall((:dg_gemm_tiled, libdg), Cint,
                       (Cchar, Cchar, Cint, Cint, Cint, Cint, Cdouble, Ptr{Ptr{Float64}},
                        Ptr{Ptr{Float64}}, Cdouble, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
                       tA, tB, m, n, k, nb, alpha, tile_pointers(A), tile_pointers(B), beta,
-                      tile_pointers(C), C_NULL))
+                      tile_pointers(C), stream))
     end
     return C
 end
@@ -318,13 +336,14 @@ GB300Arrays.  ipiv stays on the device (GB300Array{Int64,1}); info > 0 is
 the first exactly zero pivot, checked as LinearAlgebra._check_lu_success.
 """
 function lu_gb300!(A::DArray{Float64,2}, pivot::Union{RowMaximum,NoPivot}=RowMaximum();
-                   check::Bool=true, allowsingular::Bool=false)
+                   check::Bool=true, allowsingular::Bool=false,
+                   stream::Ptr{Cvoid}=device_stream(device_of(A)))
     m, n = size(A)
     nb = A.partitioning.blocksize[1]
-    ipiv = GB300Array{Int64,1}(undef, (max(min(m, n), 1),))
+    ipiv = GB300Array{Int64,1}(undef, (max(min(m, n), 1),); device=device_of(A))
     info = ccall((:dg_lu_tiled, libdg), Cint,
                  (Cint, Cint, Cint, Ptr{Ptr{Float64}}, Cint, Ptr{Int64}, Ptr{Cvoid}),
-                 m, n, nb, tile_pointers(A), pivot isa RowMaximum ? 1 : 0, pointer(ipiv), C_NULL)
+                 m, n, nb, tile_pointers(A), pivot isa RowMaximum ? 1 : 0, pointer(ipiv), stream)
     dgcheck(info)
     check && LinearAlgebra._check_lu_success(Int(info), allowsingular)
     return LU(A, ipiv, convert(LinearAlgebra.BlasInt, info))
@@ -337,14 +356,15 @@ ldiv!(F::LU, B) (src/array/linalg.jl:264-308) as one library call
 (dg_lu_solve_tiled): B's rows permuted by ipiv, then the unit-lower and the
 upper block solves.  B is blocked like the factors.
 """
-function ldiv_gb300!(F::LU{Float64,<:DArray}, B::DArray{Float64})
+function ldiv_gb300!(F::LU{Float64,<:DArray}, B::DArray{Float64};
+                     stream::Ptr{Cvoid}=device_stream(F.ipiv.device))
     A = F.factors
     n = size(A, 1)
     nb = A.partitioning.blocksize[1]
     nrhs = ndims(B) == 1 ? 1 : size(B, 2)
     dgcheck(ccall((:dg_lu_solve_tiled, libdg), Cint,
                   (Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Int64}, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
-                  n, nb, tile_pointers(A), pointer(F.ipiv), nrhs, tile_pointers(B), C_NULL))
+                  n, nb, tile_pointers(A), pointer(F.ipiv), nrhs, tile_pointers(B), stream))
     return B
 end
 

@@ -13,9 +13,14 @@
  *     1-based order of the first leading minor that is not positive definite),
  *     -i = argument i is invalid, <= -1000 = one of the DG_ERR_* codes below.
  *     dg_last_error() returns a message for the last failure on this thread.
- * Entry points are safe to call from several host threads at once when each
- * thread uses its own stream (the reference runs each task on its own Julia
- * task, ext/CUDAExt.jl:309-327).
+ * Entry points may be called from several host threads at once (the
+ * reference runs each task on its own Julia task, ext/CUDAExt.jl:309-327).
+ * Calls on different streams run concurrently: each stream handle gets its
+ * own workspace for the emulated FP64 engine and the LU, grown in stream
+ * order, and results do not depend on what runs beside them.  Calls on the
+ * same stream handle from different threads take turns (the later call's
+ * work is ordered after the earlier one's); the noalloc entry point, which
+ * has one static scratch, takes turns across all streams.
  *
  * Reference paths are within JuliaParallel/Dagger.jl v0.22.0.
  */
@@ -54,9 +59,11 @@ long long dg_kernel_launches(void);
 /* Frees library-owned workspaces and cached graphs of the current device.
  * Caller memory is never freed by the library. */
 int dg_finalize(void);
-/* Returns the device memory that the library's stream-ordered pool keeps
- * for reuse (freed workspaces of earlier calls) to the device.  Blocks still
- * in use are not touched; later calls allocate again as needed. */
+/* Returns to the device the memory that the library keeps for reuse on the
+ * current device: the per-stream workspaces that no call is using (after the
+ * work queued with them has finished) and the free blocks of the library's
+ * stream-ordered pool.  Blocks in use are not touched; later calls allocate
+ * again as needed. */
 int dg_release_memory(void);
 
 /* Device memory and streams for hosts that do not link a CUDA binding (the
@@ -422,9 +429,9 @@ int dg_batched_potrs(int count, const int *n, const int *nrhs, double *const *A,
  * allocation).  The call is synchronous: it stages descriptors from host
  * memory and synchronises `stream` before it returns, so it cannot be called
  * while `stream` is being captured into a graph.  Every call uses the same
- * array, so calls that overlap on the GPU (on different streams or host
- * threads) race; serialise them.  Arguments and results as dg_batched_potrs,
- * without the timing output. */
+ * array: calls from several host threads take turns on a library lock held
+ * until the call's work has finished.  Arguments and results as
+ * dg_batched_potrs, without the timing output. */
 int dg_batched_potrs_noalloc(int count, const int *n, const int *nrhs, double *const *A,
                              const double *const *B, double *const *X, int mode, double tol,
                              int max_iter, const int *bucket_w, int ctas_per_sm, int *info,

@@ -9,7 +9,9 @@ row and checks both results against the allocating entry point
 dg_batched_potrs on the same batch and settings (FP64: identical bits; FP32
 factor + FP64 refinement: identical bits as well, and each system's normwise
 backward error at most 1e-12).  It also checks that a batch too large for
-the static array is rejected without launching.
+the static array is rejected without launching, and that two host threads
+calling it at once on their own streams (they take turns on the array) get
+the same bits as the allocating entry point.
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test; it also passes alone in a fresh process.
@@ -90,3 +92,51 @@ def test_noalloc_rejects_a_batch_larger_than_its_scratch():
     rc, _, _ = _call("noalloc", P, 1, [32] * 5, 1)
     assert rc == _lib.DG_ERR_NOMEM
     assert "64 MiB" in _lib.last_error()
+
+
+def test_noalloc_two_threads_take_turns():
+    import threading
+    import torch
+    from dagger_gb300.batched import PackedBatch
+    widths, ctas = [32, 32, 32, 32, 32], 1
+    batches = [_batch(40, 31), _batch(40, 32)]
+    expected = []
+    for ns, rs, As, Bs in batches:
+        ref = PackedBatch(As, Bs)
+        rc, info, _ = _call("alloc", ref, 1, widths, ctas)
+        assert rc == 0 and not any(info)
+        expected.append([ref.solution(i).clone() for i in range(ref.count)])
+    got, errors = [None, None], []
+    start = threading.Barrier(2)
+
+    def worker(j):
+        try:
+            torch.cuda.set_device(0)
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                out = []
+                for _ in range(3):
+                    ns, rs, As, Bs = batches[j]
+                    P = PackedBatch(As, Bs)
+                    start.wait(timeout=120)
+                    rc, info, berr = _call("noalloc", P, 1, widths, ctas)
+                    assert rc == 0 and not any(info)
+                    assert max(berr) <= 1e-12
+                    out.append([P.solution(i).clone() for i in range(P.count)])
+                got[j] = out
+        except BaseException as e:
+            errors.append(e)
+            start.abort()
+
+    ts = [threading.Thread(target=worker, args=(j,)) for j in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(timeout=300)
+    assert not any(t.is_alive() for t in ts)
+    if errors:
+        raise errors[0]
+    for j in range(2):
+        for out in got[j]:
+            for a, b in zip(out, expected[j]):
+                assert (a == b).all()
