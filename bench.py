@@ -627,41 +627,36 @@ def _measured_bf16_peak():
 # multiplies the 28 slice pairs (s, t) with s + t <= 8.
 EMULATED_SLICES = 7
 EMULATED_PRODUCTS = 28
-# DRAM bytes (read + write) of one 1024^3 emulated tile launch, from the ncu
-# capture summarised in profiles/oz_gemm_tile_1024.md (dram__bytes_read.sum +
-# dram__bytes_write.sum); the 29 MiB of slices mostly hit L2 and C's
-# write-back stays in L2.  A constant from that capture, not measured here:
-# bench.py runs without a profiler.
+# DRAM bytes (read + write) per launch of the two emulated launches timed
+# below, from ncu captures of the same launches (dram__bytes_read.sum +
+# dram__bytes_write.sum): the 8192 x 8192 x 1024 trailing-update launch in
+# profiles/oz_gemm_trailing_8192x1024.md, the lone 1024^3 tile in
+# profiles/oz_gemm_tile_1024.md.  Constants from those captures, not
+# measured here: bench.py runs without a profiler.
+OZ_TRAILING_DRAM_BYTES = 1420808192 + 507682048
 OZ_TILE_DRAM_BYTES = 23160576
-OZ_TILE_DRAM_SOURCE = ("ncu capture of one 1024^3 launch (profiles/oz_gemm_tile_1024.md), "
-                       "not measured in this run")
+OZ_DRAM_SOURCE = ("ncu captures of the same launches (profiles/oz_gemm_trailing_8192x1024.md, "
+                  "profiles/oz_gemm_tile_1024.md), not measured in this run")
 
 
-def roofline_emulated(L, nb, dev, stream, s):
-    """The emulated FP64 tile GEMM (oz_gemm_kernel) of the trailing update,
-    C(nb x nb) -= A'B with both operands already cut into slices, timed alone
-    with CUDA events on the launching stream: EMULATED_PRODUCTS BF16 products
-    of 2 nb^3 flops per launch against the measured BF16 tensor peak."""
+def _time_oz_launch(L, m, k, dev, stream, s, reps):
+    """CUDA-event time of one oz_gemm_kernel launch C(m x m) -= A'A with
+    K = k from pre-cut slices (seconds per launch)."""
     import torch
-    ldk = (nb + 7) // 8 * 8
+    ldk = (k + 7) // 8 * 8
     g = torch.Generator(device=dev)
     g.manual_seed(11)
-    Ta = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
-    Tb = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
-    Tc = torch.randn(nb, nb, dtype=torch.float64, device=dev, generator=g)
-    sa = torch.empty(EMULATED_SLICES * ldk * nb, dtype=torch.bfloat16, device=dev)
-    sb = torch.empty(EMULATED_SLICES * ldk * nb, dtype=torch.bfloat16, device=dev)
-    ea = torch.empty(nb, dtype=torch.int64, device=dev)
-    eb = torch.empty(nb, dtype=torch.int64, device=dev)
-    L.dg_f64_slices(nb, nb, Ta.data_ptr(), nb, 1, sa.data_ptr(), ldk, ea.data_ptr(), s)
-    L.dg_f64_slices(nb, nb, Tb.data_ptr(), nb, 1, sb.data_ptr(), ldk, eb.data_ptr(), s)
+    Ta = torch.randn(m, k, dtype=torch.float64, device=dev, generator=g)  # k x m column-major
+    Tc = torch.randn(m, m, dtype=torch.float64, device=dev, generator=g)
+    sa = torch.empty(EMULATED_SLICES * ldk * m, dtype=torch.bfloat16, device=dev)
+    ea = torch.empty(m, dtype=torch.int64, device=dev)
+    L.dg_f64_slices(k, m, Ta.data_ptr(), k, 1, sa.data_ptr(), ldk, ea.data_ptr(), s)
 
     def launch():
-        L.dg_gemm_f64_slices(nb, nb, nb, -1.0, sa.data_ptr(), ldk, ea.data_ptr(), sb.data_ptr(),
-                             ldk, eb.data_ptr(), 1.0, Tc.data_ptr(), nb, None, s)
+        L.dg_gemm_f64_slices(m, m, k, -1.0, sa.data_ptr(), ldk, ea.data_ptr(), sa.data_ptr(),
+                             ldk, ea.data_ptr(), 1.0, Tc.data_ptr(), m, None, s)
     for _ in range(3):
         launch()
-    reps = 20
     g0 = torch.cuda.Event(enable_timing=True)
     g1 = torch.cuda.Event(enable_timing=True)
     g0.record(stream)
@@ -669,21 +664,46 @@ def roofline_emulated(L, nb, dev, stream, s):
         launch()
     g1.record(stream)
     torch.cuda.synchronize()
-    tg = g0.elapsed_time(g1) / 1e3 / reps
+    return g0.elapsed_time(g1) / 1e3 / reps
+
+
+def roofline_emulated(L, nb, dev, stream, s):
+    """The emulated FP64 GEMM (oz_gemm_kernel) of the trailing update, timed
+    alone with CUDA events on the launching stream against the measured BF16
+    burst peak; EMULATED_PRODUCTS BF16 products of 2 m^2 k flops per launch.
+
+    The headline figure is the launch shape that carries the factorization's
+    bulk: C(8 nb x 8 nb) -= A'A with K = nb, 64 output blocks of 128 x 64 per
+    nb x nb tile spread over one CTA per SM, several blocks per CTA (the
+    trailing updates off the critical path run this way: a CTA forms one
+    block's outputs while the tensor cores work on its next block; at N =
+    32768 they are 99 % of the emulated products).  C is 512 MiB, larger than
+    L2, so repeated launches read it from HBM.  The critical-path tile (one
+    nb^3 launch, one block per CTA, 128 of 152 SMs busy) is reported beside
+    it."""
+    m = 8 * nb
+    tt = _time_oz_launch(L, m, nb, dev, stream, s, reps=5)
+    tg = _time_oz_launch(L, nb, nb, dev, stream, s, reps=20)
     peak, src = _measured_bf16_peak()
-    achieved = EMULATED_PRODUCTS * 2.0 * nb ** 3 / tg / 1e12
-    return {"bound": "tensor", "kernel": "oz_gemm_kernel (emulated FP64 tile GEMM of the "
-                                          "trailing update, BF16 tcgen05)",
+    achieved = EMULATED_PRODUCTS * 2.0 * m * m * nb / tt / 1e12
+    tile_achieved = EMULATED_PRODUCTS * 2.0 * nb ** 3 / tg / 1e12
+    return {"bound": "tensor", "kernel": "oz_gemm_kernel (emulated FP64 trailing update, BF16 "
+                                          "tcgen05, slices cut before the launch)",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "peak_source": src,
-            "per_launch": f"{EMULATED_PRODUCTS} x 2*{nb}^3 BF16 flops (= 2*{nb}^3 FP64-equivalent), "
-                          f"{1e6 * tg:.0f} us, {nb // 128} x {nb // 64} CTAs",
-            "fp64_equivalent_tflops": 2.0 * nb ** 3 / tg / 1e12,
-            # dram__bytes_read.sum + dram__bytes_write.sum of one launch at
-            # nb = 1024 from an ncu capture of the same launch (profiles/)
-            "traffic": OZ_TILE_DRAM_BYTES if nb == 1024 else None,
-            "traffic_source": OZ_TILE_DRAM_SOURCE,
-            "traffic_unit": "bytes per launch"}
+            "per_launch": f"{EMULATED_PRODUCTS} x 2*{m}^2*{nb} BF16 flops (= 2*{m}^2*{nb} "
+                          f"FP64-equivalent), {1e6 * tt:.0f} us, "
+                          f"{(m // 128) * (m // 64)} blocks of 128 x 64 on one CTA per SM",
+            "fp64_equivalent_tflops": 2.0 * m * m * nb / tt / 1e12,
+            "traffic": OZ_TRAILING_DRAM_BYTES if nb == 1024 else None,
+            "traffic_source": OZ_DRAM_SOURCE,
+            "traffic_unit": "bytes per launch",
+            "critical_path_tile": {
+                "achieved": tile_achieved, "frac": tile_achieved / peak,
+                "per_launch": f"{EMULATED_PRODUCTS} x 2*{nb}^3 BF16 flops, {1e6 * tg:.0f} us, "
+                              f"{(nb // 128) * (nb // 64)} CTAs of one block each",
+                "fp64_equivalent_tflops": 2.0 * nb ** 3 / tg / 1e12,
+                "traffic": OZ_TILE_DRAM_BYTES if nb == 1024 else None}}
 
 
 def choose_precision(cond):

@@ -162,12 +162,22 @@ __host__ __device__ __forceinline__ int oz_col_blocks(int tri, int bj, int mblk,
   return hi > lo ? hi - lo : 0;
 }
 
-// Origin of the v-th output block of the stored part, row blocks fastest.
+// Row blocks per group of the full-matrix walk: the CTAs of one wave share
+// the slices of 1024 rows of A and of the few block columns of B they are at.
+constexpr int OZ_GROUP = 8;
+
+// Origin of the v-th output block of the stored part.  Full C: groups of
+// OZ_GROUP row blocks, each walked column by column (row blocks fastest), so
+// that the blocks in flight at once read a compact set of slices from L2
+// (going down whole block columns of a tall C streams all of A through L2
+// once per block column).  One triangle: column by column.
 __device__ __forceinline__ void oz_block(const OzParams &p, int v, int mblk, int nblk, int &i0,
                                          int &j0) {
   if (p.tri == 0) {
-    i0 = (v % mblk) * OZ_BM;
-    j0 = (v / mblk) * OZ_BN;
+    const int g = v / (OZ_GROUP * nblk), local = v - g * (OZ_GROUP * nblk);
+    const int rows = min(OZ_GROUP, mblk - g * OZ_GROUP);
+    i0 = (g * OZ_GROUP + local % rows) * OZ_BM;
+    j0 = (local / rows) * OZ_BN;
     return;
   }
   i0 = j0 = 0;

@@ -6,6 +6,7 @@ a profiler can capture exactly that kernel (ncu -k regex:<name> -c N).
     python -m dagger_gb300.profile_kernels trsm_f64   [--nb 1024]
     python -m dagger_gb300.profile_kernels batched    [--count 2000]
     python -m dagger_gb300.profile_kernels oz_gemm    [--m 8192] [--k 1024]
+    python -m dagger_gb300.profile_kernels oz_slices  [--m 8192] [--k 1024]
     python -m dagger_gb300.profile_kernels lu_panel   [--m 32768] [--k 1024]
     python -m dagger_gb300.profile_kernels potrf_f64  [--nb 1024]
     python -m dagger_gb300.profile_kernels herm       [--m 8192] [--nb 1024]
@@ -22,6 +23,9 @@ batched    the persistent batched launch on `count` systems, n in [32, 1024]
 oz_gemm    the emulated FP64 GEMM (engine 2) on an m x m output with K = k:
            two split launches and one oz_gemm_kernel launch per call
            (2 m^2 k FP64 flops, 28 BF16 products of 2 m^2 k flops each)
+oz_slices  oz_gemm_kernel alone on pre-cut slices, C(m x m) -= A'A with K = k
+           (the launch bench.py's roofline times: the slices are cut once
+           before the timed launches)
 lu_panel   the pivoted panel factorization of the tiled LU (dg_getrf) on an
            m x k column-major matrix (uniform [0, 1), seed 5) with the emulated
            engine: 32-column leaf launches and the recursion's emulated
@@ -63,7 +67,8 @@ def _time(fn, reps):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched", "oz_gemm",
-                                       "lu_panel", "potrf_f64", "herm", "diag", "tc6", "reblock"])
+                                       "oz_slices", "lu_panel", "potrf_f64", "herm", "diag", "tc6",
+                                       "reblock"])
     ap.add_argument("--nb", type=int, default=1024)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--k", type=int, default=1024)
@@ -122,6 +127,22 @@ def main(argv=None):
         fl = 2.0 * m * m * k
         print(f"oz_gemm m={m} k={k}: {ms * 1e3:.1f} us/call, {fl / ms / 1e9:.2f} FP64-equivalent "
               f"TFLOP/s, {28 * fl / ms / 1e9:.1f} BF16 TFLOP/s")
+    elif a.kernel == "oz_slices":
+        m, k = a.m, a.k
+        ldk = (k + 7) // 8 * 8
+        g = torch.Generator(device=dev)
+        g.manual_seed(11)
+        A = torch.randn(m, k, dtype=torch.float64, device=dev, generator=g)  # k x m column-major
+        C = torch.randn(m, m, dtype=torch.float64, device=dev, generator=g)
+        sl = torch.empty(7 * ldk * m, dtype=torch.bfloat16, device=dev)
+        sc = torch.empty(m, dtype=torch.int64, device=dev)
+        L.dg_f64_slices(k, m, A.data_ptr(), k, 1, sl.data_ptr(), ldk, sc.data_ptr(), s)
+        ms = _time(lambda: L.dg_gemm_f64_slices(m, m, k, -1.0, sl.data_ptr(), ldk, sc.data_ptr(),
+                                                sl.data_ptr(), ldk, sc.data_ptr(), 1.0,
+                                                C.data_ptr(), m, None, s), a.reps)
+        fl = 2.0 * m * m * k
+        print(f"oz_slices m={m} k={k}: {ms * 1e3:.1f} us/launch, {fl / ms / 1e9:.2f} "
+              f"FP64-equivalent TFLOP/s, {28 * fl / ms / 1e9:.1f} BF16 TFLOP/s")
     elif a.kernel == "trsm_f64":
         nb = a.nb
         T = torch.randn(nb, nb, dtype=torch.float64, device=dev) * 0.01
