@@ -729,7 +729,10 @@ def bench_mixed_sweep(args, d, dev):
     as N^3/3 + 2 N^2 r, the refinement's iteration counts, the normwise
     backward error (FP64, on the device), and the factor's BF16 tensor work
     (terms x N^3/3 of the trailing updates and 6 x 2 nb N^2 / 2 of the panel
-    solves) per second as a fraction of the sustained BF16 peak."""
+    solves) per second as a fraction of the sustained BF16 peak.  At the
+    smallest N and kappa <= 1e2 the single-product forms (bf16, and fp8: E4M3
+    with a power-of-two scale per vector) are measured beside the chosen
+    precision, 64 right-hand sides, marked "alternative"."""
     import torch
     nb = args.nb
     peak = _measured_bf16_sustained()
@@ -768,8 +771,10 @@ def bench_mixed_sweep(args, d, dev):
             nA = A.abs().sum(dim=1).max()
             del A
             torch.cuda.empty_cache()
-            prec = choose_precision(cond)
-            for r in (64, 1):
+            runs = [(choose_precision(cond), r, False) for r in (64, 1)]
+            if cond <= 1e2 and n == min(int(x) for x in args.sweep_n.split(",") if x):
+                runs += [("bf16", 64, True), ("fp8", 64, True)]
+            for prec, r, alternative in runs:
                 B = Bs[r]
                 X = torch.empty((r, n), dtype=torch.float64, device=dev).t()
                 Bc = B.t().contiguous().t()
@@ -815,6 +820,8 @@ def bench_mixed_sweep(args, d, dev):
                       "ir_iterations": rr.get("iterations"),
                       "gmres_iterations": rr.get("gmres_iterations"),
                       "shift": fs.get("shift"), "backward_error": be}
+                if alternative:
+                    pt["alternative"] = True
                 if prec in terms and fs.get("factor_ms"):
                     tc = terms[prec] * n ** 3 / 3.0 + 6.0 * nb * n * n
                     pt["factor_bf16_TFLOP_s"] = tc / (fs["factor_ms"] / 1e3) / 1e12

@@ -46,6 +46,8 @@ struct dg_mixed {
   double *s = nullptr;           // diagonal scaling
   double **tiles_dev = nullptr;  // caller's FP64 tiles (device array of pointers)
   void *P_hi = nullptr, *P_lo = nullptr;  // FP16 (scaled) panel operands (T x nb, K-major)
+  uint8_t *P8 = nullptr;         // FP8 form: E4M3 panel operands, two buffers (T x nb)
+  float *s8 = nullptr;           // FP8 form: their per-vector scales, two buffers (T)
   float *diag_backup = nullptr;  // diagonal block before its FP32 factorization
   double *d64 = nullptr;         // FP64 scratch of the retry
   float *panel_max = nullptr;    // per-step |panel| maximum (FP16 scaling)
@@ -419,6 +421,12 @@ static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
                                                           o3 + 2 * f->r3_stride, ik, status);
     count_launches(1);
   }
+  if (f->precision == DG_PREC_FP8) {
+    // E4M3 with a power-of-two scale per vector (column of the panel)
+    const size_t tmax = (size_t)std::max(0, n - nb);
+    DG_TRY(split_e4m3(Rk, nb, nbk, (int)T, f->P8 + (size_t)(k & 1) * tmax * nb, nb,
+                      f->s8 + (size_t)(k & 1) * tmax, ik, status, s));
+  }
   const bool fp16 = (f->precision == DG_PREC_FP16 || f->precision == DG_PREC_FP16X3);
   if (fp16) {
     const int terms = f->precision == DG_PREC_FP16X3 ? 3 : 1;
@@ -441,7 +449,8 @@ static int panel_step(dg_mixed *f, int k, cudaStream_t s) {
 // Step k's trailing update on the tensor cores, in two parts: `next` = the
 // block row of panel k+1 (so the next panel can start), else the rest.
 // BF16 forms read the factor's slices of panel k (hi; hi + mid as the hi/lo
-// pair of bf16x3; all three for bf16x6), FP16 forms the scaled P buffer.
+// pair of bf16x3; all three for bf16x6), FP16 forms the scaled P buffer, the
+// FP8 form the E4M3 buffer and its per-vector scales.
 static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
   const int n = f->n, nb = f->nb;
   const long long T = (long long)n - (long long)(k + 1) * nb;
@@ -461,7 +470,13 @@ static int trailing_tc(dg_mixed *f, int k, bool next, cudaStream_t s) {
     g.off = (long long)(k + 2) * nb;
   }
   g.k = nb; g.terms = terms; g.fp16 = fp16;
-  if (fp16) {
+  if (f->precision == DG_PREC_FP8) {
+    const size_t tmax = (size_t)std::max(0, n - nb);
+    g.fp8 = 1;
+    g.a_hi = f->P8 + (size_t)(k & 1) * tmax * nb;
+    g.a_scale = f->s8 + (size_t)(k & 1) * tmax;
+    g.b_scale = g.a_scale;
+  } else if (fp16) {
     const size_t half = (size_t)std::max(0LL, (long long)n - nb) * nb;
     g.a_hi = (char *)f->P_hi + (size_t)(k & 1) * half * 2;
     g.a_lo = (char *)f->P_lo + (size_t)(k & 1) * half * 2;
@@ -671,7 +686,8 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
   DG_CHECK_ARG(tiles != nullptr, 4);
   DG_CHECK_ARG(precision == DG_PREC_BF16 || precision == DG_PREC_BF16X3 ||
                    precision == DG_PREC_FP16 || precision == DG_PREC_FP16X3 ||
-                   precision == DG_PREC_FP32 || precision == DG_PREC_BF16X6,
+                   precision == DG_PREC_FP32 || precision == DG_PREC_BF16X6 ||
+                   precision == DG_PREC_FP8,
                5);
   DG_CHECK_ARG(shift >= 0.0, 6);
   cudaStream_t s = (cudaStream_t)stream;
@@ -687,6 +703,7 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
     return rc;
   };
   const bool fp16 = (precision == DG_PREC_FP16 || precision == DG_PREC_FP16X3);
+  const bool fp8 = precision == DG_PREC_FP8;
   f->r3_stride = wsize;
   f->v3_stride = (long long)mt * nb * nb;
   f->l3_stride = std::max(1LL, dg::lp_base(mt, nb));
@@ -697,6 +714,8 @@ extern "C" int dg_mixed_factor_ex(dg_mixed **out, int n, int nb, double *const *
       {(void **)&f->tiles_dev, sizeof(double *) * (size_t)mt * mt},
       {(void **)&f->P_hi, fp16 ? 2 * 2 * (size_t)std::max(1LL, tmax) * nb : (size_t)256},
       {(void **)&f->P_lo, fp16 ? 2 * 2 * (size_t)std::max(1LL, tmax) * nb : (size_t)256},
+      {(void **)&f->P8, fp8 ? 2 * (size_t)std::max(1LL, tmax) * nb : (size_t)256},
+      {(void **)&f->s8, fp8 ? 2 * sizeof(float) * (size_t)std::max(1LL, tmax) : (size_t)256},
       {(void **)&f->diag_backup, sizeof(float) * (size_t)nb * nb},
       {(void **)&f->d64, sizeof(double) * (size_t)nb * nb},
       {(void **)&f->panel_max, sizeof(float) * (size_t)mt},
@@ -821,7 +840,7 @@ extern "C" void dg_mixed_destroy(dg_mixed *f) {
   if (!f) return;
   // the slices of A are cut on aux2: the frees below wait for them
   if (f->ev_oz && f->stream) cudaStreamWaitEvent(f->stream, f->ev_oz, 0);
-  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->diag_backup, f->d64,
+  void *ps[] = {f->W, f->s, f->tiles_dev, f->P_hi, f->P_lo, f->P8, f->s8, f->diag_backup, f->d64,
                 f->panel_max, f->alpha_dev, f->words, f->Vinv, f->diag_scratch, f->S3r,
                 f->R3, f->V3, f->VT3, f->L3, f->ozA};
   for (void *p : ps)

@@ -16,6 +16,12 @@
 // accumulate together: about 24 significant bits, an FP32-accurate product
 // on the BF16 tensor cores (the panel solve of the mixed factor).
 //
+// FP8 form (persistent kernel only): E4M3 operands, each vector scaled by a
+// power of two so that its largest magnitude lies in [128, 256) before the
+// rounding (split_e4m3), one kind::f8f6f4 product (K = 32 per instruction, at
+// twice the BF16 rate), and the two vectors' scales applied in the epilogue.
+// Each operand value carries 4 significant bits.
+//
 // One CTA computes a 128 x BN tile of C with 4 warps:
 //   warp 0, one thread   TMA producer: per K-block of 64, loads the A and B
 //                        slabs (128B-swizzled, 1024-byte aligned stages) and
@@ -37,8 +43,10 @@
 // the copies and MMAs already issued (again bounded), frees its TMEM and
 // returns; nothing traps.
 #include <cuda.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "dg_common.cuh"
 #include "runtime.h"
@@ -256,9 +264,14 @@ struct SmemP {
   static constexpr int TOTAL = STAGES * STAGE_BYTES + 1024 + 256;
 };
 
-template <int BN, int TERMS>
+// F8: E4M3 operands (kind::f8f6f4).  A stage then holds 128 values of K per
+// row (the same 128 bytes), and each product is scaled in the epilogue by
+// the two vectors' power-of-two scales.
+template <int BN, int TERMS, bool F8>
 __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_constant__ TcParams p) {
   using S = SmemP<BN, TERMS>;
+  static_assert(!F8 || TERMS == 1, "the FP8 form has one product");
+  constexpr int KE = F8 ? 2 * BK : BK;  // K values per stage
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(smem + S::STAGES * S::STAGE_BYTES);
@@ -273,7 +286,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
   if (p.status && *(volatile int *)p.status) return;
   const int mtiles = (p.m + BM - 1) / BM, ntiles = (p.n + BN - 1) / BN;
   const int total = mtiles * ntiles;
-  const int nk = (p.k + BK - 1) / BK;
+  const int nk = (p.k + KE - 1) / KE;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S::STAGES; s++) {
@@ -321,7 +334,7 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
         }
         uint8_t *st = smem + s * S::STAGE_BYTES;
         mbar_expect_tx(&full[s], S::STAGE_BYTES);
-        const int kx = kb * BK;
+        const int kx = kb * KE;
         tma_load_2d(st, &p.a_hi, &full[s], kx, p.a_row0 + i0);
         tma_load_2d(st + S::A_BYTES, &p.b_hi, &full[s], kx, p.b_row0 + j0);
         if (TERMS == 3) {
@@ -362,7 +375,10 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
           const uint32_t koff = kk * 32;
           const uint64_t a = sw128_desc(st + koff);
           const uint64_t b = sw128_desc(st + S::A_BYTES + koff);
-          mma_bf16(d, a, b, p.idesc, (kb | kk) ? 1u : 0u);
+          if (F8)
+            mma_f8(d, a, b, p.idesc, (kb | kk) ? 1u : 0u);
+          else
+            mma_bf16(d, a, b, p.idesc, (kb | kk) ? 1u : 0u);
           if (TERMS == 3) {
             const uint64_t alo = sw128_desc(st + S::A_BYTES + S::B_BYTES + koff);
             const uint64_t blo = sw128_desc(st + 2 * S::A_BYTES + S::B_BYTES + koff);
@@ -397,6 +413,8 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int row = i0 + q * 32 + lane;
+      // FP8: the row's scale joins alpha, the columns' are applied one by one
+      const float arow = (F8 && row < p.m) ? alpha * p.a_scale[p.a_row0 + row] : alpha;
       long long r_panel = 0, base = 0;
       if (p.layout == 1) {
         const long long gi = p.off + row;
@@ -429,7 +447,8 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_persist_kernel(const __grid_co
         for (int c = 0; c < 32; c++) {
           const int col = j0 + c0 + c;
           if (col >= p.n || (upper && row > col)) continue;
-          cp0[(size_t)c * cstride] = read_c ? fmaf(alpha, v[c], beta * old[c]) : alpha * v[c];
+          const float a = F8 ? arow * p.b_scale[p.b_row0 + col] : alpha;
+          cp0[(size_t)c * cstride] = read_c ? fmaf(a, v[c], beta * old[c]) : a * v[c];
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -468,17 +487,25 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
+enum OperandType { OP_BF16, OP_FP16, OP_E4M3 };
+
+// 2-D map of a K-major operand (kdim values per vector, ldk between vectors)
+// whose boxes are 128 bytes of K by box_rows vectors, 128-byte swizzle.
 bool encode_map(CUtensorMap *map, const void *base, int kdim, int rows, int ldk, int box_rows,
-                bool fp16) {
+                OperandType type) {
   EncodeTiledFn cuTensorMapEncodeTiled = encode_fn();
   if (!cuTensorMapEncodeTiled) return false;
+  const int esize = type == OP_E4M3 ? 1 : 2;
   cuuint64_t dims[2] = {(cuuint64_t)kdim, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)ldk * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ldk * esize};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esize), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = cuTensorMapEncodeTiled(map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims,
-                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  const CUtensorMapDataType dt = type == OP_E4M3   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                 : type == OP_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                   : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  CUresult r = cuTensorMapEncodeTiled(map, dt, 2, (void *)base, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -486,7 +513,7 @@ bool encode_map(CUtensorMap *map, const void *base, int kdim, int rows, int ldk,
 template <int BN, int TERMS>
 int launch(const TcParams &p, cudaStream_t s) {
   using S = Smem<BN, TERMS>;
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];  // zero-initialised: false
   int dev = 0;
   cudaGetDevice(&dev);
   if (!attr_set[dev & 63]) {
@@ -501,14 +528,14 @@ int launch(const TcParams &p, cudaStream_t s) {
   return 0;
 }
 
-template <int BN, int TERMS>
+template <int BN, int TERMS, bool F8 = false>
 int launch_persist(const TcParams &p, int tiles_per_cta, cudaStream_t s) {
   using S = SmemP<BN, TERMS>;
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];  // zero-initialised: false
   int dev = 0;
   cudaGetDevice(&dev);
   if (!attr_set[dev & 63]) {
-    DG_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_persist_kernel<BN, TERMS>,
+    DG_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_persist_kernel<BN, TERMS, F8>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, S::TOTAL));
     attr_set[dev & 63] = true;
   }
@@ -523,7 +550,7 @@ int launch_persist(const TcParams &p, int tiles_per_cta, cudaStream_t s) {
   long long grid = dg_num_sms();
   if (tiles_per_cta > 0) grid = std::max(grid, (tiles + tiles_per_cta - 1) / tiles_per_cta);
   grid = std::min<long long>(std::min<long long>(grid, tiles), 1 << 30);
-  tc_gemm_persist_kernel<BN, TERMS><<<(unsigned)grid, 192, S::TOTAL, s>>>(p);
+  tc_gemm_persist_kernel<BN, TERMS, F8><<<(unsigned)grid, 192, S::TOTAL, s>>>(p);
   DG_CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -531,32 +558,77 @@ int launch_persist(const TcParams &p, int tiles_per_cta, cudaStream_t s) {
 
 }  // namespace
 
+// One warp per vector (column of a column-major K x ncols FP32 operand):
+// scale = 2^(e - 8) with 2^(e-1) <= max|v| < 2^e, dst = e4m3(v / scale)
+// rounded to nearest (largest magnitude in [128, 256), below E4M3's 448), the
+// vector's scale stored for the epilogue.  A zero vector keeps scale 1; a
+// vector with an infinity or NaN gets a NaN scale, so every product that uses
+// it is NaN.
+__global__ void e4m3_kernel(const float *src, long long ld, int k, int ncols, uint8_t *dst,
+                            long long ldd, float *scale, const int *a1, const int *a2) {
+  if (aborted(a1, a2)) return;
+  const long long col = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (col >= ncols) return;
+  const float *v = src + col * ld;
+  float mx = 0.f;
+  int bad = 0;
+  for (int i = lane; i < k; i += 32) {
+    const float x = v[i];
+    bad |= !isfinite(x);
+    mx = fmaxf(mx, fabsf(x));
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  bad = __any_sync(0xffffffffu, bad);
+  int e = 0;
+  frexpf(mx, &e);
+  const int sh = mx > 0.f ? min(8 - e, 127) : 0;
+  const float up = ldexpf(1.f, sh);
+  uint8_t *d = dst + col * ldd;
+  for (int i = lane; i < k; i += 32)
+    d[i] = (uint8_t)__nv_cvt_float_to_fp8(v[i] * up, __NV_SATFINITE, __NV_E4M3);
+  if (lane == 0) scale[col] = bad ? __int_as_float(0x7fc00000) : ldexpf(1.f, -sh);
+}
+
+int split_e4m3(const float *src, long long ld, int k, int ncols, uint8_t *dst, long long ldd,
+               float *scale, const int *a1, const int *a2, cudaStream_t s) {
+  if (ncols <= 0 || k <= 0) return 0;
+  const long long threads = 32LL * ncols;
+  e4m3_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(src, ld, k, ncols, dst, ldd,
+                                                                scale, a1, a2);
+  DG_CUDA_TRY(cudaGetLastError());
+  count_launches(1);
+  return 0;
+}
+
 int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
   if (g.m <= 0 || g.n <= 0) return 0;
   if (g.terms != 1 && g.terms != 3 && g.terms != 6) return DG_ERR_UNSUPPORTED;
   // K itself may be ragged: the tensor maps' K extent is g.k and the last
   // block's columns past it are filled with zeros by TMA (only the row
   // strides need 16-byte multiples)
-  if (g.k <= 0 || g.lda % 8 != 0 || g.ldb % 8 != 0) return DG_ERR_UNSUPPORTED;
+  const int lmul = g.fp8 ? 16 : 8;
+  if (g.k <= 0 || g.lda % lmul != 0 || g.ldb % lmul != 0) return DG_ERR_UNSUPPORTED;
   if (((uintptr_t)g.a_hi | (uintptr_t)g.b_hi) & 15) return DG_ERR_UNSUPPORTED;
+  if (g.fp8 && (g.terms != 1 || !g.a_scale || !g.b_scale)) return DG_ERR_UNSUPPORTED;
   if (g.terms >= 3 && (((uintptr_t)g.a_lo | (uintptr_t)g.b_lo) & 15)) return DG_ERR_UNSUPPORTED;
   if (g.terms == 6 && (((uintptr_t)g.a_mid | (uintptr_t)g.b_mid) & 15)) return DG_ERR_UNSUPPORTED;
   const int bn = (g.bn == 256 && g.terms != 6) ? 256 : 128;
   TcParams p;
   memset(&p, 0, sizeof p);
-  const bool h = g.fp16 != 0;
-  if (!encode_map(&p.a_hi, g.a_hi, g.k, g.a_rows, g.lda, BM, h) ||
-      !encode_map(&p.b_hi, g.b_hi, g.k, g.b_rows, g.ldb, bn, h)) {
+  const OperandType ty = g.fp8 ? OP_E4M3 : g.fp16 ? OP_FP16 : OP_BF16;
+  if (!encode_map(&p.a_hi, g.a_hi, g.k, g.a_rows, g.lda, BM, ty) ||
+      !encode_map(&p.b_hi, g.b_hi, g.k, g.b_rows, g.ldb, bn, ty)) {
     dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
     return DG_ERR_CUDA;
   }
-  if (g.terms >= 3 && (!encode_map(&p.a_lo, g.a_lo, g.k, g.a_rows, g.lda, BM, h) ||
-                       !encode_map(&p.b_lo, g.b_lo, g.k, g.b_rows, g.ldb, bn, h))) {
+  if (g.terms >= 3 && (!encode_map(&p.a_lo, g.a_lo, g.k, g.a_rows, g.lda, BM, ty) ||
+                       !encode_map(&p.b_lo, g.b_lo, g.k, g.b_rows, g.ldb, bn, ty))) {
     dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
     return DG_ERR_CUDA;
   }
-  if (g.terms == 6 && (!encode_map(&p.a_mid, g.a_mid, g.k, g.a_rows, g.lda, BM, h) ||
-                       !encode_map(&p.b_mid, g.b_mid, g.k, g.b_rows, g.ldb, bn, h))) {
+  if (g.terms == 6 && (!encode_map(&p.a_mid, g.a_mid, g.k, g.a_rows, g.lda, BM, ty) ||
+                       !encode_map(&p.b_mid, g.b_mid, g.k, g.b_rows, g.ldb, bn, ty))) {
     dg_set_last_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled failed");
     return DG_ERR_CUDA;
   }
@@ -567,10 +639,15 @@ int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s) {
   p.layout = g.layout; p.upper = g.upper;
   p.off = g.off; p.nb = g.nb; p.ntot = g.ntot;
   p.status = g.status;
-  p.idesc = idesc_f16kind(BM, bn, h);
+  p.idesc = g.fp8 ? idesc_e4m3(BM, bn) : idesc_f16kind(BM, bn, g.fp16 != 0);
   p.alpha_dev = g.alpha_dev;
-  if (g.terms == 6) return launch<128, 6>(p, s);
+  p.a_scale = g.a_scale;
+  p.b_scale = g.b_scale;
   const int tpc = g.tiles_per_cta;
+  if (g.fp8)
+    return bn == 256 ? launch_persist<256, 1, true>(p, tpc, s)
+                     : launch_persist<128, 1, true>(p, tpc, s);
+  if (g.terms == 6) return launch<128, 6>(p, s);
   if (g.terms == 1)
     return bn == 256 ? launch_persist<256, 1>(p, tpc, s) : launch_persist<128, 1>(p, tpc, s);
   return bn == 256 ? launch_persist<256, 3>(p, tpc, s) : launch_persist<128, 3>(p, tpc, s);
@@ -599,4 +676,47 @@ extern "C" int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const voi
   g.alpha = alpha; g.beta = beta; g.c = C; g.ldc = ldc;
   g.layout = 0; g.upper = 0; g.bn = bn; g.status = status; g.fp16 = fp16;
   return dg::tc_gemm_bf16(g, (cudaStream_t)stream);
+}
+
+// Building-block entry of the FP8 form: C = alpha * A' B + beta * C with FP32
+// K-major operands (A is k x m column-major, B is k x n) cut to E4M3 with a
+// power-of-two scale per vector (split_e4m3) and multiplied on kind::f8f6f4.
+// Allocates stream-ordered scratch for the 8-bit operands and the scales.
+extern "C" int dg_gemm_f8_tc_tn(int m, int n, int k, float alpha, const float *A, int lda,
+                                const float *B, int ldb, float beta, float *C, int ldc,
+                                void *stream) {
+  DG_CHECK_ARG(m >= 0, 1);
+  DG_CHECK_ARG(n >= 0, 2);
+  DG_CHECK_ARG(k > 0, 3);
+  DG_CHECK_ARG(lda >= k, 6);
+  DG_CHECK_ARG(ldb >= k, 8);
+  DG_CHECK_ARG(ldc >= (m > 1 ? m : 1), 11);
+  if (m == 0 || n == 0) return 0;
+  DG_CHECK_ARG(A != nullptr, 5);
+  DG_CHECK_ARG(B != nullptr, 7);
+  DG_CHECK_ARG(C != nullptr, 10);
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long ldk = (k + 15) / 16 * 16;
+  const size_t abytes = ((size_t)ldk * m + 255) & ~(size_t)255;
+  const size_t bbytes = ((size_t)ldk * n + 255) & ~(size_t)255;
+  const size_t sbytes = ((sizeof(float) * ((size_t)m + n)) + 255) & ~(size_t)255;
+  uint8_t *buf = nullptr;
+  DG_CUDA_TRY(dg::pool_malloc_async((void **)&buf, abytes + bbytes + sbytes, s));
+  uint8_t *a8 = buf, *b8 = buf + abytes;
+  float *sa = (float *)(buf + abytes + bbytes), *sb = sa + m;
+  int rc = dg::split_e4m3(A, lda, k, m, a8, ldk, sa, nullptr, nullptr, s);
+  if (!rc) rc = dg::split_e4m3(B, ldb, k, n, b8, ldk, sb, nullptr, nullptr, s);
+  if (!rc) {
+    dg::TcGemmArgs g;
+    memset(&g, 0, sizeof g);
+    g.m = m; g.n = n; g.k = k; g.terms = 1; g.fp8 = 1;
+    g.a_hi = a8; g.lda = (int)ldk; g.a_rows = m;
+    g.b_hi = b8; g.ldb = (int)ldk; g.b_rows = n;
+    g.a_scale = sa; g.b_scale = sb;
+    g.alpha = alpha; g.beta = beta; g.c = C; g.ldc = ldc;
+    g.bn = 128;
+    rc = dg::tc_gemm_bf16(g, s);
+  }
+  cudaFreeAsync(buf, s);
+  return rc;
 }

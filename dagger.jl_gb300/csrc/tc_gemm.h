@@ -1,8 +1,9 @@
-// Internal interface of the tcgen05 BF16 GEMM (tc_gemm.cu).
+// Internal interface of the tcgen05 BF16 / FP16 / FP8 GEMM (tc_gemm.cu).
 #pragma once
 
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 namespace dg {
 
@@ -23,10 +24,18 @@ struct TcParams {
   int *status;         // device status word: non-zero on entry = skip; timeout recorded
   uint32_t idesc;      // tcgen05 instruction descriptor (operand types, M, N)
   const float *alpha_dev;  // when set, alpha is read from device memory
+  // FP8 operands: the product of output (i, j) is multiplied by
+  // a_scale[a_row0 + i] * b_scale[b_row0 + j] (the vectors' power-of-two
+  // scales); null for 16-bit operands
+  const float *a_scale, *b_scale;
 };
 
 struct TcGemmArgs {
   int m, n, k, terms;                 // terms: 1 (bf16), 3 (hi/lo split) or 6 (hi/mid/lo)
+  int fp8;                            // terms 1 with E4M3 operands (one byte per value,
+                                      // lda / ldb in values, multiples of 16) and the
+                                      // per-vector scales a_scale / b_scale
+  const float *a_scale, *b_scale;
   const void *a_hi, *a_lo;            // K-major BF16 panels
   const void *a_mid, *b_mid;          // terms 6: the middle slices
   int lda, a_rows, a_row0;
@@ -49,5 +58,12 @@ struct TcGemmArgs {
 };
 
 int tc_gemm_bf16(const TcGemmArgs &g, cudaStream_t s);
+
+// E4M3 copy of ncols FP32 vectors of length k (vector c at src + c * ld), a
+// power-of-two scale per vector (dst values = v / scale[c], the largest in
+// [128, 256)), dst vector c at dst + c * ldd.  Skips when *a1 or *a2 is
+// non-zero (either may be null).
+int split_e4m3(const float *src, long long ld, int k, int ncols, uint8_t *dst, long long ldd,
+               float *scale, const int *a1, const int *a2, cudaStream_t s);
 
 }  // namespace dg

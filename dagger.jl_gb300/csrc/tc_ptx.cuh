@@ -111,6 +111,23 @@ __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_
       : "memory");
 }
 
+// Instruction descriptor of kind::f8f6f4 with E4M3 A and B (format 0 in
+// both fields), FP32 accumulation, K-major operands, M x N.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int m, int bn) {
+  return (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// D (+)= A B' with 8-bit operands: K = 32 values (32 bytes) per instruction.
+__device__ __forceinline__ void mma_f8(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                       uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))

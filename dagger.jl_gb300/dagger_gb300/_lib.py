@@ -60,7 +60,7 @@ class DgIrReport(ctypes.Structure):
                 ("converged", c_int), ("backward_error", c_double), ("solve_ms", ctypes.c_float)]
 
 
-DG_PREC = {"bf16": 1, "bf16x3": 3, "bf16x6": 6, "fp16": 11, "fp16x3": 13, "fp32": 32}
+DG_PREC = {"bf16": 1, "bf16x3": 3, "bf16x6": 6, "fp8": 8, "fp16": 11, "fp16x3": 13, "fp32": 32}
 
 # name -> (restype, argtypes); every symbol include/dagger_gb300.h declares.
 SIGNATURES = {
@@ -131,6 +131,8 @@ SIGNATURES = {
                               c_void_p]),
     "dg_gemm_f32_tc_tn": (c_int, [c_int, c_int, c_int, ctypes.c_float, c_dp, c_int, c_dp, c_int,
                                   ctypes.c_float, c_dp, c_int, c_void_p]),
+    "dg_gemm_f8_tc_tn": (c_int, [c_int, c_int, c_int, ctypes.c_float, c_dp, c_int, c_dp, c_int,
+                                 ctypes.c_float, c_dp, c_int, c_void_p]),
     "dg_potrf_inv_f32": (c_int, [c_int, c_dp, c_int, c_dp, c_int, ctypes.POINTER(c_int),
                                  c_void_p]),
     "dg_gemm_f64_emulated_tn": (c_int, [c_int, c_int, c_int, c_double, c_void_p, c_int, c_void_p,

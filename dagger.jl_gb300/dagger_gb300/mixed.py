@@ -8,8 +8,9 @@ solutions are refined in FP64 (iterative refinement, switching to GMRES-IR
 when refinement stalls) until the normwise backward error of every column is
 at most `tol`.  Precisions: 'bf16', 'bf16x3' (hi/lo split, three products),
 'bf16x6' (hi/mid/lo split, six products: FP32-accurate tensor-core updates),
-'fp16', 'fp16x3' (with per-panel power-of-two scaling) and 'fp32' (CUDA-core
-FP32 updates).
+'fp8' (E4M3 with a power-of-two scale per vector, one product at twice the
+BF16 rate: for well-conditioned matrices), 'fp16', 'fp16x3' (with per-panel
+power-of-two scaling) and 'fp32' (CUDA-core FP32 updates).
 """
 from __future__ import annotations
 
@@ -37,8 +38,8 @@ class MixedCholesky:
 
     # first diagonal shift tried when the low-precision factorization breaks
     # down (about the operand precision's unit roundoff), grown 10x per retry
-    SHIFT0 = {"bf16": 4e-3, "bf16x3": 1e-5, "bf16x6": 1e-7, "fp16": 5e-4, "fp16x3": 1e-6,
-              "fp32": 1e-7}
+    SHIFT0 = {"bf16": 4e-3, "bf16x3": 1e-5, "bf16x6": 1e-7, "fp8": 3e-2, "fp16": 5e-4,
+              "fp16x3": 1e-6, "fp32": 1e-7}
 
     def __init__(self, A: DArray, precision: str = "bf16x3", stream=None, check_: bool = True,
                  auto_shift: bool = True, shift: float = 0.0, max_shift_retries: int = 4):

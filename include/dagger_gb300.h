@@ -294,6 +294,9 @@ int dg_get_f64_engine(void);
 #define DG_PREC_FP32 32   /* FP32 CUDA-core trailing updates                */
 #define DG_PREC_BF16X6 6  /* BF16 hi/mid/lo split, six products: FP32-accurate
                              tensor-core trailing updates                    */
+#define DG_PREC_FP8 8     /* FP8 E4M3 operands with a power-of-two scale per
+                             vector, one kind::f8f6f4 product (4 significant
+                             bits: for well-conditioned matrices)            */
 
 typedef struct dg_mixed dg_mixed;
 
@@ -360,6 +363,15 @@ int dg_gemm_tc_tn(int m, int n, int k, int terms, int fp16, const void *a_hi, co
  * scratch for the slices. */
 int dg_gemm_f32_tc_tn(int m, int n, int k, float alpha, const float *A, int lda, const float *B,
                       int ldb, float beta, float *C, int ldc, void *stream);
+
+/* The FP8 form of the same product: C = alpha A'B + beta C with FP32 K-major
+ * operands (A k x m, B k x n, column-major) cut to E4M3 with a power-of-two
+ * scale per vector (each vector's largest magnitude in [128, 256) before
+ * rounding) and multiplied by one tcgen05.mma kind::f8f6f4 per K step of 32;
+ * the scales are applied to the FP32 accumulators.  Each operand value keeps
+ * 4 significant bits.  Allocates stream-ordered scratch. */
+int dg_gemm_f8_tc_tn(int m, int n, int k, float alpha, const float *A, int lda, const float *B,
+                     int ldb, float beta, float *C, int ldc, void *stream);
 
 /* The diagonal-block kernel of the mixed factor (no counterpart in the
  * reference): the FP32 Cholesky factor U (A = U'U, upper, in place) of one

@@ -94,3 +94,61 @@ def test_gemm_f32_tc(m, n, k):
     ref = -0.5 * (a @ b.T) + 2.0 * C0.double().T
     bound = 4e-6 * 0.5 * (a.abs() @ b.abs().T) + 2e-7 * (2.0 * C0.double().T).abs() + 1e-30
     assert ((C.double().T - ref).abs() / bound).max().item() <= 1.0
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 128), (1000, 700, 1024), (1024, 4000, 1024),
+                                   (5, 3, 16), (300, 129, 136)])
+def test_gemm_f8_tc(m, n, k):
+    """E4M3 operands with a power-of-two scale per vector, one kind::f8f6f4
+    product, scales applied to the FP32 accumulators: each operand value is
+    rounded to 4 significant bits (relative error <= 2^-4), values below
+    E4M3's normal range (2^-6 after scaling the vector's largest magnitude
+    into [128, 256)) to an absolute 2^-10 of the scaled range."""
+    import torch
+    import dagger_gb300 as d
+    g = torch.Generator(device="cuda")
+    g.manual_seed(m + 2 * n + k)
+    A = torch.randn(m, k, device="cuda", generator=g)   # column-major k x m
+    B = torch.randn(n, k, device="cuda", generator=g)
+    A[:, : k // 2] *= 1e3                              # mixed magnitudes along K
+    B[: n // 2] *= 1e-20                               # vectors far from 1 in scale
+    C0 = torch.randn(n, m, device="cuda", generator=g)
+    C = C0.clone()
+    rc = d.lib().dg_gemm_f8_tc_tn(m, n, k, -0.5, A.data_ptr(), k, B.data_ptr(), k, 2.0,
+                                  C.data_ptr(), m, _stream())
+    assert rc == 0, d._lib.last_error()
+    torch.cuda.synchronize()
+    a, b = A.double(), B.double()
+    ref = -0.5 * (a @ b.T) + 2.0 * C0.double().T
+    amax = a.abs().amax(dim=1, keepdim=True)            # m x 1
+    bmax = b.abs().amax(dim=1, keepdim=True).T          # 1 x n
+    sub = 2.0 ** -15 * (amax * b.abs().sum(dim=1, keepdim=True).T
+                        + a.abs().sum(dim=1, keepdim=True) * bmax)
+    bound = 0.5 * (0.1329 * (a.abs() @ b.abs().T) + sub) + 2e-7 * (2.0 * C0.double().T).abs()
+    err = (C.double().T - ref).abs()
+    assert (err <= bound + 1e-30).all().item(), (err / (bound + 1e-30)).max().item()
+    # the rounding errors are not systematic: the typical error is far below the bound
+    rel = (err / (0.5 * (a.abs() @ b.abs().T) + 1e-300)).median().item()
+    assert rel <= 2e-2, rel
+
+
+def test_gemm_f8_tc_nonfinite():
+    """A vector holding an infinity or a NaN makes every product with it NaN."""
+    import torch
+    import dagger_gb300 as d
+    m, n, k = 256, 128, 64
+    A = torch.randn(m, k, device="cuda")
+    B = torch.randn(n, k, device="cuda")
+    A[7, 3] = float("inf")
+    B[5, 0] = float("nan")
+    C = torch.zeros(n, m, device="cuda")
+    rc = d.lib().dg_gemm_f8_tc_tn(m, n, k, 1.0, A.data_ptr(), k, B.data_ptr(), k, 0.0,
+                                  C.data_ptr(), m, _stream())
+    assert rc == 0
+    torch.cuda.synchronize()
+    Ct = C.T
+    assert torch.isnan(Ct[7]).all().item() and torch.isnan(Ct[:, 5]).all().item()
+    mask = torch.ones(m, n, dtype=torch.bool, device="cuda")
+    mask[7] = False
+    mask[:, 5] = False
+    assert torch.isfinite(Ct[mask]).all().item()
