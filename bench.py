@@ -878,6 +878,7 @@ def bench_lu(args, d, dev, stream):
     (uniform [0, 1), seeded).  2/3 N^3 flops per factorization, 2 N^2 per
     vector solve.  Checked on the GPU: P A v against L (U v) for two probe
     vectors, and the solve's normwise backward error."""
+    import numpy as np
     import torch
     n, nb = args.n, args.nb
     g = torch.Generator(device=dev)
@@ -925,6 +926,7 @@ def bench_lu(args, d, dev, stream):
     torch.cuda.empty_cache()
     flops = 2.0 * n ** 3 / 3.0
     cpu = None
+    context = None
     try:  # the oracle's threaded restatement of the reference's CPU path, a bounded sample
         from oracle import lu as olu
         from oracle import native
@@ -935,6 +937,34 @@ def bench_lu(args, d, dev, stream):
         t0 = time.perf_counter()
         Fc, pc, _ = native.lu_tiled(Ac, cnb, nthreads=cores, inplace=True)
         tc = time.perf_counter() - t0
+        # The probe residual on the same matrix, factored here and by the
+        # CPU restatement (the reference's algorithm with LAPACK tiles): the
+        # residual of partial pivoting on rand(N, N) grows with N, so the
+        # line's N = 32768 figure is read against this pair.
+        Ag = torch.from_numpy(np.ascontiguousarray(olu.rand_uniform(cn, cn, args.seed)))
+        Ag = Ag.to(dev)
+        DC = d.DArray.from_array(Ag, d.Blocks(cnb, cnb))
+        Fg = d.lu_(DC, stream=stream)
+        vg = torch.randn(cn, 2, generator=g, device=dev, dtype=torch.float64)
+        Fgd = Fg.factors.collect()
+        Ug = torch.triu(Fgd) @ vg
+        LUg = torch.tril(Fgd, -1) @ Ug + Ug
+        PAg = Ag[Fg.p.to(dev)] @ vg
+        r_gpu = float(((PAg - LUg).abs().max() / PAg.abs().max()).item())
+        del Fgd, Ug, LUg, PAg, DC, Fg
+        vc = vg.cpu().numpy()
+        Lc = np.tril(Fc, -1) + np.eye(cn)
+        Uc = np.triu(Fc)
+        perm = np.arange(cn)
+        for t_, q_ in enumerate(pc - 1):
+            perm[t_], perm[q_] = perm[q_], perm[t_]
+        A8 = Ag.cpu().numpy()
+        PAc = A8[perm] @ vc
+        r_cpu = float(np.abs(PAc - Lc @ (Uc @ vc)).max() / np.abs(PAc).max())
+        context = {"n": cn, "matrix": "rand(N, N), the same matrix on both", "gpu": r_gpu,
+                   "cpu_restatement": r_cpu,
+                   "note": "max|P A v - L U v| / max|P A v| for two Gaussian probe vectors"}
+        del Ag, A8, Lc, Uc, PAc
         cpu = {"value": 2.0 * cn ** 3 / 3.0 / tc / 1e12, "unit": "TFLOP/s", "cores": cores,
                "kind": "port",
                "sample": f"CPU restatement of the Dagger datadeps lu!(A, RowMaximum()) (LAPACK "
@@ -949,6 +979,7 @@ def bench_lu(args, d, dev, stream):
             "value": flops / t / 1e12, "unit": "TFLOP/s", "ms": 1e3 * t,
             "solve_ms": 1e3 * ts, "factor_and_solve_tflops": (flops + 2.0 * n * n) / (t + ts) / 1e12,
             "n": n, "nb": nb, "engine": args.f64_engine, "probe_rel_residual": res,
+            "probe_rel_residual_context": context,
             "solve_backward_error": berr, "cpu_baseline": cpu,
             "dominant_kernel": "oz_gemm_kernel (trailing updates, the headline roofline's "
                                "kernel); the panel (lu_leaf_kernel + recursion) is the "

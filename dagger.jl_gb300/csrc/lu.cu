@@ -47,7 +47,10 @@ constexpr int kLeafWarps = kLeafThreads / 32;
 constexpr int kLeafMaxRows = 768;      // rows one CTA keeps in shared memory
 constexpr int kLeafMaxGrid = 96;       // CTAs of a leaf launch at most (their candidate rows
                                        // sit in shared memory beside the strip)
-constexpr int kLeafRowsTarget = 384;
+#ifndef DG_LU_LEAF_ROWS
+#define DG_LU_LEAF_ROWS 384
+#endif
+constexpr int kLeafRowsTarget = DG_LU_LEAF_ROWS;  // rows per CTA a leaf aims for
 constexpr int kLeafSwapMax = 2 * kLeafW;
 constexpr int kListHash = 4096;        // >= 4 x the pivots of the widest panel
 constexpr int kMaxPanelPivots = 1024;

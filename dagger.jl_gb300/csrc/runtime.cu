@@ -524,7 +524,8 @@ int run_task(const dg_task &t, int *info, cudaStream_t s) {
                          : (t.side == 'B') ? slot_diag(t.b, t.lda, t.ldb) : nullptr;
       return oz_gemm(t.m, t.n, t.k, t.alpha, t.a, t.lda, sstride, ea, t.b, t.lda, sstride, eb,
                      t.beta, t.c, t.ldc, tri, info, s, nullptr, ds, t.side == 'A' ? 1 : 2,
-                     t.diag == 'P' ? kOzBlocksPerCta : 1);
+                     t.diag == 'P' ? kOzBlocksPerCta
+                     : (t.diag >= '2' && t.diag <= '9') ? t.diag - '0' : 1);
     }
     case DG_OP_COPY:
       if (t.m <= 0 || t.n <= 0) return 0;
@@ -1778,6 +1779,11 @@ LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated) {
     L.winv = off;
     off += (size_t)kOzRingDepth * L.winv_bytes;
   }
+  // the pivots as the region writes them; copied to the caller's ipiv after
+  // the region, outside its graph (whose cache key then does not hold the
+  // caller's buffer: a new ipiv per call replays the same graph)
+  L.ipiv = off;
+  off += r256((size_t)mn * 8);
   L.total = off;
   return L;
 }
@@ -1793,6 +1799,16 @@ LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated) {
 // step (ring slots (k mod depth, i) and (k mod depth, mt + j)) and every
 // trailing tile takes one emulated product; each row panel tile is one
 // emulated product with the inverse of L(k, k).
+#ifndef DG_LU_GEMM_BLOCKS
+#define DG_LU_GEMM_BLOCKS 3
+#endif
+// Output blocks per CTA of the LU's trailing updates (2..9; 1: one each).
+// Three: a CTA forms one block's outputs while the tensor cores run the next,
+// and still hands its SM back within about 0.15 ms to a leaf, which needs
+// ~85 SMs at once (N = 32768: 874 ms against 897 with one block per CTA,
+// 929 with six).
+constexpr int kLuGemmBlocks = DG_LU_GEMM_BLOCKS;
+
 void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, bool pivot,
                      void *ws, long long *ipiv, bool emulated) {
   const int mt = (m + nb - 1) / nb, nt = (n + nb - 1) / nb, steps = mt < nt ? mt : nt;
@@ -1912,11 +1928,12 @@ void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, b
       for (int i = k + 1; i < mt; i++) {  // A(i, j) -= L(i, k) U(k, j)
         memset(&t, 0, sizeof t);
         if (emulated) {
-          // one output block per CTA: short CTAs hand their SMs back soon to
-          // the panel's leaves, which need many SMs at once
+          // a few output blocks per CTA (kLuGemmBlocks): short CTAs hand their
+          // SMs back soon to the panel's leaves, which need many SMs at once
           t.op = OP_OZ_GEMM; t.uplo = 'N'; t.m = rows(i); t.n = cols(j); t.k = kk;
           t.alpha = -1.0; t.beta = 1.0; t.a = slot(k, i); t.b = slot(k, mt + j);
           t.lda = ldk; t.ldb = nb; t.c = T(i, j); t.ldc = rows(i);
+          if (kLuGemmBlocks > 1) t.diag = (char)('0' + kLuGemmBlocks);
         } else {
           t.op = DG_OP_GEMM; t.transa = 'N'; t.transb = 'N'; t.m = rows(i); t.n = cols(j);
           t.k = kk; t.alpha = -1.0; t.beta = 1.0; t.a = T(i, k); t.lda = rows(i);
@@ -1936,7 +1953,11 @@ size_t lu_solve_bytes(int n, int nb, int nrhs, bool emulated) {
     const int w = (c + 1) * nb <= nrhs ? nb : nrhs - c * nb;
     b += r256((size_t)n * w * 8);
   }
-  return b;
+  return b + r256((size_t)n * 8);  // the pivots, copied in before the region
+}
+
+size_t lu_solve_ipiv_offset(int n, int nb, int nrhs, bool emulated) {
+  return lu_solve_bytes(n, nb, nrhs, emulated) - r256((size_t)n * 8);
 }
 
 // linalg.jl:264-308: B's rows permuted by the pivots (one permutation
@@ -2285,12 +2306,18 @@ extern "C" int dg_lu_tiled(int m, int n, int nb, double *const *tiles, int pivot
   DG_TRY(lease.acquire(L.total, (cudaStream_t)stream, &ws));
   cudaStream_t s = (cudaStream_t)stream;
   DG_TRY(lu_words_reset(ws, s));
+  long long *wpiv = (long long *)((char *)ws + L.ipiv);
   const int rc = dg::region_run_cached(
-      lu_key(30, m, n, nb, 0, pivot, emulated, ws, ipiv, tiles, (size_t)mt * nt, nullptr, 0),
-      [&](dg_region *r) { dg::build_lu_region(r, m, n, nb, tiles, pivot != 0, ws, ipiv, emulated); },
+      lu_key(30, m, n, nb, 0, pivot, emulated, ws, nullptr, tiles, (size_t)mt * nt, nullptr, 0),
+      [&](dg_region *r) { dg::build_lu_region(r, m, n, nb, tiles, pivot != 0, ws, wpiv, emulated); },
       s, true);
   if (rc) return rc;
-  if (!pivot) DG_TRY(dg::lu_iota(ipiv, m < n ? m : n, s));
+  const int mn = m < n ? m : n;
+  if (pivot)
+    DG_CUDA_TRY(cudaMemcpyAsync(ipiv, wpiv, sizeof(long long) * (size_t)mn,
+                                cudaMemcpyDeviceToDevice, s));
+  else
+    DG_TRY(dg::lu_iota(ipiv, mn, s));
   return lu_words_read(ws, s);
 }
 
@@ -2310,11 +2337,17 @@ extern "C" int dg_lu_solve_tiled(int n, int nb, double *const *tiles, const long
   dg::WsLease lease;
   void *ws = nullptr;
   DG_TRY(lease.acquire(dg::lu_solve_bytes(n, nb, nrhs, emulated), (cudaStream_t)stream, &ws));
+  // the pivots enter through the workspace, so that the graph does not hold
+  // the caller's ipiv buffer
+  long long *wpiv =
+      (long long *)((char *)ws + dg::lu_solve_ipiv_offset(n, nb, nrhs, emulated));
+  DG_CUDA_TRY(cudaMemcpyAsync(wpiv, ipiv, sizeof(long long) * (size_t)n,
+                              cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
   return dg::region_run_cached(
-      lu_key(31, n, n, nb, nrhs, 1, emulated, ws, ipiv, tiles, (size_t)mt * mt, btiles,
+      lu_key(31, n, n, nb, nrhs, 1, emulated, ws, nullptr, tiles, (size_t)mt * mt, btiles,
              (size_t)mt * bnt),
       [&](dg_region *r) {
-        dg::build_lu_solve_region(r, n, nb, tiles, ipiv, nrhs, btiles, ws, emulated);
+        dg::build_lu_solve_region(r, n, nb, tiles, wpiv, nrhs, btiles, ws, emulated);
       },
       (cudaStream_t)stream, true);
 }

@@ -29,7 +29,8 @@ constexpr int kTransferLevel = kPrioLevels, kTransferStreams = 4;
 //   OP_OZ_GEMM   a, b = slice slots (lda = ldk, ldb = slot capacity), c = FP64
 //                tile (ldc), m x n output, k = K, alpha, beta; uplo 'U' / 'L'
 //                stores one triangle; diag 'P' (off the critical path): each
-//                CTA computes kOzBlocksPerCta output blocks in turn
+//                CTA computes kOzBlocksPerCta output blocks in turn; diag
+//                '2'..'9': that many blocks per CTA
 //   OP_OZ_TRSM   DG_OP_TRSM whose recursion updates are emulated, with
 //   OP_OZ_POTRF  (likewise DG_OP_POTRF) b = slice scratch of ldb * 256 bytes
 //   OP_OZ_ZERO   c (m x n, ldc) = 0
@@ -167,7 +168,7 @@ void build_cholesky_region(dg_region *r, char uplo, int n, int nb, double *const
 // the slice slots of the trailing updates.
 struct LuLayout {
   size_t status = 0, info = 4, leaf = 256, lpiv = 0, lists = 0, panel = 0, panel_bytes = 0,
-         ozp = 0, ozp_bytes = 0, ring = 0, winv = 0, winv_bytes = 0, total = 0;
+         ozp = 0, ozp_bytes = 0, ring = 0, winv = 0, winv_bytes = 0, ipiv = 0, total = 0;
   int list_cap = 0;        // entries of one step's destination (and source) list
   size_t list_stride = 0;  // ints per step
 };
@@ -175,7 +176,9 @@ LuLayout lu_layout(int m, int n, int nb, bool pivot, bool emulated);
 // The datadeps region of lu!(A, RowMaximum()) (pivot) or lu!(A, NoPivot())
 // (src/array/lu.jl:5-54, 306-410) over the mt x nt tile grid; ws holds
 // lu_layout(m, n, nb, pivot, emulated).total bytes; ipiv (device, min(m, n)
-// int64) receives the global 1-based pivots.
+// int64) receives the global 1-based pivots (the entry point passes the
+// workspace's copy, so that the graph does not depend on the caller's
+// buffer).
 void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, bool pivot,
                      void *ws, long long *ipiv, bool emulated);
 // ldiv!(F::LU, B) (linalg.jl:264-308): B's rows permuted by ipiv, then the
@@ -183,6 +186,8 @@ void build_lu_region(dg_region *r, int m, int n, int nb, double *const *tiles, b
 // emulated) bytes (the permutation, the permuted block columns, the slice
 // slots of the emulated updates).
 size_t lu_solve_bytes(int n, int nb, int nrhs, bool emulated);
+// Offset of the pivots' copy in that workspace.
+size_t lu_solve_ipiv_offset(int n, int nb, int nrhs, bool emulated);
 void build_lu_solve_region(dg_region *r, int n, int nb, double *const *tiles,
                            const long long *ipiv, int nrhs, double *const *btiles, void *ws,
                            bool emulated);
