@@ -70,7 +70,10 @@ constexpr int OP_LU_ROWS = 112;
 constexpr int OP_LU_LINV = 113;
 constexpr int kOpLast = OP_LU_LINV;
 constexpr int kOzRingDepth = 3;  // steps whose slices can be live at once
-constexpr int kOzBlocksPerCta = 6;
+#ifndef DG_OZ_BLOCKS_PER_CTA
+#define DG_OZ_BLOCKS_PER_CTA 6
+#endif
+constexpr int kOzBlocksPerCta = DG_OZ_BLOCKS_PER_CTA;
 size_t oz_slot_bytes(long long ldk, long long cap);
 size_t oz_ring_bytes_for(int n, int nb);
 
