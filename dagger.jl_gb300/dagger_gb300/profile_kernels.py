@@ -13,6 +13,9 @@ a profiler can capture exactly that kernel (ncu -k regex:<name> -c N).
     python -m dagger_gb300.profile_kernels diag       [--nb 1024]
     python -m dagger_gb300.profile_kernels tc6        [--m 8192] [--k 1024]
     python -m dagger_gb300.profile_kernels reblock    [--m 8192]
+    python -m dagger_gb300.profile_kernels tc_f8      [--m 8192] [--k 1024]
+    python -m dagger_gb300.profile_kernels lu_tiled   [--m 8192] [--nb 1024]
+    python -m dagger_gb300.profile_kernels mixed      [--m 8192] [--nb 1024] [--prec fp32]
 
 gemm_f64   the FP64 trailing-update tile GEMM of the plain path,
            C(nb x nb) -= A' B with nb x nb tiles (2 nb^3 flops per launch)
@@ -40,6 +43,13 @@ tc6        the FP32-accurate tensor-core product C(m x 64) = A'B, K = k, of the
            mixed form's solves (split3_kernel, tc_gemm_kernel<128, 6>)
 reblock    copyto! between Blocks(1024, 1024) and Blocks(1000, 1000) of an m x m
            matrix (reblock_kernel; 16 bytes per element)
+tc_f8      the FP8 product C(m x m) = A'A, K = k (dg_gemm_f8_tc_tn: e4m3_kernel,
+           tc_gemm_persist_kernel<128, 1, true>; 2 m^2 k flops at the FP8 rate)
+lu_tiled   lu!(A, RowMaximum()) of an m x m rand matrix, Blocks(nb, nb), emulated
+           engine (dg_lu_tiled: leaves, lu_laswp_kernel, emulated updates); the
+           matrix is restored before every call
+mixed      the mixed factor of an m x m SPD matrix (G G'/m + I) with the given
+           operand precision (fp32: gemm_fma<float> trailing updates)
 Each prints the per-launch time measured with CUDA events.
 """
 from __future__ import annotations
@@ -68,13 +78,14 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("kernel", choices=["gemm_f64", "tc_gemm", "trsm_f64", "batched", "oz_gemm",
                                        "oz_slices", "lu_panel", "potrf_f64", "herm", "diag", "tc6",
-                                       "reblock"])
+                                       "reblock", "tc_f8", "lu_tiled", "mixed"])
     ap.add_argument("--nb", type=int, default=1024)
     ap.add_argument("--m", type=int, default=8192)
     ap.add_argument("--k", type=int, default=1024)
     ap.add_argument("--terms", type=int, default=3)
     ap.add_argument("--count", type=int, default=2000)
     ap.add_argument("--reps", type=int, default=4)
+    ap.add_argument("--prec", default="fp32")
     a = ap.parse_args(argv)
     L = _lib.lib()
     s = _stream(None)
@@ -185,6 +196,48 @@ def main(argv=None):
             L.dg_potrf_inv_f32(nb, M.data_ptr(), nb, V.data_ptr(), nb, ctypes.byref(info), s)
         ms = _time(call, a.reps)
         print(f"diag {nb}: {ms * 1e3:.1f} us/call (info {info.value})")
+    elif a.kernel == "tc_f8":
+        m, k = a.m, a.k
+        A = torch.randn(m, k, device=dev)
+        C = torch.zeros(m, m, device=dev)
+        ms = _time(lambda: L.dg_gemm_f8_tc_tn(m, m, k, -1.0, A.data_ptr(), k, A.data_ptr(), k,
+                                              1.0, C.data_ptr(), m, s), a.reps)
+        print(f"tc_f8 m={m} k={k}: {ms * 1e3:.1f} us/call (with the two conversions), "
+              f"{2.0 * m * m * k / ms / 1e9:.1f} FP8 TFLOP/s")
+    elif a.kernel == "lu_tiled":
+        from . import linalg
+        from .darray import Blocks, DArray
+        old = linalg.set_f64_engine("emulated")
+        g = torch.Generator(device=dev)
+        g.manual_seed(5)
+        A0 = torch.rand(a.m, a.m, generator=g, device=dev, dtype=torch.float64)
+        D0 = DArray.from_array(A0, Blocks(a.nb, a.nb))
+        DA = D0.copy()
+
+        def call():
+            DA.storage.copy_(D0.storage)
+            linalg.lu_(DA, check_=False)
+        ms = _time(call, a.reps)
+        linalg.set_f64_engine(old)
+        print(f"lu_tiled m={a.m} nb={a.nb}: {ms:.2f} ms/call, "
+              f"{2.0 * a.m ** 3 / 3.0 / ms / 1e9:.2f} TFLOP/s")
+    elif a.kernel == "mixed":
+        from .darray import Blocks, DArray
+        from .mixed import cholesky_mixed
+        g = torch.Generator(device=dev)
+        g.manual_seed(7)
+        G = torch.randn(a.m, a.m, generator=g, device=dev, dtype=torch.float64)
+        A = G @ G.T / a.m
+        A.diagonal().add_(1.0)
+        del G
+        DA = DArray.from_array(A, Blocks(a.nb, a.nb))
+        del A
+
+        def call():
+            cholesky_mixed(DA, a.prec, stream=torch.cuda.current_stream()).close()
+        ms = _time(call, a.reps)
+        print(f"mixed {a.prec} m={a.m}: {ms:.2f} ms per factorization, "
+              f"{a.m ** 3 / 3.0 / ms / 1e9:.2f} TFLOP/s")
     elif a.kernel == "tc6":
         m, k, r = a.m, a.k, 64
         A = torch.randn(m, k, device=dev)
