@@ -2119,6 +2119,25 @@ extern "C" int dg_cholesky_tiled(char uplo, int n, int nb, double *const *tiles,
       (cudaStream_t)stream, true);
 }
 
+// The kept inverses of the diagonal tiles are formed in the stream's
+// workspace, after the slice slots, and copied to the caller's winv once the
+// region has run: the region's graph then holds only workspace addresses, so
+// a new winv buffer per call replays the cached graph (mt nb^2 doubles, about
+// 0.1 ms of copy at N = 32768).
+static size_t winv_ring_bytes(int n, int nb) {
+  const size_t mt = (size_t)((n + nb - 1) / nb);
+  return ((dg::oz_ring_bytes_for(n, nb) + 255) & ~(size_t)255) + mt * nb * nb * 8;
+}
+static double *winv_in_ring(void *ring, int n, int nb) {
+  return (double *)((char *)ring + ((dg::oz_ring_bytes_for(n, nb) + 255) & ~(size_t)255));
+}
+static int winv_copy_out(double *winv, const double *wws, int n, int nb, cudaStream_t s) {
+  const size_t mt = (size_t)((n + nb - 1) / nb);
+  DG_CUDA_TRY(cudaMemcpyAsync(winv, wws, mt * nb * nb * 8, cudaMemcpyDeviceToDevice, s));
+  DG_CUDA_TRY(cudaStreamSynchronize(s));
+  return 0;
+}
+
 extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *tiles,
                                       double *winv, void *stream) {
   DG_CHECK_ARG(is_one_of(uplo, "ULul"), 1);
@@ -2130,11 +2149,15 @@ extern "C" int dg_cholesky_tiled_winv(char uplo, int n, int nb, double *const *t
   if (n == 0) return 0;
   dg::WsLease lease;
   void *ring = nullptr;
-  DG_TRY(lease.acquire(dg::oz_ring_bytes_for(n, nb), (cudaStream_t)stream, &ring));
-  return dg::region_run_cached(
-      call_key(2, uplo, n, nb, 0, 0, ring, winv, nullptr, tiles, nullptr),
-      [&](dg_region *r) { dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, winv); },
+  DG_TRY(lease.acquire(winv_ring_bytes(n, nb), (cudaStream_t)stream, &ring));
+  double *wws = winv_in_ring(ring, n, nb);
+  const int rc = dg::region_run_cached(
+      call_key(2, uplo, n, nb, 0, 0, ring, wws, nullptr, tiles, nullptr),
+      [&](dg_region *r) { dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, wws); },
       (cudaStream_t)stream, true);
+  if (rc < 0) return rc;
+  DG_TRY(winv_copy_out(winv, wws, n, nb, (cudaStream_t)stream));
+  return rc;
 }
 
 extern "C" int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *host,
@@ -2154,14 +2177,20 @@ extern "C" int dg_cholesky_tiled_host(char uplo, int n, int nb, const double *ho
   if (winv && !emulated) return DG_ERR_UNSUPPORTED;
   dg::WsLease lease;
   void *ring = nullptr;
-  if (emulated) DG_TRY(lease.acquire(dg::oz_ring_bytes_for(n, nb), (cudaStream_t)stream, &ring));
-  return dg::region_run_cached(
-      call_key(3, uplo, n, nb, 0, ldh, ring, winv, host, tiles, nullptr),
+  if (emulated)
+    DG_TRY(lease.acquire(winv ? winv_ring_bytes(n, nb) : dg::oz_ring_bytes_for(n, nb),
+                         (cudaStream_t)stream, &ring));
+  double *wws = winv ? winv_in_ring(ring, n, nb) : nullptr;
+  const int rc = dg::region_run_cached(
+      call_key(3, uplo, n, nb, 0, ldh, ring, wws, host, tiles, nullptr),
       [&](dg_region *r) {
         dg::build_upload_tasks(r, uplo, n, nb, tiles, host, ldh);
-        dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, winv);
+        dg::build_cholesky_region(r, uplo, n, nb, tiles, ring, wws);
       },
       (cudaStream_t)stream, true);
+  if (rc < 0 || !winv) return rc;
+  DG_TRY(winv_copy_out(winv, wws, n, nb, (cudaStream_t)stream));
+  return rc;
 }
 
 extern "C" int dg_cholesky_solve_tiled_winv(char uplo, int n, int nb, double *const *tiles,
