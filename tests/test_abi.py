@@ -147,3 +147,24 @@ def test_invalid_arguments_are_reported_without_a_gpu():
     assert L.dg_syrk(b'U', b'T', -1, 1, 1.0, None, 1, 0.0, None, 1, None) == -3
     assert L.dg_cholesky_tiled(b'Q', 4, 2, None, None) == -1
     assert "invalid argument" in _lib.last_error()
+
+
+def test_invalid_arguments_of_the_newer_entry_points():
+    """The tensor-core building blocks, the LU and the checks validate their
+    arguments before any CUDA call as well."""
+    from dagger_gb300 import _lib
+    L = _lib.lib()
+    # m < 0, lda < k, ldb < k, ldc < m
+    assert L.dg_gemm_f8_tc_tn(-1, 4, 16, 1.0, None, 16, None, 16, 0.0, None, 1, None) == -1
+    assert L.dg_gemm_f8_tc_tn(4, 4, 16, 1.0, None, 8, None, 16, 0.0, None, 4, None) == -6
+    assert L.dg_gemm_f8_tc_tn(4, 4, 16, 1.0, None, 16, None, 8, 0.0, None, 4, None) == -8
+    assert L.dg_gemm_f8_tc_tn(4, 4, 16, 1.0, None, 16, None, 16, 0.0, None, 2, None) == -11
+    # empty products do nothing and succeed
+    assert L.dg_gemm_f8_tc_tn(0, 4, 16, 1.0, None, 16, None, 16, 0.0, None, 1, None) == 0
+    assert L.dg_gemm_f32_tc_tn(-1, 4, 16, 1.0, None, 16, None, 16, 0.0, None, 1, None) == -1
+    # LU: nb <= 0, a pivot flag other than 0 / 1
+    assert L.dg_lu_tiled(4, 4, 0, None, 1, None, None) == -3
+    assert L.dg_lu_tiled(4, 4, 2, None, 2, None, None) == -5
+    # chkfinite of an m x n grid: mb <= 0
+    assert L.dg_chkfinite_tiled_mn(4, 4, 0, 2, None, None) == -3
+    assert L.dg_ishermitian_tiled(-1, 2, None, None) == -1
