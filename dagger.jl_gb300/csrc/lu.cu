@@ -41,7 +41,11 @@
 namespace dg {
 namespace {
 
-constexpr int kLeafW = 32;             // columns of one leaf launch
+#ifndef DG_LU_LEAF_W
+#define DG_LU_LEAF_W 32
+#endif
+constexpr int kLeafW = DG_LU_LEAF_W;    // columns of one leaf launch (16 or 32)
+static_assert(kLeafW == 16 || kLeafW == 32, "a leaf is 16 or 32 columns wide");
 constexpr int kLeafThreads = 256;
 constexpr int kLeafWarps = kLeafThreads / 32;
 constexpr int kLeafMaxRows = 768;      // rows one CTA keeps in shared memory
