@@ -8,7 +8,7 @@
 // i >= j compares a 32-row strip of tile (i, j) with the matching 32 columns
 // of tile (j, i) through 32 x 33 shared-memory transposes (both reads
 // coalesced) and stores its three sums of squares in a per-strip slot; a
-// second launch adds each pair's slots in strip order (so the verdict does
+// second launch adds each pair's slots in strip order (so the outcome does
 // not depend on scheduling) and raises the flag when the pair fails.
 // Stdlib's ishermitian compares with ==, so a NaN anywhere in a diagonal
 // tile fails the check as well.  chkfinite splits each tile's contiguous
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) herm_pair_kernel(const double *const *til
 }
 
 // One thread per off-diagonal pair: is_cross_hermitian on the strip sums.
-__global__ void herm_verdict_kernel(const double *part, int mt, int strips, int *flag) {
+__global__ void herm_decide_kernel(const double *part, int mt, int strips, int *flag) {
   const size_t npairs = (size_t)mt * (mt + 1) / 2;
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npairs;
        p += (size_t)gridDim.x * blockDim.x) {
@@ -170,7 +170,7 @@ int run_check(bool herm, int m, int n, int mb, int nb, double *const *tiles, cud
     DG_CUDA_TRY(cudaGetLastError());
     if (mt > 1) {
       const int blocks = (int)std::min<size_t>((npairs + 255) / 256, 4096);
-      herm_verdict_kernel<<<blocks, 256, 0, s>>>(part, mt, strips, flag);
+      herm_decide_kernel<<<blocks, 256, 0, s>>>(part, mt, strips, flag);
       DG_CUDA_TRY(cudaGetLastError());
     }
     dg::count_launches(mt > 1 ? 2 : 1);
