@@ -193,6 +193,11 @@ Dagger.move(::Dagger.CPUProc, ::GB300Proc, ::typeof(BLAS.gemv!)) = gb300_gemv!
 # whole-region calls: one ccall per cholesky! / ldiv!
 # ---------------------------------------------------------------------------
 tile_pointers(A::DArray) = [pointer(fetch(c)::GB300Array{Float64,2}) for c in A.chunks]
+# The library reports the global order of the first leading minor that is
+# not positive definite; potrf_checked! (src/array/cholesky.jl:2-18) records
+# the LAPACK info of the failing diagonal tile, and _chol! returns that
+# number, so the binding converts (1-based, tile k starts at k*nb + 1).
+tile_local_info(info::Integer, nb::Integer) = info <= 0 ? Int(info) : Int(info - nb * div(info - 1, nb))
 # the device holding a DArray's chunks, whose stream a whole-region call uses
 # unless the caller passes one
 device_of(A::DArray) = (fetch(first(A.chunks))::GB300Array).device
@@ -203,7 +208,7 @@ device_of(A::DArray) = (fetch(first(A.chunks))::GB300Array).device
 The datadeps region of `_chol!` (src/array/cholesky.jl:19-108) run by the
 library as one captured multi-stream CUDA graph.  All chunks must be
 GB300Arrays with Blocks(nb, nb) partitioning.  Throws PosDefException(info)
-like `potrf_checked!`.
+with the failing diagonal tile's LAPACK info, as `potrf_checked!` records it.
 """
 function cholesky_gb300!(A::DArray{Float64,2}, uplo::Char='U';
                          stream::Ptr{Cvoid}=device_stream(device_of(A)))
@@ -213,7 +218,7 @@ function cholesky_gb300!(A::DArray{Float64,2}, uplo::Char='U';
     info = ccall((:dg_cholesky_tiled, libdg), Cint, (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Cvoid}),
                  uplo, n, nb, ptrs, stream)
     dgcheck(info)
-    info > 0 && throw(PosDefException(Int(info)))
+    info > 0 && throw(PosDefException(tile_local_info(info, nb)))
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0))
 end
 
@@ -252,7 +257,7 @@ function cholesky_gb300_winv!(A::DArray{Float64,2}, uplo::Char='U';
                  (Cchar, Cint, Cint, Ptr{Ptr{Float64}}, Ptr{Float64}, Ptr{Cvoid}),
                  uplo, n, nb, tile_pointers(A), pointer(winv), stream)
     dgcheck(info)
-    info > 0 && throw(PosDefException(Int(info)))
+    info > 0 && throw(PosDefException(tile_local_info(info, nb)))
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0)), winv
 end
 
@@ -281,7 +286,7 @@ function cholesky_gb300_host!(A::DArray{Float64,2}, H::Matrix{Float64}, uplo::Ch
         ccall((:dg_host_free, libdg), Cint, (Ptr{Cvoid},), buf[])
     end
     dgcheck(info)
-    info > 0 && throw(PosDefException(Int(info)))
+    info > 0 && throw(PosDefException(tile_local_info(info, nb)))
     return Cholesky(A, uplo, convert(LinearAlgebra.BlasInt, 0))
 end
 
