@@ -82,9 +82,10 @@ struct dg_mixed {
   cudaStream_t aux = nullptr;     // lookahead stream (the next panel's step)
   cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
   // BF16 forms: the trailing updates by block row, on streams by priority
-  // (near_s[d]: the row d+2 steps ahead of the panel; far_s: the others);
-  // ev_row[r] marks block row r's latest update, which the next one waits for
-  static constexpr int kNear = 3, kFar = 8;
+  // (near_s[d]: the row d+2 steps ahead of the panel; far_s: one launch for
+  // all the others); ev_row[r] marks block row r's latest update, which the
+  // next one waits for
+  static constexpr int kNear = 3, kFar = 1;
   cudaStream_t near_s[kNear] = {}, far_s[kFar] = {};
   std::vector<cudaEvent_t> ev_row;
   // recorded by the BF16 schedule at mid-factorization: the slicing of A for
@@ -539,16 +540,18 @@ int mixed_prepare(dg_mixed *f, cudaStream_t s) {
 }
 
 // The BF16 forms' schedule, whose trailing operands are the per-panel slices
-// (no buffer is reused across steps).  Step k's update of block row r
-// (r >= k+2) is its own launch; it waits for panel k and for the row's
-// previous update (ev_row[r]), so rows never wait for one another.  The
-// launch's stream priority follows how soon the chain needs the row: row
-// k+2 (the next step's `next`) just below the chain's, then k+3 and k+4,
-// the rest at the least priority.  The critical chain on `aux` (greatest
-// priority) waits only for block row k+1's last update, then updates it by
-// panel k and factors panel k+1.  (With one launch for all rows, or rows
-// sharing a few streams of one priority, the chain waited for the previous
-// step's whole bulk update: 0.3-0.8 ms per step at N = 32768.)
+// (no buffer is reused across steps).  Step k's update of block rows k+2,
+// k+3 and k+4 are launches of their own, on streams whose priority follows
+// how soon the chain needs the row (just below the chain's); the rows past
+// them are one launch at the least priority.  Each launch waits for panel k
+// and for the previous update of its rows (an event per block row), so a
+// near row never waits for the bulk of its own step.  The critical chain on
+// `aux` (greatest priority) waits only for block row k+1's last update,
+// updates it by panel k and factors panel k+1; through the near rows it
+// depends on the bulk launch of three steps earlier.  (One launch per row
+// and step, about 30 per step at N = 32768, kept the chain's own launches
+// waiting about 1.3 ms per step behind the launches released by the same
+// panel; one launch for all rows made the chain wait for the whole bulk.)
 static int factor_by_rows(dg_mixed *f, cudaStream_t s) {
   const int mt = f->mt;
   if (!f->far_s[0]) {
@@ -568,14 +571,25 @@ static int factor_by_rows(dg_mixed *f, cudaStream_t s) {
   std::vector<char> recorded(mt, 0);
   for (int k = 0; k + 1 < mt; k++) {
     // ev_panel marks panel k here (panel 0: after the packed copy on s)
-    for (int r = k + 2; r < mt; r++) {
-      const int d = r - k - 2;
-      cudaStream_t rs = d < dg_mixed::kNear ? f->near_s[d] : f->far_s[r % dg_mixed::kFar];
+    const int far0 = k + 2 + dg_mixed::kNear;
+    for (int r = k + 2; r < std::min(far0, mt); r++) {
+      cudaStream_t rs = f->near_s[r - k - 2];
       DG_CUDA_TRY(cudaStreamWaitEvent(rs, f->ev_panel, 0));
       if (recorded[r]) DG_CUDA_TRY(cudaStreamWaitEvent(rs, f->ev_row[r], 0));
       DG_TRY(trailing_rows(f, k, r, r + 1, rs));
       DG_CUDA_TRY(cudaEventRecord(f->ev_row[r], rs));
       recorded[r] = 1;
+    }
+    if (far0 < mt) {
+      // the far rows' previous updates were the far launch of step k-1, on
+      // the same stream (the row that left the far range went to near_s)
+      cudaStream_t rs = f->far_s[0];
+      DG_CUDA_TRY(cudaStreamWaitEvent(rs, f->ev_panel, 0));
+      DG_TRY(trailing_rows(f, k, far0, mt, rs));
+      for (int r = far0; r < mt; r++) {
+        DG_CUDA_TRY(cudaEventRecord(f->ev_row[r], rs));
+        recorded[r] = 1;
+      }
     }
     if (recorded[k + 1]) DG_CUDA_TRY(cudaStreamWaitEvent(f->aux, f->ev_row[k + 1], 0));
     DG_TRY(trailing_rows(f, k, k + 1, k + 2, f->aux));
