@@ -214,10 +214,9 @@ __device__ __forceinline__ void tsync(int grp) {
 // relative, far below what the mixed form's operands carry), and updates
 // T(r, c) -= (s T(j, r)) (s T(j, c)) for j < r <= c; row j's scaling by s
 // (U(j, :), the diagonal d s = sqrt(d)) waits until step j + 1, which no
-// longer reads it.  The inverse X = U^-1 (into W) is a back substitution of
-// the same shape with 1 / U(j, j) = s kept per column: step j (from the
-// bottom) subtracts U(r, j) s W(j, c) from W(r, c) for r < j <= c and scales
-// row j at step j - 1.  piv: 32 floats of shared scratch.  factor = false only
+// longer reads it.  The inverse X = U^-1 (into W) is formed by recursive
+// doubling from 1 / U(j, j) = s kept per column (five levels of block
+// products).  piv: 32 floats of shared scratch.  factor = false only
 // inverts (T already holds U).  Returns the first failed column or -1 (valid
 // in every calling thread); on failure T is left partly factored and W unset.
 template <int NT>
@@ -249,31 +248,49 @@ __device__ int tile_chol_inv(float *T, float *W, float *piv, bool factor, int ti
   } else if (tid < DB) {
     piv[tid] = 1.0f / T[tid * DP + tid];
   }
-  // W = I, then the back substitution
+  // W = U^-1 by recursive doubling over the diagonal blocks: W starts as
+  // diag(1 / U(j, j)) (piv), and level b turns every 2b x 2b diagonal block
+  // into its inverse from the two b x b inverses on its diagonal,
+  // V12 = -V11 (U12 V22): three barriers per level, five levels, where a
+  // back substitution takes one barrier per column.
 #pragma unroll
   for (int q = 0; q < PER; q++) {
     const int e = tid + NT * q, r = e & 31, c = e >> 5;
-    W[c * DP + r] = r == c ? 1.f : 0.f;
-  }
-  tsync<NT>(grp);
-  for (int j = DB - 1; j >= 0; j--) {
-    const float sj = piv[j], sn = j < DB - 1 ? piv[j + 1] : 0.f;
-#pragma unroll
-    for (int q = 0; q < PER; q++) {
-      const int e = tid + NT * q, r = e & 31, c = e >> 5;
-      if (r < j && c >= j) W[c * DP + r] = fmaf(-(T[j * DP + r] * sj), W[c * DP + j], W[c * DP + r]);
-      if (r == j + 1 && c >= r) W[c * DP + r] *= sn;
-    }
-    tsync<NT>(grp);
-  }
-  const float p0 = piv[0];
-#pragma unroll
-  for (int q = 0; q < PER; q++) {
-    const int e = tid + NT * q, r = e & 31, c = e >> 5;
-    if (r == 0) W[c * DP + r] *= p0;
+    W[c * DP + r] = r == c ? piv[r] : 0.f;
     if (r > c) T[c * DP + r] = 0.f;  // the factor is upper triangular
   }
   tsync<NT>(grp);
+  for (int b = 1; b < DB; b <<= 1) {
+    // X = U12 V22, into the places of V12 (rows below i0 + b: no V22 reads)
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int e = tid + NT * q, r = e & 31, c = e >> 5;
+      const int i0 = r & ~(2 * b - 1);
+      if ((c & ~(2 * b - 1)) == i0 && r - i0 < b && c - i0 >= b) {
+        float x = 0.f;
+        for (int t = i0 + b; t <= c; t++) x = fmaf(T[t * DP + r], W[c * DP + t], x);
+        W[c * DP + r] = x;
+      }
+    }
+    tsync<NT>(grp);
+    float y[PER];
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int e = tid + NT * q, r = e & 31, c = e >> 5;
+      const int i0 = r & ~(2 * b - 1);
+      y[q] = 0.f;
+      if ((c & ~(2 * b - 1)) == i0 && r - i0 < b && c - i0 >= b)
+        for (int t = r; t < i0 + b; t++) y[q] = fmaf(-W[t * DP + r], W[c * DP + t], y[q]);
+    }
+    tsync<NT>(grp);
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int e = tid + NT * q, r = e & 31, c = e >> 5;
+      const int i0 = r & ~(2 * b - 1);
+      if ((c & ~(2 * b - 1)) == i0 && r - i0 < b && c - i0 >= b) W[c * DP + r] = y[q];
+    }
+    tsync<NT>(grp);
+  }
   return -1;
 }
 
@@ -287,7 +304,7 @@ __device__ __forceinline__ void upper_tile(int idx, int m, int &rr, int &cc) {
   cc = rr + idx;
 }
 
-__global__ void __launch_bounds__(DT) diag_chol_inv_kernel(const DiagArgs a) {
+__global__ void __launch_bounds__(DT, 1) diag_chol_inv_kernel(const DiagArgs a) {
   extern __shared__ float smem[];
   __shared__ int s_stop;
   __shared__ float s_piv[NG][DB];
