@@ -82,10 +82,10 @@ struct dg_mixed {
   cudaStream_t aux = nullptr;     // lookahead stream (the next panel's step)
   cudaEvent_t ev_next = nullptr, ev_panel = nullptr;
   // BF16 forms: the trailing updates by block row, on streams by priority
-  // (near_s[d]: the row d+2 steps ahead of the panel; far_s: one launch for
-  // all the others); ev_row[r] marks block row r's latest update, which the
-  // next one waits for
-  static constexpr int kNear = 3, kFar = 1;
+  // (near_s[d]: the row d+2 steps ahead of the panel; far_s: the others in
+  // kFar launches of consecutive rows); ev_row[r] marks block row r's latest
+  // update, which the next one waits for
+  static constexpr int kNear = 3, kFar = 4;
   cudaStream_t near_s[kNear] = {}, far_s[kFar] = {};
   std::vector<cudaEvent_t> ev_row;
   // recorded by the BF16 schedule at mid-factorization: the slicing of A for
@@ -543,15 +543,18 @@ int mixed_prepare(dg_mixed *f, cudaStream_t s) {
 // (no buffer is reused across steps).  Step k's update of block rows k+2,
 // k+3 and k+4 are launches of their own, on streams whose priority follows
 // how soon the chain needs the row (just below the chain's); the rows past
-// them are one launch at the least priority.  Each launch waits for panel k
-// and for the previous update of its rows (an event per block row), so a
-// near row never waits for the bulk of its own step.  The critical chain on
+// them are kFar launches of consecutive rows at the least priority.  Each
+// launch waits for panel k and for the previous update of its rows (an event
+// per block row), so a near row never waits for the bulk of its own step and
+// the bulk of step k overlaps that of step k-1.  The critical chain on
 // `aux` (greatest priority) waits only for block row k+1's last update,
 // updates it by panel k and factors panel k+1; through the near rows it
 // depends on the bulk launch of three steps earlier.  (One launch per row
 // and step, about 30 per step at N = 32768, kept the chain's own launches
 // waiting about 1.3 ms per step behind the launches released by the same
-// panel; one launch for all rows made the chain wait for the whole bulk.)
+// panel; one launch for all rows made the chain wait for the whole bulk, and
+// one launch for all far rows serialised the bulk updates of successive steps:
+// 8 % slower at N = 65536 with six products.)
 static int factor_by_rows(dg_mixed *f, cudaStream_t s) {
   const int mt = f->mt;
   if (!f->far_s[0]) {
@@ -580,13 +583,17 @@ static int factor_by_rows(dg_mixed *f, cudaStream_t s) {
       DG_CUDA_TRY(cudaEventRecord(f->ev_row[r], rs));
       recorded[r] = 1;
     }
-    if (far0 < mt) {
-      // the far rows' previous updates were the far launch of step k-1, on
-      // the same stream (the row that left the far range went to near_s)
-      cudaStream_t rs = f->far_s[0];
+    const int nfar = mt - far0;
+    for (int q = 0; q < dg_mixed::kFar && nfar > 0; q++) {
+      const int r0 = far0 + (int)((long long)nfar * q / dg_mixed::kFar);
+      const int r1 = far0 + (int)((long long)nfar * (q + 1) / dg_mixed::kFar);
+      if (r1 <= r0) continue;
+      cudaStream_t rs = f->far_s[q];
       DG_CUDA_TRY(cudaStreamWaitEvent(rs, f->ev_panel, 0));
-      DG_TRY(trailing_rows(f, k, far0, mt, rs));
-      for (int r = far0; r < mt; r++) {
+      for (int r = r0; r < r1; r++)
+        if (recorded[r]) DG_CUDA_TRY(cudaStreamWaitEvent(rs, f->ev_row[r], 0));
+      DG_TRY(trailing_rows(f, k, r0, r1, rs));
+      for (int r = r0; r < r1; r++) {
         DG_CUDA_TRY(cudaEventRecord(f->ev_row[r], rs));
         recorded[r] = 1;
       }
