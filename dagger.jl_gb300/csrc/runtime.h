@@ -14,8 +14,14 @@
 
 namespace dg {
 
-constexpr int kDefaultStreams = 16;
-constexpr int kUrgentStreams = 4;  // streams per priority level above the lowest
+#ifndef DG_REGION_STREAMS
+#define DG_REGION_STREAMS 16
+#endif
+constexpr int kDefaultStreams = DG_REGION_STREAMS;
+#ifndef DG_URGENT_STREAMS
+#define DG_URGENT_STREAMS 4
+#endif
+constexpr int kUrgentStreams = DG_URGENT_STREAMS;  // streams per priority level above the lowest
 constexpr int kPrioLevels = 6;     // stream priority levels used (fewer on the device collapse)
 // Host-to-device uploads get their own class of streams (at the least
 // priority), so that no compute task queues behind a transfer it does not need.
@@ -149,9 +155,10 @@ void clear_graphs();
 // A whole-call region: `call` hashes the entry point's arguments
 // (call_hash); when a graph for the same call is cached it is launched
 // without building the region, else build(r) fills a region that is run and
-// remembered.  The f64 engine and the device join the key.
+// remembered on `streams` streams at the lowest priority.  The f64 engine,
+// the device and the stream count join the key.
 int region_run_cached(uint64_t call, const std::function<void(dg_region *)> &build,
-                      cudaStream_t origin, bool sync);
+                      cudaStream_t origin, bool sync, int streams = kDefaultStreams);
 uint64_t call_hash(int fn, const void *args, size_t bytes, const void *const *ptrs, size_t nptrs);
 
 // oz_ring != nullptr selects the emulated-FP64 trailing updates, with
