@@ -17,9 +17,13 @@ Reported:
                every timed step (A's tiles are uploaded by tasks of the
                factorization's graph, cholesky_distribute)
   solves_per_s right-hand sides solved per second (factor included)
-  roofline     the dominant kernel (the FP64 tile GEMM of the trailing
-               update, 2 nb^3 flops per launch) timed alone with CUDA events,
-               against the FP64 FMA throughput measured in the same run
+  roofline     the dominant kernel (oz_gemm_kernel, the emulated FP64 GEMM
+               of the trailing update: 28 BF16 products per FP64 product)
+               timed alone with CUDA events on the trailing-update launch
+               shape (C 8 nb x 8 nb, K = nb, several output blocks per CTA),
+               against the measured BF16 burst peak; the critical-path tile
+               (one nb^3 launch) and the DFMA tile GEMM against the FP64 FMA
+               throughput measured in the same run sit beside it
   cpu_baseline the oracle's threaded C restatement of the reference's
                datadeps Cholesky (OpenBLAS tiles) on the host cores: one
                factor+solve of the same system (same N, tiling and RHS)
@@ -29,6 +33,12 @@ Reported:
                probed ||A - U'U|| / ||A|| for the factor
   mul          G G' on the same tiling (syrk_dagger! + copytri!), the
                reference benchmark's input construction, TFLOP/s (n^3)
+  mixed        the mixed-precision form on the same system (low-precision
+               factor + FP64 refinement to a 1e-12 backward error)
+  mixed_sweep  the mixed form over N x kappa x right-hand sides
+  lu           lu(A, RowMaximum()) and its solve on rand(N, N)
+  batched      10,000 small SPD systems in one persistent launch
+  serving      p50 / p99 latency of Poisson request streams at swept rates
 
 `--impl reference` times only the CPU baseline (the reference's algorithm
 restated in C, run with all host threads) on the same metric and the same
