@@ -14,7 +14,7 @@ from .linalg import (Cholesky, chkfinite, cholesky, cholesky_, cholesky_distribu
                      gemm_, gemm_dagger_,
                      matmul, mul_, syrk_dagger_, gemm_f64_emulated_tn, gemv_,
                      get_f64_engine, getrf_, ishermitian, issymmetric, LU, ldiv, ldiv_, lu, lu_,
-                     potrf_, set_f64_engine, syrk_, trsm_, trsv_)
+                     potrf_, set_f64_engine, syrk_, tile_local_info, trsm_, trsv_)
 from .mixed import MixedCholesky, cholesky_mixed
 
 __all__ = [
@@ -23,5 +23,5 @@ __all__ = [
     "ishermitian", "issymmetric", "potrf_", "trsm_", "syrk_", "gemm_", "trsv_", "gemv_",
     "gemm_f64_emulated_tn", "set_f64_engine", "get_f64_engine", "spawn_datadeps", "spawn", "In", "Out", "InOut", "copyto_", "PosDefException",
     "DaggerGB300Error", "lib", "LU", "lu", "lu_", "ldiv", "getrf_", "SingularException",
-    "chkfinite", "copy_reblock",
+    "chkfinite", "copy_reblock", "tile_local_info", "MixedCholesky", "cholesky_mixed",
 ]

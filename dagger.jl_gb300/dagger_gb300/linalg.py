@@ -19,7 +19,9 @@ argument meanings and error behaviour:
 Every compute call goes through libdaggergb300 (C ABI); none has a CPU path.
 A matrix that is not positive definite raises PosDefException(info) from
 cholesky / cholesky_ (potrf_checked!, cholesky.jl:2-18), or returns info
-with check=False (cholesky(A; check=false) in LinearAlgebra).
+with check=False (cholesky(A; check=false) in LinearAlgebra); info is the
+global order of the failing leading minor (tile_local_info gives the tile's
+own number, which the reference records).
 """
 from __future__ import annotations
 
@@ -31,6 +33,17 @@ import torch
 from . import _lib
 from ._lib import PosDefException, ch, check, lib
 from .darray import Blocks, DArray
+
+
+def tile_local_info(info: int, nb: int) -> int:
+    """The LAPACK info of the failing diagonal tile, as potrf_checked!
+    (cholesky.jl:2-18) records it and _chol! returns it, from the global
+    order of the first leading minor that is not positive definite (what
+    cholesky / cholesky_ report, as LinearAlgebra's dense cholesky does).
+    Tiles are Blocks(nb, nb); info <= 0 is returned unchanged."""
+    if nb <= 0:
+        raise ValueError("nb must be positive")
+    return info if info <= 0 else info - nb * ((info - 1) // nb)
 
 
 def _stream(stream=None) -> int:

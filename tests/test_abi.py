@@ -168,3 +168,15 @@ def test_invalid_arguments_of_the_newer_entry_points():
     # chkfinite of an m x n grid: mb <= 0
     assert L.dg_chkfinite_tiled_mn(4, 4, 0, 2, None, None) == -3
     assert L.dg_ishermitian_tiled(-1, 2, None, None) == -1
+
+
+def test_tile_local_info():
+    """The reference's info (the failing tile's own LAPACK info) from the
+    global order the library reports."""
+    import dagger_gb300 as d
+    assert d.tile_local_info(0, 64) == 0
+    assert d.tile_local_info(1, 64) == 1
+    assert d.tile_local_info(64, 64) == 64
+    assert d.tile_local_info(65, 64) == 1
+    assert d.tile_local_info(200, 64) == 8
+    assert d.tile_local_info(130, 128) == 2
